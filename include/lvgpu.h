@@ -1,0 +1,182 @@
+/*
+ * lvgpu.h — C ABI of the GB300 implementation of the Lagrangian Voronoi
+ * per-timestep path (LagrangianVoronoi.jl).
+ *
+ * One opaque context (`lv_ctx`) holds one VoronoiGrid: the domain, the cell
+ * list, the particle state in device memory (SoA, FP64) and the pressure
+ * solver.  Every call is ordered on the context's CUDA stream.  Calls that
+ * return host data, or that are documented as synchronising, wait for the
+ * stream; the others return as soon as their kernels are queued, and their
+ * failures (NaN velocity, destroyed mesh, ...) are reported by the next
+ * synchronising call or by lv_status().
+ *
+ * Return values: 0 on success, otherwise one of the LV_ERR_* codes;
+ * lv_last_error() gives a message.  Particle indices are 0-based; boundary
+ * labels keep the reference's values (BDARY_UP=-1, RIGHT=-2, DOWN=-3,
+ * LEFT=-4, src/polygon.jl:4-7).
+ *
+ * Threading: one context per host thread; calls on one context are not
+ * reentrant.  Host pointers are borrowed only for the duration of a call.
+ */
+#ifndef LVGPU_H
+#define LVGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define LV_OK 0
+#define LV_ERR_NAN_VELOCITY 1      /* move.jl:24-26 "Velocity field invalidated." */
+#define LV_ERR_MESH_DESTROYED 2    /* voronoigrid.jl:63-65 "The Voronoi Mesh has been destroyed." */
+#define LV_ERR_EDGE_OVERFLOW 3     /* a polygon needed more than LV_MAX_EDGES edges */
+#define LV_ERR_CELL_OVERFLOW 4     /* more cell-list entries than the capacity */
+#define LV_ERR_CG_MAXITER 5        /* a pressure solve stopped at itmax (reported in stats) */
+#define LV_ERR_BAD_ARGUMENT 6
+#define LV_ERR_CUDA 7
+#define LV_ERR_NOT_MESHED 8
+#define LV_ERR_LEARNED_WORSE 9     /* learned preconditioner fell back to Jacobi */
+#define LV_ERR_NONFINITE_POSITION 10
+#define LV_ERR_BARRIER_TIMEOUT 11  /* a grid barrier in a persistent kernel gave up */
+
+/* maximum number of edges a Voronoi polygon may have at any time */
+#define LV_MAX_EDGES 20
+
+/* boundary labels (src/polygon.jl:4-7) */
+#define LV_BDARY_UP (-1)
+#define LV_BDARY_RIGHT (-2)
+#define LV_BDARY_DOWN (-3)
+#define LV_BDARY_LEFT (-4)
+
+/* fields of the polygon state (src/celldefs.jl:7-41, PolygonNS);
+ * vector fields are [n][2], D is [n][4] column-major (D11 D21 D12 D22),
+ * phase is passed as doubles holding small integers. */
+enum lv_field {
+  LV_FIELD_X = 0, LV_FIELD_V = 1, LV_FIELD_E = 2, LV_FIELD_P = 3, LV_FIELD_RHO = 4, LV_FIELD_C2 = 5,
+  LV_FIELD_DV = 6, LV_FIELD_MASS = 7, LV_FIELD_MOMENTUM = 8, LV_FIELD_ENERGY = 9, LV_FIELD_PHASE = 10,
+  LV_FIELD_QUALITY = 11, LV_FIELD_D = 12, LV_FIELD_MU = 13,
+  /* read-only geometry derived by lv_remesh */
+  LV_FIELD_AREA = 20, LV_FIELD_CENTROID = 21
+};
+
+/* pressure solver methods */
+enum lv_method {
+  LV_METHOD_JACOBI_PCG = 0,   /* FP64 Jacobi-preconditioned CG (the fallback and the judge) */
+  LV_METHOD_MIXED_IR = 1,     /* FP32 CG inner solves inside FP64 iterative refinement */
+  LV_METHOD_LEARNED_PCG = 2   /* mixed IR preconditioned by the learned sparse factor */
+};
+
+typedef struct lv_params {
+  double xmin[2], xmax[2];   /* boundary rectangle (Rectangle, geometry.jl:94-111) */
+  double dr;                 /* resolution */
+  double h;                  /* cell-list cell size; <= 0 selects the reference default 2dr */
+  double r_max;              /* maximum neighbour distance; <= 0 selects the default 10dr */
+  int32_t xperiodic, yperiodic;
+  int32_t capacity;          /* maximum number of particles */
+  int32_t device;            /* CUDA device ordinal */
+} lv_params;
+
+typedef struct lv_solve_stats {
+  int32_t iterations;        /* CG iterations (inner iterations for mixed IR) */
+  int32_t converged;         /* 1 if ||b - A x|| <= tol ||b|| was reached */
+  int32_t outer;             /* refinement steps (mixed IR / learned) */
+  int32_t method;            /* method actually used */
+  double rel_residual;       /* final ||b - A x|| / ||b||, recomputed in FP64 */
+} lv_solve_stats;
+
+typedef struct lv_ctx lv_ctx;
+
+/* VoronoiGrid{T}(rect, dr; h, r_max, xperiodic, yperiodic)
+ * (src/voronoigrid.jl:14-50).  Returns NULL on failure. */
+lv_ctx* lv_create(const lv_params* params);
+int lv_destroy(lv_ctx* ctx);
+const char* lv_last_error(const lv_ctx* ctx);
+/* Pending device status (LV_OK or an LV_ERR_* code); synchronises. */
+int lv_status(lv_ctx* ctx);
+int lv_synchronize(lv_ctx* ctx);
+
+/* Replaces the particle set: `push!(grid.polygons, T(x = x))` for n seeds
+ * (src/populate.jl); x is [n][2].  Other fields are zeroed. */
+int lv_set_positions(lv_ctx* ctx, int32_t n, const double* x);
+int32_t lv_num_particles(const lv_ctx* ctx);
+/* Upload / download one field of all n particles (see lv_field). */
+int lv_set_field(lv_ctx* ctx, int32_t field, const double* host);
+int lv_get_field(lv_ctx* ctx, int32_t field, double* host);
+/* Device pointer of a field (for zero-copy interop); NULL if unknown. */
+void* lv_field_device_ptr(lv_ctx* ctx, int32_t field);
+
+/* remesh!(grid) (src/voronoigrid.jl:89-108): re-bins every seed and rebuilds
+ * every Voronoi polygon by half-plane clipping, then orders its edges
+ * (sort_edges!, src/IO.jl:35-48).  Synchronises and returns the status. */
+int lv_remesh(lv_ctx* ctx);
+/* Same, without the final synchronisation (status via lv_status). */
+int lv_remesh_async(lv_ctx* ctx);
+
+/* Geometry of the last remesh.  nedges[n]; verts[n][LV_MAX_EDGES][4]
+ * (v1x v1y v2x v2y) and labels[n][LV_MAX_EDGES] in the polygon's edge order;
+ * any pointer may be NULL. */
+int lv_get_geometry(lv_ctx* ctx, int32_t* nedges, double* verts, int32_t* labels);
+/* Interior faces in `neighbors(p, grid)` order (src/iterators.jl:23-33):
+ * rowptr[n+1]; nbr, lrr = lr_ratio(x-y, e), mid = midpoint(e), y = p.x +
+ * get_arrow(q.x, p.x), len = len(e).  Returns the face count through *nfaces
+ * when the arrays are NULL. */
+int lv_get_faces(lv_ctx* ctx, int64_t* nfaces, int64_t* rowptr, int32_t* nbr, double* lrr, double* mid, double* y,
+                 double* len);
+/* Cell list: starts[ncells+1] and items (particle indices in insertion order);
+ * ncells = n1*n2 (column-major, neighborlist.jl:11-44). */
+int lv_get_cell_list(lv_ctx* ctx, int64_t* ncells, int64_t* nitems, int32_t* starts, int32_t* items);
+
+/* Physics steps — names and arguments follow the reference's exports. */
+int lv_move(lv_ctx* ctx, double dt);                                   /* move!  (move.jl:9-21), remeshes */
+int lv_ideal_eos(lv_ctx* ctx, double gamma, double Pmin);              /* ideal_eos!  (pressure.jl:49-55) */
+int lv_stiffened_eos(lv_ctx* ctx, double gamma, double P0);            /* stiffened_eos! (pressure.jl:64-70) */
+int lv_find_rho(lv_ctx* ctx);                                          /* find_rho! (pressure.jl:36-40) */
+int lv_gravity_step(lv_ctx* ctx, double gx, double gy, double dt);     /* gravity_step! (pressure.jl:77-82) */
+int lv_pressure_step(lv_ctx* ctx, double dt);                          /* pressure_step! (pressure.jl:10-25) */
+int lv_find_D(lv_ctx* ctx);                                            /* find_D! (diffusion.jl:8-19) */
+int lv_viscous_step(lv_ctx* ctx, double dt, int32_t artificial_viscosity); /* viscous_step! (diffusion.jl:39-53) */
+/* bdary_friction!(grid, vDirichlet, dt) (diffusion.jl:64-79) with a constant
+ * wall velocity per boundary label: vwall[4][2] indexed by -label-1. */
+int lv_bdary_friction(lv_ctx* ctx, const double* vwall, double dt);
+int lv_find_dv(lv_ctx* ctx, double dt, double alpha);                 /* find_dv! (relaxation.jl:10-25) */
+int lv_relaxation_step(lv_ctx* ctx, double dt, int32_t rusanov);      /* relaxation_step! (relaxation.jl:36-73), remeshes */
+
+/* PressureSolver(grid) options (pressure.jl:142-159): method, relative
+ * residual tolerance and iteration cap. */
+int lv_set_solver(lv_ctx* ctx, int32_t method, double tol, int32_t itmax);
+/* find_pressure!(solver, dt, niter; boundary_velocity) (pressure.jl:215-224).
+ * vbc[4][2] (constant boundary velocity per label) may be NULL (zero_vbc).
+ * stats[niter] may be NULL; when given, the call synchronises. */
+int lv_find_pressure(lv_ctx* ctx, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats);
+/* Pieces of find_pressure! for inspection: PressureOperator refresh!
+ * (pressure.jl:104-117) into the device CSR; solver refresh! (pressure.jl:162-203). */
+int lv_pressure_operator(lv_ctx* ctx, double dt);
+int lv_pressure_rhs(lv_ctx* ctx, double dt, int32_t gp_step, const double* vbc);
+/* Export of the assembled system: diag[n] (the reference's diagonal term),
+ * rowptr[n+1], col[nnz], w[nnz] (off-diagonal weights w_ij), b[n]; with NULL
+ * arrays only *nnz is returned. */
+int lv_export_system(lv_ctx* ctx, int64_t* nnz, double* diag, int64_t* rowptr, int32_t* col, double* w, double* b);
+/* Solve A x = b on the current operator with the current method; b and x are
+ * host arrays of n doubles, x holds the initial guess on entry. */
+int lv_solve(lv_ctx* ctx, const double* b, double* x, lv_solve_stats* stats);
+/* y = A x on the current operator (host arrays). */
+int lv_operator_apply(lv_ctx* ctx, const double* x, double* y);
+
+/* MultiphaseSolver / multiphase_projection! (relaxation.jl:137-206). */
+int lv_multiphase_projection(lv_ctx* ctx, double quality_threshold, lv_solve_stats* stats);
+
+/* Per-kernel-family device times in ms accumulated since the last reset:
+ * out[0] mesh, [1] operators, [2] pressure solve, [3] other.  Returns the
+ * number of entries written. */
+int lv_get_timings(lv_ctx* ctx, double* out, int32_t cap);
+int lv_reset_timings(lv_ctx* ctx);
+/* Number of kernel launches issued by the context since creation. */
+int64_t lv_launch_count(const lv_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LVGPU_H */

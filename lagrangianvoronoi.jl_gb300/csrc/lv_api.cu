@@ -1,0 +1,688 @@
+// C ABI of liblvgpu (include/lvgpu.h): context, device memory, transfers and
+// the entry points that sequence the kernels of lv_mesh.cu, lv_physics.cu
+// and lv_solver.cu on the context's stream.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "lv_internal.cuh"
+
+int lv_fail(lv_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int lv_cuda_check(lv_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return LV_OK;
+  return lv_fail(c, LV_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+template <class T>
+T* dalloc(lv_ctx* c, size_t count, bool* ok) {
+  void* p = nullptr;
+  if (count == 0) count = 1;
+  if (cudaMalloc(&p, sizeof(T) * count) != cudaSuccess) {
+    *ok = false;
+    return nullptr;
+  }
+  cudaMemset(p, 0, sizeof(T) * count);
+  c->allocs.push_back(p);
+  return static_cast<T*>(p);
+}
+
+// neighborlist.jl:29-41: the visited prefix of the cell path (every node with
+// rr <= rr_max, then the first node beyond, at which the search either stops
+// or reports a destroyed mesh); offsets range over the reference's swapped
+// bounds i1 in [1-n2, n2-1], i2 in [1-n1, n1-1]; order = stable sort by |key|^2,
+// then stable sort by rr.
+std::vector<PathNodeDev> build_path(const GridDev& g) {
+  struct Node {
+    long long i1, i2, keysq;
+    double rr;
+  };
+  const long long R = (long long)ceil(sqrt(g.rr_max) / g.h) + 3;
+  const long long lo2 = std::max<long long>(1 - (long long)g.n1, -R), hi2 = std::min<long long>(g.n1 - 1, R);
+  const long long lo1 = std::max<long long>(1 - (long long)g.n2, -R), hi1 = std::min<long long>(g.n2 - 1, R);
+  std::vector<Node> all;
+  for (long long i2 = lo2; i2 <= hi2; ++i2)
+    for (long long i1 = lo1; i1 <= hi1; ++i1) {
+      long long a = std::max<long long>(0, llabs(i1) - 1), b = std::max<long long>(0, llabs(i2) - 1);
+      volatile double hh = g.h * g.h;  // keep (h*h)*k, as the reference's h^2*(...)
+      double rr = hh * (double)(a * a + b * b);
+      all.push_back({i1, i2, i1 * i1 + i2 * i2, rr});
+    }
+  std::stable_sort(all.begin(), all.end(), [](const Node& p, const Node& q) { return p.keysq < q.keysq; });
+  std::stable_sort(all.begin(), all.end(), [](const Node& p, const Node& q) { return p.rr < q.rr; });
+  std::vector<PathNodeDev> out;
+  for (const auto& nd : all) {
+    out.push_back(PathNodeDev{(int)nd.i1, (int)nd.i2, nd.rr});
+    if (nd.rr > g.rr_max) break;
+  }
+  return out;
+}
+
+int nimages(const GridDev& g) { return 1 + (g.xper ? 2 : 0) + (g.yper ? 2 : 0) + ((g.xper && g.yper) ? 4 : 0); }
+
+int decode_status(int flags) {
+  if (flags & LV_FLAG_NAN_VELOCITY) return LV_ERR_NAN_VELOCITY;
+  if (flags & LV_FLAG_NONFINITE) return LV_ERR_NONFINITE_POSITION;
+  if (flags & LV_FLAG_MESH_DESTROYED) return LV_ERR_MESH_DESTROYED;
+  if (flags & LV_FLAG_EDGE_OVERFLOW) return LV_ERR_EDGE_OVERFLOW;
+  if (flags & LV_FLAG_CELL_OVERFLOW) return LV_ERR_CELL_OVERFLOW;
+  if (flags & LV_FLAG_BARRIER_TIMEOUT) return LV_ERR_BARRIER_TIMEOUT;
+  return LV_OK;
+}
+
+const char* status_message(int code) {
+  switch (code) {
+    case LV_ERR_NAN_VELOCITY: return "Velocity field invalidated.";
+    case LV_ERR_MESH_DESTROYED: return "The Voronoi Mesh has been destroyed.";
+    case LV_ERR_EDGE_OVERFLOW: return "a Voronoi polygon exceeded LV_MAX_EDGES edges";
+    case LV_ERR_CELL_OVERFLOW: return "cell list capacity exceeded";
+    case LV_ERR_NONFINITE_POSITION: return "non-finite particle position";
+    case LV_ERR_BARRIER_TIMEOUT: return "grid barrier timed out in a persistent kernel";
+    default: return "";
+  }
+}
+
+// Reads and clears the device status word (synchronises the stream).
+int sync_status(lv_ctx* c) {
+  cudaError_t e = cudaMemcpyAsync(c->status_host, c->status, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "stream synchronize");
+  int flags = *c->status_host;
+  if (flags) {
+    cudaMemsetAsync(c->status, 0, sizeof(int), c->stream);
+    int code = decode_status(flags);
+    return lv_fail(c, code, status_message(code));
+  }
+  return LV_OK;
+}
+
+struct Timer {
+  lv_ctx* c;
+  int slot;
+  Timer(lv_ctx* cc, int s) : c(cc), slot(s) {
+    if (c->timing) cudaEventRecord(c->ev0, c->stream);
+  }
+  ~Timer() {
+    if (c->timing) {
+      cudaEventRecord(c->ev1, c->stream);
+      cudaEventSynchronize(c->ev1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      c->t_ms[slot] += ms;
+    }
+  }
+};
+
+__global__ void k_split_phase(const double* __restrict__ src, int* dst, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (int)src[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+lv_ctx* lv_create(const lv_params* prm) {
+  if (!prm || prm->capacity <= 0 || !(prm->dr > 0)) return nullptr;
+  if (!(prm->xmax[0] > prm->xmin[0]) || !(prm->xmax[1] > prm->xmin[1])) return nullptr;
+  lv_ctx* c = new lv_ctx();
+  c->prm = *prm;
+  c->dev = prm->device;
+  if (cudaSetDevice(c->dev) != cudaSuccess) {
+    delete c;
+    return nullptr;
+  }
+  GridDev& g = c->g;
+  const double dr = prm->dr;
+  const double h = prm->h > 0 ? prm->h : 2.0 * dr;
+  const double r_max = prm->r_max > 0 ? prm->r_max : 10.0 * dr;
+  g.dr = dr;
+  g.h = h;
+  g.xper = prm->xperiodic ? 1 : 0;
+  g.yper = prm->yperiodic ? 1 : 0;
+  g.bminx = prm->xmin[0];
+  g.bminy = prm->xmin[1];
+  g.bmaxx = prm->xmax[0];
+  g.bmaxy = prm->xmax[1];
+  // voronoigrid.jl:29-33: cropping rectangle enlarged by r_max in periodic directions
+  const double rx = g.xper ? r_max : 0.0, ry = g.yper ? r_max : 0.0;
+  g.cminx = g.bminx - rx;
+  g.cminy = g.bminy - ry;
+  g.cmaxx = g.bmaxx + rx;
+  g.cmaxy = g.bmaxy + ry;
+  g.xperiod = g.bmaxx - g.bminx;
+  g.yperiod = g.bmaxy - g.bminy;
+  g.rr_max = r_max * r_max;
+  // neighborlist.jl:18-27
+  g.ox = g.cminx - h;
+  g.oy = g.cminy - h;
+  g.n1 = (int)floor((g.cmaxx - g.cminx) / h) + 3;
+  g.n2 = (int)floor((g.cmaxy - g.cminy) / h) + 3;
+  const double bigm = std::max(std::max(fabs(g.cminx), fabs(g.cmaxx)), std::max(fabs(g.cminy), fabs(g.cmaxy)));
+  g.bigm = (float)(bigm * (1.0 + 1e-6));
+  g.delta32 = (float)(ldexp(1.0, -22) * (bigm + std::max(g.xperiod, g.yperiod)));
+  c->path_host = build_path(g);
+  g.npath = (int)c->path_host.size();
+
+  cudaDeviceProp p;
+  cudaGetDeviceProperties(&p, c->dev);
+  c->num_sms = p.multiProcessorCount;
+  if (!p.cooperativeLaunch) {
+    delete c;
+    return nullptr;
+  }
+  cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  const char* tenv = getenv("LVGPU_TIMING");
+  c->timing = tenv && tenv[0] == '1';
+
+  const int cap = (prm->capacity + 31) / 32 * 32;
+  c->cap = cap;
+  bool ok = true;
+  StateDev& s = c->s;
+  s.x = dalloc<double2>(c, cap, &ok);
+  s.v = dalloc<double2>(c, cap, &ok);
+  s.dv = dalloc<double2>(c, cap, &ok);
+  s.mom = dalloc<double2>(c, cap, &ok);
+  s.Da = dalloc<double2>(c, cap, &ok);
+  s.Db = dalloc<double2>(c, cap, &ok);
+  s.GP = dalloc<double2>(c, cap, &ok);
+  s.e = dalloc<double>(c, cap, &ok);
+  s.P = dalloc<double>(c, cap, &ok);
+  s.rho = dalloc<double>(c, cap, &ok);
+  s.c2 = dalloc<double>(c, cap, &ok);
+  s.mass = dalloc<double>(c, cap, &ok);
+  s.energy = dalloc<double>(c, cap, &ok);
+  s.quality = dalloc<double>(c, cap, &ok);
+  s.mu = dalloc<double>(c, cap, &ok);
+  s.phase = dalloc<int>(c, cap, &ok);
+
+  MeshDev& m = c->m;
+  m.cap = cap;
+  const size_t ell = (size_t)LV_MAX_EDGES * cap;
+  m.nedges = dalloc<int>(c, cap, &ok);
+  m.nfaces = dalloc<int>(c, cap + 1, &ok);
+  m.ev1 = dalloc<double2>(c, ell, &ok);
+  m.ev2 = dalloc<double2>(c, ell, &ok);
+  m.elab = dalloc<int>(c, ell, &ok);
+  m.fnbr = dalloc<int>(c, ell, &ok);
+  m.flrr = dalloc<double>(c, ell, &ok);
+  m.flen = dalloc<double>(c, ell, &ok);
+  m.fm = dalloc<double2>(c, ell, &ok);
+  m.fy = dalloc<double2>(c, ell, &ok);
+  m.area = dalloc<double>(c, cap, &ok);
+  m.centroid = dalloc<double2>(c, cap, &ok);
+
+  CellsDev& cl = c->c;
+  cl.ncells = g.n1 * g.n2;
+  cl.cstart = dalloc<int>(c, (size_t)cl.ncells + 1, &ok);
+  cl.ccount = dalloc<int>(c, cl.ncells, &ok);
+  cl.item_cap = cap * nimages(g);
+  cl.citem = dalloc<int>(c, cl.item_cap, &ok);
+  cl.cpos = dalloc<float2>(c, cl.item_cap, &ok);
+
+  SolverDev& sv = c->sv;
+  sv.nnz_cap = (int64_t)ell;
+  sv.rowptr = dalloc<int>(c, cap + 1, &ok);
+  sv.col = dalloc<int>(c, ell, &ok);
+  sv.w = dalloc<double>(c, ell, &ok);
+  sv.w32 = dalloc<float>(c, ell, &ok);
+  sv.diag = dalloc<double>(c, cap, &ok);
+  sv.adiag = dalloc<double>(c, cap, &ok);
+  sv.dinv = dalloc<double>(c, cap, &ok);
+  sv.b = dalloc<double>(c, cap, &ok);
+  sv.xs = dalloc<double>(c, cap, &ok);
+  sv.r = dalloc<double>(c, 2 * (size_t)cap, &ok);
+  sv.z = dalloc<double>(c, cap, &ok);
+  sv.p = dalloc<double>(c, 2 * (size_t)cap, &ok);
+  sv.q = dalloc<double>(c, cap, &ok);
+  const size_t tmp_n = std::max<size_t>(3 * (size_t)cap, (size_t)cl.ncells / 512 + 64);
+  sv.tmp = dalloc<double>(c, tmp_n, &ok);
+  sv.dinv32 = dalloc<float>(c, cap, &ok);
+  sv.r32 = dalloc<float>(c, cap, &ok);
+  sv.z32 = dalloc<float>(c, cap, &ok);
+  sv.p32 = dalloc<float>(c, cap, &ok);
+  sv.q32 = dalloc<float>(c, cap, &ok);
+  sv.d32 = dalloc<float>(c, cap, &ok);
+  sv.part = dalloc<double>(c, 8 * 4096, &ok);
+  sv.bar = dalloc<unsigned>(c, 4, &ok);
+  sv.iters = dalloc<int>(c, 64, &ok);
+  sv.dstats = dalloc<double>(c, 3 * 64, &ok);
+  c->status = dalloc<int>(c, 1, &ok);
+  c->path = dalloc<PathNodeDev>(c, c->path_host.size(), &ok);
+  if (cudaMallocHost(&c->status_host, sizeof(int)) != cudaSuccess) ok = false;
+  if (!ok) {
+    lv_destroy(c);
+    return nullptr;
+  }
+  cudaMemcpy(c->path, c->path_host.data(), sizeof(PathNodeDev) * c->path_host.size(), cudaMemcpyHostToDevice);
+  cudaDeviceSynchronize();
+  return c;
+}
+
+int lv_destroy(lv_ctx* c) {
+  if (!c) return LV_OK;
+  cudaSetDevice(c->dev);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->status_host) cudaFreeHost(c->status_host);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return LV_OK;
+}
+
+const char* lv_last_error(const lv_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int lv_status(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  return sync_status(c);
+}
+
+int lv_synchronize(lv_ctx* c) { return lv_status(c); }
+
+int lv_set_positions(lv_ctx* c, int32_t n, const double* x) {
+  if (!c || n < 0 || (n > 0 && !x)) return LV_ERR_BAD_ARGUMENT;
+  if (n > c->prm.capacity) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "more particles than the context capacity");
+  c->n = n;
+  cudaStream_t s = c->stream;
+  StateDev& st = c->s;
+  const size_t cap = c->cap;
+  for (double2* p : {st.x, st.v, st.dv, st.mom, st.Da, st.Db, st.GP}) cudaMemsetAsync(p, 0, 16 * cap, s);
+  for (double* p : {st.e, st.P, st.rho, st.c2, st.mass, st.energy, st.quality, st.mu}) cudaMemsetAsync(p, 0, 8 * cap, s);
+  cudaMemsetAsync(st.phase, 0, 4 * cap, s);
+  cudaError_t e = cudaMemcpyAsync(st.x, x, 16 * (size_t)n, cudaMemcpyHostToDevice, s);
+  c->meshed = false;
+  c->op_ready = false;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return lv_cuda_check(c, e, "lv_set_positions");
+}
+
+int32_t lv_num_particles(const lv_ctx* c) { return c ? c->n : 0; }
+
+static double* dptr1(lv_ctx* c, int f) {
+  StateDev& s = c->s;
+  switch (f) {
+    case LV_FIELD_E: return s.e;
+    case LV_FIELD_P: return s.P;
+    case LV_FIELD_RHO: return s.rho;
+    case LV_FIELD_C2: return s.c2;
+    case LV_FIELD_MASS: return s.mass;
+    case LV_FIELD_ENERGY: return s.energy;
+    case LV_FIELD_QUALITY: return s.quality;
+    case LV_FIELD_MU: return s.mu;
+    case LV_FIELD_AREA: return c->m.area;
+    default: return nullptr;
+  }
+}
+static double2* dptr2(lv_ctx* c, int f) {
+  StateDev& s = c->s;
+  switch (f) {
+    case LV_FIELD_X: return s.x;
+    case LV_FIELD_V: return s.v;
+    case LV_FIELD_DV: return s.dv;
+    case LV_FIELD_MOMENTUM: return s.mom;
+    case LV_FIELD_CENTROID: return c->m.centroid;
+    default: return nullptr;
+  }
+}
+
+int lv_set_field(lv_ctx* c, int32_t f, const double* h) {
+  if (!c || !h) return LV_ERR_BAD_ARGUMENT;
+  const size_t n = c->n;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (f == LV_FIELD_AREA || f == LV_FIELD_CENTROID)
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "geometry fields are read-only");
+  if (double* d = dptr1(c, f)) {
+    e = cudaMemcpyAsync(d, h, 8 * n, cudaMemcpyHostToDevice, s);
+  } else if (double2* d2 = dptr2(c, f)) {
+    e = cudaMemcpyAsync(d2, h, 16 * n, cudaMemcpyHostToDevice, s);
+    if (f == LV_FIELD_X) {
+      c->meshed = false;
+      c->op_ready = false;
+    }
+  } else if (f == LV_FIELD_D) {
+    e = cudaMemcpy2DAsync(c->s.Da, 16, h, 32, 16, n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(c->s.Db, 16, h + 2, 32, 16, n, cudaMemcpyHostToDevice, s);
+  } else if (f == LV_FIELD_PHASE) {
+    double* tmp = c->sv.tmp;
+    e = cudaMemcpyAsync(tmp, h, 8 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && n > 0) {
+      k_split_phase<<<lv_blocks((int)n, 256), 256, 0, s>>>(tmp, c->s.phase, (int)n);
+      c->launches++;
+      e = cudaGetLastError();
+    }
+  } else {
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "unknown field");
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return lv_cuda_check(c, e, "lv_set_field");
+}
+
+int lv_get_field(lv_ctx* c, int32_t f, double* h) {
+  if (!c || !h) return LV_ERR_BAD_ARGUMENT;
+  const size_t n = c->n;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (double* d = dptr1(c, f)) {
+    e = cudaMemcpyAsync(h, d, 8 * n, cudaMemcpyDeviceToHost, s);
+  } else if (double2* d2 = dptr2(c, f)) {
+    e = cudaMemcpyAsync(h, d2, 16 * n, cudaMemcpyDeviceToHost, s);
+  } else if (f == LV_FIELD_D) {
+    e = cudaMemcpy2DAsync(h, 32, c->s.Da, 16, 16, n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpy2DAsync(h + 2, 32, c->s.Db, 16, 16, n, cudaMemcpyDeviceToHost, s);
+  } else if (f == LV_FIELD_PHASE) {
+    std::vector<int> tmp(n);
+    e = cudaMemcpyAsync(tmp.data(), c->s.phase, 4 * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    for (size_t i = 0; i < n; ++i) h[i] = tmp[i];
+    return lv_cuda_check(c, e, "lv_get_field");
+  } else {
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "unknown field");
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return lv_cuda_check(c, e, "lv_get_field");
+}
+
+void* lv_field_device_ptr(lv_ctx* c, int32_t f) {
+  if (!c) return nullptr;
+  if (double* d = dptr1(c, f)) return d;
+  if (double2* d2 = dptr2(c, f)) return d2;
+  if (f == LV_FIELD_PHASE) return c->s.phase;
+  return nullptr;
+}
+
+int lv_remesh_async(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 0);
+  return lv_mesh_remesh(c);
+}
+
+int lv_remesh(lv_ctx* c) {
+  int rc = lv_remesh_async(c);
+  if (rc) return rc;
+  return sync_status(c);
+}
+
+int lv_get_geometry(lv_ctx* c, int32_t* nedges, double* verts, int32_t* labels) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
+  const int n = c->n, cap = c->cap;
+  std::vector<int> ne(n);
+  cudaStream_t s = c->stream;
+  cudaMemcpyAsync(ne.data(), c->m.nedges, 4 * n, cudaMemcpyDeviceToHost, s);
+  std::vector<double2> v1, v2;
+  std::vector<int> lab;
+  if (verts) {
+    v1.resize((size_t)LV_MAX_EDGES * cap);
+    v2.resize((size_t)LV_MAX_EDGES * cap);
+    cudaMemcpyAsync(v1.data(), c->m.ev1, 16 * v1.size(), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(v2.data(), c->m.ev2, 16 * v2.size(), cudaMemcpyDeviceToHost, s);
+  }
+  if (labels) {
+    lab.resize((size_t)LV_MAX_EDGES * cap);
+    cudaMemcpyAsync(lab.data(), c->m.elab, 4 * lab.size(), cudaMemcpyDeviceToHost, s);
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_get_geometry");
+  for (int i = 0; i < n; ++i) {
+    if (nedges) nedges[i] = ne[i];
+    for (int k = 0; k < ne[i] && k < LV_MAX_EDGES; ++k) {
+      const size_t src = (size_t)k * cap + i, dst = (size_t)i * LV_MAX_EDGES + k;
+      if (verts) {
+        verts[4 * dst] = v1[src].x;
+        verts[4 * dst + 1] = v1[src].y;
+        verts[4 * dst + 2] = v2[src].x;
+        verts[4 * dst + 3] = v2[src].y;
+      }
+      if (labels) labels[dst] = lab[src];
+    }
+  }
+  return LV_OK;
+}
+
+int lv_get_faces(lv_ctx* c, int64_t* nfaces, int64_t* rowptr, int32_t* nbr, double* lrr, double* mid, double* y,
+                 double* len) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
+  const int n = c->n, cap = c->cap;
+  cudaStream_t s = c->stream;
+  std::vector<int> nf(n);
+  cudaMemcpyAsync(nf.data(), c->m.nfaces, 4 * n, cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_get_faces");
+  int64_t tot = 0;
+  for (int i = 0; i < n; ++i) tot += nf[i];
+  if (nfaces) *nfaces = tot;
+  if (!rowptr && !nbr) return LV_OK;
+  const size_t ell = (size_t)LV_MAX_EDGES * cap;
+  std::vector<int> fn(ell);
+  std::vector<double> fl(ell), fle(ell);
+  std::vector<double2> fm(ell), fy(ell);
+  cudaMemcpyAsync(fn.data(), c->m.fnbr, 4 * ell, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(fl.data(), c->m.flrr, 8 * ell, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(fle.data(), c->m.flen, 8 * ell, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(fm.data(), c->m.fm, 16 * ell, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(fy.data(), c->m.fy, 16 * ell, cudaMemcpyDeviceToHost, s);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_get_faces");
+  int64_t k = 0;
+  for (int i = 0; i < n; ++i) {
+    if (rowptr) rowptr[i] = k;
+    for (int t = 0; t < nf[i]; ++t, ++k) {
+      const size_t src = (size_t)t * cap + i;
+      if (nbr) nbr[k] = fn[src];
+      if (lrr) lrr[k] = fl[src];
+      if (len) len[k] = fle[src];
+      if (mid) {
+        mid[2 * k] = fm[src].x;
+        mid[2 * k + 1] = fm[src].y;
+      }
+      if (y) {
+        y[2 * k] = fy[src].x;
+        y[2 * k + 1] = fy[src].y;
+      }
+    }
+  }
+  if (rowptr) rowptr[n] = k;
+  return LV_OK;
+}
+
+int lv_get_cell_list(lv_ctx* c, int64_t* ncells, int64_t* nitems, int32_t* starts, int32_t* items) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  const int nc = c->c.ncells;
+  if (ncells) *ncells = nc;
+  int tot = 0;
+  cudaMemcpyAsync(&tot, c->c.cstart + nc, 4, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_get_cell_list");
+  if (nitems) *nitems = tot;
+  if (starts) cudaMemcpyAsync(starts, c->c.cstart, 4 * ((size_t)nc + 1), cudaMemcpyDeviceToHost, c->stream);
+  if (items) cudaMemcpyAsync(items, c->c.citem, 4 * (size_t)std::min(tot, c->c.item_cap), cudaMemcpyDeviceToHost, c->stream);
+  e = cudaStreamSynchronize(c->stream);
+  return lv_cuda_check(c, e, "lv_get_cell_list");
+}
+
+// ------------------------------------------------------------ physics
+
+int lv_move(lv_ctx* c, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 0);
+  return lv_phys_move(c, dt);
+}
+int lv_ideal_eos(lv_ctx* c, double gamma, double Pmin) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_eos(c, 0, gamma, Pmin);
+}
+int lv_stiffened_eos(lv_ctx* c, double gamma, double P0) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_eos(c, 1, gamma, P0);
+}
+int lv_find_rho(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_eos(c, 2, 0.0, 0.0);
+}
+int lv_gravity_step(lv_ctx* c, double gx, double gy, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_gravity(c, gx, gy, dt);
+}
+int lv_pressure_step(lv_ctx* c, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_pressure_step(c, dt);
+}
+int lv_find_D(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_find_D(c);
+}
+int lv_viscous_step(lv_ctx* c, double dt, int32_t av) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_viscous(c, dt, av);
+}
+int lv_bdary_friction(lv_ctx* c, const double* vwall, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_friction(c, vwall, dt);
+}
+int lv_find_dv(lv_ctx* c, double dt, double alpha) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_find_dv(c, dt, alpha);
+}
+int lv_relaxation_step(lv_ctx* c, double dt, int32_t rusanov) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 0);
+  return lv_phys_relax(c, dt, rusanov);
+}
+
+// ------------------------------------------------------------ pressure
+
+int lv_set_solver(lv_ctx* c, int32_t method, double tol, int32_t itmax) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (method < LV_METHOD_JACOBI_PCG || method > LV_METHOD_LEARNED_PCG || !(tol > 0) || itmax <= 0)
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "lv_set_solver: bad method, tol or itmax");
+  c->method = method;
+  c->tol = tol;
+  c->itmax = itmax;
+  return LV_OK;
+}
+
+int lv_pressure_operator(lv_ctx* c, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 2);
+  return lv_solver_assemble(c, dt);
+}
+
+int lv_pressure_rhs(lv_ctx* c, double dt, int32_t gp_step, const double* vbc) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 2);
+  return lv_phys_rhs(c, dt, gp_step, vbc);
+}
+
+int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
+  if (!c || niter < 0 || niter > 63) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 63]");
+  Timer t(c, 2);
+  int rc = lv_solver_assemble(c, dt);
+  if (rc) return rc;
+  for (int it = 1; it <= niter; ++it) {
+    rc = lv_phys_rhs(c, dt, it > 1, vbc);
+    if (rc) return rc;
+    rc = lv_solver_solve(c, c->s.P, nullptr, it - 1);
+    if (rc) return rc;
+  }
+  if (stats) {
+    rc = lv_solver_fetch_stats(c, stats, niter);
+    if (rc) return rc;
+    return sync_status(c);
+  }
+  return LV_OK;
+}
+
+int lv_export_system(lv_ctx* c, int64_t* nnz, double* diag, int64_t* rowptr, int32_t* col, double* w, double* b) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  const int n = c->n;
+  std::vector<int> rp(n + 1);
+  cudaMemcpyAsync(rp.data(), c->sv.rowptr, 4 * ((size_t)n + 1), cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_export_system");
+  if (nnz) *nnz = rp[n];
+  if (rowptr)
+    for (int i = 0; i <= n; ++i) rowptr[i] = rp[i];
+  if (diag) cudaMemcpyAsync(diag, c->sv.diag, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  if (col) cudaMemcpyAsync(col, c->sv.col, 4 * (size_t)rp[n], cudaMemcpyDeviceToHost, c->stream);
+  if (w) cudaMemcpyAsync(w, c->sv.w, 8 * (size_t)rp[n], cudaMemcpyDeviceToHost, c->stream);
+  if (b) cudaMemcpyAsync(b, c->sv.b, 8 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  e = cudaStreamSynchronize(c->stream);
+  return lv_cuda_check(c, e, "lv_export_system");
+}
+
+int lv_solve(lv_ctx* c, const double* b, double* x, lv_solve_stats* stats) {
+  if (!c || !b || !x) return LV_ERR_BAD_ARGUMENT;
+  const size_t n = c->n;
+  double* xd = c->sv.xs;
+  cudaMemcpyAsync(c->sv.b, b, 8 * n, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(xd, x, 8 * n, cudaMemcpyHostToDevice, c->stream);
+  int rc = lv_solver_solve(c, xd, nullptr, 0);
+  if (rc) return rc;
+  cudaMemcpyAsync(x, xd, 8 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (stats) {
+    rc = lv_solver_fetch_stats(c, stats, 1);
+    if (rc) return rc;
+  }
+  return sync_status(c);
+}
+
+int lv_operator_apply(lv_ctx* c, const double* x, double* y) {
+  if (!c || !x || !y) return LV_ERR_BAD_ARGUMENT;
+  const size_t n = c->n;
+  double* xd = c->sv.xs;
+  double* yd = c->sv.q;
+  cudaMemcpyAsync(xd, x, 8 * n, cudaMemcpyHostToDevice, c->stream);
+  int rc = lv_solver_apply(c, xd, yd);
+  if (rc) return rc;
+  cudaMemcpyAsync(y, yd, 8 * n, cudaMemcpyDeviceToHost, c->stream);
+  return sync_status(c);
+}
+
+int lv_multiphase_projection(lv_ctx* c, double quality_threshold, lv_solve_stats* stats) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 3);
+  return lv_phys_multiphase(c, quality_threshold, stats);
+}
+
+int lv_get_timings(lv_ctx* c, double* out, int32_t cap) {
+  if (!c || !out) return 0;
+  int k = 0;
+  for (; k < cap && k < 4; ++k) out[k] = c->t_ms[k];
+  return k;
+}
+
+int lv_reset_timings(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  for (double& t : c->t_ms) t = 0;
+  return LV_OK;
+}
+
+int64_t lv_launch_count(const lv_ctx* c) { return c ? c->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+// Internal declarations shared by the CUDA translation units of liblvgpu.
+//
+// Device data layout (all FP64 unless noted, one entry per particle):
+//   state   x, v, dv, momentum, Da (D11,D21), Db (D12,D22), GP : double2[cap]
+//           e, P, rho, c2, mass, energy, quality, mu             : double[cap]
+//           phase                                                : int32[cap]
+//   mesh    per-polygon edge list and interior-face list in slot-major
+//           ("ELL") layout: slot k of particle i lives at [k*cap + i], so a
+//           warp reading slot k of 32 consecutive particles is coalesced.
+//   cells   cell list as CSR over the n1*n2 cells: cstart[ncells+1],
+//           citem[] (particle index), cpos32[] (float2 copy of its position).
+//   solver  CSR of the pressure operator: rowptr[n+1], col[nnz], w[nnz]
+//           (off-diagonal weights), adiag = diag + sum_j w_ij, dinv = 1/adiag.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lvgpu.h"
+
+#define LV_SIGNUM_EPS (2.0 * 2.220446049250313e-16) /* polygon.jl:2 */
+
+// Status bits set on the device with atomicOr; decoded on the host.
+#define LV_FLAG_NAN_VELOCITY 0x1
+#define LV_FLAG_MESH_DESTROYED 0x2
+#define LV_FLAG_EDGE_OVERFLOW 0x4
+#define LV_FLAG_CELL_OVERFLOW 0x8
+#define LV_FLAG_NONFINITE 0x10
+#define LV_FLAG_BARRIER_TIMEOUT 0x20
+
+// Domain and cell-list constants passed to kernels by value.
+struct GridDev {
+  double bminx, bminy, bmaxx, bmaxy;  // boundary rectangle
+  double cminx, cminy, cmaxx, cmaxy;  // cropping rectangle
+  double ox, oy;                      // cell-list origin = cropping.xmin - (h, h)
+  double h, rr_max, xperiod, yperiod, dr;
+  int xper, yper;
+  int n1, n2;
+  int npath;
+  float delta32;  // bound on |float(a) - float(b) - (a - b)| for positions inside the cropping box
+  float bigm;     // max |coordinate| inside the cropping box
+};
+
+// One node of the candidate path (neighborlist.jl:29-41): cell offset and
+// squared distance lower bound.
+struct PathNodeDev {
+  int di1, di2;
+  double rr;
+};
+
+struct StateDev {
+  double2 *x, *v, *dv, *mom, *Da, *Db, *GP;
+  double *e, *P, *rho, *c2, *mass, *energy, *quality, *mu;
+  int* phase;
+};
+
+struct MeshDev {
+  int cap;  // slot stride
+  int* nedges;
+  int* nfaces;
+  double2 *ev1, *ev2;
+  int* elab;
+  int* fnbr;
+  double *flrr, *flen;
+  double2 *fm, *fy;
+  double* area;
+  double2* centroid;
+};
+
+struct CellsDev {
+  int ncells;
+  int* cstart;   // [ncells + 1]
+  int* ccount;   // [ncells] counts, then cursors
+  int* citem;    // [item_cap]
+  float2* cpos;  // [item_cap]
+  int item_cap;
+};
+
+struct SolverDev {
+  int* rowptr;  // [cap + 1]
+  int* col;     // [nnz_cap]
+  double* w;    // [nnz_cap]
+  float* w32;   // FP32 copy for the mixed-precision inner solve
+  double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
+  float *dinv32, *r32, *z32, *p32, *q32, *d32;
+  double* part;       // reduction partials [4][maxblocks]
+  unsigned* bar;      // grid barrier {count, generation}
+  int* iters;         // device-side stats
+  double* dstats;     // device-side stats
+  int64_t nnz_cap;
+};
+
+struct lv_ctx {
+  lv_params prm;
+  GridDev g;
+  std::vector<PathNodeDev> path_host;
+  PathNodeDev* path = nullptr;
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int n = 0;
+  int cap = 0;
+  bool meshed = false;
+  StateDev s{};
+  MeshDev m{};
+  CellsDev c{};
+  SolverDev sv{};
+  int* status = nullptr;      // device status word
+  int* status_host = nullptr; // pinned
+  int method = LV_METHOD_JACOBI_PCG;
+  double tol = 1e-8;
+  int itmax = 10000;
+  bool op_ready = false;
+  std::string err;
+  int64_t launches = 0;
+  // timings
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double t_ms[4] = {0, 0, 0, 0};
+  bool timing = false;
+  std::vector<void*> allocs;
+};
+
+// ---- host helpers (lv_api.cu)
+int lv_fail(lv_ctx* c, int code, const std::string& msg);
+int lv_cuda_check(lv_ctx* c, cudaError_t e, const char* what);
+
+// ---- mesh (lv_mesh.cu)
+int lv_mesh_remesh(lv_ctx* c);
+int lv_scan_int(lv_ctx* c, const int* in, int* out, int len);  // exclusive, out[len] = total
+
+// ---- physics (lv_physics.cu)
+int lv_phys_move(lv_ctx* c, double dt);
+int lv_phys_eos(lv_ctx* c, int kind, double gamma, double p);
+int lv_phys_gravity(lv_ctx* c, double gx, double gy, double dt);
+int lv_phys_pressure_step(lv_ctx* c, double dt);
+int lv_phys_find_D(lv_ctx* c);
+int lv_phys_viscous(lv_ctx* c, double dt, int av);
+int lv_phys_friction(lv_ctx* c, const double* vwall, double dt);
+int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
+int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc);
+int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
+
+// ---- solver (lv_solver.cu)
+int lv_solver_assemble(lv_ctx* c, double dt);
+int lv_solver_solve(lv_ctx* c, double* dst_P, lv_solve_stats* st_dev_or_null, int stats_slot);
+int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev);
+int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
+
+#define LV_LAUNCH_CHECK(c, what)                                   \
+  do {                                                             \
+    (c)->launches++;                                               \
+    cudaError_t _e = cudaGetLastError();                           \
+    if (_e != cudaSuccess) return lv_cuda_check((c), _e, (what));  \
+  } while (0)
+
+static inline int lv_blocks(int n, int tpb) { return (n + tpb - 1) / tpb; }

@@ -1,0 +1,655 @@
+// Per-particle physics operators of the time step, one thread per polygon.
+//
+// Every operator walks the polygon's interior faces in the order of
+// `neighbors(p, grid)` (src/iterators.jl:23-33) from the slot-major face
+// arrays written by the clipping kernel (neighbour index, lr_ratio, midpoint,
+// neighbour position y, edge length), so no geometry is recomputed here.
+// Two-pass operators of the reference (a read phase and a write phase over
+// all polygons) are two kernel launches.
+//
+// Compiled with --fmad=false: expressions keep the reference's evaluation
+// order and rounding, so results are bit-identical to a sequential FP64
+// evaluation of the same formulas in the same face order.
+#include <math.h>
+
+#include "lv_internal.cuh"
+
+namespace {
+
+constexpr int TPB = 256;
+
+__device__ __forceinline__ double jmax(double a, double b) { return (b > a) ? b : a; }
+__device__ __forceinline__ double jmin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dot2(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+
+// ------------------------------------------------------------------- EOS
+
+// ideal_eos! (pressure.jl:49-55), stiffened_eos! (pressure.jl:64-70),
+// find_rho! (pressure.jl:36-40).  kind 0: ideal (p = Pmin), 1: stiffened
+// (p = P0), 2: density only.
+__global__ void k_eos(StateDev s, MeshDev m, int n, int kind, double gamma, double pp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double rho = s.mass[i] / m.area[i];
+  s.rho[i] = rho;
+  if (kind == 2) return;
+  double2 v = s.v[i];
+  double eint = s.e[i] - 0.5 * (v.x * v.x + v.y * v.y);
+  double P = (gamma - 1.0) * rho * eint;
+  s.P[i] = P;
+  if (kind == 0)
+    s.c2[i] = gamma * jmax(P, pp) / rho;
+  else
+    s.c2[i] = gamma * (P + pp) / rho;
+}
+
+// gravity_step! (pressure.jl:77-82)
+__global__ void k_gravity(StateDev s, int n, double gx, double gy, double dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 v = s.v[i];
+  s.v[i] = make_double2(v.x + dt * gx, v.y + dt * gy);
+}
+
+// ------------------------------------------------------------ pressure step
+
+// pressure_step! (pressure.jl:10-25), velocity pass.
+__global__ void k_pstep_v(StateDev s, MeshDev m, int n, double dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double Pi = s.P[i], mi = s.mass[i];
+  double2 vi = s.v[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f];
+    const double c = dt / mi * lrr * (Pi - s.P[j]);
+    vi.x = vi.x + c * (mm.x - xi.x);
+    vi.y = vi.y + c * (mm.y - xi.y);
+  }
+  s.v[i] = vi;
+}
+
+// pressure_step! energy pass (uses the updated velocities).
+__global__ void k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double Pi = s.P[i], mi = s.mass[i];
+  const double2 vi = s.v[i];
+  const double2 Pv = make_double2(Pi * vi.x, Pi * vi.y);
+  double ei = s.e[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double Pj = s.P[j];
+    const double2 vj = s.v[j];
+    const double2 Pvj = make_double2(Pj * vj.x, Pj * vj.y);
+    const double a = (mm.x - xi.x) * Pv.x + (mm.y - xi.y) * Pv.y;
+    const double b = (mm.x - y.x) * Pvj.x + (mm.y - y.y) * Pvj.y;
+    ei -= dt * lrr / mi * (a - b);
+  }
+  s.e[i] = ei;
+}
+
+// ------------------------------------------------------------- RHS refresh
+
+// refresh!(solver, dt, gp_step, vbc) first loop (pressure.jl:167-187):
+// b, the warm start P and the pressure gradient GP.
+__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
+  const double2 xi = s.x[i];
+  const double Pi = s.P[i];
+  const double2 vi = s.v[i];
+  double bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
+  double gpx = 0.0, gpy = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 vj = s.v[j];
+    bi -= (lrr / dt) * ((vi.x - vj.x) * (mm.x - y.x) + (vi.y - vj.y) * (mm.y - y.y));
+    const double c = lrr * (Pi - s.P[j]);
+    gpx = gpx - c * (mm.x - xi.x);
+    gpy = gpy - c * (mm.y - xi.y);
+  }
+  if (nf < ne) {
+    for (int k = 0; k < ne; ++k) {
+      const size_t f = (size_t)k * cap + i;
+      const int lab = m.elab[f];
+      if (lab >= 0) continue;
+      const double2 a = m.ev1[f], b = m.ev2[f];
+      const double dSx = a.y - b.y, dSy = b.x - a.x;
+      double wx, wy;
+      switch (lab) {
+        case LV_BDARY_UP: wx = vbc_ud.x; wy = vbc_ud.y; break;
+        case LV_BDARY_RIGHT: wx = vbc_rl.x; wy = vbc_rl.y; break;
+        case LV_BDARY_DOWN: wx = vbc_ud.z; wy = vbc_ud.w; break;
+        default: wx = vbc_rl.z; wy = vbc_rl.w; break;
+      }
+      bi -= (dSx * (wx - vi.x) + dSy * (wy - vi.y)) / dt;
+    }
+  }
+  sv.b[i] = bi;
+  sv.xs[i] = Pi;
+  const double mi = s.mass[i];
+  s.GP[i] = make_double2(gpx / mi, gpy / mi);
+}
+
+// refresh! second loop (pressure.jl:189-201): explicit part of the Laplacian.
+__global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double2 gi = s.GP[i];
+  double bi = sv.b[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 gj = s.GP[j];
+    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+    bi += lrr * ((gi.x - gj.x) * (mm.x - zx) + (gi.y - gj.y) * (mm.y - zy));
+  }
+  sv.b[i] = bi;
+}
+
+// ---------------------------------------------------------- viscosity, D
+
+// find_D! (diffusion.jl:8-19)
+__global__ void k_find_D(StateDev s, MeshDev m, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 vi = s.v[i];
+  double d11 = 0.0, d21 = 0.0, d12 = 0.0, d22 = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 vj = s.v[j];
+    const double ax = vi.x - vj.x, ay = vi.y - vj.y, bx = mm.x - y.x, by = mm.y - y.y;
+    d11 += lrr * (ax * bx);
+    d21 += lrr * (ay * bx);
+    d12 += lrr * (ax * by);
+    d22 += lrr * (ay * by);
+  }
+  const double A = m.area[i];
+  d11 = d11 / A;
+  d21 = d21 / A;
+  d12 = d12 / A;
+  d22 = d22 / A;
+  s.Da[i] = make_double2(0.5 * (d11 + d11), 0.5 * (d21 + d12));
+  s.Db[i] = make_double2(0.5 * (d12 + d21), 0.5 * (d22 + d22));
+}
+
+// getS (diffusion.jl:22-29): viscous stress, stored in GP-sized scratch as
+// two double2 per particle (S11,S21) and (S12,S22).
+__global__ void k_stress(StateDev s, int n, double avdr, double2* Sa, double2* Sb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 a = s.Da[i], b = s.Db[i];
+  const double divv = a.x + b.y;
+  double mu = s.mu[i];
+  if (divv < 0.0) mu -= divv * s.rho[i] * (avdr * avdr);
+  const double c = 2.0 * mu;
+  Sa[i] = make_double2(c * (a.x - divv / 3.0), c * a.y);
+  Sb[i] = make_double2(c * b.x, c * (b.y - divv / 3.0));
+}
+
+// viscous_step! velocity pass (diffusion.jl:41-46)
+__global__ void k_visc_v(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
+                         const double2* __restrict__ Sb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double mi = s.mass[i];
+  const double2 sa = Sa[i], sb = Sb[i];
+  double2 vi = s.v[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f];
+    const double2 qa = Sa[j], qb = Sb[j];
+    const double c = dt * lrr / mi;
+    const double M11 = c * (sa.x - qa.x), M21 = c * (sa.y - qa.y), M12 = c * (sb.x - qb.x), M22 = c * (sb.y - qb.y);
+    const double dx = mm.x - xi.x, dy = mm.y - xi.y;
+    vi.x = vi.x - (M11 * dx + M12 * dy);
+    vi.y = vi.y - (M21 * dx + M22 * dy);
+  }
+  s.v[i] = vi;
+}
+
+// viscous_step! energy pass (diffusion.jl:47-52)
+__global__ void k_visc_e(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
+                         const double2* __restrict__ Sb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double mi = s.mass[i];
+  const double2 sa = Sa[i], sb = Sb[i];
+  const double2 vi = s.v[i];
+  const double Svx = sa.x * vi.x + sb.x * vi.y, Svy = sa.y * vi.x + sb.y * vi.y;
+  double ei = s.e[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 qa = Sa[j], qb = Sb[j];
+    const double2 vj = s.v[j];
+    const double Sqx = qa.x * vj.x + qb.x * vj.y, Sqy = qa.y * vj.x + qb.y * vj.y;
+    const double a = (mm.x - xi.x) * Svx + (mm.y - xi.y) * Svy;
+    const double b = (mm.x - y.x) * Sqx + (mm.y - y.y) * Sqy;
+    ei += dt * lrr / mi * (a - b);
+  }
+  s.e[i] = ei;
+}
+
+// bdary_friction! (diffusion.jl:64-79) with a constant wall velocity per label.
+__global__ void k_friction(StateDev s, MeshDev m, int n, double dt, double4 w_ud, double4 w_rl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
+  if (nf == ne) {
+    // no boundary edge: v = v/1.0 leaves v unchanged
+    return;
+  }
+  const double2 xi = s.x[i];
+  const double mu = s.mu[i], mi = s.mass[i];
+  double tmp = 1.0;
+  double2 vi = s.v[i];
+  double ei = s.e[i];
+  for (int k = 0; k < ne; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int lab = m.elab[f];
+    if (lab >= 0) continue;
+    const double2 a = m.ev1[f], b = m.ev2[f];
+    const double mx = 0.5 * (a.x + b.x), my = 0.5 * (a.y + b.y);
+    const double nx0 = a.y - b.y, ny0 = b.x - a.x;
+    const double nn = sqrt(nx0 * nx0 + ny0 * ny0);
+    const double nx = nx0 / nn, ny = ny0 / nn;
+    const double lx = a.x - b.x, ly = a.y - b.y;
+    const double len = sqrt(lx * lx + ly * ly);
+    const double lrr = len / fabs((mx - xi.x) * nx + (my - xi.y) * ny);
+    double wx, wy;
+    switch (lab) {
+      case LV_BDARY_UP: wx = w_ud.x; wy = w_ud.y; break;
+      case LV_BDARY_RIGHT: wx = w_rl.x; wy = w_rl.y; break;
+      case LV_BDARY_DOWN: wx = w_ud.z; wy = w_ud.w; break;
+      default: wx = w_rl.z; wy = w_rl.w; break;
+    }
+    const double fx = mu * lrr * wx / mi, fy = mu * lrr * wy / mi;
+    tmp += dt * mu * lrr / mi;
+    ei += dt * (fx * vi.x + fy * vi.y);
+    vi.x = vi.x + dt * fx;
+    vi.y = vi.y + dt * fy;
+  }
+  s.v[i] = make_double2(vi.x / tmp, vi.y / tmp);
+  s.e[i] = ei;
+}
+
+// ---------------------------------------------------------- relaxation
+
+// find_dv! (relaxation.jl:10-25)
+__global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double2 c = m.centroid[i];
+  double rmax = 0.0, rmin = __longlong_as_double(0x7ff0000000000000LL);
+  for (int k = 0; k < nf; ++k) {
+    const double2 y = m.fy[(size_t)k * cap + i];
+    const double dx = xi.x - y.x, dy = xi.y - y.y;
+    const double r = sqrt(dx * dx + dy * dy);
+    rmax = jmax(rmax, r);
+    rmin = jmin(rmin, r);
+  }
+  const double q = rmin / rmax;
+  s.quality[i] = q;
+  const double2 a = s.Da[i], b = s.Db[i];
+  const double nD = sqrt(a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y);
+  const double lambda = alpha * nD / (q * q);
+  const double f = lambda / (1.0 + dt * lambda);
+  s.dv[i] = make_double2(f * (c.x - xi.x), f * (c.y - xi.y));
+}
+
+// relaxation_step! first loop (relaxation.jl:37-66): conservative remap of
+// mass, momentum and energy along dv with the Rusanov flux.
+__global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const double rp = s.rho[i], ep = s.e[i];
+  const double2 vp = s.v[i], dvp = s.dv[i];
+  const int php = s.phase[i];
+  double mass = s.mass[i];
+  double momx = mass * vp.x, momy = mass * vp.y;
+  double energy = mass * ep;
+  const double ndvp = sqrt(dvp.x * dvp.x + dvp.y * dvp.y);
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    if (s.phase[j] != php) continue;
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+    const double rq = s.rho[j], eq = s.e[j];
+    const double2 vq = s.v[j], dvq = s.dv[j];
+    const double pqx = xi.x - y.x, pqy = xi.y - y.y;
+    const double mzx = mm.x - zx, mzy = mm.y - zy;
+    const double pdvpq = dvp.x * pqx + dvp.y * pqy;
+    const double qdvpq = dvq.x * pqx + dvq.y * pqy;
+    const double pdvmz = dvp.x * mzx + dvp.y * mzy;
+    const double qdvmz = dvq.x * mzx + dvq.y * mzy;
+    const double kk = dt * lrr;
+    mass += kk * ((pdvmz * rp - qdvmz * rq) - 0.5 * (pdvpq * rp + qdvpq * rq));
+    const double a1 = pdvmz * rp, a2 = qdvmz * rq, b1 = pdvpq * rp, b2 = qdvpq * rq;
+    const double t1x = a1 * vp.x - a2 * vq.x, t1y = a1 * vp.y - a2 * vq.y;
+    const double t2x = b1 * vp.x + b2 * vq.x, t2y = b1 * vp.y + b2 * vq.y;
+    momx = momx + kk * (t1x - 0.5 * t2x);
+    momy = momy + kk * (t1y - 0.5 * t2y);
+    energy += kk * ((pdvmz * rp * ep - qdvmz * rq * eq) - 0.5 * (pdvpq * rp * ep + qdvpq * rq * eq));
+    if (rusanov) {
+      const double ndvq = sqrt(dvq.x * dvq.x + dvq.y * dvq.y);
+      const double a = jmax(ndvp, ndvq);
+      const double l = m.flen[f];
+      const double cr = 0.5 * dt * l * a;
+      mass += cr * (rq - rp);
+      momx = momx + cr * (rq * vq.x - rp * vp.x);
+      momy = momy + cr * (rq * vq.y - rp * vp.y);
+      energy += cr * (rq * eq - rp * ep);
+    }
+  }
+  s.mass[i] = mass;
+  s.mom[i] = make_double2(momx, momy);
+  s.energy[i] = energy;
+}
+
+// relaxation_step! second loop (relaxation.jl:67-71)
+__global__ void k_relax_update(StateDev s, int n, double dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double mass = s.mass[i];
+  const double2 mom = s.mom[i];
+  s.v[i] = make_double2(mom.x / mass, mom.y / mass);
+  s.e[i] = s.energy[i] / mass;
+  const double2 x = s.x[i], dv = s.dv[i];
+  s.x[i] = make_double2(x.x + dt * dv.x, x.y + dt * dv.y);
+}
+
+// ----------------------------------------------------------------- move
+
+// least_positive_residue / periodic_wrap (voronoigrid.jl:181-192)
+__device__ __forceinline__ double lpr(double x, double d) { return fmod(fmod(x, d) + d, d); }
+
+__device__ __forceinline__ bool try_move(const GridDev& g, double2& x, double2 v, double dt) {
+  double nx = x.x + dt * v.x, ny = x.y + dt * v.y;
+  const double wx = lpr(nx - g.bminx, g.xperiod) + g.bminx;
+  const double wy = lpr(ny - g.bminy, g.yperiod) + g.bminy;
+  if (g.xper) nx = nx + (wx - nx);
+  if (g.yper) ny = ny + (wy - ny);
+  if (g.bminx <= nx && nx <= g.bmaxx && g.bminy <= ny && ny <= g.bmaxy) {
+    x = make_double2(nx, ny);
+    return true;
+  }
+  return false;
+}
+
+// move! (move.jl:9-21) and try_move! (move.jl:23-33), without the remesh.
+__global__ void k_move(GridDev g, StateDev s, MeshDev m, int n, double dt, int* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 x = s.x[i];
+  double2 v = s.v[i];
+  if (isnan(v.x) || isnan(v.y)) {
+    atomicOr(status, LV_FLAG_NAN_VELOCITY);
+    return;
+  }
+  if (try_move(g, x, v, dt)) {
+    s.x[i] = x;
+    return;
+  }
+  const int cap = m.cap, ne = m.nedges[i];
+  for (int k = 0; k < ne; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    if (m.elab[f] >= 0) continue;
+    const double2 a = m.ev1[f], b = m.ev2[f];
+    const double nx0 = a.y - b.y, ny0 = b.x - a.x;
+    const double nn = sqrt(nx0 * nx0 + ny0 * ny0);
+    const double nx = nx0 / nn, ny = ny0 / nn;
+    const double d = v.x * nx + v.y * ny;
+    v.x = v.x - d * nx;
+    v.y = v.y - d * ny;
+  }
+  if (isnan(v.x) || isnan(v.y)) {
+    atomicOr(status, LV_FLAG_NAN_VELOCITY);
+    return;
+  }
+  if (!try_move(g, x, v, dt)) {
+    v = make_double2(0.0, 0.0);
+    try_move(g, x, v, dt);
+  }
+  s.x[i] = x;
+  s.v[i] = v;
+}
+
+// ----------------------------------------------------- multiphase projector
+
+// relaxation.jl:157-169: b_i = -sum_{cross-phase faces} lrr (dot(dv_i - dv_j, m - z)
+//                                   - 0.5 dot(dv_i + dv_j, x_i - y))
+__global__ void k_mp_rhs(StateDev s, MeshDev m, int n, double* b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i], dvi = s.dv[i];
+  const int ph = s.phase[i];
+  double bi = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    if (s.phase[j] == ph) continue;
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 dvj = s.dv[j];
+    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+    const double a = (dvi.x - dvj.x) * (mm.x - zx) + (dvi.y - dvj.y) * (mm.y - zy);
+    const double c = (dvi.x + dvj.x) * (xi.x - y.x) + (dvi.y + dvj.y) * (xi.y - y.y);
+    bi -= lrr * (a - 0.5 * c);
+  }
+  b[i] = bi;
+}
+
+// relaxation.jl:92-106: tmp_i = -(1/area) sum lrr (x_i - x_j)(m - x_i)
+__global__ void k_mp_apply1(StateDev s, MeshDev m, int n, const double* __restrict__ xin, double2* tmp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const int ph = s.phase[i];
+  double tx = 0.0, ty = 0.0;
+  const double xv = xin[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    if (s.phase[j] == ph) continue;
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f];
+    const double c = lrr * (xv - xin[j]);
+    tx = tx - c * (mm.x - xi.x);
+    ty = ty - c * (mm.y - xi.y);
+  }
+  const double A = m.area[i];
+  tmp[i] = make_double2(tx / A, ty / A);
+}
+
+// relaxation.jl:107-121
+__global__ void k_mp_apply2(StateDev s, MeshDev m, int n, const double2* __restrict__ tmp, double* res) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const int ph = s.phase[i];
+  const double2 ti = tmp[i];
+  double r = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    if (s.phase[j] == ph) continue;
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 tj = tmp[j];
+    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+    const double a = (ti.x - tj.x) * (mm.x - zx) + (ti.y - tj.y) * (mm.y - zy);
+    const double c = (ti.x + tj.x) * (xi.x - y.x) + (ti.y + tj.y) * (xi.y - y.y);
+    r -= lrr * (a - 0.5 * c);
+  }
+  res[i] = r;
+}
+
+// relaxation.jl:190-204: dv += lrr (q_i - q_j)(m - x_i)/area on cross-phase faces
+__global__ void k_mp_correct(StateDev s, MeshDev m, int n, const double* __restrict__ q, double threshold) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (s.quality[i] < threshold) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double2 xi = s.x[i];
+  const int ph = s.phase[i];
+  const double A = m.area[i];
+  double2 d = s.dv[i];
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    if (s.phase[j] == ph) continue;
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f];
+    const double c = lrr * (q[i] - q[j]);
+    d.x = d.x + (c * (mm.x - xi.x)) / A;
+    d.y = d.y + (c * (mm.y - xi.y)) / A;
+  }
+  s.dv[i] = d;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- host
+
+#define LAUNCH(kernel, ...)                                                     \
+  do {                                                                          \
+    kernel<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(__VA_ARGS__);           \
+    LV_LAUNCH_CHECK(c, #kernel);                                                \
+  } while (0)
+
+static int need_mesh(lv_ctx* c) {
+  if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed (call lv_remesh first)");
+  return LV_OK;
+}
+
+int lv_phys_eos(lv_ctx* c, int kind, double gamma, double p) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_eos, c->s, c->m, c->n, kind, gamma, p);
+  return LV_OK;
+}
+
+int lv_phys_gravity(lv_ctx* c, double gx, double gy, double dt) {
+  LAUNCH(k_gravity, c->s, c->n, gx, gy, dt);
+  return LV_OK;
+}
+
+int lv_phys_pressure_step(lv_ctx* c, double dt) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_pstep_v, c->s, c->m, c->n, dt);
+  LAUNCH(k_pstep_e, c->s, c->m, c->n, dt);
+  return LV_OK;
+}
+
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc) {
+  if (int rc = need_mesh(c)) return rc;
+  double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (vbc)
+    for (int k = 0; k < 8; ++k) w[k] = vbc[k];
+  // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
+  double4 ud = make_double4(w[0], w[1], w[4], w[5]);
+  double4 rl = make_double4(w[2], w[3], w[6], w[7]);
+  LAUNCH(k_rhs, c->s, c->m, c->sv, c->n, dt, ud, rl);
+  if (gp_step) LAUNCH(k_rhs_gp, c->s, c->m, c->sv, c->n);
+  return LV_OK;
+}
+
+int lv_phys_find_D(lv_ctx* c) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_find_D, c->s, c->m, c->n);
+  return LV_OK;
+}
+
+int lv_phys_viscous(lv_ctx* c, double dt, int av) {
+  if (int rc = need_mesh(c)) return rc;
+  double2* Sa = reinterpret_cast<double2*>(c->sv.r);  // 2 x n doubles of scratch each
+  double2* Sb = reinterpret_cast<double2*>(c->sv.p);
+  const double avdr = av ? c->g.dr : 0.0;
+  LAUNCH(k_stress, c->s, c->n, avdr, Sa, Sb);
+  LAUNCH(k_visc_v, c->s, c->m, c->n, dt, Sa, Sb);
+  LAUNCH(k_visc_e, c->s, c->m, c->n, dt, Sa, Sb);
+  return LV_OK;
+}
+
+int lv_phys_friction(lv_ctx* c, const double* vwall, double dt) {
+  if (int rc = need_mesh(c)) return rc;
+  double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (vwall)
+    for (int k = 0; k < 8; ++k) w[k] = vwall[k];
+  double4 ud = make_double4(w[0], w[1], w[4], w[5]);
+  double4 rl = make_double4(w[2], w[3], w[6], w[7]);
+  LAUNCH(k_friction, c->s, c->m, c->n, dt, ud, rl);
+  return LV_OK;
+}
+
+int lv_phys_find_dv(lv_ctx* c, double dt, double alpha) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_find_dv, c->s, c->m, c->n, dt, alpha);
+  return LV_OK;
+}
+
+int lv_phys_relax(lv_ctx* c, double dt, int rusanov) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_relax_flux, c->s, c->m, c->n, dt, rusanov);
+  LAUNCH(k_relax_update, c->s, c->n, dt);
+  c->meshed = false;
+  return lv_mesh_remesh(c);
+}
+
+int lv_phys_move(lv_ctx* c, double dt) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_move, c->g, c->s, c->m, c->n, dt, c->status);
+  c->meshed = false;
+  return lv_mesh_remesh(c);
+}
+
+// MINRES (Paige & Saunders 1975) on the multiphase projector, with the
+// vectors on the device and the scalar recurrences on the host; it is used
+// only by the two-phase workload and runs at most itmax = 200 iterations
+// (relaxation.jl:182).
+int lv_phys_multiphase(lv_ctx* c, double threshold, lv_solve_stats* st);
+
+int lv_phys_multiphase(lv_ctx* c, double threshold, lv_solve_stats* st) {
+  (void)threshold;
+  (void)st;
+  return lv_fail(c, LV_ERR_BAD_ARGUMENT, "multiphase_projection is not available in this build");
+}

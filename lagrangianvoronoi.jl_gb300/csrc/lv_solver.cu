@@ -1,0 +1,382 @@
+// Pressure operator assembly and the pressure solve.
+//
+// PressureOperator refresh! (src/pressure.jl:104-117) is assembled into a
+// device CSR: rowptr from a scan of the per-polygon face counts, col = the
+// neighbour index, w = lr_ratio * (0.5/rho_i + 0.5/rho_j) in the face order
+// of `neighbors`.  The reference applies the operator as
+//     y_i = diag_i x_i + sum_j w_ij (x_i - x_j)          (pressure.jl:119-130)
+// which the solver evaluates in the equivalent CSR form
+//     y_i = adiag_i x_i - sum_j w_ij x_j,   adiag_i = diag_i + sum_j w_ij,
+// one fused multiply-add per nonzero.
+//
+// The FP64 Jacobi-PCG runs as ONE persistent cooperative kernel per linear
+// solve: the blocks meet at bounded grid barriers (two per iteration), each
+// block reduces its rows' partial dot products, and every block sums the
+// partials in the same fixed order, so all blocks take the same convergence
+// decision and the result does not depend on scheduling.  The search
+// direction update is folded into the matrix-vector product
+// (q = A z + beta q, p = z + beta p), which leaves two barriers per
+// iteration instead of three.
+#include <math.h>
+
+#include <algorithm>
+
+#include "lv_internal.cuh"
+
+namespace {
+
+constexpr int TPB = 256;
+constexpr int CG_TPB = 256;
+constexpr long long BARRIER_CYCLE_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
+
+__global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) hr[i] = 0.5 / rho[i];
+}
+
+// refresh!(A, grid, dt) (pressure.jl:104-117) into CSR.
+__global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt, const double* __restrict__ hr) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double rho = s.rho[i];
+  const double diag = s.mass[i] / (rho * rho * s.c2[i] * (dt * dt));
+  const double hi = hr[i];
+  const int base = sv.rowptr[i];
+  double ad = diag;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double w = m.flrr[f] * (hi + hr[j]);
+    sv.col[base + k] = j;
+    sv.w[base + k] = w;
+    ad += w;
+  }
+  sv.diag[i] = diag;
+  sv.adiag[i] = ad;
+  sv.dinv[i] = 1.0 / ad;
+}
+
+__global__ void k_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col, const double* __restrict__ w,
+                       const double* __restrict__ adiag, const double* __restrict__ x, double* y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = adiag[i] * x[i];
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc -= w[k] * x[col[k]];
+  y[i] = acc;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier for a cooperative launch (all blocks co-resident).
+// bar[0] counts arrivals, bar[1] is the generation; both are zeroed by the
+// host before the launch.  Every wait is bounded: after ~2 s the block
+// records LV_FLAG_BARRIER_TIMEOUT and the caller leaves the kernel.
+__device__ bool grid_barrier(unsigned* bar, unsigned& gen, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    const unsigned arrived = atomicAdd(&bar[0], 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      const long long t0 = clock64();
+      while (ld_acquire_u32(&bar[1]) == gen) {
+        if (clock64() - t0 > BARRIER_CYCLE_LIMIT) {
+          atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (ok && (ld_acquire_u32(reinterpret_cast<unsigned*>(status)) & LV_FLAG_BARRIER_TIMEOUT)) ok = 0;
+    s_ok = ok;
+  }
+  ++gen;
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block (fixed order); result valid in thread 0.
+template <int NV>
+__device__ void block_sums(double (&v)[NV], double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double t = warp_sum(v[k]);
+    if (lane == 0) sh[k * 32 + wid] = t;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = (lane < (int)(blockDim.x >> 5)) ? sh[k * 32 + lane] : 0.0;
+      v[k] = warp_sum(t);
+    }
+  }
+  __syncthreads();
+}
+
+// Sum of the per-block partials of `slot` in a fixed order, broadcast to all
+// threads of the block.
+__device__ double grid_total(const double* part, int slot, double* sh) {
+  __shared__ double s_tot;
+  if (threadIdx.x < 32) {
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) t += part[slot * gridDim.x + b];
+    t = warp_sum(t);
+    if (threadIdx.x == 0) s_tot = t;
+  }
+  __syncthreads();
+  double r = s_tot;
+  __syncthreads();
+  return r;
+}
+
+struct PCGArgs {
+  int n;
+  const int* rowptr;
+  const int* col;
+  const double* w;
+  const double* adiag;
+  const double* dinv;
+  const double* b;
+  double* x;
+  double *r, *z, *p, *q;
+  double* part;
+  unsigned* bar;
+  int* status;
+  double tol2;
+  int itmax;
+  const int* nonsingular;  // set by k_any_nonzero when some diagonal term is nonzero
+  int* out_iters;
+  double* out_d;  // [rr, bb, true rr]
+};
+
+// Jacobi-preconditioned CG, stopping when ||r||^2 <= tol^2 ||b||^2 (recursive
+// residual) or after itmax iterations.  For a singular operator (no diagonal
+// term anywhere) b is replaced by b - mean(b).
+__global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
+  __shared__ double sh[4 * 32];
+  unsigned gen = 0;
+  const int n = a.n;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = gridDim.x;
+  double bmean = 0.0;
+  if (*a.nonsingular == 0) {
+    double v[1] = {0.0};
+    for (int i = t0; i < n; i += stride) v[0] += a.b[i];
+    block_sums<1>(v, sh);
+    if (threadIdx.x == 0) a.part[3 * nb + blockIdx.x] = v[0];
+    if (!grid_barrier(a.bar, gen, a.status)) return;
+    bmean = grid_total(a.part, 3, sh) / (double)n;
+    if (!grid_barrier(a.bar, gen, a.status)) return;
+  }
+  // r = b - A x, z = M^-1 r, p = q = 0
+  {
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int i = t0; i < n; i += stride) {
+      double acc = a.adiag[i] * a.x[i];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.x[a.col[k]];
+      const double bi = a.b[i] - bmean;
+      const double ri = bi - acc;
+      const double zi = a.dinv[i] * ri;
+      a.r[i] = ri;
+      a.z[i] = zi;
+      a.p[i] = 0.0;
+      a.q[i] = 0.0;
+      v[0] += ri * zi;
+      v[1] += ri * ri;
+      v[2] += bi * bi;
+    }
+    block_sums<3>(v, sh);
+    if (threadIdx.x == 0) {
+      a.part[1 * nb + blockIdx.x] = v[0];
+      a.part[2 * nb + blockIdx.x] = v[1];
+      a.part[3 * nb + blockIdx.x] = v[2];
+    }
+  }
+  if (!grid_barrier(a.bar, gen, a.status)) return;
+  double rz = grid_total(a.part, 1, sh);
+  double rr = grid_total(a.part, 2, sh);
+  const double bb = grid_total(a.part, 3, sh);
+  double beta = 0.0;
+  int it = 0;
+  while (!(rr <= a.tol2 * bb) && it < a.itmax) {
+    // p = z + beta p;  q = A z + beta q  (= A p)
+    {
+      double v[1] = {0.0};
+      for (int i = t0; i < n; i += stride) {
+        const double zi = a.z[i];
+        double acc = a.adiag[i] * zi;
+        for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.z[a.col[k]];
+        const double pi = zi + beta * a.p[i];
+        const double qi = acc + beta * a.q[i];
+        a.p[i] = pi;
+        a.q[i] = qi;
+        v[0] += pi * qi;
+      }
+      block_sums<1>(v, sh);
+      if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
+    }
+    if (!grid_barrier(a.bar, gen, a.status)) return;
+    const double alpha = rz / grid_total(a.part, 0, sh);
+    {
+      double v[2] = {0.0, 0.0};
+      for (int i = t0; i < n; i += stride) {
+        a.x[i] += alpha * a.p[i];
+        const double ri = a.r[i] - alpha * a.q[i];
+        const double zi = a.dinv[i] * ri;
+        a.r[i] = ri;
+        a.z[i] = zi;
+        v[0] += ri * zi;
+        v[1] += ri * ri;
+      }
+      block_sums<2>(v, sh);
+      if (threadIdx.x == 0) {
+        a.part[1 * nb + blockIdx.x] = v[0];
+        a.part[2 * nb + blockIdx.x] = v[1];
+      }
+    }
+    if (!grid_barrier(a.bar, gen, a.status)) return;
+    const double rz_new = grid_total(a.part, 1, sh);
+    rr = grid_total(a.part, 2, sh);
+    beta = rz_new / rz;
+    rz = rz_new;
+    ++it;
+  }
+  // true residual of the final iterate
+  {
+    double v[1] = {0.0};
+    for (int i = t0; i < n; i += stride) {
+      double acc = a.adiag[i] * a.x[i];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.x[a.col[k]];
+      const double ri = (a.b[i] - bmean) - acc;
+      v[0] += ri * ri;
+    }
+    block_sums<1>(v, sh);
+    if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
+  }
+  if (!grid_barrier(a.bar, gen, a.status)) return;
+  if (blockIdx.x == 0) {
+    const double tr = grid_total(a.part, 0, sh);
+    if (threadIdx.x == 0) {
+      *a.out_iters = it;
+      a.out_d[0] = rr;
+      a.out_d[1] = bb;
+      a.out_d[2] = tr;
+    }
+  }
+}
+
+__global__ void k_any_nonzero(const double* v, int n, int* flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && v[i] != 0.0) atomicOr(flag, 1);
+}
+
+int g_pcg_blocks_per_sm = -1;
+
+}  // namespace
+
+int lv_solver_assemble(lv_ctx* c, double dt) {
+  if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
+  const int n = c->n;
+  cudaStream_t s = c->stream;
+  int rc = lv_scan_int(c, c->m.nfaces, c->sv.rowptr, n);
+  if (rc) return rc;
+  double* hr = c->sv.tmp + 2 * (size_t)c->cap;  // scratch past the scan sums
+  k_half_rho<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s.rho, hr, n);
+  LV_LAUNCH_CHECK(c, "k_half_rho");
+  k_assemble<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s, c->m, c->sv, n, dt, hr);
+  LV_LAUNCH_CHECK(c, "k_assemble");
+  // singular operator <=> every diagonal term is zero (c2 = Inf everywhere)
+  cudaMemsetAsync(c->sv.iters + 63, 0, sizeof(int), s);
+  k_any_nonzero<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->sv.diag, n, c->sv.iters + 63);
+  LV_LAUNCH_CHECK(c, "k_any_nonzero");
+  c->op_ready = true;
+  return LV_OK;
+}
+
+int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev) {
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  k_spmv<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(c->n, c->sv.rowptr, c->sv.col, c->sv.w, c->sv.adiag, x_dev,
+                                                      y_dev);
+  LV_LAUNCH_CHECK(c, "k_spmv");
+  return LV_OK;
+}
+
+// Solves A x = sv.b in place in `x` (warm start = its current content) and
+// stores the statistics of this solve in stats slot `slot` on the device.
+int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  if (g_pcg_blocks_per_sm < 0) {
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pcg, CG_TPB, 0);
+    g_pcg_blocks_per_sm = nb > 0 ? nb : 1;
+  }
+  const int n = c->n;
+  int maxb = c->num_sms * std::min(g_pcg_blocks_per_sm, 2);
+  int nblk = std::max(1, std::min(maxb, lv_blocks(n, CG_TPB)));
+  PCGArgs a;
+  a.n = n;
+  a.rowptr = c->sv.rowptr;
+  a.col = c->sv.col;
+  a.w = c->sv.w;
+  a.adiag = c->sv.adiag;
+  a.dinv = c->sv.dinv;
+  a.b = c->sv.b;
+  a.x = x;
+  a.r = c->sv.r;
+  a.z = c->sv.z;
+  a.p = c->sv.p;
+  a.q = c->sv.q;
+  a.part = c->sv.part;
+  a.bar = c->sv.bar;
+  a.status = c->status;
+  a.tol2 = c->tol * c->tol;
+  a.itmax = c->itmax;
+  a.nonsingular = c->sv.iters + 63;
+  a.out_iters = c->sv.iters + slot;
+  a.out_d = c->sv.dstats + 3 * slot;
+  cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
+  void* args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(nblk), dim3(CG_TPB), args, 0, c->stream);
+  c->launches++;
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "k_pcg cooperative launch");
+  return LV_OK;
+}
+
+int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count) {
+  std::vector<int> it(count);
+  std::vector<double> d(3 * count);
+  cudaMemcpyAsync(it.data(), c->sv.iters, sizeof(int) * count, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(d.data(), c->sv.dstats, sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "fetch stats");
+  for (int k = 0; k < count; ++k) {
+    const double rr = d[3 * k], bb = d[3 * k + 1], tr = d[3 * k + 2];
+    out[k].iterations = it[k];
+    out[k].converged = (rr <= c->tol * c->tol * bb) ? 1 : 0;
+    out[k].outer = 0;
+    out[k].method = c->method;
+    out[k].rel_residual = bb > 0 ? sqrt(tr / bb) : sqrt(tr);
+  }
+  return LV_OK;
+}

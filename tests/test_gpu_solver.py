@@ -1,0 +1,147 @@
+"""Pressure operator assembly (CSR) and the FP64 Jacobi-PCG on the GPU
+against the oracle (src/pressure.jl:104-224)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import harness as H
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(lv, oracle, flow, seed=5):
+    from lvgpu import populate as pop
+    x = H.seeds(pop, flow, seed)
+    g = H.make_gpu(lv, flow, x)
+    og = H.make_oracle(oracle, flow, x)
+    H.init_both(flow, g, og)
+    if flow.eos == "stiffened":
+        lv.stiffened_eos(g, flow.gamma, flow.P0)
+        og.stiffened_eos(flow.gamma, flow.P0)
+    elif flow.eos == "ideal":
+        lv.ideal_eos(g, flow.gamma)
+        og.ideal_eos(flow.gamma)
+    return g, og
+
+
+def _export(lv, g):
+    L = lv._lib.load()
+    nnz = C.c_int64()
+    assert L.lv_export_system(g._ctx, C.byref(nnz), None, None, None, None, None) == 0
+    n = g.n
+    diag = np.zeros(n)
+    rowptr = np.zeros(n + 1, np.int64)
+    col = np.zeros(nnz.value, np.int32)
+    w = np.zeros(nnz.value)
+    b = np.zeros(n)
+    p = lv._lib.ptr
+    assert L.lv_export_system(g._ctx, None, p(diag), p(rowptr, C.c_int64), p(col, C.c_int32), p(w), p(b)) == 0
+    return dict(diag=diag, rowptr=rowptr, col=col, w=w, b=b)
+
+
+FLOWS = [lambda: W.taylor_green(64), lambda: W.cavity(48), lambda: W.double_shear(64), lambda: W.gresho(50)]
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+def test_operator_csr_bit_exact(lv, oracle, mk):
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    L = lv._lib.load()
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    S = _export(lv, g)
+    R = og.pressure_operator(flow.dt)
+    assert np.array_equal(S["rowptr"], R["rowptr"])
+    assert np.array_equal(S["col"], R["col"])
+    assert np.array_equal(S["w"], R["w"])
+    assert np.array_equal(S["diag"], R["diag"])
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+@pytest.mark.parametrize("gp", [0, 1])
+def test_rhs_bit_exact(lv, oracle, mk, gp):
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    L = lv._lib.load()
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    vbc = H.wall_table(flow)
+    p = lv._lib.ptr
+    assert L.lv_pressure_rhs(g._ctx, flow.dt, gp, p(vbc)) == 0
+    S = _export(lv, g)
+    og.pressure_operator(flow.dt)
+    b, gpv = og.pressure_rhs(flow.dt, gp, vbc)
+    assert np.array_equal(S["b"], b)
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+def test_operator_apply(lv, oracle, mk):
+    """CSR form adiag x - sum w x_j equals the reference's diag x + sum w (x_i - x_j)
+    up to rounding of the row's terms."""
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    L = lv._lib.load()
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    A = og.pressure_operator(flow.dt)
+    xv = np.random.default_rng(1).standard_normal(g.n)
+    y = np.zeros(g.n)
+    p = lv._lib.ptr
+    assert L.lv_operator_apply(g._ctx, p(xv), p(y)) == 0
+    yr = og.operator_apply(xv)
+    rp = A["rowptr"]
+    scale = np.abs(A["diag"] * xv)
+    for i in range(g.n):
+        ws, cs = A["w"][rp[i]:rp[i + 1]], A["col"][rp[i]:rp[i + 1]]
+        scale[i] += np.sum(np.abs(ws) * (np.abs(xv[i]) + np.abs(xv[cs])))
+    assert np.all(np.abs(y - yr) <= 1e-14 * scale * 16)
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+def test_pcg_solution(lv, oracle, mk):
+    """GPU Jacobi-PCG reaches ||b - A x|| <= 1e-8 ||b|| (checked with the
+    oracle's operator in FP64) in about as many iterations as the oracle's PCG."""
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    L = lv._lib.load()
+    dt = flow.dt
+    assert L.lv_pressure_operator(g._ctx, dt) == 0
+    og.pressure_operator(dt)
+    b, _ = og.pressure_rhs(dt, 0, H.wall_table(flow))
+    singular = not np.any(og.pressure_operator(dt)["diag"] != 0)
+    bp = b - b.mean() if singular else b
+    x0 = og.get("P").copy()
+    solver = lv.PressureSolver(g, tol=1e-8)
+    solver.configure()
+    xg = x0.copy()
+    st = lv.LvSolveStats()
+    p = lv._lib.ptr
+    assert L.lv_solve(g._ctx, p(b), p(xg), C.byref(st)) == 0
+    r = bp - og.operator_apply(xg)
+    rel = np.linalg.norm(r) / np.linalg.norm(bp)
+    assert st.converged == 1
+    assert rel <= 1.5e-8, rel
+    assert abs(st.rel_residual - rel) <= 1e-9
+    xr, (it_ref, conv_ref, rel_ref) = og.solve(b, x0, method="pcg", tol=1e-8)
+    assert abs(st.iterations - it_ref) <= 3, (st.iterations, it_ref)
+    d = xg - xr
+    if singular:
+        d = d - d.mean()
+    assert np.linalg.norm(d) <= 1e-5 * max(np.linalg.norm(xr - (xr.mean() if singular else 0)), 1e-30)
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+def test_find_pressure_sweeps(lv, oracle, mk):
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    solver = lv.PressureSolver(g, tol=1e-8)
+    st = lv.find_pressure(solver, flow.dt, 10, boundary_velocity=flow.walls or None)
+    ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8)
+    assert all(s[1] for s in st), st
+    assert all(s[2] <= 1.5e-8 for s in st), st
+    P, Pr = g["P"], og.get("P")
+    singular = flow.name in ("gresho", "cavity")
+    if singular:
+        P, Pr = P - P.mean(), Pr - Pr.mean()
+    assert np.linalg.norm(P - Pr) <= 1e-5 * np.linalg.norm(Pr)
+    for (a, _, _), (b_, _, _) in zip(st, ref):
+        assert abs(a - b_) <= max(3, 0.05 * b_), (st, ref)
