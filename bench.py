@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Benchmark of the Lagrangian Voronoi time step on GB300.
+
+Workload: the Taylor-Green vortex flow, periodic unit square, 256 x 256 =
+65,536 seeds on a jittered lattice (SplitMix64 seed 12345, U(-0.1h, 0.1h)),
+u = sin(2 pi x) cos(2 pi y), v = -cos(2 pi x) sin(2 pi y), Re = 100,
+dt = 5e-4, FP64, stiffened gas (c0 = 50, gamma = 1.4), pressure solved by
+FP64 Jacobi-PCG to ||r|| <= 1e-8 ||b|| in each of the 10 fixed-point sweeps.
+One step is the reference's step! (move!, stiffened_eos!, find_pressure!,
+pressure_step!, find_D!, viscous_step!, find_dv!, relaxation_step!) with
+both remeshes.
+
+Metric: particle-steps/s (particles x steps / device time of the steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's algorithm
+(the oracle, reference solver settings: MINRES atol = rtol = 1e-6,
+itmax = 1000) on all host cores for the same workload.  With --gpus N > 1
+(torchrun) every rank runs an independent replica of the workload.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+NX = NY = 256
+N = NX * NY
+WORKLOAD = "taylor_green_256x256"
+METRIC = "particle-steps/s at 1 GB300; pressure solve ms & CG iters, learned vs plain PCG @1e-8"
+UNIT = "particle-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def load_package():
+    import __graft_entry__ as ge
+    ge.build()
+    return ge._package()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def flow():
+    import workloads as W
+    return W.taylor_green(NX)
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4) if r[k].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ our arm
+
+def setup_grid(lv, fl):
+    import harness as H
+    from lvgpu import populate as pop
+    import workloads as W
+    x = H.seeds(pop, fl)
+    g = lv.VoronoiGrid(lv.Rectangle(fl.xlims, fl.ylims), fl.dr, xperiodic=True, yperiodic=True)
+    g.push(x)
+    lv.remesh(g)
+    for k, v in W.initial_fields(fl, g["x"], g["area"]).items():
+        g[k] = v
+    return g
+
+
+def gpu_step(lv, g, solver, fl):
+    dt = fl.dt
+    lv.move(g, dt)
+    lv.stiffened_eos(g, fl.gamma, fl.P0)
+    lv.find_pressure(solver, dt, 10, stats=False)
+    lv.pressure_step(g, dt)
+    lv.find_D(g)
+    lv.viscous_step(g, dt, fl.artificial_viscosity)
+    lv.find_dv(g, dt)
+    lv.relaxation_step(g, dt)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    lv = load_package()
+    L = lv._lib.load()
+    fl = flow()
+    g = setup_grid(lv, fl)
+    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
+    stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        gpu_step(lv, g, solver, fl)
+    g.synchronize()
+
+    # ---- timed region: K steps, device time from events on the library's stream,
+    # an L2 flush (512 MiB write) between steps outside the events
+    fam = lv._lib.KERNEL_FAMILIES
+    L.lv_kernel_timing(g._ctx, 1)
+    for f in fam.values():
+        L.lv_kernel_time(g._ctx, f, None, None, 1)
+    s0, i0 = C.c_int64(), C.c_int64()
+    L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
+    launches0 = g.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+            gpu_step(lv, g, solver, fl)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        g.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    barrier(world)
+    launches = g.launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = float(sum(step_ms))
+    s1, i1 = C.c_int64(), C.c_int64()
+    L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
+    solves, iters = s1.value - s0.value, i1.value - i0.value
+    kt = {}
+    for name, f in fam.items():
+        nl, ms = C.c_int64(), C.c_double()
+        L.lv_kernel_time(g._ctx, f, C.byref(nl), C.byref(ms), 1)
+        kt[name] = (nl.value, ms.value)
+    L.lv_kernel_timing(g._ctx, 0)
+    max_ms = allmax(world, dev_ms)
+
+    # ---- end to end through the public API: per step, host (pinned) -> device
+    # upload of the evolving state, the step, device -> host read of the result
+    pin = {k: torch.empty(g.get(k).shape, dtype=torch.float64, pin_memory=True).numpy() for k in
+           ("v", "e", "P", "mass")}
+    outs = {k: torch.empty(g.get(k).shape, dtype=torch.float64, pin_memory=True).numpy() for k in
+            ("x", "v", "e", "P", "mass")}
+    for k in pin:
+        pin[k][...] = g.get(k)
+    h2d = sum(a.nbytes for a in pin.values())
+    d2h = sum(a.nbytes for a in outs.values())
+    e2e_steps = max(1, args.steps)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k, a in pin.items():
+            g.set(k, a)
+        gpu_step(lv, g, solver, fl)
+        for k, a in outs.items():
+            fid, _ = lv._lib.FIELDS[k]
+            rc = L.lv_get_field(g._ctx, fid, lv._lib.ptr(a))
+            assert rc == 0
+        for k in pin:
+            pin[k][...] = outs[k]
+    g.synchronize()
+    e2e_s = allmax(world, time.perf_counter() - t0)
+
+    if rank != 0:
+        return None
+    value = world * N * args.steps / (max_ms / 1e3)
+    e2e_value = world * N * e2e_steps / e2e_s
+    ms_per_step = max_ms / args.steps
+    clocks = clk.summary()
+
+    # ---- roofline of the dominant kernel family
+    nnz = None
+    try:
+        nnzc = C.c_int64()
+        L.lv_export_system(g._ctx, C.byref(nnzc), None, None, None, None, None)
+        nnz = nnzc.value
+    except Exception:
+        pass
+    F = nnz if nnz is not None else 6 * N
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # algorithmic bytes per unit (per particle): FP64 PCG iteration
+    # (8+4)*nnz + 4N + 4*8N + 3*8N with nnz = F + N (diagonal included);
+    # clip + geometry 16N + 28F + 28N
+    pcg_bytes = iters * (12 * (F + N) + 4 * N + 56 * N)
+    clip_bytes = kt["clip"][0] * (16 * N + 28 * F + 28 * N)
+    fams = {"pcg": pcg_bytes, "clip": clip_bytes}
+    dom = max(("pcg", "clip"), key=lambda k: kt[k][1])
+    dom_ms = kt[dom][1]
+    dom_launches = max(kt[dom][0], 1)
+    achieved = (fams[dom] / dom_launches) / ((dom_ms / dom_launches) / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
+        "config": {"workload": WORKLOAD, "particles": N, "solver": "jacobi_pcg fp64 tol 1e-8, 10 sweeps/step",
+                   "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": f"replicas x{world}",
+                   "l2": "512 MiB buffer written between timed steps (state ~15 MB fits in L2)"},
+        "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1]) / args.steps,
+                     "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
+                     "solves": solves},
+        "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},
+        "roofline": {"kernel": "k_pcg" if dom == "pcg" else "k_clip", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                     "peak_source": peak_src},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "wall_s_timed": wall,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, sample_steps=2)
+    return line
+
+
+# ------------------------------------------------------------ reference arm
+
+def oracle_grid(fl):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lvref
+    import harness as H
+    import workloads as W
+    from importlib import util
+    spec = util.spec_from_file_location("pop_b", os.path.join(ROOT, "lagrangianvoronoi.jl_gb300", "populate.py"))
+    pop = util.module_from_spec(spec)
+    spec.loader.exec_module(pop)
+    lvref.build()
+    threads = lvref.set_threads(os.cpu_count() or 1)
+    x = H.seeds(pop, fl)
+    og = lvref.OracleGrid(fl.xlims, fl.ylims, fl.dr, len(x), xperiodic=True, yperiodic=True, max_edges=20)
+    og.set("x", x)
+    assert og.remesh() == 0
+    for k, v in W.initial_fields(fl, x, og.edges()["area"]).items():
+        og.set(k, v)
+    return og, threads
+
+
+def oracle_step(og, fl):
+    dt = fl.dt
+    assert og.move(dt) == 0
+    og.stiffened_eos(fl.gamma, fl.P0)
+    og.find_pressure(dt, 10, None, method="minres", tol=1e-6, itmax=1000)
+    og.pressure_step(dt)
+    og.find_D()
+    og.viscous_step(dt, fl.artificial_viscosity)
+    og.find_dv(dt)
+    assert og.relaxation_step(dt) == 0
+
+
+def cpu_baseline(args, sample_steps=2):
+    fl = flow()
+    og, threads = oracle_grid(fl)
+    oracle_step(og, fl)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(sample_steps):
+        oracle_step(og, fl)
+    dt = time.perf_counter() - t0
+    return {"value": N * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample_steps} full steps of {WORKLOAD} after 1 warm-up step, oracle restatement "
+                      f"with the reference's solver (MINRES atol=rtol=1e-6, itmax=1000), OpenMP {threads} threads"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    fl = flow()
+    og, threads = oracle_grid(fl)
+    for _ in range(args.warmup):
+        oracle_step(og, fl)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle_step(og, fl)
+    dt = time.perf_counter() - t0
+    value = N * args.steps / dt
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
+        "config": {"workload": WORKLOAD, "particles": N,
+                   "solver": "minres fp64 atol=rtol=1e-6 itmax=1000, 10 sweeps/step (reference settings)",
+                   "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps; the reference is "
+                                   "Julia and no Julia runtime exists on this machine, so its algorithm runs as "
+                                   "the C++ restatement (oracle/)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        line = run_reference(args, world, rank)
+    else:
+        line = run_ours(args, world, rank, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

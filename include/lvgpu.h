@@ -167,6 +167,27 @@ int lv_operator_apply(lv_ctx* ctx, const double* x, double* y);
 /* MultiphaseSolver / multiphase_projection! (relaxation.jl:137-206). */
 int lv_multiphase_projection(lv_ctx* ctx, double quality_threshold, lv_solve_stats* stats);
 
+/* The CUDA stream (cudaStream_t) every call of this context is ordered on;
+ * callers may record events or enqueue their own work on it. */
+void* lv_stream(lv_ctx* ctx);
+
+/* Kernel families timed by lv_kernel_timing. */
+#define LV_KF_BIN 0      /* cell-list re-binning (count, scan, scatter, order) */
+#define LV_KF_CLIP 1     /* Voronoi clipping + geometry + faces (k_clip) */
+#define LV_KF_PCG 2      /* persistent pressure-solve kernels */
+#define LV_KF_RHS 3      /* operator assembly and right-hand side */
+#define LV_KF_OPS 4      /* per-particle physics operators */
+#define LV_KF_COUNT 5
+/* When enabled, every launch of every family is bracketed by CUDA events on
+ * the context's stream (no synchronisation).  lv_kernel_time synchronises
+ * and returns, for one family, the launches and total device ms since the
+ * last reset (reset != 0 clears the family). */
+int lv_kernel_timing(lv_ctx* ctx, int32_t enable);
+int lv_kernel_time(lv_ctx* ctx, int32_t family, int64_t* launches, double* ms, int32_t reset);
+/* Cumulative pressure-solver counters since creation: linear solves and CG
+ * iterations (inner iterations for the mixed-precision solver); synchronises. */
+int lv_solver_counters(lv_ctx* ctx, int64_t* solves, int64_t* iterations);
+
 /* Per-kernel-family device times in ms accumulated since the last reset:
  * out[0] mesh, [1] operators, [2] pressure solve, [3] other.  Returns the
  * number of entries written. */

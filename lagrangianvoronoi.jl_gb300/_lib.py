@@ -77,7 +77,12 @@ SIGNATURES = {
     "lv_get_timings": (C.c_int, [_vp, _pd, _i32]),
     "lv_reset_timings": (C.c_int, [_vp]),
     "lv_launch_count": (_i64, [_vp]),
+    "lv_stream": (_vp, [_vp]),
+    "lv_kernel_timing": (C.c_int, [_vp, _i32]),
+    "lv_kernel_time": (C.c_int, [_vp, _i32, _pi64, _pd, _i32]),
+    "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
 }
+KERNEL_FAMILIES = {"bin": 0, "clip": 1, "pcg": 2, "rhs": 3, "ops": 4}
 
 _LIB = None
 

@@ -130,6 +130,27 @@ __global__ void k_split_phase(const double* __restrict__ src, int* dst, int n) {
 
 }  // namespace
 
+KernelTimer::KernelTimer(lv_ctx* cc, int f) : c(cc), fam(f) {
+  if (!c->ktiming) return;
+  auto& k = c->kev[fam];
+  if (k.used + 2 > k.ev.size()) {
+    for (int t = 0; t < 64; ++t) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      k.ev.push_back(e);
+    }
+  }
+  cudaEventRecord(k.ev[k.used], c->stream);
+}
+
+KernelTimer::~KernelTimer() {
+  if (!c->ktiming) return;
+  auto& k = c->kev[fam];
+  cudaEventRecord(k.ev[k.used + 1], c->stream);
+  k.used += 2;
+  k.launches += 1;
+}
+
 extern "C" {
 
 lv_ctx* lv_create(const lv_params* prm) {
@@ -256,6 +277,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.q32 = dalloc<float>(c, cap, &ok);
   sv.d32 = dalloc<float>(c, cap, &ok);
   sv.part = dalloc<double>(c, 8 * 4096, &ok);
+  sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);
   sv.iters = dalloc<int>(c, 64, &ok);
   sv.dstats = dalloc<double>(c, 3 * 64, &ok);
@@ -278,6 +300,8 @@ int lv_destroy(lv_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
+  for (auto& k : c->kev)
+    for (cudaEvent_t e : k.ev) cudaEventDestroy(e);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -684,5 +708,44 @@ int lv_reset_timings(lv_ctx* c) {
 }
 
 int64_t lv_launch_count(const lv_ctx* c) { return c ? c->launches : 0; }
+
+void* lv_stream(lv_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int lv_kernel_timing(lv_ctx* c, int32_t enable) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  c->ktiming = enable != 0;
+  return LV_OK;
+}
+
+int lv_kernel_time(lv_ctx* c, int32_t fam, int64_t* launches, double* ms, int32_t reset) {
+  if (!c || fam < 0 || fam >= LV_KF_COUNT) return LV_ERR_BAD_ARGUMENT;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_kernel_time");
+  auto& k = c->kev[fam];
+  double tot = 0.0;
+  for (size_t t = 0; t + 1 < k.used; t += 2) {
+    float x = 0.0f;
+    cudaEventElapsedTime(&x, k.ev[t], k.ev[t + 1]);
+    tot += x;
+  }
+  if (launches) *launches = k.launches;
+  if (ms) *ms = tot;
+  if (reset) {
+    k.used = 0;
+    k.launches = 0;
+  }
+  return LV_OK;
+}
+
+int lv_solver_counters(lv_ctx* c, int64_t* solves, int64_t* iterations) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  long long h[2] = {0, 0};
+  cudaMemcpyAsync(h, c->sv.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_solver_counters");
+  if (solves) *solves = h[0];
+  if (iterations) *iterations = h[1];
+  return LV_OK;
+}
 
 }  // extern "C"

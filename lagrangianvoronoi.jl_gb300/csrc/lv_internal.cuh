@@ -85,6 +85,7 @@ struct SolverDev {
   float* w32;   // FP32 copy for the mixed-precision inner solve
   double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
   float *dinv32, *r32, *z32, *p32, *q32, *d32;
+  long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
   unsigned* bar;      // grid barrier {count, generation}
   int* iters;         // device-side stats
@@ -120,6 +121,22 @@ struct lv_ctx {
   double t_ms[4] = {0, 0, 0, 0};
   bool timing = false;
   std::vector<void*> allocs;
+  // per-family kernel timing (lv_kernel_timing)
+  bool ktiming = false;
+  struct KEvents {
+    std::vector<cudaEvent_t> ev;  // start/end pairs
+    size_t used = 0;              // events recorded since the last reset
+    int64_t launches = 0;
+  } kev[LV_KF_COUNT];
+};
+
+// Brackets the launches of one kernel family with CUDA events when kernel
+// timing is on (lv_api.cu).
+struct KernelTimer {
+  lv_ctx* c;
+  int fam;
+  KernelTimer(lv_ctx* cc, int f);
+  ~KernelTimer();
 };
 
 // ---- host helpers (lv_api.cu)

@@ -530,6 +530,8 @@ int lv_mesh_remesh(lv_ctx* c) {
   if (n <= 0) return lv_fail(c, LV_ERR_NOT_MESHED, "remesh: no particles");
   cudaStream_t s = c->stream;
   const int nc = c->c.ncells;
+  {
+  KernelTimer kt(c, LV_KF_BIN);
   cudaMemsetAsync(c->c.ccount, 0, sizeof(int) * nc, s);
   k_bin_count<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->c.ccount, c->status);
   LV_LAUNCH_CHECK(c, "k_bin_count");
@@ -541,14 +543,18 @@ int lv_mesh_remesh(lv_ctx* c) {
   LV_LAUNCH_CHECK(c, "k_bin_scatter");
   k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap);
   LV_LAUNCH_CHECK(c, "k_bin_order");
+  }
   const size_t smem = (size_t)ME * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 2 * sizeof(float));
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr_set = true;
   }
-  k_clip<<<lv_blocks(n, CLIP_TPB), CLIP_TPB, smem, s>>>(c->g, c->path, c->s.x, n, c->c, c->m, c->status, 1);
-  LV_LAUNCH_CHECK(c, "k_clip");
+  {
+    KernelTimer kt(c, LV_KF_CLIP);
+    k_clip<<<lv_blocks(n, CLIP_TPB), CLIP_TPB, smem, s>>>(c->g, c->path, c->s.x, n, c->c, c->m, c->status, 1);
+    LV_LAUNCH_CHECK(c, "k_clip");
+  }
   c->meshed = true;
   c->op_ready = false;
   return LV_OK;

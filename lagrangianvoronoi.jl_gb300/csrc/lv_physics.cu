@@ -551,11 +551,13 @@ __global__ void k_mp_correct(StateDev s, MeshDev m, int n, const double* __restr
 
 // ------------------------------------------------------------------- host
 
-#define LAUNCH(kernel, ...)                                                     \
+#define LAUNCH_F(fam, kernel, ...)                                              \
   do {                                                                          \
+    KernelTimer _kt(c, fam);                                                    \
     kernel<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(__VA_ARGS__);           \
     LV_LAUNCH_CHECK(c, #kernel);                                                \
   } while (0)
+#define LAUNCH(kernel, ...) LAUNCH_F(LV_KF_OPS, kernel, __VA_ARGS__)
 
 static int need_mesh(lv_ctx* c) {
   if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed (call lv_remesh first)");
@@ -588,8 +590,8 @@ int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc) {
   // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
   double4 ud = make_double4(w[0], w[1], w[4], w[5]);
   double4 rl = make_double4(w[2], w[3], w[6], w[7]);
-  LAUNCH(k_rhs, c->s, c->m, c->sv, c->n, dt, ud, rl);
-  if (gp_step) LAUNCH(k_rhs_gp, c->s, c->m, c->sv, c->n);
+  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt, ud, rl);
+  if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n);
   return LV_OK;
 }
 

@@ -167,6 +167,7 @@ struct PCGArgs {
   const int* nonsingular;  // set by k_any_nonzero when some diagonal term is nonzero
   int* out_iters;
   double* out_d;  // [rr, bb, true rr]
+  long long* counters;
 };
 
 // Jacobi-preconditioned CG, stopping when ||r||^2 <= tol^2 ||b||^2 (recursive
@@ -279,6 +280,8 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     const double tr = grid_total(a.part, 0, sh);
     if (threadIdx.x == 0) {
       *a.out_iters = it;
+      a.counters[0] += 1;
+      a.counters[1] += it;
       a.out_d[0] = rr;
       a.out_d[1] = bb;
       a.out_d[2] = tr;
@@ -299,6 +302,7 @@ int lv_solver_assemble(lv_ctx* c, double dt) {
   if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
   const int n = c->n;
   cudaStream_t s = c->stream;
+  KernelTimer kt(c, LV_KF_RHS);
   int rc = lv_scan_int(c, c->m.nfaces, c->sv.rowptr, n);
   if (rc) return rc;
   double* hr = c->sv.tmp + 2 * (size_t)c->cap;  // scratch past the scan sums
@@ -355,8 +359,10 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
   a.nonsingular = c->sv.iters + 63;
   a.out_iters = c->sv.iters + slot;
   a.out_d = c->sv.dstats + 3 * slot;
+  a.counters = c->sv.counters;
   cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
   void* args[] = {&a};
+  KernelTimer kt(c, LV_KF_PCG);
   cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(nblk), dim3(CG_TPB), args, 0, c->stream);
   c->launches++;
   if (e != cudaSuccess) return lv_cuda_check(c, e, "k_pcg cooperative launch");

@@ -122,6 +122,8 @@ class OracleGrid:
         assert st == 0
 
     def get(self, name):
+        if name in ("area", "centroid"):
+            return self.edges()[name]
         f = FIELD_NAMES[name]
         k = NCOMP.get(f, 1)
         a = np.empty(self.n * k, dtype=np.float64)

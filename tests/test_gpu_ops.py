@@ -100,8 +100,8 @@ def test_find_dv_relaxation(lv, oracle, mk):
 def test_move(lv, oracle, mk):
     flow = mk()
     g, og = _setup(lv, oracle, flow)
-    # a velocity large enough to push boundary particles out of a walled domain
-    v = g["v"] + 40.0 * flow.dr / flow.dt * np.array([0.3, -0.2])
+    # a velocity that pushes the boundary layer out of a walled domain
+    v = g["v"] + 3.0 * flow.dr / flow.dt * np.array([0.3, -0.2])
     g["v"] = v
     og.set("v", v)
     lv.move(g, flow.dt)
@@ -119,3 +119,18 @@ def test_move_nan_velocity_is_reported(lv, oracle):
         lv.move(g, flow.dt)
         g.synchronize()
     assert e.value.code == 1
+
+
+def test_destroyed_mesh_is_reported(lv, oracle):
+    """Piling every particle against the walls destroys the mesh: the oracle
+    and the GPU both report it (voronoigrid.jl:63-65)."""
+    flow = W.cavity(48)
+    g, og = _setup(lv, oracle, flow)
+    v = g["v"] + 40.0 * flow.dr / flow.dt * np.array([0.3, -0.2])
+    g["v"] = v
+    og.set("v", v)
+    assert og.move(flow.dt) == 2
+    with pytest.raises(lv.LvError) as e:
+        lv.move(g, flow.dt)
+        g.synchronize()
+    assert e.value.code == 2
