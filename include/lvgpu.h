@@ -164,6 +164,29 @@ int lv_solve(lv_ctx* ctx, const double* b, double* x, lv_solve_stats* stats);
 /* y = A x on the current operator (host arrays). */
 int lv_operator_apply(lv_ctx* ctx, const double* x, double* y);
 
+/* FP64 Jacobi-PCG on a system the caller already holds in device memory,
+ * without allocating anything.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc, such as hosts that reserve the
+ * whole device memory for their own allocator up front, or time-step loops
+ * that must not stall, since cudaMalloc synchronises the device and can take
+ * milliseconds.
+ * Inputs (device pointers): the reference's operator in the form
+ * lv_export_system returns, diag[n], rowptr[n+1] (int32), col[nnz], w[nnz],
+ * and b[n]; x[n] holds the initial guess on entry and the solution on return.
+ * The solver's scratch is a static device array sized for at most
+ * LV_NOALLOC_MAX_ROWS rows (about 24 MiB, held by every GPU that loads the
+ * library until exit); larger n returns LV_ERR_BAD_ARGUMENT.  The first call
+ * on a device looks up the array's device address, so make that first call
+ * before anything that forbids such a lookup.  Every call shares the array,
+ * so calls that overlap on the GPU race; run them on one stream.  With
+ * iterations and rel_residual both NULL the call only queues work on
+ * `stream` (a cudaStream_t, NULL = default stream); otherwise it waits for it
+ * and returns LV_OK when ||b - A x|| <= tol ||b||, else LV_ERR_CG_MAXITER. */
+#define LV_NOALLOC_MAX_ROWS 524288
+int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t* rowptr, const int32_t* col, const double* w,
+                         const double* b, double* x, double tol, int32_t itmax, void* stream, int32_t* iterations,
+                         double* rel_residual);
+
 /* MultiphaseSolver / multiphase_projection! (relaxation.jl:137-206). */
 int lv_multiphase_projection(lv_ctx* ctx, double quality_threshold, lv_solve_stats* stats);
 

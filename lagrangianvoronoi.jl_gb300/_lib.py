@@ -81,6 +81,7 @@ SIGNATURES = {
     "lv_kernel_timing": (C.c_int, [_vp, _i32]),
     "lv_kernel_time": (C.c_int, [_vp, _i32, _pi64, _pd, _i32]),
     "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
+    "lv_pcg_solve_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i32, _vp, _pi32, _pd]),
 }
 KERNEL_FAMILIES = {"bin": 0, "clip": 1, "pcg": 2, "rhs": 3, "ops": 4}
 

@@ -386,3 +386,120 @@ int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count) {
   }
   return LV_OK;
 }
+
+// ===================================================================
+// Allocation-free solve (lv_pcg_solve_noalloc).
+//
+// Callers that cannot allocate device memory still get the FP64
+// Jacobi-PCG: the kernel's scratch lives in the file-scope array below
+// instead of buffers from cudaMalloc.  The array is sized for
+// LV_NOALLOC_MAX_ROWS rows and every GPU that loads this library keeps it
+// (about 24 MiB) until the process exits.  All calls share it, and it keeps
+// the contents of the last call.  Two calls that overlap on the GPU race on
+// it.
+// ===================================================================
+
+namespace {
+
+constexpr int NOALLOC_VECS = 6;                   // adiag, dinv, r, z, p, q
+constexpr int NOALLOC_PART = 4 * 4096;            // reduction partials
+constexpr int NOALLOC_MISC = 64;                  // barrier, flags, statistics
+constexpr size_t NOALLOC_DOUBLES = (size_t)NOALLOC_VECS * LV_NOALLOC_MAX_ROWS + NOALLOC_PART + NOALLOC_MISC;
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_DOUBLES];
+
+// adiag_i = diag_i + sum_j w_ij, dinv_i = 1/adiag_i, and the flag telling
+// whether any diagonal term is nonzero (nonsingular operator).
+__global__ void k_noalloc_diag(int n, const double* __restrict__ diag, const int* __restrict__ rowptr,
+                               const double* __restrict__ w, double* adiag, double* dinv, int* nonsingular) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double d = diag[i];
+  double ad = d;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) ad += w[k];
+  adiag[i] = ad;
+  dinv[i] = 1.0 / ad;
+  if (d != 0.0) atomicOr(nonsingular, 1);
+}
+
+// Device address of the scratch array, looked up once per device.
+double* g_noalloc_dev[64] = {nullptr};
+bool g_noalloc_ready[64] = {false};
+
+}  // namespace
+
+extern "C" int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t* rowptr, const int32_t* col,
+                                    const double* w, const double* b, double* x, double tol, int32_t itmax,
+                                    void* stream, int32_t* iterations, double* rel_residual) {
+  if (n <= 0 || n > LV_NOALLOC_MAX_ROWS) return LV_ERR_BAD_ARGUMENT;
+  if (!diag || !rowptr || !col || !w || !b || !x || !(tol > 0) || itmax <= 0) return LV_ERR_BAD_ARGUMENT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return LV_ERR_CUDA;
+  // First call on this device: resolve the array's device address with the
+  // device current.  The host-side name g_noalloc_scratch is only a stand-in
+  // and must never be passed to a kernel.
+  if (!g_noalloc_ready[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LV_ERR_CUDA;
+    g_noalloc_dev[dev] = static_cast<double*>(p);
+    g_noalloc_ready[dev] = true;
+  }
+  double* base = g_noalloc_dev[dev];
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t M = LV_NOALLOC_MAX_ROWS;
+  double* adiag = base;
+  double* dinv = base + M;
+  double* misc = base + NOALLOC_VECS * M + NOALLOC_PART;
+  unsigned* bar = reinterpret_cast<unsigned*>(misc);          // 2 words
+  int* status = reinterpret_cast<int*>(misc + 1);
+  int* nonsingular = reinterpret_cast<int*>(misc + 2);
+  int* iters = reinterpret_cast<int*>(misc + 3);
+  double* outd = misc + 4;                                     // rr, bb, true rr
+  long long* counters = reinterpret_cast<long long*>(misc + 8);
+  // what must start at zero: barrier, status, flag, counters
+  if (cudaMemsetAsync(misc, 0, sizeof(double) * 10, s) != cudaSuccess) return LV_ERR_CUDA;
+  k_noalloc_diag<<<lv_blocks(n, TPB), TPB, 0, s>>>(n, diag, rowptr, w, adiag, dinv, nonsingular);
+  if (cudaGetLastError() != cudaSuccess) return LV_ERR_CUDA;
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return LV_ERR_CUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, CG_TPB, 0) != cudaSuccess || per_sm < 1)
+    return LV_ERR_CUDA;
+  const int nblk = std::max(1, std::min(sms * std::min(per_sm, 2), lv_blocks(n, CG_TPB)));
+  PCGArgs a;
+  a.n = n;
+  a.rowptr = rowptr;
+  a.col = col;
+  a.w = w;
+  a.adiag = adiag;
+  a.dinv = dinv;
+  a.b = b;
+  a.x = x;
+  a.r = base + 2 * M;
+  a.z = base + 3 * M;
+  a.p = base + 4 * M;
+  a.q = base + 5 * M;
+  a.part = base + NOALLOC_VECS * M;
+  a.bar = bar;
+  a.status = status;
+  a.tol2 = tol * tol;
+  a.itmax = itmax;
+  a.nonsingular = nonsingular;
+  a.out_iters = iters;
+  a.out_d = outd;
+  a.counters = counters;
+  void* args[] = {&a};
+  if (cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(nblk), dim3(CG_TPB), args, 0, s) != cudaSuccess)
+    return LV_ERR_CUDA;
+  if (!iterations && !rel_residual) return LV_OK;
+  int it = 0, st = 0;
+  double d3[3] = {0, 0, 0};
+  if (cudaMemcpyAsync(&it, iters, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(d3, outd, sizeof(d3), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return LV_ERR_CUDA;
+  if (st & LV_FLAG_BARRIER_TIMEOUT) return LV_ERR_BARRIER_TIMEOUT;
+  if (iterations) *iterations = it;
+  if (rel_residual) *rel_residual = d3[1] > 0 ? sqrt(d3[2] / d3[1]) : sqrt(d3[2]);
+  return (d3[0] <= tol * tol * d3[1]) ? LV_OK : LV_ERR_CG_MAXITER;
+}
