@@ -73,36 +73,31 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 }
 
 // Grid barrier for a cooperative launch (all blocks co-resident).
-// bar[0] counts arrivals, bar[1] is the generation; both are zeroed by the
-// host before the launch.  Every wait is bounded: after ~2 s the block
-// records LV_FLAG_BARRIER_TIMEOUT and the caller leaves the kernel.
-__device__ bool grid_barrier(unsigned* bar, unsigned& gen, int* status) {
+// bar[0] is an arrival word, zeroed by the host before the launch: block 0
+// adds 2^31 - (nblocks - 1), every other block adds 1, so the word's top bit
+// flips exactly when the last block arrives and its low bits return to zero
+// for the next barrier.  Every wait is bounded: after ~2 s the block records
+// LV_FLAG_BARRIER_TIMEOUT and the caller leaves the kernel.
+__device__ bool grid_barrier(unsigned* bar, int* status) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
+    const unsigned inc = (blockIdx.x == 0) ? (0x80000000u - (gridDim.x - 1)) : 1u;
     __threadfence();
-    const unsigned arrived = atomicAdd(&bar[0], 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&bar[0], 0u);
-      __threadfence();
-      atomicAdd(&bar[1], 1u);
-    } else {
-      const long long t0 = clock64();
-      while (ld_acquire_u32(&bar[1]) == gen) {
-        if (clock64() - t0 > BARRIER_CYCLE_LIMIT) {
-          atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
+    const unsigned old = atomicAdd(bar, inc);
+    const long long t0 = clock64();
+    while (((old ^ ld_acquire_u32(bar)) & 0x80000000u) == 0u) {
+      if (clock64() - t0 > BARRIER_CYCLE_LIMIT) {
+        atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
+        ok = 0;
+        break;
       }
     }
     __threadfence();
     if (ok && (ld_acquire_u32(reinterpret_cast<unsigned*>(status)) & LV_FLAG_BARRIER_TIMEOUT)) ok = 0;
     s_ok = ok;
   }
-  ++gen;
   __syncthreads();
   return s_ok != 0;
 }
@@ -175,7 +170,6 @@ struct PCGArgs {
 // term anywhere) b is replaced by b - mean(b).
 __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
   __shared__ double sh[4 * 32];
-  unsigned gen = 0;
   const int n = a.n;
   const int stride = gridDim.x * blockDim.x;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -186,9 +180,9 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     for (int i = t0; i < n; i += stride) v[0] += a.b[i];
     block_sums<1>(v, sh);
     if (threadIdx.x == 0) a.part[3 * nb + blockIdx.x] = v[0];
-    if (!grid_barrier(a.bar, gen, a.status)) return;
+    if (!grid_barrier(a.bar, a.status)) return;
     bmean = grid_total(a.part, 3, sh) / (double)n;
-    if (!grid_barrier(a.bar, gen, a.status)) return;
+    if (!grid_barrier(a.bar, a.status)) return;
   }
   // r = b - A x, z = M^-1 r, p = q = 0
   {
@@ -214,7 +208,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
       a.part[3 * nb + blockIdx.x] = v[2];
     }
   }
-  if (!grid_barrier(a.bar, gen, a.status)) return;
+  if (!grid_barrier(a.bar, a.status)) return;
   double rz = grid_total(a.part, 1, sh);
   double rr = grid_total(a.part, 2, sh);
   const double bb = grid_total(a.part, 3, sh);
@@ -237,7 +231,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
       block_sums<1>(v, sh);
       if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
     }
-    if (!grid_barrier(a.bar, gen, a.status)) return;
+    if (!grid_barrier(a.bar, a.status)) return;
     const double alpha = rz / grid_total(a.part, 0, sh);
     {
       double v[2] = {0.0, 0.0};
@@ -256,7 +250,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
         a.part[2 * nb + blockIdx.x] = v[1];
       }
     }
-    if (!grid_barrier(a.bar, gen, a.status)) return;
+    if (!grid_barrier(a.bar, a.status)) return;
     const double rz_new = grid_total(a.part, 1, sh);
     rr = grid_total(a.part, 2, sh);
     beta = rz_new / rz;
@@ -275,7 +269,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     block_sums<1>(v, sh);
     if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
   }
-  if (!grid_barrier(a.bar, gen, a.status)) return;
+  if (!grid_barrier(a.bar, a.status)) return;
   if (blockIdx.x == 0) {
     const double tr = grid_total(a.part, 0, sh);
     if (threadIdx.x == 0) {
@@ -289,12 +283,220 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident pipelined Jacobi-PCG for systems whose rows fit in the
+// registers of one cooperative grid (at most R rows per thread).
+//
+// Pipelined CG (Ghysels & Vanroose, Parallel Computing 40, 2014, Alg. 3)
+// needs one global reduction and one matrix-vector product per iteration,
+// and the product can start before the reduction finishes, so each iteration
+// costs a single grid barrier.  Every thread keeps its rows' CSR entries (the
+// first KR of each row) and all eight CG vectors in registers; the only
+// vectors exchanged through global memory are m = M^-1 w (double-buffered by
+// iteration parity) and, at (re)starts, u and x.  The recursive residual is
+// confirmed by an explicit residual b - A x before the kernel exits; if it
+// misses the tolerance, CG restarts from it (at most 3 times).
+// ---------------------------------------------------------------------------
+constexpr int SP_TPB = 128;
+constexpr int KR = 8;
+
+template <int R>
+struct RowRegs {
+  int i[R];
+  int beg[R], cnt[R];
+  int cc[R][KR];
+  double ww[R][KR];
+  double adg[R], dnv[R], bb[R];
+};
+
+template <int R>
+__device__ __forceinline__ void row_apply(const RowRegs<R>& rr, const PCGArgs& a, const double* __restrict__ vg,
+                                          const double (&own)[R], double (&out)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    double acc = rr.adg[r] * own[r];
+#pragma unroll
+    for (int k = 0; k < KR; ++k)
+      if (k < rr.cnt[r]) acc -= rr.ww[r][k] * vg[rr.cc[r][k]];
+    for (int k = KR; k < rr.cnt[r]; ++k) acc -= a.w[rr.beg[r] + k] * vg[a.col[rr.beg[r] + k]];
+    out[r] = acc;
+  }
+}
+
+template <int NV>
+__device__ void grid_totals(const double* part, int slot0, double (&tot)[NV]) {
+  __shared__ double s_tot[NV];
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double t = 0.0;
+      for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) t += part[(slot0 + v) * gridDim.x + b];
+      t = warp_sum(t);
+      if (threadIdx.x == 0) s_tot[v] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < NV; ++v) tot[v] = s_tot[v];
+  __syncthreads();
+}
+
+template <int R>
+__global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, double* mbuf0, double* mbuf1) {
+  __shared__ double sh[4 * 32];
+  const int n = a.n;
+  const int nb = gridDim.x;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  RowRegs<R> rr;
+  double x[R], r[R], u[R], w[R], z[R], q[R], s[R], p[R], m[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int i = t0 + k * stride;
+    rr.i[k] = i;
+    const bool on = i < n;
+    rr.beg[k] = on ? a.rowptr[i] : 0;
+    rr.cnt[k] = on ? a.rowptr[i + 1] - rr.beg[k] : 0;
+#pragma unroll
+    for (int e = 0; e < KR; ++e) {
+      const bool have = e < rr.cnt[k];
+      rr.cc[k][e] = have ? a.col[rr.beg[k] + e] : 0;
+      rr.ww[k][e] = have ? a.w[rr.beg[k] + e] : 0.0;
+    }
+    rr.adg[k] = on ? a.adiag[i] : 0.0;
+    rr.dnv[k] = on ? a.dinv[i] : 0.0;
+    rr.bb[k] = on ? a.b[i] : 0.0;
+    x[k] = on ? a.x[i] : 0.0;
+  }
+  // singular operator: project b to zero mean
+  if (*a.nonsingular == 0) {
+    double v[1] = {0.0};
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[0] += rr.bb[k];
+    block_sums<1>(v, sh);
+    if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
+    if (!grid_barrier(a.bar, a.status)) return;
+    double t[1];
+    grid_totals<1>(a.part, 0, t);
+    const double mean = t[0] / (double)n;
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (rr.i[k] < n) rr.bb[k] -= mean;
+    if (!grid_barrier(a.bar, a.status)) return;
+  }
+  int it = 0;
+  double bnorm2 = 0.0, rtrue2 = 0.0, rho = 0.0;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    // r = b - A x (x exchanged through a.x), u = M^-1 r
+    double ax[R];
+    row_apply<R>(rr, a, a.x, x, ax);
+    double v[2] = {0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const bool on = rr.i[k] < n;
+      r[k] = on ? rr.bb[k] - ax[k] : 0.0;
+      u[k] = rr.dnv[k] * r[k];
+      if (on) ubuf[rr.i[k]] = u[k];
+      v[0] += r[k] * r[k];
+      v[1] += rr.bb[k] * rr.bb[k];
+    }
+    block_sums<2>(v, sh);
+    if (threadIdx.x == 0) {
+      a.part[0 * nb + blockIdx.x] = v[0];
+      a.part[1 * nb + blockIdx.x] = v[1];
+    }
+    if (!grid_barrier(a.bar, a.status)) return;
+    double t2[2];
+    grid_totals<2>(a.part, 0, t2);
+    rtrue2 = t2[0];
+    bnorm2 = t2[1];
+    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax) break;
+    // w = A u
+    row_apply<R>(rr, a, ubuf, u, w);
+    double gamma_old = 1.0, alpha_old = 1.0;
+    bool first = true;
+    int parity = 0;
+    while (true) {
+      double* mb = parity ? mbuf1 : mbuf0;
+      double v3[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        v3[0] += r[k] * u[k];
+        v3[1] += w[k] * u[k];
+        v3[2] += r[k] * r[k];
+        m[k] = rr.dnv[k] * w[k];
+        if (rr.i[k] < n) mb[rr.i[k]] = m[k];
+      }
+      block_sums<3>(v3, sh);
+      const int slot = 2 + 3 * parity;
+      if (threadIdx.x == 0) {
+        a.part[(slot + 0) * nb + blockIdx.x] = v3[0];
+        a.part[(slot + 1) * nb + blockIdx.x] = v3[1];
+        a.part[(slot + 2) * nb + blockIdx.x] = v3[2];
+      }
+      if (!grid_barrier(a.bar, a.status)) return;
+      double t3[3];
+      grid_totals<3>(a.part, slot, t3);
+      const double gamma = t3[0], delta = t3[1];
+      rho = t3[2];
+      if (rho <= a.tol2 * bnorm2 || it >= a.itmax) break;
+      double nv[R];
+      row_apply<R>(rr, a, mb, m, nv);
+      double alpha, beta;
+      if (first) {
+        beta = 0.0;
+        alpha = gamma / delta;
+        first = false;
+      } else {
+        beta = gamma / gamma_old;
+        alpha = gamma / (delta - beta * gamma / alpha_old);
+      }
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (beta == 0.0) {
+          z[k] = nv[k]; q[k] = m[k]; s[k] = w[k]; p[k] = u[k];
+        } else {
+          z[k] = nv[k] + beta * z[k];
+          q[k] = m[k] + beta * q[k];
+          s[k] = w[k] + beta * s[k];
+          p[k] = u[k] + beta * p[k];
+        }
+        x[k] += alpha * p[k];
+        r[k] -= alpha * s[k];
+        u[k] -= alpha * q[k];
+        w[k] -= alpha * z[k];
+      }
+      gamma_old = gamma;
+      alpha_old = alpha;
+      parity ^= 1;
+      ++it;
+    }
+    // publish x for the explicit residual of the next attempt
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (rr.i[k] < n) a.x[rr.i[k]] = x[k];
+    if (!grid_barrier(a.bar, a.status)) return;
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k)
+    if (rr.i[k] < n) a.x[rr.i[k]] = x[k];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *a.out_iters = it;
+    a.out_d[0] = rtrue2;
+    a.out_d[1] = bnorm2;
+    a.out_d[2] = rtrue2;
+    a.counters[0] += 1;
+    a.counters[1] += it;
+  }
+}
+
 __global__ void k_any_nonzero(const double* v, int n, int* flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && v[i] != 0.0) atomicOr(flag, 1);
 }
 
 int g_pcg_blocks_per_sm = -1;
+int g_reg_blocks_per_sm[2] = {-1, -1};
 
 }  // namespace
 
@@ -361,8 +563,32 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
   a.out_d = c->sv.dstats + 3 * slot;
   a.counters = c->sv.counters;
   cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
-  void* args[] = {&a};
   KernelTimer kt(c, LV_KF_PCG);
+  // small systems: register-resident pipelined CG, one barrier per iteration
+  if (g_reg_blocks_per_sm[0] < 0) {
+    int b1 = 0, b2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_pcg_reg<1>, SP_TPB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_pcg_reg<2>, SP_TPB, 0);
+    g_reg_blocks_per_sm[0] = b1;
+    g_reg_blocks_per_sm[1] = b2;
+  }
+  for (int R = 1; R <= 2; ++R) {
+    const int per_sm = std::min(g_reg_blocks_per_sm[R - 1], 2);
+    if (per_sm < 1) continue;
+    const int cap_blocks = c->num_sms * per_sm;
+    const int need = lv_blocks(n, SP_TPB * R);
+    if (need > cap_blocks) continue;
+    double* ubuf = c->sv.tmp;
+    double* mb0 = c->sv.tmp + c->cap;
+    double* mb1 = c->sv.r + c->cap;  // second half of r (2*cap doubles)
+    void* rargs[] = {&a, &ubuf, &mb0, &mb1};
+    const void* fn = (R == 1) ? (const void*)k_pcg_reg<1> : (const void*)k_pcg_reg<2>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(std::max(need, 1)), dim3(SP_TPB), rargs, 0, c->stream);
+    c->launches++;
+    if (e != cudaSuccess) return lv_cuda_check(c, e, "k_pcg_reg cooperative launch");
+    return LV_OK;
+  }
+  void* args[] = {&a};
   cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(nblk), dim3(CG_TPB), args, 0, c->stream);
   c->launches++;
   if (e != cudaSuccess) return lv_cuda_check(c, e, "k_pcg cooperative launch");
