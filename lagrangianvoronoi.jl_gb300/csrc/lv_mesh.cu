@@ -199,6 +199,26 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 }
 
 // ---------------------------------------------------------------- clipping
+//
+// One thread per polygon (FP64 work is priced per warp instruction on this
+// GPU, so full warps of independent polygons use the FP64 pipe best).  The
+// polygon lives in shared memory in the reference's edge order.  Besides the
+// FP64 edges each slot keeps float offsets of both vertices from the seed
+// and a float upper bound of 4|v1 - x|^2, so that:
+//  * a candidate's fate is decided in float whenever that is provably
+//    exact: "cannot cut" (all vertices strictly inside the half-plane with a
+//    margin covering every rounding) is skipped, and vertex signs away from
+//    the bisector come from float; only vertices within the margin and the
+//    two crossing edges (whose intersection must be exact) are evaluated in
+//    FP64 with the reference's expressions;
+//  * the influence radius is an upper bound, which can only admit extra
+//    candidates that cannot cut (no-ops), and is replaced by the exact FP64
+//    value where the reference's "mesh destroyed" test needs it;
+//  * work is done in rounds: every thread first advances through its
+//    candidates with float/integer work until it meets one that may cut, then
+//    the warp performs the FP64 clips of that round together.
+// Any case the float path cannot certify (a clip with other than two
+// crossing edges) runs the reference's clip verbatim in FP64.
 
 constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
@@ -209,8 +229,11 @@ struct Poly {
   double* v2x;
   double* v2y;
   int* lab;
-  float* r32x;  // float copy of v1 - x, for the conservative prefilter
-  float* r32y;
+  float* r1x;  // v1 - x (float)
+  float* r1y;
+  float* r2x;  // v2 - x (float)
+  float* r2y;
+  float* d2;   // upper bound of 4 |v1 - x|^2
   int t;
   __device__ __forceinline__ int at(int k) const { return k * CLIP_TPB + t; }
 };
@@ -219,27 +242,63 @@ __device__ __forceinline__ int signum_eps(double f) {  // polygon.jl:9-16
   return (f < -LV_SIGNUM_EPS) ? -1 : ((f > LV_SIGNUM_EPS) ? 1 : 0);
 }
 
-__device__ __forceinline__ double jmax(double a, double b) { return (b > a) ? b : a; }
+// float upper bound of 4 (dx^2 + dy^2) for a float pair already rounded
+// from the FP64 offset (relative error <= 2^-24 each)
+__device__ __forceinline__ float d2_up(float dx, float dy) { return 4.0f * (dx * dx + dy * dy) * (1.0f + 1e-6f); }
 
-// polygon.jl:101-107
-__device__ double influence_rr(const Poly& P, int ne, double px, double py) {
+__device__ __forceinline__ void set_v1(const Poly& P, int k, double vx, double vy, double px, double py) {
+  const int a = P.at(k);
+  P.v1x[a] = vx;
+  P.v1y[a] = vy;
+  const float fx = (float)(vx - px), fy = (float)(vy - py);
+  P.r1x[a] = fx;
+  P.r1y[a] = fy;
+  P.d2[a] = d2_up(fx, fy);
+}
+
+__device__ __forceinline__ void set_v2(const Poly& P, int k, double vx, double vy, double px, double py) {
+  const int a = P.at(k);
+  P.v2x[a] = vx;
+  P.v2y[a] = vy;
+  P.r2x[a] = (float)(vx - px);
+  P.r2y[a] = (float)(vy - py);
+}
+
+__device__ __forceinline__ void copy_slot(const Poly& P, int dst, int src) {
+  const int a = P.at(dst), l = P.at(src);
+  P.v1x[a] = P.v1x[l];
+  P.v1y[a] = P.v1y[l];
+  P.v2x[a] = P.v2x[l];
+  P.v2y[a] = P.v2y[l];
+  P.lab[a] = P.lab[l];
+  P.r1x[a] = P.r1x[l];
+  P.r1y[a] = P.r1y[l];
+  P.r2x[a] = P.r2x[l];
+  P.r2y[a] = P.r2y[l];
+  P.d2[a] = P.d2[l];
+}
+
+__device__ __forceinline__ float prr_upper(const Poly& P, int ne) {
+  float m = 0.0f;
+  for (int k = 0; k < ne; ++k) m = fmaxf(m, P.d2[P.at(k)]);
+  return m;
+}
+
+// polygon.jl:101-107, exact
+__device__ double influence_rr_exact(const Poly& P, int ne, double px, double py) {
   double rr = 0.0;
   for (int k = 0; k < ne; ++k) {
-    double dx = P.v1x[P.at(k)] - px, dy = P.v1y[P.at(k)] - py;
-    rr = jmax(rr, 4.0 * (dx * dx + dy * dy));
+    const double dx = P.v1x[P.at(k)] - px, dy = P.v1y[P.at(k)] - py;
+    const double t = 4.0 * (dx * dx + dy * dy);
+    rr = (t > rr) ? t : rr;
   }
   return rr;
 }
 
-__device__ __forceinline__ void refresh_r32(const Poly& P, int k, double px, double py) {
-  P.r32x[P.at(k)] = (float)(P.v1x[P.at(k)] - px);
-  P.r32y[P.at(k)] = (float)(P.v1y[P.at(k)] - py);
-}
-
-// polygon.jl:51-97, with FastVector's swap-delete (fastvector.jl:44-50).
-// Returns 1 when a new edge was added, 0 otherwise, -1 on overflow.
-__device__ int clip_halfplane(const Poly& P, int& ne, double px, double py, double yx, double yy, int label,
-                               int& nev) {
+// polygon.jl:51-97 verbatim in FP64, with FastVector's swap-delete
+// (fastvector.jl:44-50).  Returns 1 when a new edge was added, 0 otherwise,
+// -1 on overflow; nev counts crossing events.
+__device__ int clip_exact(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, int& nev) {
   const double dfx = yx - px, dfy = yy - py;
   const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
   const double c = dfx * mx + dfy * my;
@@ -263,26 +322,13 @@ __device__ int clip_halfplane(const Poly& P, int& ne, double px, double py, doub
       Xy = inv * ty;
       if (s1 == 0) { Xx = a1x; Xy = a1y; }
       if (s2 == 0) { Xx = a2x; Xy = a2y; }
-      if (s1 == 1) {
-        P.v1x[a] = Xx;
-        P.v1y[a] = Xy;
-        refresh_r32(P, i, px, py);
-      } else {
-        P.v2x[a] = Xx;
-        P.v2y[a] = Xy;
-      }
+      if (s1 == 1)
+        set_v1(P, i, Xx, Xy, px, py);
+      else
+        set_v2(P, i, Xx, Xy, px, py);
     }
     if (1 <= s12) {
-      if (ne - 1 > i) {
-        const int l = P.at(ne - 1);
-        P.v1x[a] = P.v1x[l];
-        P.v1y[a] = P.v1y[l];
-        P.v2x[a] = P.v2x[l];
-        P.v2y[a] = P.v2y[l];
-        P.lab[a] = P.lab[l];
-        P.r32x[a] = P.r32x[l];
-        P.r32y[a] = P.r32y[l];
-      }
+      if (ne - 1 > i) copy_slot(P, i, ne - 1);
       --ne;
     } else {
       ++i;
@@ -292,36 +338,178 @@ __device__ int clip_halfplane(const Poly& P, int& ne, double px, double py, doub
   if (!ynull && !(Xx == Yx && Xy == Yy)) {
     if (ne >= ME) return -1;
     const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
-    const int a = P.at(ne);
     if (ax * by - ay * bx > 0.0) {
-      P.v1x[a] = Yx; P.v1y[a] = Yy; P.v2x[a] = Xx; P.v2y[a] = Xy;
+      set_v1(P, ne, Yx, Yy, px, py);
+      set_v2(P, ne, Xx, Xy, px, py);
     } else {
-      P.v1x[a] = Xx; P.v1y[a] = Xy; P.v2x[a] = Yx; P.v2y[a] = Yy;
+      set_v1(P, ne, Xx, Xy, px, py);
+      set_v2(P, ne, Yx, Yy, px, py);
     }
-    P.lab[a] = label;
-    refresh_r32(P, ne, px, py);
+    P.lab[P.at(ne)] = label;
     ++ne;
     return 1;
   }
   return 0;
 }
 
-// Conservative FP32 test: returns true only when the FP64 clip of this
-// candidate provably changes nothing, i.e. every vertex v of the polygon has
-// dot(y - x, v) - dot(y - x, (x + y)/2) < -SIGNUM_EPS in FP64.  d32 is the
-// float offset y - x (error <= g.delta32 per component), the vertices are
-// float offsets r = v - x (relative error 2^-24).  The bound covers the float
-// rounding of d and r, the float arithmetic, and the FP64 rounding of the
-// reference expression (which uses absolute coordinates up to g.bigm).
-__device__ __forceinline__ bool prefilter_no_cut(const Poly& P, int ne, float dx, float dy, float rmax,
+// Same result as clip_exact (bit for bit) for the common case of exactly two
+// crossing edges.  Returns 2 when it cannot certify the case (the caller then
+// runs clip_exact on the unchanged polygon), otherwise as clip_exact.
+//
+// Vertex signs: f32 = d.r - |d|^2/2 with d = float(y - x) and r the stored
+// float offset; the FP64 value f of the reference differs from the exact
+// value of f32's expression by at most 2^-24-relative rounding of d, r and
+// the float arithmetic (<= 1e-6 (D R + D^2) with D = |d|, R >= |r|) plus the
+// FP64 rounding of the reference expression in absolute coordinates
+// (<= 4e-15 D M, M = max |coordinate|), so |f32| > that margin + 2 eps
+// decides signum(f) exactly; otherwise f is evaluated in FP64.
+__device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm) {
+  const double dfx = yx - px, dfy = yy - py;
+  const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
+  const double c = dfx * mx + dfy * my;
+  const float dx = (float)dfx, dy = (float)dfy;
+  const float dd2 = dx * dx + dy * dy;
+  const float D = sqrtf(dd2) * 1.0001f;
+  float R = 0.0f;
+  for (int k = 0; k < ne; ++k) R = fmaxf(R, P.d2[P.at(k)]);
+  R = 0.5f * sqrtf(R) * 1.0001f;
+  const float margin = 1e-6f * (D * R + D * D) + 4e-15f * D * bigm + 1e-14f;
+  const float half = 0.5f * dd2;
+  // pre-pass: per-edge code 0 keep, 1 event-keep, 2 event-delete, 3 delete
+  unsigned long long code = 0ull;  // 2 bits per slot
+  int nev = 0;
+  int e0_slot = 0, e1_slot = 0, e0_s1 = 0, e0_s2 = 0, e1_s1 = 0, e1_s2 = 0;
+  double e0_f1 = 0.0, e0_f2 = 0.0, e1_f1 = 0.0, e1_f2 = 0.0;
+  for (int k = 0; k < ne; ++k) {
+    const int a = P.at(k);
+    const float g1 = dx * P.r1x[a] + dy * P.r1y[a] - half;
+    const float g2 = dx * P.r2x[a] + dy * P.r2y[a] - half;
+    int s1, s2;
+    double f1 = 0.0, f2 = 0.0;
+    bool exact1 = false, exact2 = false;
+    if (g1 < -margin) s1 = -1;
+    else if (g1 > margin) s1 = 1;
+    else { f1 = dfx * P.v1x[a] + dfy * P.v1y[a] - c; s1 = signum_eps(f1); exact1 = true; }
+    if (g2 < -margin) s2 = -1;
+    else if (g2 > margin) s2 = 1;
+    else { f2 = dfx * P.v2x[a] + dfy * P.v2y[a] - c; s2 = signum_eps(f2); exact2 = true; }
+    const int s12 = s1 + s2;
+    unsigned cd = 0;
+    if (0 <= s12 && s12 <= 1 && (s1 | s2) != 0) {
+      if (nev >= 2) return 2;
+      if (!exact1) f1 = dfx * P.v1x[a] + dfy * P.v1y[a] - c;
+      if (!exact2) f2 = dfx * P.v2x[a] + dfy * P.v2y[a] - c;
+      if (nev == 0) {
+        e0_slot = k; e0_s1 = s1; e0_s2 = s2; e0_f1 = f1; e0_f2 = f2;
+      } else {
+        e1_slot = k; e1_s1 = s1; e1_s2 = s2; e1_f1 = f1; e1_f2 = f2;
+      }
+      ++nev;
+      cd = (s12 >= 1) ? 2u : 1u;
+    } else if (s12 >= 1) {
+      cd = 3u;
+    }
+    code |= (unsigned long long)cd << (2 * k);
+  }
+  if (nev == 0) {
+    if (code != 0ull) return 2;  // deletions without crossings: degenerate
+    return 0;
+  }
+  if (nev != 2) return 2;
+  // intersection points of the two crossing edges (from their original data)
+  double X0x, X0y, X1x, X1y;
+  {
+    const int a = P.at(e0_slot);
+    const double a1x = P.v1x[a], a1y = P.v1y[a], a2x = P.v2x[a], a2y = P.v2y[a];
+    if (e0_s2 == 0) { X0x = a2x; X0y = a2y; }
+    else if (e0_s1 == 0) { X0x = a1x; X0y = a1y; }
+    else {
+      const double inv = 1.0 / (e0_f1 - e0_f2);
+      X0x = inv * (e0_f1 * a2x - e0_f2 * a1x);
+      X0y = inv * (e0_f1 * a2y - e0_f2 * a1y);
+    }
+  }
+  {
+    const int a = P.at(e1_slot);
+    const double a1x = P.v1x[a], a1y = P.v1y[a], a2x = P.v2x[a], a2y = P.v2y[a];
+    if (e1_s2 == 0) { X1x = a2x; X1y = a2y; }
+    else if (e1_s1 == 0) { X1x = a1x; X1y = a1y; }
+    else {
+      const double inv = 1.0 / (e1_f1 - e1_f2);
+      X1x = inv * (e1_f1 * a2x - e1_f2 * a1x);
+      X1y = inv * (e1_f1 * a2y - e1_f2 * a1y);
+    }
+  }
+  // the reference's sequential pass over the slots with swap-delete; the
+  // crossing identity (2 bits: 0 none, 1 first, 2 second in slot order)
+  // travels with its slot.
+  unsigned long long ident = (1ull << (2 * e0_slot)) | (2ull << (2 * e1_slot));
+  int visited_first = 0, visited_last = 0;  // crossing id (1 or 2) visited first / last
+  int fs0 = -1, fs1 = -1;                  // final slot of a kept crossing
+  int i = 0;
+  int nn = ne;
+  while (i < nn) {
+    const unsigned cd = (unsigned)((code >> (2 * i)) & 3ull);
+    const unsigned id = (unsigned)((ident >> (2 * i)) & 3ull);
+    if (id) {
+      if (visited_first == 0) visited_first = (int)id;
+      else visited_last = (int)id;
+    }
+    if (cd >= 2u) {
+      if (nn - 1 > i) {
+        copy_slot(P, i, nn - 1);
+        const unsigned long long lastc = (code >> (2 * (nn - 1))) & 3ull;
+        const unsigned long long lasti = (ident >> (2 * (nn - 1))) & 3ull;
+        code = (code & ~(3ull << (2 * i))) | (lastc << (2 * i));
+        ident = (ident & ~(3ull << (2 * i))) | (lasti << (2 * i));
+      }
+      --nn;
+    } else {
+      if (id == 1) fs0 = i;
+      if (id == 2) fs1 = i;
+      ++i;
+    }
+  }
+  if (fs0 >= 0) {
+    if (e0_s1 == 1) set_v1(P, fs0, X0x, X0y, px, py);
+    else set_v2(P, fs0, X0x, X0y, px, py);
+  }
+  if (fs1 >= 0) {
+    if (e1_s1 == 1) set_v1(P, fs1, X1x, X1y, px, py);
+    else set_v2(P, fs1, X1x, X1y, px, py);
+  }
+  ne = nn;
+  // new edge from X = the crossing visited last, Y = the one visited first
+  const double Xx = (visited_last == 1) ? X0x : X1x, Xy = (visited_last == 1) ? X0y : X1y;
+  const double Yx = (visited_first == 1) ? X0x : X1x, Yy = (visited_first == 1) ? X0y : X1y;
+  if (Xx == Yx && Xy == Yy) return 0;
+  if (ne >= ME) return -1;
+  const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
+  if (ax * by - ay * bx > 0.0) {
+    set_v1(P, ne, Yx, Yy, px, py);
+    set_v2(P, ne, Xx, Xy, px, py);
+  } else {
+    set_v1(P, ne, Xx, Xy, px, py);
+    set_v2(P, ne, Yx, Yy, px, py);
+  }
+  P.lab[P.at(ne)] = label;
+  ++ne;
+  return 1;
+}
+
+// Conservative float test: true only when the FP64 clip by this candidate
+// provably changes nothing (every vertex strictly inside the half-plane by
+// more than the rounding margin).  d32 = float(q) - float(x) carries an
+// absolute error <= g.delta32 per component.
+__device__ __forceinline__ bool prefilter_no_cut(const Poly& P, int ne, float dx, float dy, float prr_up,
                                                  const GridDev& g) {
   const float d2 = dx * dx + dy * dy;
   const float D = sqrtf(d2) + 2.0f * g.delta32;
-  const float R = rmax * 1.0001f;
+  const float R = 0.5f * sqrtf(prr_up) * 1.0001f;
   const float margin = 2.0f * g.delta32 * (R + 2.0f * D) + 4e-6f * (D * R + D * D) + 4e-15f * D * g.bigm + 1e-14f;
   const float half = 0.5f * d2;
   for (int k = 0; k < ne; ++k) {
-    const float f = dx * P.r32x[P.at(k)] + dy * P.r32y[P.at(k)] - half;
+    const float f = dx * P.r1x[P.at(k)] + dy * P.r1y[P.at(k)] - half;
     if (!(f < -margin)) return false;
   }
   return true;
@@ -336,11 +524,9 @@ __device__ __forceinline__ void get_arrow(const GridDev& g, double ax, double ay
   if (g.yper && fabs(vy) > 0.5 * g.yperiod) vy -= (vy > 0 ? 1.0 : -1.0) * g.yperiod;
 }
 
-__device__ __forceinline__ bool veq_bits(double a, double b) { return a == b; }
-
 __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
                                                    const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
-                                                   int* status, int use_prefilter) {
+                                                   int* status) {
   extern __shared__ double smem[];
   const int t = threadIdx.x;
   const int i = blockIdx.x * CLIP_TPB + t;
@@ -350,101 +536,115 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
   P.v2x = P.v1y + ME * CLIP_TPB;
   P.v2y = P.v2x + ME * CLIP_TPB;
   P.lab = reinterpret_cast<int*>(P.v2y + ME * CLIP_TPB);
-  P.r32x = reinterpret_cast<float*>(P.lab + ME * CLIP_TPB);
-  P.r32y = P.r32x + ME * CLIP_TPB;
+  P.r1x = reinterpret_cast<float*>(P.lab + ME * CLIP_TPB);
+  P.r1y = P.r1x + ME * CLIP_TPB;
+  P.r2x = P.r1y + ME * CLIP_TPB;
+  P.r2y = P.r2x + ME * CLIP_TPB;
+  P.d2 = P.r2y + ME * CLIP_TPB;
   P.t = t;
-  if (i >= n) return;
+  const bool active = i < n;
 
-  const double2 xi = x[i];
-  const double px = xi.x, py = xi.y;
-  // reset! (polygon.jl:37-47): the cropping rectangle, edges B->A, A->D, D->C, C->B
-  {
+  double px = 0.0, py = 0.0;
+  int ne = 0;
+  if (active) {
+    const double2 xi = x[i];
+    px = xi.x;
+    py = xi.y;
+    // reset! (polygon.jl:37-47): the cropping rectangle, edges B->A, A->D, D->C, C->B
     const double Ax = g.cminx, Ay = g.cminy, Cx = g.cmaxx, Cy = g.cmaxy;
     const double Bx = Cx, By = Ay, Dx = Ax, Dy = Cy;
-    const double e1[4][4] = {{Bx, By, Ax, Ay}, {Ax, Ay, Dx, Dy}, {Dx, Dy, Cx, Cy}, {Cx, Cy, Bx, By}};
-    const int labs[4] = {LV_BDARY_DOWN, LV_BDARY_LEFT, LV_BDARY_UP, LV_BDARY_RIGHT};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int a = P.at(k);
-      P.v1x[a] = e1[k][0];
-      P.v1y[a] = e1[k][1];
-      P.v2x[a] = e1[k][2];
-      P.v2y[a] = e1[k][3];
-      P.lab[a] = labs[k];
-      refresh_r32(P, k, px, py);
+    set_v1(P, 0, Bx, By, px, py); set_v2(P, 0, Ax, Ay, px, py); P.lab[P.at(0)] = LV_BDARY_DOWN;
+    set_v1(P, 1, Ax, Ay, px, py); set_v2(P, 1, Dx, Dy, px, py); P.lab[P.at(1)] = LV_BDARY_LEFT;
+    set_v1(P, 2, Dx, Dy, px, py); set_v2(P, 2, Cx, Cy, px, py); P.lab[P.at(2)] = LV_BDARY_UP;
+    set_v1(P, 3, Cx, Cy, px, py); set_v2(P, 3, Bx, By, px, py); P.lab[P.at(3)] = LV_BDARY_RIGHT;
+    ne = 4;
+  }
+  int flag = 0;
+  bool done = !active;
+  long long k1 = 0, k2 = 0;
+  if (active) {
+    const double f1 = floor((px - g.ox) / g.h), f2 = floor((py - g.oy) / g.h);
+    if (!(fabs(f1) < 1e15) || !(fabs(f2) < 1e15)) {
+      flag = LV_FLAG_NONFINITE;
+      done = true;
+    } else {
+      k1 = (long long)f1 + 1;
+      k2 = (long long)f2 + 1;
     }
   }
-  int ne = 4;
-  int flag = 0;
-  double prr = influence_rr(P, ne, px, py);
-  const double dxo = px - g.ox, dyo = py - g.oy;
-  const double f1 = floor(dxo / g.h), f2 = floor(dyo / g.h);
-  if (!(fabs(f1) < 1e15) || !(fabs(f2) < 1e15)) {
-    flag = LV_FLAG_NONFINITE;
-  } else {
-    const long long k1 = (long long)f1 + 1, k2 = (long long)f2 + 1;
-    // The float prefilter assumes the polygon's edges form a closed chain, so
-    // that the v1 vertices are all the vertices.  A clip with other than
-    // exactly two crossing events (degenerate input) can open the chain; the
-    // prefilter is then switched off for this polygon.
-    bool chain_ok = true;
-    const float x32 = (float)px, y32 = (float)py;
-    const float xp32 = (float)g.xperiod, yp32 = (float)g.yperiod;
-    // voronoigrid.jl:53-81
-    for (int pn = 0; pn < g.npath; ++pn) {
-      const double rr = path[pn].rr;
-      if (rr > prr) break;
-      if (rr > g.rr_max) {
-        flag = LV_FLAG_MESH_DESTROYED;
-        break;
-      }
-      const long long c1 = k1 + path[pn].di1, c2 = k2 + path[pn].di2;
-      if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) continue;
-      const int cell = (int)((c1 - 1) + (long long)g.n1 * (c2 - 1));
-      const int sa = cl.cstart[cell], sb = cl.cstart[cell + 1];
-      for (int s = sa; s < sb; ++s) {
-        const int j = cl.citem[s];
-        if (j == i) continue;  // y == x exactly: get_arrow(x, x) = 0
-        if (use_prefilter && chain_ok) {
-          const float2 q32 = cl.cpos[s];
-          float ddx = q32.x - x32, ddy = q32.y - y32;
-          bool far_image = false;
-          if (g.xper) {
-            if (fabsf(ddx) > 0.45f * xp32) far_image = true;
-          }
-          if (g.yper) {
-            if (fabsf(ddy) > 0.45f * yp32) far_image = true;
-          }
-          if (!far_image) {
-            // distance test norm_squared(x - y) > prr, decided in float when unambiguous
-            const float d2 = ddx * ddx + ddy * ddy;
-            const float dd = sqrtf(d2);
-            const float prr32 = (float)prr;
-            const float lo = d2 * (1.0f - 1e-6f) - 4.0f * g.delta32 * dd - 4.0f * g.delta32 * g.delta32;
-            if (lo > prr32 * (1.0f + 1e-6f)) continue;
-            const float rmax = 0.5f * sqrtf(prr32) * (1.0f + 1e-6f);
-            if (prefilter_no_cut(P, ne, ddx, ddy, rmax, g)) continue;
-          }
-        }
-        const double2 xq = x[j];
-        double vx, vy;
-        get_arrow(g, xq.x, xq.y, px, py, vx, vy);
-        const double yx = px + vx, yy = py + vy;
-        if (veq_bits(px, yx) && veq_bits(py, yy)) continue;
-        const double ex = px - yx, ey = py - yy;
-        if (ex * ex + ey * ey > prr) continue;
-        int nev = 0;
-        const int r = clip_halfplane(P, ne, px, py, yx, yy, j, nev);
-        if (nev != 0 && !(r == 1 && nev == 2)) chain_ok = false;
-        if (r < 0) {
-          flag = LV_FLAG_EDGE_OVERFLOW;
+  const float x32 = (float)px, y32 = (float)py;
+  const float xp32 = (float)g.xperiod, yp32 = (float)g.yperiod;
+  float prr_up = active ? prr_upper(P, ne) : 0.0f;
+  bool chain_ok = true;
+  int pn = -1, s = 0, se = 0;
+  // voronoigrid.jl:53-81, in rounds
+  while (true) {
+    bool have = false;
+    int cj = 0;
+    while (!done && !have) {
+      if (s >= se) {
+        ++pn;
+        if (pn >= g.npath) {
+          done = true;
           break;
         }
-        if (r) prr = influence_rr(P, ne, px, py);
+        const double rr = path[pn].rr;
+        if ((float)rr > prr_up) {  // prr_up >= prr: never earlier than the reference
+          done = true;
+          break;
+        }
+        if (rr > g.rr_max) {
+          // the reference stops here if rr > prr, and throws otherwise
+          if (!(rr > influence_rr_exact(P, ne, px, py))) flag = LV_FLAG_MESH_DESTROYED;
+          done = true;
+          break;
+        }
+        const long long c1 = k1 + path[pn].di1, c2 = k2 + path[pn].di2;
+        if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) {
+          s = se = 0;
+          continue;
+        }
+        const int cell = (int)((c1 - 1) + (long long)g.n1 * (c2 - 1));
+        s = cl.cstart[cell];
+        se = cl.cstart[cell + 1];
+        continue;
       }
-      if (flag) break;
+      const int j = cl.citem[s];
+      const float2 q32 = cl.cpos[s];
+      ++s;
+      if (j == i) continue;  // y == x exactly: get_arrow(x, x) = 0
+      const float ddx = q32.x - x32, ddy = q32.y - y32;
+      const bool far_image = (g.xper && fabsf(ddx) > 0.45f * xp32) || (g.yper && fabsf(ddy) > 0.45f * yp32);
+      if (!far_image) {
+        const float d2 = ddx * ddx + ddy * ddy;
+        const float lo = d2 * (1.0f - 1e-6f) - 4.0f * g.delta32 * sqrtf(d2) - 4.0f * g.delta32 * g.delta32;
+        if (lo > prr_up * (1.0f + 1e-6f)) continue;  // farther than the influence radius: cannot cut
+        if (chain_ok && prefilter_no_cut(P, ne, ddx, ddy, prr_up, g)) continue;
+      }
+      have = true;
+      cj = j;
+    }
+    if (!__any_sync(0xffffffffu, have)) break;
+    if (have) {
+      const double2 xq = x[cj];
+      double vx, vy;
+      get_arrow(g, xq.x, xq.y, px, py, vx, vy);
+      const double yx = px + vx, yy = py + vy;
+      int r = 2;
+      if (chain_ok) r = clip_fast(P, ne, px, py, yx, yy, cj, g.bigm);
+      if (r == 2) {
+        int nev = 0;
+        r = clip_exact(P, ne, px, py, yx, yy, cj, nev);
+        if (nev != 0 && !(r == 1 && nev == 2)) chain_ok = false;
+      }
+      if (r < 0) {
+        flag = LV_FLAG_EDGE_OVERFLOW;
+        done = true;
+      }
+      prr_up = prr_upper(P, ne);
     }
   }
+  if (!active) return;
   if (flag) atomicOr(status, flag);
 
   // sort_edges! (IO.jl:35-48)
@@ -544,7 +744,7 @@ int lv_mesh_remesh(lv_ctx* c) {
   k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap);
   LV_LAUNCH_CHECK(c, "k_bin_order");
   }
-  const size_t smem = (size_t)ME * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 2 * sizeof(float));
+  const size_t smem = (size_t)ME * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 5 * sizeof(float));
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -552,7 +752,7 @@ int lv_mesh_remesh(lv_ctx* c) {
   }
   {
     KernelTimer kt(c, LV_KF_CLIP);
-    k_clip<<<lv_blocks(n, CLIP_TPB), CLIP_TPB, smem, s>>>(c->g, c->path, c->s.x, n, c->c, c->m, c->status, 1);
+    k_clip<<<lv_blocks(n, CLIP_TPB), CLIP_TPB, smem, s>>>(c->g, c->path, c->s.x, n, c->c, c->m, c->status);
     LV_LAUNCH_CHECK(c, "k_clip");
   }
   c->meshed = true;
