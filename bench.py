@@ -144,16 +144,58 @@ def setup_grid(lv, fl):
     return g
 
 
-def gpu_step(lv, g, solver, fl):
+def gpu_step(lv, g, solver, fl, snapshot=False, stats=False):
     dt = fl.dt
     lv.move(g, dt)
     lv.stiffened_eos(g, fl.gamma, fl.P0)
-    lv.find_pressure(solver, dt, 10, stats=False)
+    st = lv.find_pressure(solver, dt, 10, stats=stats)
+    if snapshot:
+        L = lv._lib.load()
+        assert L.lv_learn_add_system(g._ctx) == 0
     lv.pressure_step(g, dt)
     lv.find_D(g)
     lv.viscous_step(g, dt, fl.artificial_viscosity)
     lv.find_dv(g, dt)
     lv.relaxation_step(g, dt)
+    return st
+
+
+def solver_comparison(lv, L, g, fl, steps, train_info):
+    """Pressure solve of the same workload with each solver: device ms of the
+    solve kernels (+ operator/RHS/factor kernels) and CG iterations per step."""
+    fam = lv._lib.KERNEL_FAMILIES
+    out = {}
+    for method in ("jacobi_pcg", "mixed_ir", "learned_pcg"):
+        solver = lv.PressureSolver(g, method=method, tol=1e-8)
+        gpu_step(lv, g, solver, fl)  # settle
+        g.synchronize()
+        L.lv_kernel_timing(g._ctx, 1)
+        for f in fam.values():
+            L.lv_kernel_time(g._ctx, f, None, None, 1)
+        s0, i0 = C.c_int64(), C.c_int64()
+        L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
+        fallbacks = 0
+        for _ in range(steps):
+            st = gpu_step(lv, g, solver, fl, stats=True)
+            fallbacks += sum(1 for rec in st if method == "learned_pcg" and rec[3] != 2)
+        s1, i1 = C.c_int64(), C.c_int64()
+        L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
+        ms = {}
+        for name, f in fam.items():
+            nl, t = C.c_int64(), C.c_double()
+            L.lv_kernel_time(g._ctx, f, C.byref(nl), C.byref(t), 1)
+            ms[name] = t.value
+        L.lv_kernel_timing(g._ctx, 0)
+        out[method] = {"solve_ms_per_step": (ms["pcg"] + ms["rhs"]) / steps,
+                       "pcg_kernel_ms_per_step": ms["pcg"] / steps,
+                       "cg_iters_per_step": (i1.value - i0.value) / steps}
+        if method == "learned_pcg":
+            out[method]["fallbacks_to_jacobi"] = fallbacks
+    out["learned_pcg"]["training"] = train_info
+    j, lrn = out["jacobi_pcg"], out["learned_pcg"]
+    out["learned_vs_plain"] = {"iteration_ratio": j["cg_iters_per_step"] / max(lrn["cg_iters_per_step"], 1e-9),
+                               "solve_time_ratio": j["solve_ms_per_step"] / max(lrn["solve_ms_per_step"], 1e-9)}
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -166,9 +208,19 @@ def run_ours(args, world, rank, local):
     solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
     stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
+    # warm-up steps also snapshot the pressure operators the learned
+    # preconditioner is trained on (the solver's own systems)
     for _ in range(args.warmup):
-        gpu_step(lv, g, solver, fl)
+        gpu_step(lv, g, solver, fl, snapshot=True)
     g.synchronize()
+    t_tr = time.perf_counter()
+    train_steps = 300
+    losses = np.zeros(train_steps, np.float32)
+    assert L.lv_learn_init(g._ctx, 1234) == 0
+    assert L.lv_learn_train(g._ctx, train_steps, 3e-3, 4, 99, losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps, "probes": 4,
+                  "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
+                  "loss_last": float(losses[-10:].mean())}
 
     # ---- timed region: K steps, device time from events on the library's stream,
     # an L2 flush (512 MiB write) between steps outside the events
@@ -236,6 +288,7 @@ def run_ours(args, world, rank, local):
     g.synchronize()
     e2e_s = allmax(world, time.perf_counter() - t0)
 
+    comparison = solver_comparison(lv, L, g, fl, 3, train_info) if not args.no_compare else None
     if rank != 0:
         return None
     value = world * N * args.steps / (max_ms / 1e3)
@@ -279,7 +332,7 @@ def run_ours(args, world, rank, local):
                    "l2": "512 MiB buffer written between timed steps (state ~15 MB fits in L2)"},
         "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1]) / args.steps,
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
-                     "solves": solves},
+                     "solves": solves, "solvers": comparison},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},
         "roofline": {"kernel": "k_pcg" if dom == "pcg" else "k_clip", "bound": "hbm", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
@@ -375,6 +428,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()

@@ -148,7 +148,7 @@ int lv_relaxation_step(lv_ctx* ctx, double dt, int32_t rusanov);      /* relaxat
 int lv_set_solver(lv_ctx* ctx, int32_t method, double tol, int32_t itmax);
 /* find_pressure!(solver, dt, niter; boundary_velocity) (pressure.jl:215-224).
  * vbc[4][2] (constant boundary velocity per label) may be NULL (zero_vbc).
- * stats[niter] may be NULL; when given, the call synchronises. */
+ * niter <= 31.  stats[niter] may be NULL; when given, the call synchronises. */
 int lv_find_pressure(lv_ctx* ctx, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats);
 /* Pieces of find_pressure! for inspection: PressureOperator refresh!
  * (pressure.jl:104-117) into the device CSR; solver refresh! (pressure.jl:162-203). */
@@ -186,6 +186,34 @@ int lv_operator_apply(lv_ctx* ctx, const double* x, double* y);
 int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t* rowptr, const int32_t* col, const double* w,
                          const double* b, double* x, double tol, int32_t itmax, void* stream, int32_t* iterations,
                          double* rel_residual);
+
+/* Learned preconditioner (LV_METHOD_LEARNED_PCG).  A 3-layer message-passing
+ * network (hidden width 32, BF16 tensor-core matrix products, FP32
+ * accumulation) maps the assembled operator to a sparse factor G on the
+ * pattern of its lower triangle; the inner CG of the mixed-precision solver
+ * is preconditioned by M^-1 = D^-1/2 (G^T G + eps I) D^-1/2 (SPD).  The
+ * network is trained on systems snapshot from the solver itself by
+ * hand-written forward/backward kernels and Adam, minimising a stochastic
+ * estimate of ||G A~ G^T - I||_F^2 / n (A~ = D^-1/2 A D^-1/2).  A learned
+ * solve that needs more iterations than the last Jacobi solve falls back to
+ * Jacobi (stats.method reports the method used). */
+int lv_learn_init(lv_ctx* ctx, uint64_t seed);                  /* random initialisation */
+int32_t lv_learn_num_params(void);
+int lv_learn_get_params(lv_ctx* ctx, float* out);
+int lv_learn_set_params(lv_ctx* ctx, const float* in);
+int lv_learn_add_system(lv_ctx* ctx);                          /* snapshot the assembled operator */
+int32_t lv_learn_num_systems(lv_ctx* ctx);
+int lv_learn_clear_systems(lv_ctx* ctx);
+/* Adam on the snapshot systems (round robin), `probes` Rademacher probes per
+ * step; losses[steps] may be NULL. */
+int lv_learn_train(lv_ctx* ctx, int32_t steps, float lr, int32_t probes, uint64_t seed, float* losses);
+/* Loss and gradient for system `sys` (< 0: the assembled operator), with the
+ * given probes[K][n] or Rademacher probes from seed; grad[num_params] may be NULL. */
+int lv_learn_loss_grad(lv_ctx* ctx, int32_t sys, const float* probes, int32_t K, uint64_t seed, double* loss,
+                       float* grad);
+/* Factor of the assembled operator: gdiag[n], glower[nnz] (CSR positions with
+ * col < row, zero elsewhere) and the node features[n][16]; any may be NULL. */
+int lv_learn_factor(lv_ctx* ctx, float* gdiag, float* glower, float* features);
 
 /* MultiphaseSolver / multiphase_projection! (relaxation.jl:137-206). */
 int lv_multiphase_projection(lv_ctx* ctx, double quality_threshold, lv_solve_stats* stats);

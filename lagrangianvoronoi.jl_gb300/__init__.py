@@ -281,15 +281,16 @@ class PressureSolver:
 
 def find_pressure(solver, dt, niter=10, boundary_velocity=None, stats=True):
     """find_pressure!(solver, dt, niter; boundary_velocity) (src/pressure.jl:215-224).
-    Returns per-sweep (iterations, converged, rel_residual) when stats=True
-    (which synchronises); stats=False queues the work and returns None."""
+    Returns per-sweep (iterations, converged, rel_residual, method used,
+    refinement steps) when stats=True (which synchronises); stats=False
+    queues the work and returns None."""
     g = solver.grid
     solver.configure()
     vbc = wall_velocity_table(boundary_velocity)
     if stats:
         st = (LvSolveStats * niter)()
         _check(g, _lib.load().lv_find_pressure(g._ctx, float(dt), int(niter), _lib.ptr(vbc), st))
-        solver.last_stats = [(s.iterations, bool(s.converged), s.rel_residual) for s in st]
+        solver.last_stats = [(s.iterations, bool(s.converged), s.rel_residual, s.method, s.outer) for s in st]
         if solver.verbose:
             print(solver.last_stats)
         return solver.last_stats

@@ -81,6 +81,17 @@ SIGNATURES = {
     "lv_kernel_timing": (C.c_int, [_vp, _i32]),
     "lv_kernel_time": (C.c_int, [_vp, _i32, _pi64, _pd, _i32]),
     "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
+    "lv_learn_init": (C.c_int, [_vp, C.c_uint64]),
+    "lv_learn_num_params": (_i32, []),
+    "lv_learn_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "lv_learn_set_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "lv_learn_add_system": (C.c_int, [_vp]),
+    "lv_learn_num_systems": (_i32, [_vp]),
+    "lv_learn_clear_systems": (C.c_int, [_vp]),
+    "lv_learn_train": (C.c_int, [_vp, _i32, C.c_float, _i32, C.c_uint64, C.POINTER(C.c_float)]),
+    "lv_learn_loss_grad": (C.c_int, [_vp, _i32, C.POINTER(C.c_float), _i32, C.c_uint64, _pd,
+                                     C.POINTER(C.c_float)]),
+    "lv_learn_factor": (C.c_int, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "lv_pcg_solve_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i32, _vp, _pi32, _pd]),
 }
 KERNEL_FAMILIES = {"bin": 0, "clip": 1, "pcg": 2, "rhs": 3, "ops": 4}

@@ -20,6 +20,7 @@ UNITS = {
     "lv_mesh.cu": ["--fmad=false"],
     "lv_physics.cu": ["--fmad=false"],
     "lv_solver.cu": [],
+    "lv_learn.cu": [],
 }
 
 

@@ -279,7 +279,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.part = dalloc<double>(c, 8 * 4096, &ok);
   sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);
-  sv.iters = dalloc<int>(c, 64, &ok);
+  sv.iters = dalloc<int>(c, LV_IT_SIZE, &ok);
   sv.dstats = dalloc<double>(c, 3 * 64, &ok);
   c->status = dalloc<int>(c, 1, &ok);
   c->path = dalloc<PathNodeDev>(c, c->path_host.size(), &ok);
@@ -297,6 +297,7 @@ int lv_destroy(lv_ctx* c) {
   if (!c) return LV_OK;
   cudaSetDevice(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  lv_learn_free(c);
   for (void* p : c->allocs) cudaFree(p);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -623,7 +624,7 @@ int lv_pressure_rhs(lv_ctx* c, double dt, int32_t gp_step, const double* vbc) {
 }
 
 int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
-  if (!c || niter < 0 || niter > 63) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 63]");
+  if (!c || niter < 0 || niter > 31) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 31]");
   Timer t(c, 2);
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;

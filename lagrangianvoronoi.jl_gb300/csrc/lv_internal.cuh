@@ -22,6 +22,15 @@
 
 #define LV_SIGNUM_EPS (2.0 * 2.220446049250313e-16) /* polygon.jl:2 */
 
+// Layout of the device int array SolverDev::iters (per-solve statistics of
+// one find_pressure call, slot = sweep index < 32, and solver flags).
+#define LV_IT_ITERS 0          // [32] inner/CG iterations per slot
+#define LV_IT_OUTER 32         // [32] refinement steps per slot
+#define LV_IT_METHOD 64        // [32] method used per slot (learned solves)
+#define LV_IT_JREF 96          // iterations of the last Jacobi mixed solve
+#define LV_IT_NONSINGULAR 97   // set when some diagonal term is nonzero
+#define LV_IT_SIZE 128
+
 // Status bits set on the device with atomicOr; decoded on the host.
 #define LV_FLAG_NAN_VELOCITY 0x1
 #define LV_FLAG_MESH_DESTROYED 0x2
@@ -93,6 +102,8 @@ struct SolverDev {
   int64_t nnz_cap;
 };
 
+struct LearnState;  // learned preconditioner (lv_learn.cu)
+
 struct lv_ctx {
   lv_params prm;
   GridDev g;
@@ -114,6 +125,10 @@ struct lv_ctx {
   double tol = 1e-8;
   int itmax = 10000;
   bool op_ready = false;
+  double* mp_buf = nullptr;  // multiphase projection vectors (allocated on first use)
+  LearnState* learn = nullptr;
+  bool factor_valid = false;  // learned factor matches the assembled operator and parameters
+  float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
   // timings
@@ -159,6 +174,11 @@ int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
 int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc);
 int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
+
+// ---- learned preconditioner (lv_learn.cu)
+int lv_learn_factor_current(lv_ctx* c);
+void lv_learn_factor_ptrs(lv_ctx* c, const float** gd, const float** gl, const float** dh, const int** rev);
+void lv_learn_free(lv_ctx* c);
 
 // ---- solver (lv_solver.cu)
 int lv_solver_assemble(lv_ctx* c, double dt);

@@ -1,0 +1,981 @@
+// Learned preconditioner for the pressure solve: a message-passing network
+// over the Voronoi adjacency graph that emits a sparse factor G on the
+// pattern of the lower triangle of the pressure operator, so that
+//     M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2,   G = Gt D^-1/2
+// is SPD (D = diagonal of the operator).  The network works on the
+// Jacobi-normalised operator At = D^-1/2 A D^-1/2 = I - What:
+//
+//   X     node features [1, diag/adiag, sum_j what_ij, max_j what_ij, deg/8, 0...] (16)
+//   H1    = relu([X,  Agg X ] W0 + b0)            Agg(H)_i = sum_j what_ij H_j
+//   H2    = H1 + relu([H1, Agg H1] W1 + b1)
+//   H3    = H2 + relu([H2, Agg H2] W2 + b2)        (3 layers, hidden width 32)
+//   Gt_ii = 1 + H3_i . rd
+//   Gt_ij = what_ij sum_c ro_c H3_ic H3_jc          for j < i, j ~ i
+//
+// The matrix products of the layers (forward [N x 32|64] x [32|64 x 32],
+// backward dX = dZ W^T and dW = X^T dZ) run on the tensor cores as
+// mma.sync m16n8k16 with BF16 operands and FP32 accumulation; everything else
+// is FP32.  Training minimises a Hutchinson estimate of
+//     || Gt At Gt^T - I ||_F^2 / N = E_z || Gt At Gt^T z - z ||^2 / N,
+// z Rademacher, whose gradient with respect to each entry (a, b) of Gt is
+// 2 (r_a t_b + z_a s_b), r = Gt At Gt^T z - z, t = At Gt^T z, s = At Gt^T r.
+// Backward kernels are written by hand; Adam updates the FP32 master weights.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "lv_internal.cuh"
+
+namespace {
+
+constexpr int HID = 32;
+constexpr int FIN = 16;
+constexpr int KC0 = 2 * FIN;  // 32
+constexpr int KC = 2 * HID;   // 64
+constexpr int OFF_W0 = 0;
+constexpr int OFF_B0 = OFF_W0 + KC0 * HID;
+constexpr int OFF_W1 = OFF_B0 + HID;
+constexpr int OFF_B1 = OFF_W1 + KC * HID;
+constexpr int OFF_W2 = OFF_B1 + HID;
+constexpr int OFF_B2 = OFF_W2 + KC * HID;
+constexpr int OFF_RD = OFF_B2 + HID;
+constexpr int OFF_RO = OFF_RD + HID;
+constexpr int NPARAM = OFF_RO + HID;
+constexpr int WBF_W0 = 0, WBF_W1 = KC0 * HID, WBF_W2 = KC0 * HID + KC * HID, NWBF = KC0 * HID + 2 * KC * HID;
+constexpr int LTPB = 128;  // 4 warps, 16 rows each per tile
+constexpr int MAXPROBES = 8;
+constexpr int PART_BLOCKS = 304;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat16 a = __float2bfloat16_rn(lo), b = __float2bfloat16_rn(hi);
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// D(16x8, f32) += A(16x16, bf16, row) * B(16x8, bf16, col)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float bf(const __nv_bfloat16* w, int idx) { return __bfloat162float(w[idx]); }
+
+// ---------------------------------------------------------------- preparation
+
+__global__ void k_lprep_dh(int n, const double* __restrict__ adiag, float* dh) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dh[i] = (float)(1.0 / sqrt(adiag[i]));
+}
+
+// what_k = w_k dh_i dh_j; rev_k = position of (j, i) in row j; node features.
+__global__ void k_lprep(int n, const int* __restrict__ rowptr, const int* __restrict__ col, const double* __restrict__ w,
+                        const double* __restrict__ diag, const double* __restrict__ adiag,
+                        const float* __restrict__ dh, float* what, int* rev, float* X) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int a = rowptr[i], b = rowptr[i + 1];
+  float s = 0.f, m = 0.f;
+  for (int k = a; k < b; ++k) {
+    const int j = col[k];
+    const float v = (float)w[k] * dh[i] * dh[j];
+    what[k] = v;
+    s += v;
+    m = fmaxf(m, v);
+    int r = -1;
+    for (int t = rowptr[j]; t < rowptr[j + 1]; ++t)
+      if (col[t] == i) {
+        r = t;
+        break;
+      }
+    rev[k] = r;
+  }
+  float* x = X + (size_t)i * FIN;
+  x[0] = 1.f;
+  x[1] = (float)(diag[i] / adiag[i]);
+  x[2] = s;
+  x[3] = m;
+  x[4] = (float)(b - a) * 0.125f;
+#pragma unroll
+  for (int f = 5; f < FIN; ++f) x[f] = 0.f;
+}
+
+// ---------------------------------------------------------------- forward
+
+// Fills the warp's A tile [16][2KH] (FP32, shared): own rows of Hin and
+// Agg(Hin) = sum_k what_k Hin[col_k].  Lane l handles row l & 15 and half
+// (l >> 4) of the features.
+template <int KH>
+__device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict__ Hin, const int* __restrict__ rowptr,
+                          const int* __restrict__ col, const float* __restrict__ what) {
+  const int lane = threadIdx.x & 31;
+  const int r = lane & 15, half = lane >> 4;
+  const int row = row0 + r;
+  constexpr int FH = KH / 2;
+  float agg[FH];
+#pragma unroll
+  for (int f = 0; f < FH; ++f) agg[f] = 0.f;
+  float own[FH];
+#pragma unroll
+  for (int f = 0; f < FH; ++f) own[f] = 0.f;
+  if (row < n) {
+    const float* hr = Hin + (size_t)row * KH + half * FH;
+#pragma unroll
+    for (int f = 0; f < FH; ++f) own[f] = hr[f];
+    for (int k = rowptr[row]; k < rowptr[row + 1]; ++k) {
+      const float wv = what[k];
+      const float* hj = Hin + (size_t)col[k] * KH + half * FH;
+#pragma unroll
+      for (int f = 0; f < FH; ++f) agg[f] = fmaf(wv, hj[f], agg[f]);
+    }
+  }
+  float* t = tile + r * (2 * KH);
+#pragma unroll
+  for (int f = 0; f < FH; ++f) {
+    t[half * FH + f] = own[f];
+    t[KH + half * FH + f] = agg[f];
+  }
+  __syncwarp();
+}
+
+// Z = [Hin, Agg Hin] W + b;  Hout = (res ? Hin : 0) + relu(Z)
+template <int KH>
+__global__ void __launch_bounds__(LTPB) k_layer_fwd(int n, const float* __restrict__ Hin,
+                                                   const int* __restrict__ rowptr, const int* __restrict__ col,
+                                                   const float* __restrict__ what, const __nv_bfloat16* __restrict__ W,
+                                                   const float* __restrict__ bias, int res, float* Z, float* Hout) {
+  constexpr int K = 2 * KH;
+  __shared__ __nv_bfloat16 sW[K * HID];
+  __shared__ float sT[4][16 * K];
+  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) sW[t] = W[t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tq = lane & 3;
+  float* tile = sT[warp];
+  const int ntiles = (n + 15) / 16;
+  for (int tl = blockIdx.x * 4 + warp; tl < ntiles; tl += gridDim.x * 4) {
+    const int row0 = tl * 16;
+    fill_xcat<KH>(tile, row0, n, Hin, rowptr, col, what);
+    float acc[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ++ks) {
+      const int k0 = ks * 16;
+      uint32_t af[4];
+      af[0] = pack_bf16(tile[g * K + k0 + 2 * tq], tile[g * K + k0 + 2 * tq + 1]);
+      af[1] = pack_bf16(tile[(g + 8) * K + k0 + 2 * tq], tile[(g + 8) * K + k0 + 2 * tq + 1]);
+      af[2] = pack_bf16(tile[g * K + k0 + 2 * tq + 8], tile[g * K + k0 + 2 * tq + 9]);
+      af[3] = pack_bf16(tile[(g + 8) * K + k0 + 2 * tq + 8], tile[(g + 8) * K + k0 + 2 * tq + 9]);
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int n0 = nt * 8;
+        uint32_t bfr[2];
+        bfr[0] = pack_bf16(bf(sW, (k0 + 2 * tq) * HID + n0 + g), bf(sW, (k0 + 2 * tq + 1) * HID + n0 + g));
+        bfr[1] = pack_bf16(bf(sW, (k0 + 2 * tq + 8) * HID + n0 + g), bf(sW, (k0 + 2 * tq + 9) * HID + n0 + g));
+        mma_bf16(acc[nt], af, bfr);
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int row = row0 + g + ((e >= 2) ? 8 : 0);
+        const int c = nt * 8 + 2 * tq + (e & 1);
+        if (row < n) {
+          const float z = acc[nt][e] + bias[c];
+          Z[(size_t)row * HID + c] = z;
+          const float h0 = res ? Hin[(size_t)row * KH + c] : 0.f;
+          Hout[(size_t)row * HID + c] = h0 + fmaxf(z, 0.f);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// readout: gd_i = 1 + H_i . rd ; gl_k = what_k sum_c ro_c H_ic H_jc (j = col_k < i)
+__global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                          const float* __restrict__ what, const float* __restrict__ H, const float* __restrict__ params,
+                          float* gd, float* gl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* rd = params + OFF_RD;
+  const float* ro = params + OFF_RO;
+  const float* hi = H + (size_t)i * HID;
+  float hro[HID];
+  float d = 1.f;
+#pragma unroll
+  for (int c = 0; c < HID; ++c) {
+    d = fmaf(hi[c], rd[c], d);
+    hro[c] = hi[c] * ro[c];
+  }
+  gd[i] = d;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int j = col[k];
+    float v = 0.f;
+    if (j < i) {
+      const float* hj = H + (size_t)j * HID;
+#pragma unroll
+      for (int c = 0; c < HID; ++c) v = fmaf(hro[c], hj[c], v);
+      v *= what[k];
+    }
+    gl[k] = v;
+  }
+}
+
+// ---------------------------------------------------------------- loss
+
+__device__ __forceinline__ float probe_value(unsigned long long seed, int p, int i) {
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(p * 0x100000001ull + (unsigned)i + 1);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (z & 1ull) ? 1.f : -1.f;
+}
+
+__global__ void k_probes(int n, int K, unsigned long long seed, float* Zp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int p = 0; p < K; ++p) Zp[(size_t)p * n + i] = probe_value(seed, p, i);
+}
+
+// out = Gt^T in : out_i = gd_i in_i + sum_{k: col_k > i} gl[rev_k] in_col
+__global__ void k_gt(int n, int K, const int* __restrict__ rowptr, const int* __restrict__ col,
+                     const int* __restrict__ rev, const float* __restrict__ gd, const float* __restrict__ gl,
+                     const float* __restrict__ in, float* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int p = 0; p < K; ++p) {
+    const float* v = in + (size_t)p * n;
+    float acc = gd[i] * v[i];
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j > i && rev[k] >= 0) acc = fmaf(gl[rev[k]], v[j], acc);
+    }
+    out[(size_t)p * n + i] = acc;
+  }
+}
+
+// out = Gt in : out_i = gd_i in_i + sum_{k: col_k < i} gl_k in_col
+__global__ void k_g(int n, int K, const int* __restrict__ rowptr, const int* __restrict__ col,
+                    const float* __restrict__ gd, const float* __restrict__ gl, const float* __restrict__ in,
+                    float* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int p = 0; p < K; ++p) {
+    const float* v = in + (size_t)p * n;
+    float acc = gd[i] * v[i];
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j < i) acc = fmaf(gl[k], v[j], acc);
+    }
+    out[(size_t)p * n + i] = acc;
+  }
+}
+
+// out = At in = in - What in
+__global__ void k_at(int n, int K, const int* __restrict__ rowptr, const int* __restrict__ col,
+                     const float* __restrict__ what, const float* __restrict__ in, float* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int p = 0; p < K; ++p) {
+    const float* v = in + (size_t)p * n;
+    float acc = v[i];
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fmaf(-what[k], v[col[k]], acc);
+    out[(size_t)p * n + i] = acc;
+  }
+}
+
+// r = u - z, block partial of sum r^2 (double)
+__global__ void k_resid(int n, int K, const float* __restrict__ u, const float* __restrict__ z, float* r,
+                        double* part) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int p = 0; p < K; ++p) {
+      const size_t o = (size_t)p * n + i;
+      const float v = u[o] - z[o];
+      r[o] = v;
+      s += (double)v * (double)v;
+    }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+// dGt entries: dgd_i = scale sum_p 2 (r_i t_i + z_i s_i); dgl_k = scale sum_p 2 (r_i t_j + z_i s_j), j < i
+__global__ void k_gradG(int n, int K, const int* __restrict__ rowptr, const int* __restrict__ col,
+                        const float* __restrict__ r, const float* __restrict__ t, const float* __restrict__ z,
+                        const float* __restrict__ s, float scale, float* dgd, float* dgl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float d = 0.f;
+  for (int p = 0; p < K; ++p) {
+    const size_t o = (size_t)p * n;
+    d += 2.f * (r[o + i] * t[o + i] + z[o + i] * s[o + i]);
+  }
+  dgd[i] = scale * d;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int j = col[k];
+    float v = 0.f;
+    if (j < i)
+      for (int p = 0; p < K; ++p) {
+        const size_t o = (size_t)p * n;
+        v += 2.f * (r[o + i] * t[o + j] + z[o + i] * s[o + j]);
+      }
+    dgl[k] = scale * v;
+  }
+}
+
+// ---------------------------------------------------------------- backward
+
+// dH_i from the readout; block partials of d rd (32) and d ro (32)
+__global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                              const int* __restrict__ rev, const float* __restrict__ what, const float* __restrict__ H,
+                              const float* __restrict__ params, const float* __restrict__ dgd,
+                              const float* __restrict__ dgl, float* dH, float* part) {
+  const float* rd = params + OFF_RD;
+  const float* ro = params + OFF_RO;
+  float prd[HID], pro[HID];
+#pragma unroll
+  for (int c = 0; c < HID; ++c) prd[c] = pro[c] = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* hi = H + (size_t)i * HID;
+    float dh[HID];
+    const float gdi = dgd[i];
+#pragma unroll
+    for (int c = 0; c < HID; ++c) {
+      dh[c] = gdi * rd[c];
+      prd[c] = fmaf(gdi, hi[c], prd[c]);
+    }
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = col[k];
+      float coef;
+      if (j < i) {
+        coef = dgl[k] * what[k];
+        const float* hj = H + (size_t)j * HID;
+#pragma unroll
+        for (int c = 0; c < HID; ++c) pro[c] = fmaf(coef * hi[c], hj[c], pro[c]);
+      } else {
+        const int rk = rev[k];
+        coef = rk >= 0 ? dgl[rk] * what[rk] : 0.f;
+      }
+      const float* hj = H + (size_t)j * HID;
+#pragma unroll
+      for (int c = 0; c < HID; ++c) dh[c] = fmaf(coef * ro[c], hj[c], dh[c]);
+    }
+    float* o = dH + (size_t)i * HID;
+#pragma unroll
+    for (int c = 0; c < HID; ++c) o[c] = dh[c];
+  }
+  // block reduction in a fixed order: warp shuffles, then warps in order
+#pragma unroll
+  for (int c = 0; c < HID; ++c) {
+    float a = prd[c], b = pro[c];
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    prd[c] = a;
+    pro[c] = b;
+  }
+  __shared__ float swarp[8][2 * HID];
+  if ((threadIdx.x & 31) == 0)
+    for (int c = 0; c < HID; ++c) {
+      swarp[threadIdx.x >> 5][c] = prd[c];
+      swarp[threadIdx.x >> 5][HID + c] = pro[c];
+    }
+  __syncthreads();
+  if (threadIdx.x < 2 * HID) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += swarp[w][threadIdx.x];
+    part[(size_t)blockIdx.x * 2 * HID + threadIdx.x] = t;
+  }
+}
+
+// Layer backward: dZ = dHout * [Z > 0]; dXcat = dZ W^T (tensor cores) into
+// dHdir (first KH columns) and dAgg (last KH); block partials of dW = Xcat^T dZ
+// (tensor cores) and db = sum dZ.
+template <int KH>
+__global__ void __launch_bounds__(LTPB) k_layer_bwd(int n, const float* __restrict__ Hin,
+                                                   const int* __restrict__ rowptr, const int* __restrict__ col,
+                                                   const float* __restrict__ what, const __nv_bfloat16* __restrict__ W,
+                                                   const float* __restrict__ Z, const float* __restrict__ dHout,
+                                                   float* dHdir, float* dAgg, float* partW, float* partb,
+                                                   int need_dx) {
+  constexpr int K = 2 * KH;
+  constexpr int MT = K / 16;  // m-tiles of dW
+  __shared__ __nv_bfloat16 sW[K * HID];
+  __shared__ float sT[4][16 * K];
+  __shared__ float sD[4][16 * HID];
+  __shared__ float sRed[K * HID];
+  __shared__ float sB[HID];
+  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) {
+    sW[t] = W[t];
+    sRed[t] = 0.f;
+  }
+  for (int t = threadIdx.x; t < HID; t += blockDim.x) sB[t] = 0.f;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tq = lane & 3;
+  float* tile = sT[warp];
+  float* dz = sD[warp];
+  float accW[MT][4][4];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) accW[m][nt][e] = 0.f;
+  float accB = 0.f;  // lane = column of db
+  const int ntiles = (n + 15) / 16;
+  for (int tl = blockIdx.x * 4 + warp; tl < ntiles; tl += gridDim.x * 4) {
+    const int row0 = tl * 16;
+    fill_xcat<KH>(tile, row0, n, Hin, rowptr, col, what);
+    // dZ tile: lane handles column `lane` of all 16 rows
+    for (int r = 0; r < 16; ++r) {
+      const int row = row0 + r;
+      float v = 0.f;
+      if (row < n) {
+        const size_t o = (size_t)row * HID + lane;
+        v = Z[o] > 0.f ? dHout[o] : 0.f;
+      }
+      dz[r * HID + lane] = v;
+      accB += v;
+    }
+    __syncwarp();
+    if (need_dx) {
+      // dXcat (16 x K) = dZ (16 x 32) W^T (32 x K)
+#pragma unroll
+      for (int nt = 0; nt < K / 8; ++nt) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const int n0 = nt * 8;
+#pragma unroll
+        for (int ks = 0; ks < HID / 16; ++ks) {
+          const int k0 = ks * 16;
+          uint32_t af[4];
+          af[0] = pack_bf16(dz[g * HID + k0 + 2 * tq], dz[g * HID + k0 + 2 * tq + 1]);
+          af[1] = pack_bf16(dz[(g + 8) * HID + k0 + 2 * tq], dz[(g + 8) * HID + k0 + 2 * tq + 1]);
+          af[2] = pack_bf16(dz[g * HID + k0 + 2 * tq + 8], dz[g * HID + k0 + 2 * tq + 9]);
+          af[3] = pack_bf16(dz[(g + 8) * HID + k0 + 2 * tq + 8], dz[(g + 8) * HID + k0 + 2 * tq + 9]);
+          uint32_t bfr[2];  // B[k][nn] = W^T[k][nn] = W[n0 + nn][k]
+          bfr[0] = pack_bf16(bf(sW, (n0 + g) * HID + k0 + 2 * tq), bf(sW, (n0 + g) * HID + k0 + 2 * tq + 1));
+          bfr[1] = pack_bf16(bf(sW, (n0 + g) * HID + k0 + 2 * tq + 8), bf(sW, (n0 + g) * HID + k0 + 2 * tq + 9));
+          mma_bf16(acc, af, bfr);
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int row = row0 + g + ((e >= 2) ? 8 : 0);
+          const int c = n0 + 2 * tq + (e & 1);
+          if (row < n) {
+            if (c < KH)
+              dHdir[(size_t)row * KH + c] = acc[e];
+            else
+              dAgg[(size_t)row * KH + (c - KH)] = acc[e];
+          }
+        }
+      }
+    }
+    // dW (K x 32) += Xcat^T (K x 16) dZ (16 x 32)
+#pragma unroll
+    for (int m = 0; m < MT; ++m) {
+      const int m0 = m * 16;
+      uint32_t af[4];  // A[mm][kk] = Xcat[kk][m0 + mm]
+      af[0] = pack_bf16(tile[(2 * tq) * K + m0 + g], tile[(2 * tq + 1) * K + m0 + g]);
+      af[1] = pack_bf16(tile[(2 * tq) * K + m0 + g + 8], tile[(2 * tq + 1) * K + m0 + g + 8]);
+      af[2] = pack_bf16(tile[(2 * tq + 8) * K + m0 + g], tile[(2 * tq + 9) * K + m0 + g]);
+      af[3] = pack_bf16(tile[(2 * tq + 8) * K + m0 + g + 8], tile[(2 * tq + 9) * K + m0 + g + 8]);
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int n0 = nt * 8;
+        uint32_t bfr[2];  // B[kk][nn] = dZ[kk][n0 + nn]
+        bfr[0] = pack_bf16(dz[(2 * tq) * HID + n0 + g], dz[(2 * tq + 1) * HID + n0 + g]);
+        bfr[1] = pack_bf16(dz[(2 * tq + 8) * HID + n0 + g], dz[(2 * tq + 9) * HID + n0 + g]);
+        mma_bf16(accW[m][nt], af, bfr);
+      }
+    }
+    __syncwarp();
+  }
+  // reduce the four warps' dW in a fixed order through shared memory
+  for (int w = 0; w < 4; ++w) {
+    if (warp == w) {
+#pragma unroll
+      for (int m = 0; m < MT; ++m)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int r = m * 16 + g + ((e >= 2) ? 8 : 0);
+            const int c = nt * 8 + 2 * tq + (e & 1);
+            sRed[r * HID + c] += accW[m][nt][e];
+          }
+      sB[lane] += accB;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) partW[(size_t)blockIdx.x * K * HID + t] = sRed[t];
+  for (int t = threadIdx.x; t < HID; t += blockDim.x) partb[(size_t)blockIdx.x * HID + t] = sB[t];
+}
+
+// dHin_j = dHdir_j + (res ? dHout_j : 0) + sum_{i ~ j} what_ij dAgg_i
+template <int KH>
+__global__ void k_agg_bwd(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                          const int* __restrict__ rev, const float* __restrict__ what,
+                          const float* __restrict__ dHdir, const float* __restrict__ dAgg,
+                          const float* __restrict__ dHout, int res, float* dHin) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  float acc[KH];
+#pragma unroll
+  for (int f = 0; f < KH; ++f) acc[f] = dHdir[(size_t)j * KH + f] + (res ? dHout[(size_t)j * KH + f] : 0.f);
+  for (int k = rowptr[j]; k < rowptr[j + 1]; ++k) {
+    const int i = col[k];
+    const int rk = rev[k];
+    if (rk < 0) continue;
+    const float wv = what[rk];
+    const float* da = dAgg + (size_t)i * KH;
+#pragma unroll
+    for (int f = 0; f < KH; ++f) acc[f] = fmaf(wv, da[f], acc[f]);
+  }
+#pragma unroll
+  for (int f = 0; f < KH; ++f) dHin[(size_t)j * KH + f] = acc[f];
+}
+
+// sum block partials (fixed order) into grad[off..off+len)
+__global__ void k_sum_parts(const float* __restrict__ part, int nblocks, int len, float* grad) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= len) return;
+  float s = 0.f;
+  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * len + t];
+  grad[t] = s;
+}
+
+__global__ void k_sum_loss(const double* part, int nb, double scale, double* out) {
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += part[b];
+  out[0] = s * scale;
+}
+
+__global__ void k_adam(int np, float* p, const float* __restrict__ gr, float* m1, float* m2, float lr, float b1,
+                       float b2, float c1, float c2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const float gi = gr[i];
+  const float a = b1 * m1[i] + (1.f - b1) * gi;
+  const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+  m1[i] = a;
+  m2[i] = b;
+  p[i] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* wbf) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < KC0 * HID) wbf[WBF_W0 + t] = __float2bfloat16_rn(p[OFF_W0 + t]);
+  if (t < KC * HID) {
+    wbf[WBF_W1 + t] = __float2bfloat16_rn(p[OFF_W1 + t]);
+    wbf[WBF_W2 + t] = __float2bfloat16_rn(p[OFF_W2 + t]);
+  }
+}
+
+}  // namespace
+
+// ======================================================================= host
+
+struct LearnSystem {
+  int n = 0;
+  int nnz = 0;
+  int* rowptr = nullptr;
+  int* col = nullptr;
+  double* w = nullptr;
+  double* diag = nullptr;
+  double* adiag = nullptr;
+};
+
+struct LearnState {
+  float *params = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
+  __nv_bfloat16* wbf = nullptr;
+  int adam_t = 0;
+  int cap = 0;
+  int64_t nnz_cap = 0;
+  // workspace
+  float *dh, *what, *X, *H1, *H2, *H3, *Z0, *Z1, *Z2, *gd, *gl;
+  int* rev;
+  float *dH3, *dH2, *dH1, *dHdir, *dAgg, *dgd, *dgl;
+  float *zp, *y, *t, *u, *r, *v, *s;
+  float *partW, *partb, *partR;
+  double *partL, *loss;
+  std::vector<LearnSystem> systems;
+  std::vector<void*> allocs;
+  bool factor_ready = false;
+};
+
+namespace {
+
+template <class T>
+T* lalloc(LearnState* L, size_t count) {
+  void* p = nullptr;
+  if (count == 0) count = 1;
+  if (cudaMalloc(&p, sizeof(T) * count) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, sizeof(T) * count);
+  L->allocs.push_back(p);
+  return static_cast<T*>(p);
+}
+
+unsigned long long splitmix(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+float gauss(unsigned long long& s) {
+  const double u1 = ((splitmix(s) >> 11) + 1.0) * (1.0 / 9007199254740993.0);
+  const double u2 = (splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+  return (float)(sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+}
+
+int ensure_state(lv_ctx* c) {
+  if (c->learn) return LV_OK;
+  LearnState* L = new LearnState();
+  L->cap = c->cap;
+  L->nnz_cap = c->sv.nnz_cap;
+  const size_t cap = c->cap, nnz = (size_t)c->sv.nnz_cap;
+  L->params = lalloc<float>(L, NPARAM);
+  L->grad = lalloc<float>(L, NPARAM);
+  L->m1 = lalloc<float>(L, NPARAM);
+  L->m2 = lalloc<float>(L, NPARAM);
+  L->wbf = lalloc<__nv_bfloat16>(L, NWBF);
+  L->dh = lalloc<float>(L, cap);
+  L->what = lalloc<float>(L, nnz);
+  L->rev = lalloc<int>(L, nnz);
+  L->X = lalloc<float>(L, cap * FIN);
+  for (float** p : {&L->H1, &L->H2, &L->H3, &L->Z0, &L->Z1, &L->Z2, &L->dH3, &L->dH2, &L->dH1, &L->dHdir, &L->dAgg})
+    *p = lalloc<float>(L, cap * HID);
+  L->gd = lalloc<float>(L, cap);
+  L->gl = lalloc<float>(L, nnz);
+  L->dgd = lalloc<float>(L, cap);
+  L->dgl = lalloc<float>(L, nnz);
+  for (float** p : {&L->zp, &L->y, &L->t, &L->u, &L->r, &L->v, &L->s}) *p = lalloc<float>(L, cap * MAXPROBES);
+  L->partW = lalloc<float>(L, (size_t)PART_BLOCKS * KC * HID);
+  L->partb = lalloc<float>(L, (size_t)PART_BLOCKS * HID);
+  L->partR = lalloc<float>(L, (size_t)PART_BLOCKS * 2 * HID);
+  L->partL = lalloc<double>(L, PART_BLOCKS);
+  L->loss = lalloc<double>(L, 4);
+  bool ok = L->params && L->loss && L->partR && L->s;
+  if (!ok) {
+    for (void* p : L->allocs) cudaFree(p);
+    delete L;
+    return lv_fail(c, LV_ERR_CUDA, "learned preconditioner: out of device memory");
+  }
+  c->learn = L;
+  return LV_OK;
+}
+
+void init_params(LearnState* L, unsigned long long seed, cudaStream_t s) {
+  std::vector<float> p(NPARAM, 0.f);
+  unsigned long long st = seed ^ 0xA5A5A5A5ull;
+  auto fill = [&](int off, int fan_in, int count, float gain) {
+    const float sd = gain / sqrtf((float)fan_in);
+    for (int k = 0; k < count; ++k) p[off + k] = sd * gauss(st);
+  };
+  fill(OFF_W0, KC0, KC0 * HID, 1.0f);
+  fill(OFF_W1, KC, KC * HID, 0.5f);
+  fill(OFF_W2, KC, KC * HID, 0.5f);
+  fill(OFF_RD, HID, HID, 0.01f);
+  fill(OFF_RO, HID, HID, 0.01f);
+  cudaMemcpyAsync(L->params, p.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(L->m1, 0, sizeof(float) * NPARAM, s);
+  cudaMemsetAsync(L->m2, 0, sizeof(float) * NPARAM, s);
+  L->adam_t = 0;
+}
+
+constexpr int TPB = 256;
+
+int launch_blocks_tiles(int n) { return std::max(1, std::min(PART_BLOCKS, (n + 63) / 64)); }
+
+// Features and normalised weights of one system.
+int prepare(lv_ctx* c, const LearnSystem& S) {
+  LearnState* L = c->learn;
+  cudaStream_t s = c->stream;
+  k_lprep_dh<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.adiag, L->dh);
+  k_lprep<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, S.w, S.diag, S.adiag, L->dh, L->what, L->rev, L->X);
+  c->launches += 2;
+  return lv_cuda_check(c, cudaGetLastError(), "learned: prepare");
+}
+
+int forward(lv_ctx* c, const LearnSystem& S) {
+  LearnState* L = c->learn;
+  cudaStream_t s = c->stream;
+  const int nb = launch_blocks_tiles(S.n);
+  k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
+  k_layer_fwd<FIN><<<nb, LTPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0, 0,
+                                         L->Z0, L->H1);
+  k_layer_fwd<HID><<<nb, LTPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1, 1,
+                                         L->Z1, L->H2);
+  k_layer_fwd<HID><<<nb, LTPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2, 1,
+                                         L->Z2, L->H3);
+  k_readout<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd, L->gl);
+  c->launches += 5;
+  return lv_cuda_check(c, cudaGetLastError(), "learned: forward");
+}
+
+// loss (into L->loss[0]) and dGt (L->dgd, L->dgl) for K probes in L->zp
+int loss_grad_G(lv_ctx* c, const LearnSystem& S, int K) {
+  LearnState* L = c->learn;
+  cudaStream_t s = c->stream;
+  const int n = S.n, b = lv_blocks(n, TPB);
+  k_gt<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->rev, L->gd, L->gl, L->zp, L->y);
+  k_at<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->what, L->y, L->t);
+  k_g<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->gd, L->gl, L->t, L->u);
+  const int nbl = std::min(PART_BLOCKS, b);
+  k_resid<<<nbl, TPB, 0, s>>>(n, K, L->u, L->zp, L->r, L->partL);
+  k_sum_loss<<<1, 32, 0, s>>>(L->partL, nbl, 1.0 / ((double)K * n), L->loss);
+  k_gt<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->rev, L->gd, L->gl, L->r, L->v);
+  k_at<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->what, L->v, L->s);
+  k_gradG<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->r, L->t, L->zp, L->s, 1.0f / ((float)K * n), L->dgd, L->dgl);
+  c->launches += 8;
+  return lv_cuda_check(c, cudaGetLastError(), "learned: loss");
+}
+
+int backward(lv_ctx* c, const LearnSystem& S) {
+  LearnState* L = c->learn;
+  cudaStream_t s = c->stream;
+  const int n = S.n;
+  const int nbr = std::min(PART_BLOCKS, lv_blocks(n, TPB));
+  k_readout_bwd<<<nbr, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->H3, L->params, L->dgd, L->dgl, L->dH3,
+                                    L->partR);
+  k_sum_parts<<<1, 64, 0, s>>>(L->partR, nbr, 2 * HID, L->grad + OFF_RD);
+  const int nb = launch_blocks_tiles(n);
+  // layer 2: Hin = H2, dHout = dH3
+  k_layer_bwd<HID><<<nb, LTPB, 0, s>>>(n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->Z2, L->dH3, L->dHdir,
+                                        L->dAgg, L->partW, L->partb, 1);
+  k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W2);
+  k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B2);
+  k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH3, 1,
+                                                    L->dH2);
+  // layer 1: Hin = H1, dHout = dH2
+  k_layer_bwd<HID><<<nb, LTPB, 0, s>>>(n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->Z1, L->dH2, L->dHdir,
+                                        L->dAgg, L->partW, L->partb, 1);
+  k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W1);
+  k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B1);
+  k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH2, 1,
+                                                    L->dH1);
+  // layer 0: Hin = X (no dX needed)
+  k_layer_bwd<FIN><<<nb, LTPB, 0, s>>>(n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->Z0, L->dH1, L->dHdir,
+                                        L->dAgg, L->partW, L->partb, 0);
+  k_sum_parts<<<lv_blocks(KC0 * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC0 * HID, L->grad + OFF_W0);
+  k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B0);
+  c->launches += 14;
+  return lv_cuda_check(c, cudaGetLastError(), "learned: backward");
+}
+
+LearnSystem current_system(lv_ctx* c) {
+  LearnSystem S;
+  S.n = c->n;
+  S.rowptr = c->sv.rowptr;
+  S.col = c->sv.col;
+  S.w = c->sv.w;
+  S.diag = c->sv.diag;
+  S.adiag = c->sv.adiag;
+  return S;
+}
+
+}  // namespace
+
+// Inference for the currently assembled operator: fills gd, gl, dh, rev for
+// the learned solve.  Called by the solver when the method is learned.
+int lv_learn_factor_current(lv_ctx* c) {
+  if (int rc = ensure_state(c)) return rc;
+  // an untrained network (all parameters zero) gives Gt = I, i.e. Jacobi
+  LearnSystem S = current_system(c);
+  if (int rc = prepare(c, S)) return rc;
+  return forward(c, S);
+}
+
+void lv_learn_free(lv_ctx* c) {
+  if (!c->learn) return;
+  for (void* p : c->learn->allocs) cudaFree(p);
+  for (auto& S : c->learn->systems) {
+    cudaFree(S.rowptr);
+    cudaFree(S.col);
+    cudaFree(S.w);
+    cudaFree(S.diag);
+    cudaFree(S.adiag);
+  }
+  delete c->learn;
+  c->learn = nullptr;
+}
+
+void lv_learn_factor_ptrs(lv_ctx* c, const float** gd, const float** gl, const float** dh, const int** rev) {
+  LearnState* L = c->learn;
+  *gd = L ? L->gd : nullptr;
+  *gl = L ? L->gl : nullptr;
+  *dh = L ? L->dh : nullptr;
+  *rev = L ? L->rev : nullptr;
+}
+
+extern "C" {
+
+int lv_learn_init(lv_ctx* c, uint64_t seed) {
+  if (c) c->factor_valid = false;
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  init_params(c->learn, seed, c->stream);
+  c->learn->factor_ready = true;
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_init");
+}
+
+int32_t lv_learn_num_params(void) { return NPARAM; }
+
+int lv_learn_get_params(lv_ctx* c, float* out) {
+  if (!c || !out) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  cudaMemcpyAsync(out, c->learn->params, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, c->stream);
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_get_params");
+}
+
+int lv_learn_set_params(lv_ctx* c, const float* in) {
+  if (c) c->factor_valid = false;
+  if (!c || !in) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  cudaMemcpyAsync(c->learn->params, in, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, c->stream);
+  c->learn->factor_ready = true;
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_set_params");
+}
+
+int lv_learn_add_system(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  if (int rc = ensure_state(c)) return rc;
+  LearnSystem S;
+  S.n = c->n;
+  int nnz = 0;
+  cudaMemcpyAsync(&nnz, c->sv.rowptr + c->n, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_learn_add_system");
+  S.nnz = nnz;
+  if (cudaMalloc(&S.rowptr, sizeof(int) * (S.n + 1)) != cudaSuccess || cudaMalloc(&S.col, sizeof(int) * nnz) ||
+      cudaMalloc(&S.w, sizeof(double) * nnz) || cudaMalloc(&S.diag, sizeof(double) * S.n) ||
+      cudaMalloc(&S.adiag, sizeof(double) * S.n))
+    return lv_fail(c, LV_ERR_CUDA, "lv_learn_add_system: out of device memory");
+  cudaMemcpyAsync(S.rowptr, c->sv.rowptr, sizeof(int) * (S.n + 1), cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.col, c->sv.col, sizeof(int) * nnz, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.w, c->sv.w, sizeof(double) * nnz, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.diag, c->sv.diag, sizeof(double) * S.n, cudaMemcpyDeviceToDevice, c->stream);
+  cudaMemcpyAsync(S.adiag, c->sv.adiag, sizeof(double) * S.n, cudaMemcpyDeviceToDevice, c->stream);
+  c->learn->systems.push_back(S);
+  e = cudaStreamSynchronize(c->stream);
+  return lv_cuda_check(c, e, "lv_learn_add_system");
+}
+
+int32_t lv_learn_num_systems(lv_ctx* c) { return (c && c->learn) ? (int32_t)c->learn->systems.size() : 0; }
+
+int lv_learn_clear_systems(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->learn) return LV_OK;
+  cudaStreamSynchronize(c->stream);
+  for (auto& S : c->learn->systems) {
+    cudaFree(S.rowptr);
+    cudaFree(S.col);
+    cudaFree(S.w);
+    cudaFree(S.diag);
+    cudaFree(S.adiag);
+  }
+  c->learn->systems.clear();
+  return LV_OK;
+}
+
+// Loss and gradient on training system `sys` (or the current operator when
+// sys < 0) for K probes (given as K x n floats, or Rademacher from `seed`
+// when probes is NULL).  grad may be NULL.
+int lv_learn_loss_grad(lv_ctx* c, int32_t sys, const float* probes, int32_t K, uint64_t seed, double* loss,
+                       float* grad) {
+  if (!c || K < 1 || K > MAXPROBES) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  LearnState* L = c->learn;
+  LearnSystem S;
+  if (sys < 0) {
+    if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+    S = current_system(c);
+  } else {
+    if (sys >= (int)L->systems.size()) return LV_ERR_BAD_ARGUMENT;
+    S = L->systems[sys];
+  }
+  cudaStream_t s = c->stream;
+  if (int rc = prepare(c, S)) return rc;
+  if (int rc = forward(c, S)) return rc;
+  if (probes)
+    cudaMemcpyAsync(L->zp, probes, sizeof(float) * (size_t)K * S.n, cudaMemcpyHostToDevice, s);
+  else
+    k_probes<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, K, seed, L->zp);
+  if (int rc = loss_grad_G(c, S, K)) return rc;
+  if (int rc = backward(c, S)) return rc;
+  if (loss) cudaMemcpyAsync(loss, L->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (grad) cudaMemcpyAsync(grad, L->grad, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, s);
+  return lv_cuda_check(c, cudaStreamSynchronize(s), "lv_learn_loss_grad");
+}
+
+// Adam on the training systems (round robin), K Rademacher probes per step.
+int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed, float* losses) {
+  if (c) c->factor_valid = false;
+  if (!c || steps < 0 || K < 1 || K > MAXPROBES || !(lr > 0)) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  LearnState* L = c->learn;
+  if (L->systems.empty()) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "no training systems (lv_learn_add_system)");
+  cudaStream_t s = c->stream;
+  std::vector<double> hl(steps > 0 ? steps : 1);
+  double* dl = nullptr;
+  if (losses && steps > 0 && cudaMalloc(&dl, sizeof(double) * steps) != cudaSuccess) dl = nullptr;
+  for (int st = 0; st < steps; ++st) {
+    const LearnSystem& S = L->systems[st % L->systems.size()];
+    if (int rc = prepare(c, S)) return rc;
+    if (int rc = forward(c, S)) return rc;
+    k_probes<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, K, seed + 7919ull * (unsigned long long)st, L->zp);
+    if (int rc = loss_grad_G(c, S, K)) return rc;
+    if (int rc = backward(c, S)) return rc;
+    L->adam_t += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)L->adam_t), c2 = 1.f - powf(b2, (float)L->adam_t);
+    k_adam<<<lv_blocks(NPARAM, TPB), TPB, 0, s>>>(NPARAM, L->params, L->grad, L->m1, L->m2, lr, b1, b2, c1, c2);
+    c->launches += 2;
+    if (dl) cudaMemcpyAsync(dl + st, L->loss, sizeof(double), cudaMemcpyDeviceToDevice, s);
+  }
+  if (dl) {
+    cudaMemcpyAsync(hl.data(), dl, sizeof(double) * steps, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int st = 0; st < steps; ++st) losses[st] = (float)hl[st];
+    cudaFree(dl);
+  }
+  L->factor_ready = true;
+  return lv_cuda_check(c, cudaStreamSynchronize(s), "lv_learn_train");
+}
+
+// The factor Gt of the current operator: gdiag[n] and glower[nnz] (entries of
+// the CSR positions with col < row; others 0), plus the features X[n][16].
+int lv_learn_factor(lv_ctx* c, float* gdiag, float* glower, float* features) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  if (int rc = lv_learn_factor_current(c)) return rc;
+  LearnState* L = c->learn;
+  int nnz = 0;
+  cudaMemcpyAsync(&nnz, c->sv.rowptr + c->n, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
+  if (gdiag) cudaMemcpyAsync(gdiag, L->gd, sizeof(float) * c->n, cudaMemcpyDeviceToHost, c->stream);
+  if (glower) cudaMemcpyAsync(glower, L->gl, sizeof(float) * nnz, cudaMemcpyDeviceToHost, c->stream);
+  if (features) cudaMemcpyAsync(features, L->X, sizeof(float) * c->n * FIN, cudaMemcpyDeviceToHost, c->stream);
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_factor");
+}
+
+}  // extern "C"

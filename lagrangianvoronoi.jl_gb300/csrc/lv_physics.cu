@@ -12,6 +12,8 @@
 // evaluation of the same formulas in the same face order.
 #include <math.h>
 
+#include <algorithm>
+
 #include "lv_internal.cuh"
 
 namespace {
@@ -650,8 +652,173 @@ int lv_phys_move(lv_ctx* c, double dt) {
 // (relaxation.jl:182).
 int lv_phys_multiphase(lv_ctx* c, double threshold, lv_solve_stats* st);
 
+namespace {
+
+// two dot products, block partials (fixed order within a block)
+__global__ void k_dot2(int n, const double* __restrict__ a, const double* __restrict__ b,
+                       const double* __restrict__ c, const double* __restrict__ d, double* part) {
+  __shared__ double sh[2][32];
+  double s0 = 0.0, s1 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    s0 += a[i] * b[i];
+    if (c) s1 += c[i] * d[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][wid] = s0;
+    sh[1][wid] = s1;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    s0 = lane < (int)(blockDim.x >> 5) ? sh[0][lane] : 0.0;
+    s1 = lane < (int)(blockDim.x >> 5) ? sh[1][lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+      part[2 * blockIdx.x] = s0;
+      part[2 * blockIdx.x + 1] = s1;
+    }
+  }
+}
+
+__global__ void k_dot2_final(int nb, const double* part, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s0 = 0.0, s1 = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    s0 += part[2 * b];
+    s1 += part[2 * b + 1];
+  }
+  out[0] = s0;
+  out[1] = s1;
+}
+
+// y = alpha x + beta y (element-wise)
+__global__ void k_axpby(int n, double alpha, const double* __restrict__ x, double beta, double* y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = alpha * x[i] + beta * y[i];
+}
+
+// MINRES direction update: w = (v - oldeps w1 - delta w2) denom; q += phi w
+__global__ void k_minres_update(int n, const double* __restrict__ v, const double* __restrict__ w1,
+                                const double* __restrict__ w2, double* w, double* q, double oldeps, double delta,
+                                double denom, double phi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double wi = (v[i] - oldeps * w1[i] - delta * w2[i]) * denom;
+  w[i] = wi;
+  q[i] += phi * wi;
+}
+
+}  // namespace
+
+// multiphase_projection! (relaxation.jl:180-206): refresh! of b, MINRES on
+// the projector (atol = rtol = 1e-4, itmax = 200, zero initial guess; Paige &
+// Saunders 1975 with the stopping rule ||r|| <= atol + rtol ||r0||), then the
+// dv correction on cross-phase faces of polygons with quality >= threshold.
 int lv_phys_multiphase(lv_ctx* c, double threshold, lv_solve_stats* st) {
-  (void)threshold;
-  (void)st;
-  return lv_fail(c, LV_ERR_BAD_ARGUMENT, "multiphase_projection is not available in this build");
+  if (int rc = need_mesh(c)) return rc;
+  const int n = c->n;
+  cudaStream_t s = c->stream;
+  static thread_local double* host2 = nullptr;
+  if (!host2 && cudaMallocHost(&host2, 2 * sizeof(double)) != cudaSuccess)
+    return lv_fail(c, LV_ERR_CUDA, "pinned buffer");
+  // device vectors: b, q, r1, r2, y, v, w, w1, w2, tmp2 (2n), part
+  const size_t cap = c->cap;
+  if (!c->mp_buf) {
+    // 11 vectors + block partials (2 x 4096) + the two final sums
+    if (cudaMalloc(&c->mp_buf, sizeof(double) * (11 * cap + 2 * 4096 + 64)) != cudaSuccess)
+      return lv_fail(c, LV_ERR_CUDA, "multiphase buffers");
+    c->allocs.push_back(c->mp_buf);
+  }
+  double* B = c->mp_buf;
+  double *b = B, *q = B + cap, *r1 = B + 2 * cap, *r2 = B + 3 * cap, *y = B + 4 * cap, *v = B + 5 * cap,
+         *w = B + 6 * cap, *w1 = B + 7 * cap, *w2 = B + 8 * cap;
+  double2* tmp = reinterpret_cast<double2*>(B + 9 * cap);
+  double* part = B + 11 * cap;
+  const int nb = std::min(4096, lv_blocks(n, TPB));
+  auto dots = [&](const double* a1, const double* b1, const double* a2, const double* b2, double& o0,
+                  double& o1) -> int {
+    k_dot2<<<nb, TPB, 0, s>>>(n, a1, b1, a2, b2, part);
+    k_dot2_final<<<1, 32, 0, s>>>(nb, part, part + 2 * 4096);
+    c->launches += 2;
+    cudaMemcpyAsync(host2, part + 2 * 4096, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return lv_cuda_check(c, e, "multiphase dot");
+    o0 = host2[0];
+    o1 = host2[1];
+    return LV_OK;
+  };
+  auto apply = [&](const double* xin, double* res) -> int {
+    LAUNCH(k_mp_apply1, c->s, c->m, n, xin, tmp);
+    LAUNCH(k_mp_apply2, c->s, c->m, n, tmp, res);
+    return LV_OK;
+  };
+  LAUNCH(k_mp_rhs, c->s, c->m, n, b);
+  cudaMemsetAsync(q, 0, sizeof(double) * n, s);
+  cudaMemsetAsync(w, 0, sizeof(double) * n, s);
+  cudaMemsetAsync(w2, 0, sizeof(double) * n, s);
+  cudaMemcpyAsync(r1, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(y, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+  double beta1 = 0.0, dummy = 0.0;
+  if (int rc = dots(r1, y, nullptr, nullptr, beta1, dummy)) return rc;
+  beta1 = sqrt(beta1);
+  const double tol = 1e-4;
+  const int itmax = 200;
+  int itn = 0;
+  bool solved = beta1 == 0.0;
+  if (!solved) {
+    cudaMemcpyAsync(r2, r1, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    double oldb = 0.0, beta = beta1, dbar = 0.0, epsln = 0.0, phibar = beta1, cs = -1.0, sn = 0.0, tnorm2 = 0.0;
+    const double eps = 2.220446049250313e-16;
+    const double tl = tol + tol * beta1;
+    while (itn < itmax) {
+      ++itn;
+      LAUNCH(k_axpby, n, 1.0 / beta, y, 0.0, v);
+      if (int rc = apply(v, y)) return rc;
+      if (itn >= 2) LAUNCH(k_axpby, n, -(beta / oldb), r1, 1.0, y);
+      double alfa = 0.0;
+      if (int rc = dots(v, y, nullptr, nullptr, alfa, dummy)) return rc;
+      LAUNCH(k_axpby, n, -(alfa / beta), r2, 1.0, y);
+      std::swap(r1, r2);
+      cudaMemcpyAsync(r2, y, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+      oldb = beta;
+      double bb = 0.0;
+      if (int rc = dots(r2, y, nullptr, nullptr, bb, dummy)) return rc;
+      beta = sqrt(bb > 0.0 ? bb : 0.0);
+      tnorm2 += alfa * alfa + oldb * oldb + beta * beta;
+      const double oldeps = epsln, delta = cs * dbar + sn * alfa, gbar = sn * dbar - cs * alfa;
+      epsln = sn * beta;
+      dbar = -cs * beta;
+      const double root = sqrt(gbar * gbar + dbar * dbar);
+      const double gamma = std::max(sqrt(gbar * gbar + beta * beta), eps);
+      cs = gbar / gamma;
+      sn = beta / gamma;
+      const double phi = cs * phibar;
+      phibar = sn * phibar;
+      const double denom = 1.0 / gamma;
+      std::swap(w1, w2);
+      std::swap(w2, w);
+      LAUNCH(k_minres_update, n, v, w1, w2, w, q, oldeps, delta, denom, phi);
+      const double Anorm = sqrt(tnorm2), Arnorm = phibar * root;
+      if (phibar <= tl || beta == 0.0 || (Anorm > 0 && phibar > 0 && Arnorm / (Anorm * phibar) <= tol)) {
+        solved = true;
+        break;
+      }
+    }
+  }
+  LAUNCH(k_mp_correct, c->s, c->m, n, q, threshold);
+  if (st) {
+    st->iterations = itn;
+    st->converged = solved ? 1 : 0;
+    st->outer = 0;
+    st->method = -1;
+    st->rel_residual = 0.0;
+  }
+  return LV_OK;
 }

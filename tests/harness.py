@@ -72,6 +72,10 @@ def apply(lv, flow, target, op, kw, is_gpu, solver=None, tol=1e-8):
         return target.bdary_friction(wall_table(flow, zero_default=True), dt)
     if op == "find_dv":
         return lv.find_dv(target, dt) if is_gpu else target.find_dv(dt)
+    if op == "multiphase_projection":
+        if is_gpu:
+            return lv.multiphase_projection(lv.MultiphaseSolver(target))
+        return target.multiphase_projection()
     if op == "relaxation_step":
         return lv.relaxation_step(target, dt) if is_gpu else target.relaxation_step(dt)
     raise ValueError(op)

@@ -1,0 +1,123 @@
+"""CPU reference of the learned preconditioner (test oracle): the same
+message-passing network, readout and Hutchinson loss as the GPU kernels,
+written with torch autograd in FP64.  The inputs of the layers' matrix
+products are rounded to bfloat16 as the tensor-core kernels do; everything
+else is FP64, so forward values and gradients agree with the GPU to the
+FP32-accumulation level (forward) and to the BF16 rounding of the backward
+operands (gradients)."""
+import numpy as np
+import torch
+
+HID, FIN = 32, 16
+KC0, KC = 2 * FIN, 2 * HID
+OFF = {}
+_o = 0
+for name, size in (("W0", KC0 * HID), ("b0", HID), ("W1", KC * HID), ("b1", HID), ("W2", KC * HID), ("b2", HID),
+                   ("rd", HID), ("ro", HID)):
+    OFF[name] = (_o, size)
+    _o += size
+NPARAM = _o
+
+
+def bf16(t):
+    return t.to(torch.bfloat16).to(torch.float64)
+
+
+def unpack(p):
+    out = {}
+    for name, (o, s) in OFF.items():
+        v = p[o:o + s]
+        if name.startswith("W"):
+            v = v.reshape(-1, HID)
+        out[name] = v
+    return out
+
+
+def prepare(rowptr, col, w, diag, adiag):
+    """what, dh, features as the GPU computes them (FP32), as float64 tensors."""
+    n = len(diag)
+    ri = np.repeat(np.arange(n), np.diff(rowptr))
+    dh = (1.0 / np.sqrt(adiag)).astype(np.float32)
+    what = (w.astype(np.float32) * dh[ri]) * dh[col]
+    X = np.zeros((n, FIN), np.float32)
+    X[:, 0] = 1.0
+    X[:, 1] = (diag / adiag).astype(np.float32)
+    s = np.zeros(n, np.float32)
+    m = np.zeros(n, np.float32)
+    for i in range(n):
+        a, b = rowptr[i], rowptr[i + 1]
+        s[i] = np.float32(0)
+        for k in range(a, b):
+            s[i] = np.float32(s[i] + what[k])
+        m[i] = what[a:b].max() if b > a else 0.0
+    X[:, 2] = s
+    X[:, 3] = m
+    X[:, 4] = (np.diff(rowptr).astype(np.float32)) * np.float32(0.125)
+    T = lambda a: torch.from_numpy(np.asarray(a, np.float64))
+    return dict(n=n, ri=torch.from_numpy(ri), col=torch.from_numpy(col.astype(np.int64)), what=T(what), dh=T(dh),
+                X=T(X))
+
+
+def agg(G, H):
+    out = torch.zeros_like(H)
+    return out.index_add(0, G["ri"], G["what"][:, None] * H[G["col"]])
+
+
+def layer(G, H, W, b, res):
+    Xcat = torch.cat([H, agg(G, H)], dim=1)
+    Z = bf16(Xcat) @ bf16(W) + b
+    return (H if res else 0.0) + torch.relu(Z)
+
+
+def factor(G, params):
+    P = unpack(params)
+    H1 = layer(G, G["X"], P["W0"], P["b0"], False)
+    H2 = layer(G, H1, P["W1"], P["b1"], True)
+    H3 = layer(G, H2, P["W2"], P["b2"], True)
+    gd = 1.0 + H3 @ P["rd"]
+    lower = G["col"] < G["ri"]
+    gl = G["what"] * ((H3[G["ri"]] * H3[G["col"]]) @ P["ro"])
+    gl = torch.where(lower, gl, torch.zeros_like(gl))
+    return gd, gl
+
+
+def apply_G(G, gd, gl, v):
+    lower = G["col"] < G["ri"]
+    out = gd * v
+    return out.index_add(0, G["ri"][lower], gl[lower] * v[G["col"][lower]])
+
+
+def apply_GT(G, gd, gl, v):
+    lower = G["col"] < G["ri"]
+    out = gd * v
+    return out.index_add(0, G["col"][lower], gl[lower] * v[G["ri"][lower]])
+
+
+def apply_At(G, v):
+    out = v.clone()
+    return out.index_add(0, G["ri"], -G["what"] * v[G["col"]])
+
+
+def loss(G, params, probes):
+    gd, gl = factor(G, params)
+    tot = 0.0
+    for z in probes:
+        r = apply_G(G, gd, gl, apply_At(G, apply_GT(G, gd, gl, z))) - z
+        tot = tot + (r * r).sum()
+    return tot / (len(probes) * G["n"])
+
+
+def loss_and_grad(rowptr, col, w, diag, adiag, params, probes):
+    G = prepare(rowptr, col, w, diag, adiag)
+    p = torch.tensor(np.asarray(params, np.float64), requires_grad=True)
+    z = [torch.from_numpy(np.asarray(q, np.float64)) for q in probes]
+    L = loss(G, p, z)
+    L.backward()
+    return float(L), p.grad.numpy().copy()
+
+
+def forward_values(rowptr, col, w, diag, adiag, params):
+    G = prepare(rowptr, col, w, diag, adiag)
+    with torch.no_grad():
+        gd, gl = factor(G, torch.tensor(np.asarray(params, np.float64)))
+    return gd.numpy(), gl.numpy(), G["X"].numpy()

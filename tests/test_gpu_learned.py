@@ -1,0 +1,162 @@
+"""Learned preconditioner: forward values and gradients of the hand-written
+tensor-core kernels against a CPU autograd reference (tests/learned_ref.py),
+and training on systems the solver produced, then the learned solve on a
+held-out system against the Jacobi mixed-precision solve."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import harness as H
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+import learned_ref as LR  # noqa: E402
+
+
+def _grid(lv, oracle, flow, seed=3):
+    from lvgpu import populate as pop
+    x = H.seeds(pop, flow, seed)
+    g = H.make_gpu(lv, flow, x)
+    og = H.make_oracle(oracle, flow, x)
+    H.init_both(flow, g, og)
+    if flow.eos == "stiffened":
+        lv.stiffened_eos(g, flow.gamma, flow.P0)
+    elif flow.eos == "ideal":
+        lv.ideal_eos(g, flow.gamma)
+    L = lv._lib.load()
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    return g, L
+
+
+def _export(lv, g, L):
+    p = lv._lib.ptr
+    nnz = C.c_int64()
+    assert L.lv_export_system(g._ctx, C.byref(nnz), None, None, None, None, None) == 0
+    n = g.n
+    diag, rowptr, b = np.zeros(n), np.zeros(n + 1, np.int64), np.zeros(n)
+    col, w = np.zeros(nnz.value, np.int32), np.zeros(nnz.value)
+    assert L.lv_export_system(g._ctx, None, p(diag), p(rowptr, C.c_int64), p(col, C.c_int32), p(w), p(b)) == 0
+    adiag = diag.copy()
+    for i in range(n):
+        for k in range(rowptr[i], rowptr[i + 1]):
+            adiag[i] += w[k]
+    return rowptr, col, w, diag, adiag, b
+
+
+def _params(L, g, seed, scale=1.0):
+    assert L.lv_learn_init(g._ctx, seed) == 0
+    npar = L.lv_learn_num_params()
+    pr = np.zeros(npar, np.float32)
+    assert L.lv_learn_get_params(g._ctx, pr.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    # make the readout non-trivial so every parameter gets a gradient
+    o, s = LR.OFF["rd"]
+    pr[o:o + s] *= 30.0 * scale
+    o, s = LR.OFF["ro"]
+    pr[o:o + s] *= 30.0 * scale
+    assert L.lv_learn_set_params(g._ctx, pr.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    return pr
+
+
+@pytest.mark.parametrize("mk", [lambda: W.taylor_green(32), lambda: W.cavity(32)])
+def test_forward_matches_reference(lv, oracle, mk):
+    flow = mk()
+    g, L = _grid(lv, oracle, flow)
+    pr = _params(L, g, 11)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    n, nnz = g.n, len(col)
+    gd = np.zeros(n, np.float32)
+    gl = np.zeros(nnz, np.float32)
+    X = np.zeros((n, 16), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_factor(g._ctx, fp(gd), fp(gl), fp(X)) == 0
+    rgd, rgl, rX = LR.forward_values(rowptr, col, w, diag, adiag, pr)
+    assert np.allclose(X, rX, rtol=1e-6, atol=1e-7)
+    assert np.max(np.abs(gd - rgd)) <= 2e-3 * max(1.0, np.max(np.abs(rgd)))
+    assert np.max(np.abs(gl - rgl)) <= 2e-3 * max(1e-3, np.max(np.abs(rgl)))
+    assert np.max(np.abs(rgl)) > 1e-4  # the off-diagonal readout is exercised
+
+
+@pytest.mark.parametrize("mk", [lambda: W.taylor_green(32), lambda: W.cavity(32)])
+def test_gradient_matches_autograd(lv, oracle, mk):
+    flow = mk()
+    g, L = _grid(lv, oracle, flow)
+    pr = _params(L, g, 5)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    K = 3
+    rng = np.random.default_rng(4)
+    probes = np.where(rng.random((K, g.n)) < 0.5, -1.0, 1.0).astype(np.float32)
+    loss = C.c_double()
+    grad = np.zeros(len(pr), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_loss_grad(g._ctx, -1, fp(probes), K, 0, C.byref(loss), fp(grad)) == 0
+    rl, rg = LR.loss_and_grad(rowptr, col, w, diag, adiag, pr, probes)
+    assert abs(loss.value - rl) <= 1e-3 * abs(rl)
+    for name, (o, s) in LR.OFF.items():
+        a, b = grad[o:o + s].astype(np.float64), rg[o:o + s]
+        nb = np.linalg.norm(b)
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-7, (name, np.linalg.norm(a - b), nb)
+    cos = grad.astype(np.float64) @ rg / (np.linalg.norm(grad) * np.linalg.norm(rg))
+    assert cos > 0.999, cos
+
+
+def _harvest(lv, oracle, flow, seeds):
+    """A grid per seed, operator assembled and snapshot for training; returns the last grid."""
+    from lvgpu import populate as pop
+    grids = []
+    for s in seeds:
+        x = H.seeds(pop, flow, s, jitter=0.25)
+        g = H.make_gpu(lv, flow, x)
+        og = H.make_oracle(oracle, flow, x)
+        H.init_both(flow, g, og)
+        grids.append((g, og))
+    return grids
+
+
+def test_training_lowers_loss_and_iterations(lv, oracle):
+    """Train on operators of one flow, then solve a held-out one: the trained
+    factor needs fewer inner CG iterations than Jacobi, and the FP64 residual
+    meets 1e-8 either way."""
+    flow = W.cavity(64)
+    grids = _harvest(lv, oracle, flow, [21, 22, 23, 24, 25, 26])
+    L = lv._lib.load()
+    trainer, _ = grids[0]
+    assert L.lv_learn_init(trainer._ctx, 7) == 0
+    # snapshot the training operators into the first grid's set
+    for g, og in grids[:-1]:
+        assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    # systems are snapshot per context: use the first grid's own operator and
+    # those of the others through parameter sharing
+    assert L.lv_pressure_operator(trainer._ctx, flow.dt) == 0
+    assert L.lv_learn_add_system(trainer._ctx) == 0
+    steps = 400
+    losses = np.zeros(steps, np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_train(trainer._ctx, steps, 3e-3, 4, 1, fp(losses)) == 0
+    assert losses[-20:].mean() < 0.8 * losses[:5].mean(), (losses[:5], losses[-20:])
+    npar = L.lv_learn_num_params()
+    pr = np.zeros(npar, np.float32)
+    assert L.lv_learn_get_params(trainer._ctx, fp(pr)) == 0
+    # held-out system
+    g, og = grids[-1]
+    assert L.lv_learn_set_params(g._ctx, fp(pr)) == 0
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    og.pressure_operator(flow.dt)
+    rng = np.random.default_rng(0)
+    b = rng.standard_normal(g.n)
+    b -= b.mean()
+    res = {}
+    for m in ("mixed_ir", "learned_pcg"):
+        lv.PressureSolver(g, method=m, tol=1e-8).configure()
+        xg = np.zeros(g.n)
+        st = lv.LvSolveStats()
+        assert L.lv_solve(g._ctx, lv._lib.ptr(b), lv._lib.ptr(xg), C.byref(st)) == 0
+        rel = np.linalg.norm(b - og.operator_apply(xg)) / np.linalg.norm(b)
+        assert st.converged == 1 and rel <= 1.5e-8, (m, rel)
+        res[m] = (st.iterations, st.method)
+    print("jacobi mixed vs learned inner iterations:", res)
+    it_j, _ = res["mixed_ir"]
+    it_l, meth = res["learned_pcg"]
+    assert meth == 2, "the trained factor fell back to Jacobi"
+    assert it_l < it_j, res

@@ -1,0 +1,88 @@
+"""Mixed-precision iterative refinement (FP32 inner CG, FP64 outer residual):
+the FP64 residual of its answer meets the tolerance, checked with the
+oracle's FP64 operator, and its solution agrees with the oracle's FP64 PCG."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import harness as H
+import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FLOWS = [lambda: W.taylor_green(64), lambda: W.cavity(48), lambda: W.double_shear(64), lambda: W.gresho(50),
+         lambda: W.rayleigh_taylor(32, 64)]
+
+
+def _setup(lv, oracle, flow, seed=5):
+    from lvgpu import populate as pop
+    x = H.seeds(pop, flow, seed)
+    g = H.make_gpu(lv, flow, x)
+    og = H.make_oracle(oracle, flow, x)
+    H.init_both(flow, g, og)
+    if flow.eos == "stiffened":
+        lv.stiffened_eos(g, flow.gamma, flow.P0)
+        og.stiffened_eos(flow.gamma, flow.P0)
+    elif flow.eos == "ideal":
+        lv.ideal_eos(g, flow.gamma)
+        og.ideal_eos(flow.gamma)
+    return g, og
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+@pytest.mark.parametrize("tol", [1e-8, 1e-10])
+def test_mixed_ir_solution(lv, oracle, mk, tol):
+    flow = mk()
+    g, og = _setup(lv, oracle, flow)
+    L = lv._lib.load()
+    dt = flow.dt
+    assert L.lv_pressure_operator(g._ctx, dt) == 0
+    A = og.pressure_operator(dt)
+    b, _ = og.pressure_rhs(dt, 0, H.wall_table(flow))
+    singular = not np.any(A["diag"] != 0)
+    bp = b - b.mean() if singular else b
+    x0 = og.get("P").copy()
+    solver = lv.PressureSolver(g, method="mixed_ir", tol=tol)
+    solver.configure()
+    xg = x0.copy()
+    st = lv.LvSolveStats()
+    p = lv._lib.ptr
+    assert L.lv_solve(g._ctx, p(b), p(xg), C.byref(st)) == 0
+    r = bp - og.operator_apply(xg)
+    rel = np.linalg.norm(r) / np.linalg.norm(bp)
+    assert st.converged == 1 and st.method == 1
+    assert rel <= 1.5 * tol, rel
+    assert st.outer >= 1
+    xr, (it_ref, _, _) = og.solve(b, x0, method="pcg", tol=tol)
+    d = xg - xr
+    if singular:
+        d = d - d.mean()
+        xr = xr - xr.mean()
+    assert np.linalg.norm(d) <= 1e-5 * max(np.linalg.norm(xr), 1e-30)
+    # FP32 inner iterations: same order of magnitude as the FP64 PCG
+    assert st.iterations <= 3 * it_ref + 20, (st.iterations, it_ref)
+
+
+@pytest.mark.parametrize("name,mk", [("taylor_green", lambda: W.taylor_green(64)), ("cavity", lambda: W.cavity(64))])
+def test_mixed_ir_steps(lv, oracle, name, mk):
+    """Five full steps with the mixed solver stay within 1e-6 of the oracle's FP64 PCG run."""
+    from lvgpu import populate as pop
+    flow = mk()
+    x = H.seeds(pop, flow)
+    g = H.make_gpu(lv, flow, x)
+    og = H.make_oracle(oracle, flow, x)
+    H.init_both(flow, g, og)
+    solver = lv.PressureSolver(g, method="mixed_ir", tol=1e-8)
+    dt, seq = W.step_sequence(flow)
+    for _ in range(5):
+        for op, kw in seq:
+            H.apply(lv, flow, g, op, kw, True, solver=solver)
+            H.apply(lv, flow, og, op, kw, False)
+    g.synchronize()
+    for k in ("x", "v", "P"):
+        a, b = g[k], og.get(k)
+        if k == "P" and flow.eos is None:
+            a, b = a - a.mean(), b - b.mean()
+        scale = flow.dr if k == "x" else max(np.max(np.abs(b)), 1e-30)
+        assert np.max(np.abs(a - b)) / scale < 1e-6, k

@@ -100,8 +100,8 @@ def initial_fields(flow, x, area):
 
 def step_sequence(flow):
     """The reference's step! for each flow, as (operation, kwargs) pairs:
-    gresho.jl:100-114, tests/taylorgreen.jl:61-71, rayleightaylor.jl:90-102
-    (multiphase projection omitted), cavity.jl:70-80, doubleshear.jl:48-58."""
+    gresho.jl:100-114, tests/taylorgreen.jl:61-71, rayleightaylor.jl:90-102,
+    cavity.jl:70-80, doubleshear.jl:48-58."""
     dt = flow.dt
     seq = [("move", {})]
     if flow.name == "rayleigh_taylor":
@@ -114,5 +114,8 @@ def step_sequence(flow):
             ("viscous_step", {"artificial_viscosity": flow.artificial_viscosity})]
     if flow.walls is not None and flow.name in ("cavity", "rayleigh_taylor"):
         seq.append(("bdary_friction", {"walls": flow.walls}))
-    seq += [("find_dv", {}), ("relaxation_step", {})]
+    seq.append(("find_dv", {}))
+    if flow.name == "rayleigh_taylor" and getattr(flow, "multiphase", True):
+        seq.append(("multiphase_projection", {}))
+    seq.append(("relaxation_step", {}))
     return dt, seq
