@@ -37,6 +37,14 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 NX = NY = 256
 N = NX * NY
 WORKLOAD = "taylor_green_256x256"
+
+
+def set_size(nx):
+    """The benchmark workload is 256 x 256; other sizes are for profiling."""
+    global NX, NY, N, WORKLOAD
+    NX = NY = int(nx)
+    N = NX * NY
+    WORKLOAD = f"taylor_green_{NX}x{NY}"
 METRIC = "particle-steps/s at 1 GB300; pressure solve ms & CG iters, learned vs plain PCG @1e-8"
 UNIT = "particle-steps/s"
 L2_FLUSH_BYTES = 512 << 20
@@ -214,10 +222,11 @@ def run_ours(args, world, rank, local):
         gpu_step(lv, g, solver, fl, snapshot=True)
     g.synchronize()
     t_tr = time.perf_counter()
-    train_steps = 300
-    losses = np.zeros(train_steps, np.float32)
+    train_steps = 0 if args.no_compare else 300
+    losses = np.zeros(max(train_steps, 1), np.float32)
     assert L.lv_learn_init(g._ctx, 1234) == 0
-    assert L.lv_learn_train(g._ctx, train_steps, 3e-3, 4, 99, losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    if train_steps:
+        assert L.lv_learn_train(g._ctx, train_steps, 3e-3, 4, 99, losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
     train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps, "probes": 4,
                   "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
                   "loss_last": float(losses[-10:].mean())}
@@ -297,14 +306,10 @@ def run_ours(args, world, rank, local):
     clocks = clk.summary()
 
     # ---- roofline of the dominant kernel family
-    nnz = None
-    try:
-        nnzc = C.c_int64()
-        L.lv_export_system(g._ctx, C.byref(nnzc), None, None, None, None, None)
-        nnz = nnzc.value
-    except Exception:
-        pass
-    F = nnz if nnz is not None else 6 * N
+    # interior faces (= off-diagonal nonzeros of the pressure operator)
+    nfc = C.c_int64()
+    rc = L.lv_get_faces(g._ctx, C.byref(nfc), None, None, None, None, None, None)
+    F = nfc.value if rc == 0 and nfc.value > 0 else 6 * N
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
@@ -319,17 +324,14 @@ def run_ours(args, world, rank, local):
     dom_ms = kt[dom][1]
     dom_launches = max(kt[dom][0], 1)
     achieved = (fams[dom] / dom_launches) / ((dom_ms / dom_launches) / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(dom)
+    traffic = read_traffic(WORKLOAD, dom)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
         "config": {"workload": WORKLOAD, "particles": N, "solver": "jacobi_pcg fp64 tol 1e-8, 10 sweeps/step",
                    "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": f"replicas x{world}",
-                   "l2": "512 MiB buffer written between timed steps (state ~15 MB fits in L2)"},
+                   "l2": "512 MiB buffer written between timed steps (the 256x256 state, ~15 MB, fits in L2)"},
         "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1]) / args.steps,
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
                      "solves": solves, "solvers": comparison},
@@ -345,6 +347,20 @@ def run_ours(args, world, rank, local):
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, sample_steps=2)
     return line
+
+
+def read_traffic(workload, family):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    of the family's kernel on this workload, from the committed ncu summary
+    table profiles/traffic.txt (columns: family workload bytes_per_launch ...)."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        f = ln.split()
+        if len(f) >= 3 and not ln.startswith("#") and f[0] == family and f[1] == workload:
+            return float(f[2])
+    return None
 
 
 # ------------------------------------------------------------ reference arm
@@ -429,7 +445,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
+    ap.add_argument("--nx", type=int, default=256, help="lattice side (the workload is 256; others for profiling)")
     args = ap.parse_args()
+    set_size(args.nx)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
     if args.impl == "reference":

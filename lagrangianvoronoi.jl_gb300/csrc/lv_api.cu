@@ -276,6 +276,9 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.p32 = dalloc<float>(c, cap, &ok);
   sv.q32 = dalloc<float>(c, cap, &ok);
   sv.d32 = dalloc<float>(c, cap, &ok);
+  sv.e32 = dalloc<float>(c, cap, &ok);
+  sv.f32a = dalloc<float>(c, cap, &ok);
+  sv.f32b = dalloc<float>(c, cap, &ok);
   sv.part = dalloc<double>(c, 8 * 4096, &ok);
   sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);

@@ -93,7 +93,7 @@ struct SolverDev {
   double* w;    // [nnz_cap]
   float* w32;   // FP32 copy for the mixed-precision inner solve
   double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
-  float *dinv32, *r32, *z32, *p32, *q32, *d32;
+  float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
   long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
   unsigned* bar;      // grid barrier {count, generation}

@@ -919,6 +919,235 @@ __global__ void __launch_bounds__(SP_TPB) k_lpcg_reg(PCGArgs a, LearnArgs la) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Streaming variant of the mixed-precision solve for systems too large for
+// the register-resident kernel: the same algorithm (FP64 refinement, FP32
+// inner CG with double-float dots, Jacobi or learned preconditioner), with
+// every vector in global memory and grid-stride loops over the rows.
+// ---------------------------------------------------------------------------
+struct StreamArgs {
+  const float* w32;   // FP32 copy of the off-diagonal weights
+  const float* dg32;  // FP32 diagonal term
+  const float* dinv32;
+  double* r64;        // FP64 residual scratch
+  float *r, *z, *p, *q, *d, *rh, *t;
+};
+
+__device__ __forceinline__ float apply32_row(int i, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                             const float* __restrict__ w32, float dg, const float* __restrict__ v) {
+  const float vi = v[i];
+  float acc = dg * vi;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fmaf(w32[k], vi - v[col[k]], acc);
+  return acc;
+}
+
+__global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, StreamArgs sa) {
+  __shared__ double sh[4 * 32];
+  __shared__ float2 shf[4 * 32];
+  __shared__ int s_flag[2];
+  const int n = a.n;
+  const int nb = gridDim.x;
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  float2* part32 = reinterpret_cast<float2*>(a.part);
+  double bmean = 0.0;
+  if (*a.nonsingular == 0) {
+    double v[1] = {0.0};
+    for (int i = t0; i < n; i += stride) v[0] += a.b[i];
+    block_sums<1>(v, sh);
+    if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
+    if (!grid_barrier(a.bar, a.status)) return;
+    double t[1];
+    grid_totals<1>(a.part, 0, t);
+    bmean = t[0] / (double)n;
+    if (!grid_barrier(a.bar, a.status)) return;
+  }
+  const int jref = *la.jref;
+  const int cap = jref > 0 ? jref : a.itmax;
+  bool learned = la.learned != 0;
+  int it = 0, outer = 0;
+  double bnorm2 = 0.0, rtrue2 = 0.0;
+  // z = M^-1 r (learned mode: two neighbour exchanges)
+  auto precond = [&]() -> bool {
+    if (!learned) {
+      for (int i = t0; i < n; i += stride) sa.z[i] = sa.dinv32[i] * sa.r[i];
+      return true;
+    }
+    for (int i = t0; i < n; i += stride) sa.rh[i] = la.dh[i] * sa.r[i];
+    if (!grid_barrier(a.bar, a.status)) return false;
+    for (int i = t0; i < n; i += stride) {
+      float t = la.gd[i] * sa.rh[i];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
+        const int j = a.col[k];
+        if (j < i) t = fmaf(la.gl[k], sa.rh[j], t);
+      }
+      sa.t[i] = t;
+    }
+    if (!grid_barrier(a.bar, a.status)) return false;
+    for (int i = t0; i < n; i += stride) {
+      float u = la.gd[i] * sa.t[i];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
+        const int j = a.col[k];
+        if (j > i && la.rev[k] >= 0) u = fmaf(la.gl[la.rev[k]], sa.t[j], u);
+      }
+      sa.z[i] = la.dh[i] * fmaf(la.eps, sa.rh[i], u);
+    }
+    return true;
+  };
+  for (; outer < MIR_MAX_OUTER; ++outer) {
+    double v[2] = {0.0, 0.0};
+    for (int i = t0; i < n; i += stride) {
+      const double xi = a.x[i];
+      double acc = a.diag[i] * xi;
+      for (int e = a.rowptr[i]; e < a.rowptr[i + 1]; ++e) acc += a.w[e] * (xi - a.x[a.col[e]]);
+      const double bi = a.b[i] - bmean;
+      const double ri = bi - acc;
+      sa.r64[i] = ri;
+      v[0] += ri * ri;
+      v[1] += bi * bi;
+    }
+    block_sums<2>(v, sh);
+    if (threadIdx.x == 0) {
+      a.part[0 * nb + blockIdx.x] = v[0];
+      a.part[1 * nb + blockIdx.x] = v[1];
+    }
+    if (!grid_barrier(a.bar, a.status)) return;
+    {
+      double t2[2];
+      grid_totals<2>(a.part, 0, t2);
+      rtrue2 = t2[0];
+      bnorm2 = t2[1];
+    }
+    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax) break;
+    const double sigma = sqrt(rtrue2);
+    const double inv_sigma = 1.0 / sigma;
+    for (int i = t0; i < n; i += stride) {
+      sa.r[i] = (float)(sa.r64[i] * inv_sigma);
+      sa.d[i] = 0.f;
+      sa.p[i] = 0.f;
+      sa.q[i] = 0.f;
+    }
+    const float rho_stop = fmaxf(MIR_INNER_TOL * MIR_INNER_TOL, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
+    if (!precond()) return;
+    float rz;
+    {
+      float2 v1[1] = {make_float2(0.f, 0.f)};
+      for (int i = t0; i < n; i += stride) v1[0] = df_add(v1[0], df_prod(sa.r[i], sa.z[i]));
+      df_block_sums<1>(v1, shf);
+      if (threadIdx.x == 0) part32[2 * nb + blockIdx.x] = v1[0];
+      if (!grid_barrier(a.bar, a.status)) return;
+      float t1[1];
+      df_grid_totals<1>(part32, 2, t1);
+      rz = t1[0];
+    }
+    float beta = 0.f;
+    while (true) {
+      float2 v1[1] = {make_float2(0.f, 0.f)};
+      for (int i = t0; i < n; i += stride) {
+        const float az = apply32_row(i, a.rowptr, a.col, sa.w32, sa.dg32[i], sa.z);
+        const float pi = fmaf(beta, sa.p[i], sa.z[i]);
+        const float qi = fmaf(beta, sa.q[i], az);
+        sa.p[i] = pi;
+        sa.q[i] = qi;
+        v1[0] = df_add(v1[0], df_prod(pi, qi));
+      }
+      df_block_sums<1>(v1, shf);
+      if (threadIdx.x == 0) part32[3 * nb + blockIdx.x] = v1[0];
+      if (!grid_barrier(a.bar, a.status)) return;
+      float pq[1];
+      df_grid_totals<1>(part32, 3, pq);
+      const float alpha = rz / pq[0];
+      ++it;
+      float rr2, rzn;
+      if (!learned) {
+        float2 v2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        for (int i = t0; i < n; i += stride) {
+          sa.d[i] = fmaf(alpha, sa.p[i], sa.d[i]);
+          const float ri = fmaf(-alpha, sa.q[i], sa.r[i]);
+          const float zi = sa.dinv32[i] * ri;
+          sa.r[i] = ri;
+          sa.z[i] = zi;
+          v2[0] = df_add(v2[0], df_prod(ri, ri));
+          v2[1] = df_add(v2[1], df_prod(ri, zi));
+        }
+        df_block_sums<2>(v2, shf);
+        if (threadIdx.x == 0) {
+          part32[4 * nb + blockIdx.x] = v2[0];
+          part32[5 * nb + blockIdx.x] = v2[1];
+        }
+        if (!grid_barrier(a.bar, a.status)) return;
+        float t2[2];
+        df_grid_totals<2>(part32, 4, t2);
+        rr2 = t2[0];
+        rzn = t2[1];
+      } else {
+        float2 v2[1] = {make_float2(0.f, 0.f)};
+        for (int i = t0; i < n; i += stride) {
+          sa.d[i] = fmaf(alpha, sa.p[i], sa.d[i]);
+          const float ri = fmaf(-alpha, sa.q[i], sa.r[i]);
+          sa.r[i] = ri;
+          v2[0] = df_add(v2[0], df_prod(ri, ri));
+        }
+        df_block_sums<1>(v2, shf);
+        if (threadIdx.x == 0) part32[4 * nb + blockIdx.x] = v2[0];
+        if (!precond()) return;  // its first barrier also publishes the ||r|| partials
+        float t1[1];
+        df_grid_totals<1>(part32, 4, t1);
+        rr2 = t1[0];
+        rzn = 0.f;
+      }
+      if (threadIdx.x == 0) {
+        const int stop = (rr2 <= rho_stop || it >= a.itmax || !(pq[0] > 0.f)) ? 1 : 0;
+        s_flag[0] = stop;
+        s_flag[1] = (learned && it >= cap && !stop) ? 1 : 0;
+      }
+      __syncthreads();
+      const int stop = s_flag[0], fall = s_flag[1];
+      __syncthreads();
+      if (stop) break;
+      if (fall) {
+        learned = false;
+        break;
+      }
+      if (learned) {
+        float2 v3[1] = {make_float2(0.f, 0.f)};
+        for (int i = t0; i < n; i += stride) v3[0] = df_add(v3[0], df_prod(sa.r[i], sa.z[i]));
+        df_block_sums<1>(v3, shf);
+        if (threadIdx.x == 0) part32[5 * nb + blockIdx.x] = v3[0];
+        if (!grid_barrier(a.bar, a.status)) return;
+        float t1[1];
+        df_grid_totals<1>(part32, 5, t1);
+        rzn = t1[0];
+      }
+      beta = rzn / rz;
+      rz = rzn;
+    }
+    for (int i = t0; i < n; i += stride) a.x[i] += sigma * (double)sa.d[i];
+    if (!grid_barrier(a.bar, a.status)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *a.out_iters = it;
+    *la.out_outer = outer;
+    *la.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
+    if (!la.learned) *la.jref = it;
+    a.out_d[0] = rtrue2;
+    a.out_d[1] = bnorm2;
+    a.out_d[2] = rtrue2;
+    a.counters[0] += 1;
+    a.counters[1] += it;
+  }
+}
+
+__global__ void k_to_f32(int n, const int* __restrict__ rowptr, const double* __restrict__ w,
+                         const double* __restrict__ diag, const double* __restrict__ dinv, float* w32, float* dg32,
+                         float* dinv32) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) w32[k] = (float)w[k];
+  dg32[i] = (float)diag[i];
+  dinv32[i] = (float)dinv[i];
+}
+
 __global__ void k_any_nonzero(const double* v, int n, int* flag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && v[i] != 0.0) atomicOr(flag, 1);
@@ -927,6 +1156,7 @@ __global__ void k_any_nonzero(const double* v, int n, int* flag) {
 int g_pcg_blocks_per_sm = -1;
 int g_reg_blocks_per_sm[2] = {-1, -1};
 int g_lpcg_blocks_per_sm[2] = {-1, -1};
+int g_str_blocks_per_sm = -1;
 
 }  // namespace
 
@@ -1038,7 +1268,50 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
       if (e != cudaSuccess) return lv_cuda_check(c, e, "k_lpcg_reg cooperative launch");
       return LV_OK;
     }
-    // larger systems fall through to the FP64 streaming solver
+    // larger systems: the streaming variant
+    {
+      LearnArgs la;
+      if (learned) {
+        lv_learn_factor_ptrs(c, &la.gd, &la.gl, &la.dh, &la.rev);
+        if (!la.gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
+      } else {
+        la.gd = la.gl = la.dh = nullptr;
+        la.rev = nullptr;
+      }
+      la.eps = c->learn_eps;
+      la.rhat = la.tbuf = la.zbuf = nullptr;
+      la.jref = c->sv.iters + LV_IT_JREF;
+      la.out_outer = c->sv.iters + LV_IT_OUTER + slot;
+      la.out_method = c->sv.iters + LV_IT_METHOD + slot;
+      la.learned = learned ? 1 : 0;
+      StreamArgs sa;
+      k_to_f32<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, c->sv.rowptr, c->sv.w, c->sv.diag, c->sv.dinv, c->sv.w32,
+                                                           c->sv.d32, c->sv.dinv32);
+      c->launches++;
+      sa.w32 = c->sv.w32;
+      sa.dg32 = c->sv.d32;
+      sa.dinv32 = c->sv.dinv32;
+      sa.r64 = c->sv.r;
+      sa.r = c->sv.r32;
+      sa.z = c->sv.z32;
+      sa.p = c->sv.p32;
+      sa.q = c->sv.q32;
+      sa.d = c->sv.e32;
+      sa.rh = c->sv.f32a;
+      sa.t = c->sv.f32b;
+      if (g_str_blocks_per_sm < 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_lpcg_str, CG_TPB, 0);
+        g_str_blocks_per_sm = b > 0 ? b : 1;
+      }
+      const int nbs = std::max(1, std::min(c->num_sms * std::min(g_str_blocks_per_sm, 4), lv_blocks(n, CG_TPB)));
+      void* sargs[] = {&a, &la, &sa};
+      cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_lpcg_str, dim3(nbs), dim3(CG_TPB), sargs, 0,
+                                                  c->stream);
+      c->launches++;
+      if (e != cudaSuccess) return lv_cuda_check(c, e, "k_lpcg_str cooperative launch");
+      return LV_OK;
+    }
   }
   // small systems: register-resident pipelined CG, one barrier per iteration
   if (g_reg_blocks_per_sm[0] < 0) {
