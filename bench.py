@@ -196,7 +196,8 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
         L.lv_kernel_timing(g._ctx, 0)
         out[method] = {"solve_ms_per_step": (ms["pcg"] + ms["rhs"]) / steps,
                        "pcg_kernel_ms_per_step": ms["pcg"] / steps,
-                       "cg_iters_per_step": (i1.value - i0.value) / steps}
+                       "cg_iters_per_step": (i1.value - i0.value) / steps,
+                       "us_per_iteration": 1e3 * ms["pcg"] / max(i1.value - i0.value, 1)}
         if method == "learned_pcg":
             out[method]["fallbacks_to_jacobi"] = fallbacks
     out["learned_pcg"]["training"] = train_info

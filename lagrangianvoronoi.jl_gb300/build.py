@@ -21,6 +21,7 @@ UNITS = {
     "lv_physics.cu": ["--fmad=false"],
     "lv_solver.cu": [],
     "lv_learn.cu": [],
+    "lv_fcg.cu": [],
 }
 
 

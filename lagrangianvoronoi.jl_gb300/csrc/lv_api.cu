@@ -280,6 +280,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.f32a = dalloc<float>(c, cap, &ok);
   sv.f32b = dalloc<float>(c, cap, &ok);
   sv.part = dalloc<double>(c, 8 * 4096, &ok);
+  sv.fslots = dalloc<unsigned long long>(c, LV_FCG_SLOT_WORDS, &ok);
   sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);
   sv.iters = dalloc<int>(c, LV_IT_SIZE, &ok);
@@ -301,6 +302,7 @@ int lv_destroy(lv_ctx* c) {
   cudaSetDevice(c->dev);
   if (c->stream) cudaStreamSynchronize(c->stream);
   lv_learn_free(c);
+  lv_fcg_free(c);
   for (void* p : c->allocs) cudaFree(p);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->ev0) cudaEventDestroy(c->ev0);

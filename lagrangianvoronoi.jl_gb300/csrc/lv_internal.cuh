@@ -29,6 +29,7 @@
 #define LV_IT_METHOD 64        // [32] method used per slot (learned solves)
 #define LV_IT_JREF 96          // iterations of the last Jacobi mixed solve
 #define LV_IT_NONSINGULAR 97   // set when some diagonal term is nonzero
+#define LV_IT_EPOCH 98         // last reduction epoch of the flag-reduced solver
 #define LV_IT_SIZE 128
 
 // Status bits set on the device with atomicOr; decoded on the host.
@@ -100,6 +101,12 @@ struct SolverDev {
   int* iters;         // device-side stats
   double* dstats;     // device-side stats
   int64_t nnz_cap;
+  unsigned long long* fslots;  // flag-published reduction words (lv_fcg.cu)
+  // explicit learned M^-1 on the two-hop pattern (lv_fcg.cu, allocated on first use)
+  int *mcnt = nullptr, *mcol = nullptr;
+  float *mval = nullptr, *mdiag = nullptr;
+  int* mok = nullptr;
+  int mrows = 0;
 };
 
 struct LearnState;  // learned preconditioner (lv_learn.cu)
@@ -185,6 +192,13 @@ int lv_solver_assemble(lv_ctx* c, double dt);
 int lv_solver_solve(lv_ctx* c, double* dst_P, lv_solve_stats* st_dev_or_null, int stats_slot);
 int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev);
 int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
+
+// ---- flag-reduced mixed-precision solver (lv_fcg.cu)
+#define LV_FCG_SLOT_WORDS (6 * 4 * 1024)
+int lv_fcg_capacity(lv_ctx* c);
+int lv_fcg_build_minv(lv_ctx* c);
+int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned);
+void lv_fcg_free(lv_ctx* c);
 
 #define LV_LAUNCH_CHECK(c, what)                                   \
   do {                                                             \

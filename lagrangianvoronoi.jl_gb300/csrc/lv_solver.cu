@@ -1231,8 +1231,11 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     if (learned && !c->factor_valid) {
       KernelTimer kf(c, LV_KF_RHS);
       if (int rc = lv_learn_factor_current(c)) return rc;
+      if (int rc = lv_fcg_build_minv(c)) return rc;
       c->factor_valid = true;
     }
+    // systems that fit one or two blocks per SM: flag-reduced solver
+    if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);
     if (g_lpcg_blocks_per_sm[0] < 0) {
       int b1 = 0, b2 = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lpcg_reg<1>, SP_TPB, 0);
