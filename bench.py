@@ -223,12 +223,15 @@ def run_ours(args, world, rank, local):
         gpu_step(lv, g, solver, fl, snapshot=True)
     g.synchronize()
     t_tr = time.perf_counter()
-    train_steps = 0 if args.no_compare else 300
+    train_steps = 0 if args.no_compare else args.train_steps
     losses = np.zeros(max(train_steps, 1), np.float32)
     assert L.lv_learn_init(g._ctx, 1234) == 0
     if train_steps:
-        assert L.lv_learn_train(g._ctx, train_steps, 3e-3, 4, 99, losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
-    train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps, "probes": 4,
+        assert L.lv_learn_train(g._ctx, train_steps, args.train_lr, args.train_probes, 99,
+                                losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps,
+                  "objective": "fsai-kaporin" if args.train_probes == 0 else f"hutchinson x{args.train_probes}",
+                  "lr": args.train_lr,
                   "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
                   "loss_last": float(losses[-10:].mean())}
 
@@ -447,6 +450,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
     ap.add_argument("--nx", type=int, default=256, help="lattice side (the workload is 256; others for profiling)")
+    ap.add_argument("--train-steps", type=int, default=400, help="Adam steps of the learned preconditioner")
+    ap.add_argument("--train-probes", type=int, default=0, help="0: FSAI/Kaporin objective; K: Hutchinson, K probes")
+    ap.add_argument("--train-lr", type=float, default=5e-3)
     args = ap.parse_args()
     set_size(args.nx)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

@@ -204,11 +204,14 @@ int lv_learn_set_params(lv_ctx* ctx, const float* in);
 int lv_learn_add_system(lv_ctx* ctx);                          /* snapshot the assembled operator */
 int32_t lv_learn_num_systems(lv_ctx* ctx);
 int lv_learn_clear_systems(lv_ctx* ctx);
-/* Adam on the snapshot systems (round robin), `probes` Rademacher probes per
- * step; losses[steps] may be NULL. */
+/* Adam on the snapshot systems (round robin); losses[steps] may be NULL.
+ * probes = 0: the exact FSAI (Kaporin) objective (1/n)[tr(Gt At Gt^T) -
+ * 2 sum log Gt_ii]; probes = K in 1..8: a Hutchinson estimate of
+ * ||Gt At Gt^T - I||_F^2 / n with K Rademacher probes per step. */
 int lv_learn_train(lv_ctx* ctx, int32_t steps, float lr, int32_t probes, uint64_t seed, float* losses);
-/* Loss and gradient for system `sys` (< 0: the assembled operator), with the
- * given probes[K][n] or Rademacher probes from seed; grad[num_params] may be NULL. */
+/* Loss and gradient for system `sys` (< 0: the assembled operator): K = 0 the
+ * FSAI (Kaporin) objective, K >= 1 the Hutchinson loss with the given
+ * probes[K][n] or Rademacher probes from seed; grad[num_params] may be NULL. */
 int lv_learn_loss_grad(lv_ctx* ctx, int32_t sys, const float* probes, int32_t K, uint64_t seed, double* loss,
                        float* grad);
 /* Factor of the assembled operator: gdiag[n], glower[nnz] (CSR positions with

@@ -1,20 +1,22 @@
-// Mixed-precision pressure solve with flag-published reductions
-// (LV_METHOD_MIXED_IR and LV_METHOD_LEARNED_PCG on systems whose rows fit
-// the registers of one block per SM).
+// Mixed-precision pressure solve (LV_METHOD_MIXED_IR and LV_METHOD_LEARNED_PCG)
+// for systems whose rows fit the registers of one block per SM.
 //
 // The operator is the reference's PressureOperator (pressure.jl:89-130):
 //   (A x)_i = diag_i x_i + sum_j w_ij (x_i - x_j).
-// Outer loop in FP64: r = b - A x in that difference form, checked against
-// tol ||b||; inner solve of A d = r / ||r|| by preconditioned CG in FP32
-// (dot products summed by warp butterflies, then over blocks in a fixed
-// order); x += ||r|| d.  The preconditioner is Jacobi or
-// the learned M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2 (Gt from lv_learn.cu),
-// held as an explicit sparse matrix on the two-hop pattern of the operator
-// so that applying it needs one neighbour exchange.
+// x and the true residual b - A x (that difference form, exact on constants)
+// are FP64 and checked against tol ||b||.  In between, preconditioned CG runs
+// in FP32 on the residual scaled to unit norm; each refinement step folds
+// the FP32 correction into x and restarts from the FP64 residual (k_fcg).  The preconditioner is Jacobi or the learned
+// M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2 (Gt from lv_learn.cu), held as an
+// explicit sparse matrix on the two-hop pattern of the operator so that
+// applying it needs one neighbour exchange.
 //
-// Reductions: one grid-wide phase per reduction (fphase below), which also
-// makes the neighbour values stored before it visible after it.  An iteration
-// costs two phases (Jacobi) or three (learned: r is exchanged for M^-1 r).
+// Synchronisation: dot products travel through grid-wide phases (fphase: each
+// block publishes its partial sums and one arrival; every block sums all
+// partials in the same fixed order); neighbour values through point-to-point
+// exchanges (nexchange: per-block flags, each block waits only for the blocks
+// whose rows it reads).  A Jacobi iteration costs one exchange and one phase,
+// a learned one two exchanges and one phase.
 #include "lv_internal.cuh"
 
 namespace {
@@ -25,10 +27,11 @@ constexpr int FKR = 8;    // operator entries per row held in registers
 constexpr int FKM = 12;   // preconditioner off-diagonal entries per row held in registers
 constexpr int MMAX = 64;  // preconditioner off-diagonal entries per row (storage slots)
 constexpr long long FCG_SPIN_LIMIT = 4000000000LL;  // cycles (about 2 s)
-constexpr float FCG_INNER_TOL = 1e-5f;
-constexpr int FCG_MAX_OUTER = 30;
+constexpr float FCG_UPDATE_DROP = 1e-5f;  // FP32 residual reduction per refinement step
+constexpr int FCG_MAX_UPDATES = 200;
 
 constexpr int RG_WORDS = 4;  // partial-sum words per block and phase
+constexpr int FLAG_STRIDE = 32;  // exchange flags sit on separate 128-byte lines (packed flags halve the speed)
 constexpr int FCG_MAX_BLOCKS = 1024;
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -47,9 +50,10 @@ struct FcgArgs {
   const double* b;
   double* x;  // FP64 iterate, also the exchange buffer of the outer residual
   float* rbuf;
-  float* zbuf;
+  float* ubuf;    // u exchange
   unsigned long long* slots;  // partial words [2 parities][RG_WORDS][nb] (as 32-bit words)
   unsigned* counter;          // arrivals, zeroed before the launch
+  unsigned* flags;            // per-block exchange epochs, one 128-byte line each (FLAG_STRIDE words)
   int* status;
   double tol2;
   int itmax;
@@ -178,13 +182,32 @@ __device__ bool fphase(const FcgArgs& a, unsigned ph, const T (&v)[NV], T (&tot)
   return true;
 }
 
-// synchronisation-only phase: values stored before it are visible after it
-__device__ bool fbarrier(const FcgArgs& a, unsigned ph) {
-  __shared__ int s_ok;
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Neighbour exchange number e: the values this block stored before it are
+// visible to the blocks that read them, and this block sees the values of
+// the blocks in its mask (the owners of the columns its rows reference).
+// Point to point: each block raises its own flag and waits only for its
+// neighbours' flags.  Consecutive exchanges are always separated by a
+// grid-wide phase, so one buffer per exchanged vector suffices.
+__device__ bool nexchange(const FcgArgs& a, unsigned e, const unsigned* mask) {
   __syncthreads();
-  if (threadIdx.x == 0) s_ok = arrive_wait(a, ph);
-  __syncthreads();
-  return s_ok != 0;
+  if (threadIdx.x == 0) st_release_u32(a.flags + (size_t)blockIdx.x * FLAG_STRIDE, e);
+  int to = 0;
+  const int t = threadIdx.x;
+  if (t < a.nb && ((mask[t >> 5] >> (t & 31)) & 1u)) {
+    const long long t0 = clock64();
+    while (ld_acquire_u32(a.flags + (size_t)t * FLAG_STRIDE) < e) {
+      if (clock64() - t0 > FCG_SPIN_LIMIT) {
+        to = 1;
+        atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
+        break;
+      }
+    }
+  }
+  return __syncthreads_or(to) == 0;
 }
 
 template <int R>
@@ -237,7 +260,26 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     rr.bb[k] = on ? a.b[i] : 0.0;
     x[k] = on ? a.x[i] : 0.0;
   }
+  // blocks owning the columns of this block's rows (operator and M^-1)
+  __shared__ unsigned s_mask[FCG_MAX_BLOCKS / 32];
+  for (int t = threadIdx.x; t < FCG_MAX_BLOCKS / 32; t += FCG_TPB) s_mask[t] = 0u;
+  __syncthreads();
+  {
+    const int rpb = a.rows_per_block;
+    const int me = blockIdx.x;
+    auto mark = [&](int j) {
+      const int bj = j / rpb;
+      if (bj != me) atomicOr(&s_mask[bj >> 5], 1u << (bj & 31));
+    };
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      if (!rr.on[k]) continue;
+      for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) mark(a.col[e]);
+      for (int e = 0; e < rr.mn[k]; ++e) mark(a.mcol[(size_t)e * a.mstride + rr.i[k]]);
+    }
+  }
   unsigned ep = 0;  // phases completed in this launch
+  unsigned xe = 0;  // neighbour exchanges completed in this launch
   bool ok = true;
   // singular operator: project b to zero mean
   if (*a.nonsingular == 0) {
@@ -253,27 +295,75 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   const int jref = *a.jref;
   const int cap = jref > 0 ? jref : a.itmax;
   bool learned = learned0;
-  int it = 0, outer = 0;
+  int it = 0, updates = 0;
   double bnorm2 = 0.0, rtrue2 = 0.0;
-  bool xdirty = false;
-  float r[R], z[R], p[R], q[R], d[R];
-  // z = M^-1 r from the published r (learned mode)
-  auto apply_m = [&]() {
+  float r[R], u[R], w[R], p[R], s[R], d[R];
+  // out = A v with the neighbours' values from buf (FP32 difference form)
+  auto spmv = [&](const float* buf, const float(&own)[R], float(&out)[R]) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-      float t = rr.md[k] * r[k];
+      float acc = rr.dg[k] * own[k];
 #pragma unroll
-      for (int e = 0; e < FKM; ++e)
-        if (e < rr.mn[k]) t = fmaf(rr.mv[k][e], __ldcg(a.rbuf + rr.mc[k][e]), t);
-      for (int e = FKM; e < rr.mn[k]; ++e) {
-        const size_t s = (size_t)e * a.mstride + rr.i[k];
-        t = fmaf(a.mval[s], __ldcg(a.rbuf + a.mcol[s]), t);
-      }
-      z[k] = t;
+      for (int e = 0; e < FKR; ++e)
+        if (e < rr.cnt[k]) acc = fmaf(rr.ww[k][e], own[k] - __ldcg(buf + rr.cc[k][e]), acc);
+      for (int e = FKR; e < rr.cnt[k]; ++e)
+        acc = fmaf((float)a.w[rr.beg[k] + e], own[k] - __ldcg(buf + a.col[rr.beg[k] + e]), acc);
+      out[k] = acc;
     }
   };
-  for (; ok && outer < FCG_MAX_OUTER; ++outer) {
-    if (xdirty && !(ok = fbarrier(a, ++ep))) break;
+  // out = M^-1 v (learned) with the neighbours' values from buf
+  auto mapply = [&](const float* buf, const float(&own)[R], float(&out)[R]) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      float t = rr.md[k] * own[k];
+#pragma unroll
+      for (int e = 0; e < FKM; ++e)
+        if (e < rr.mn[k]) t = fmaf(rr.mv[k][e], __ldcg(buf + rr.mc[k][e]), t);
+      for (int e = FKM; e < rr.mn[k]; ++e) {
+        const size_t q = (size_t)e * a.mstride + rr.i[k];
+        t = fmaf(a.mval[q], __ldcg(buf + a.mcol[q]), t);
+      }
+      out[k] = t;
+    }
+  };
+  // u = M^-1 r (the learned preconditioner needs r from the neighbours)
+  auto precond = [&]() -> bool {
+    if (learned) {
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        if (rr.on[k]) a.rbuf[rr.i[k]] = r[k];
+      if (!nexchange(a, ++xe, s_mask)) return false;
+      mapply(a.rbuf, r, u);
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) u[k] = rr.dnv[k] * r[k];
+    }
+    return true;
+  };
+  // FP32 CG on A d = r / sigma, single-reduction form (Chronopoulos & Gear,
+  // J. Comput. Appl. Math. 25, 1989; D'Azevedo, Eijkhout & Romine, LAPACK
+  // Working Note 56, 1993): gamma = (r, u), delta = (A u, u) and ||r||^2 in
+  // one grid-wide phase, alpha = gamma / (delta - beta gamma / alpha_old);
+  // u = M^-1 r and w = A u are computed directly each iteration (only s = A p
+  // is a recurrence), their neighbour values moved by point-to-point
+  // exchanges.  Iterative refinement: once the FP32 residual has dropped by
+  // FCG_UPDATE_DROP, or the target is in reach, x += sigma d in FP64, the
+  // residual is recomputed in FP64 (difference form) and CG restarts on it.
+  // (Continuing the old directions across the replacement instead breaks the
+  // orthogonality the single-reduction alpha relies on, and stalled on the
+  // singular operators of incompressible flows.)
+  double sigma = 1.0;
+  bool have_d = false, first = true, fall = false;
+  float gam_old = 1.f, alpha = 1.f;
+  while (ok) {
+    if (have_d) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        x[k] += sigma * (double)d[k];
+        if (rr.on[k]) a.x[rr.i[k]] = x[k];
+      }
+      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+    }
     double r64[R];
     double v[2] = {0.0, 0.0}, t2[2];
 #pragma unroll
@@ -290,123 +380,63 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     if (!(ok = fphase<2, double>(a, ++ep, v, t2))) break;
     rtrue2 = t2[0];
     bnorm2 = t2[1];
-    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax) break;
-    const double sigma = sqrt(rtrue2);
+    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax || updates >= FCG_MAX_UPDATES) break;
+    sigma = sqrt(rtrue2);
     const double inv_sigma = 1.0 / sigma;
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       r[k] = (float)(r64[k] * inv_sigma);
       d[k] = 0.f;
-      p[k] = 0.f;
-      q[k] = 0.f;
     }
-    const float rho_stop = fmaxf(FCG_INNER_TOL * FCG_INNER_TOL, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
-    float gam;
-    {
-      if (learned) {
-#pragma unroll
-        for (int k = 0; k < R; ++k)
-          if (rr.on[k]) a.rbuf[rr.i[k]] = r[k];
-        if (!(ok = fbarrier(a, ++ep))) break;
-        apply_m();
-      } else {
-#pragma unroll
-        for (int k = 0; k < R; ++k) z[k] = rr.dnv[k] * r[k];
-      }
-      float v1[1] = {0.f}, t1[1];
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        if (rr.on[k]) a.zbuf[rr.i[k]] = z[k];
-        v1[0] = fmaf(r[k], z[k], v1[0]);
-      }
-      if (!(ok = fphase<1, float>(a, ++ep, v1, t1))) break;
-      gam = t1[0];
+    have_d = true;
+    ++updates;
+    first = true;  // CG restarts from the refined iterate
+    if (fall) {
+      // the learned preconditioner needed more iterations than Jacobi did:
+      // continue from the current iterate with Jacobi
+      learned = false;
+      fall = false;
     }
-    float beta = 0.f;
-    bool fall = false;
+    const float rho_upd = fmaxf(FCG_UPDATE_DROP * FCG_UPDATE_DROP, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
+    if (!(ok = precond())) break;
     while (true) {
-      // p = z + beta p; q = A z + beta q (= A p)
-      float v1[1] = {0.f}, t1[1];
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        if (rr.on[k]) a.ubuf[rr.i[k]] = u[k];
+      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+      spmv(a.ubuf, u, w);
+      float v3[3] = {0.f, 0.f, 0.f}, t3[3];
 #pragma unroll
       for (int k = 0; k < R; ++k) {
-        float az = rr.dg[k] * z[k];
-#pragma unroll
-        for (int e = 0; e < FKR; ++e)
-          if (e < rr.cnt[k]) az = fmaf(rr.ww[k][e], z[k] - __ldcg(a.zbuf + rr.cc[k][e]), az);
-        for (int e = FKR; e < rr.cnt[k]; ++e)
-          az = fmaf((float)a.w[rr.beg[k] + e], z[k] - __ldcg(a.zbuf + a.col[rr.beg[k] + e]), az);
-        p[k] = fmaf(beta, p[k], z[k]);
-        q[k] = fmaf(beta, q[k], az);
-        v1[0] = fmaf(p[k], q[k], v1[0]);
+        v3[0] = fmaf(r[k], u[k], v3[0]);
+        v3[1] = fmaf(w[k], u[k], v3[1]);
+        v3[2] = fmaf(r[k], r[k], v3[2]);
       }
-      if (!(ok = fphase<1, float>(a, ++ep, v1, t1))) break;
-      const float pq = t1[0];
-      const float alpha = gam / pq;
+      if (!(ok = fphase<3, float>(a, ++ep, v3, t3))) break;
+      const float gam = t3[0], delta = t3[1], rho = t3[2];
+      if (rho <= rho_upd || it >= a.itmax || !(delta > 0.f)) break;
+      if (learned && it >= cap) {
+        fall = true;
+        break;
+      }
+      const float beta = first ? 0.f : gam / gam_old;
+      alpha = first ? gam / delta : gam / (delta - beta * gam / alpha);
 #pragma unroll
       for (int k = 0; k < R; ++k) {
+        p[k] = first ? u[k] : fmaf(beta, p[k], u[k]);
+        s[k] = first ? w[k] : fmaf(beta, s[k], w[k]);
         d[k] = fmaf(alpha, p[k], d[k]);
-        r[k] = fmaf(-alpha, q[k], r[k]);
+        r[k] = fmaf(-alpha, s[k], r[k]);
       }
+      gam_old = gam;
+      first = false;
       ++it;
-      float rho, gnew;
-      if (learned) {
-        float v2[1] = {0.f}, t2f[1];
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          if (rr.on[k]) a.rbuf[rr.i[k]] = r[k];
-          v2[0] = fmaf(r[k], r[k], v2[0]);
-        }
-        if (!(ok = fphase<1, float>(a, ++ep, v2, t2f))) break;
-        rho = t2f[0];
-        const bool stop = rho <= rho_stop || it >= a.itmax || !(pq > 0.f);
-        if (stop) break;
-        if (it >= cap) {
-          fall = true;
-          break;
-        }
-        apply_m();
-        float v3[1] = {0.f}, t3[1];
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          if (rr.on[k]) a.zbuf[rr.i[k]] = z[k];
-          v3[0] = fmaf(r[k], z[k], v3[0]);
-        }
-        if (!(ok = fphase<1, float>(a, ++ep, v3, t3))) break;
-        gnew = t3[0];
-      } else {
-        float v2[2] = {0.f, 0.f}, t2f[2];
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          z[k] = rr.dnv[k] * r[k];
-          if (rr.on[k]) a.zbuf[rr.i[k]] = z[k];
-          v2[0] = fmaf(r[k], r[k], v2[0]);
-          v2[1] = fmaf(r[k], z[k], v2[1]);
-        }
-        if (!(ok = fphase<2, float>(a, ++ep, v2, t2f))) break;
-        rho = t2f[0];
-        gnew = t2f[1];
-        if (rho <= rho_stop || it >= a.itmax || !(pq > 0.f)) break;
-      }
-      beta = gnew / gam;
-      gam = gnew;
+      if (!(ok = precond())) break;
     }
-    if (!ok) break;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      x[k] += sigma * (double)d[k];
-      if (rr.on[k]) a.x[rr.i[k]] = x[k];
-    }
-    xdirty = true;
-    if (fall) learned = false;  // continue the refinement with Jacobi
-  }
-  if (ok && xdirty) {
-#pragma unroll
-    for (int k = 0; k < R; ++k)
-      if (rr.on[k]) a.x[rr.i[k]] = x[k];
   }
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
     *a.out_iters = it;
-    *a.out_outer = outer;
+    *a.out_outer = updates;
     *a.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
     if (!a.learned) *a.jref = it;
     a.out_d[0] = rtrue2;
@@ -477,6 +507,8 @@ __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* _
 }
 
 int g_fcg_blocks_per_sm[2] = {-1, -1};
+
+
 
 }  // namespace
 
@@ -580,9 +612,10 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.b = c->sv.b;
   a.x = x;
   a.rbuf = c->sv.r32;
-  a.zbuf = c->sv.z32;
+  a.ubuf = c->sv.f32a;
   a.slots = c->sv.fslots;
   a.counter = c->sv.bar + 2;
+  a.flags = reinterpret_cast<unsigned*>(c->sv.fslots + 8192);
   a.status = c->status;
   a.tol2 = c->tol * c->tol;
   a.itmax = c->itmax;
@@ -601,6 +634,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.out_d = c->sv.dstats + 3 * slot;
   a.counters = c->sv.counters;
   cudaMemsetAsync(c->sv.bar + 2, 0, sizeof(unsigned), c->stream);
+  cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * FLAG_STRIDE * nb, c->stream);
   void* args[] = {&a};
   const void* fn = R == 1 ? (const void*)k_fcg<1> : (const void*)k_fcg<2>;
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(FCG_TPB), args, 0, c->stream);

@@ -194,7 +194,7 @@ int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev);
 int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
 
 // ---- flag-reduced mixed-precision solver (lv_fcg.cu)
-#define LV_FCG_SLOT_WORDS (6 * 4 * 1024)
+#define LV_FCG_SLOT_WORDS (8192 + 16 * 1024)  // u64: partial words, then 128-byte exchange flags
 int lv_fcg_capacity(lv_ctx* c);
 int lv_fcg_build_minv(lv_ctx* c);
 int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned);

@@ -5,7 +5,8 @@
 // is SPD (D = diagonal of the operator).  The network works on the
 // Jacobi-normalised operator At = D^-1/2 A D^-1/2 = I - What:
 //
-//   X     node features [1, diag/adiag, sum_j what_ij, max_j what_ij, deg/8, 0...] (16)
+//   X     node features [1, diag/adiag, sum_j what_ij, max_j what_ij, deg/8,
+//         sum_{j<i} what_ij, #{j<i}/8, max_{j<i} what_ij, 0...] (16)
 //   H1    = relu([X,  Agg X ] W0 + b0)            Agg(H)_i = sum_j what_ij H_j
 //   H2    = H1 + relu([H1, Agg H1] W1 + b1)
 //   H3    = H2 + relu([H2, Agg H2] W2 + b2)        (3 layers, hidden width 32)
@@ -15,7 +16,11 @@
 // The matrix products of the layers (forward [N x 32|64] x [32|64 x 32],
 // backward dX = dZ W^T and dW = X^T dZ) run on the tensor cores as
 // mma.sync m16n8k16 with BF16 operands and FP32 accumulation; everything else
-// is FP32.  Training minimises a Hutchinson estimate of
+// is FP32.  Training minimises either the exact FSAI (Kaporin) objective
+//     (1/N) [ tr(Gt At Gt^T) - 2 sum_i log Gt_ii ]
+// (Kolotilina & Yeremin, SIAM J. Matrix Anal. Appl. 14, 1993; Kaporin,
+// Numer. Linear Algebra Appl. 1, 1994), whose minimiser on the pattern is the
+// FSAI factor, or a Hutchinson estimate of
 //     || Gt At Gt^T - I ||_F^2 / N = E_z || Gt At Gt^T z - z ||^2 / N,
 // z Rademacher, whose gradient with respect to each entry (a, b) of Gt is
 // 2 (r_a t_b + z_a s_b), r = Gt At Gt^T z - z, t = At Gt^T z, s = At Gt^T r.
@@ -78,13 +83,19 @@ __global__ void k_lprep(int n, const int* __restrict__ rowptr, const int* __rest
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int a = rowptr[i], b = rowptr[i + 1];
-  float s = 0.f, m = 0.f;
+  float s = 0.f, m = 0.f, sl = 0.f, ml = 0.f;
+  int nl = 0;
   for (int k = a; k < b; ++k) {
     const int j = col[k];
     const float v = (float)w[k] * dh[i] * dh[j];
     what[k] = v;
     s += v;
     m = fmaxf(m, v);
+    if (j < i) {
+      sl += v;
+      ml = fmaxf(ml, v);
+      ++nl;
+    }
     int r = -1;
     for (int t = rowptr[j]; t < rowptr[j + 1]; ++t)
       if (col[t] == i) {
@@ -99,8 +110,12 @@ __global__ void k_lprep(int n, const int* __restrict__ rowptr, const int* __rest
   x[2] = s;
   x[3] = m;
   x[4] = (float)(b - a) * 0.125f;
+  // the factor is lower-triangular in the index order: the lower neighbours
+  x[5] = sl;
+  x[6] = (float)nl * 0.125f;
+  x[7] = ml;
 #pragma unroll
-  for (int f = 5; f < FIN; ++f) x[f] = 0.f;
+  for (int f = 8; f < FIN; ++f) x[f] = 0.f;
 }
 
 // ---------------------------------------------------------------- forward
@@ -335,6 +350,69 @@ __global__ void k_gradG(int n, int K, const int* __restrict__ rowptr, const int*
         v += 2.f * (r[o + i] * t[o + j] + z[o + i] * s[o + j]);
       }
     dgl[k] = scale * v;
+  }
+}
+
+// Exact FSAI (Kaporin) objective, one thread per row i with S_i = {i} and the
+// lower neighbours of i (the pattern of row i of Gt):
+//     L = (1/n) sum_i [ g_i^T At g_i - 2 log Gt_ii ],   g_i = row i of Gt,
+// whose minimiser on the pattern is the FSAI factor (each row solves
+// At[S,S] g = e_i / g_ii).  tv_j = (Gt At)_ij = g_j - sum_{m in S, m ~ j}
+// g_m what(m, j) for j in S; dL/dGt_ij = (2 tv_j - [j = i] 2 / Gt_ii) / n.
+constexpr int KMAX = LV_MAX_EDGES + 1;
+__global__ void k_kaporin(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                          const int* __restrict__ rev, const float* __restrict__ what, const float* __restrict__ gd,
+                          const float* __restrict__ gl, float scale, float* dgd, float* dgl, double* part) {
+  __shared__ double sh[32];
+  double lsum = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int a = rowptr[i], b = rowptr[i + 1];
+    int mem[KMAX], pos[KMAX];  // member rows and their CSR position in row i (-1: i itself)
+    float g[KMAX], tv[KMAX];
+    int S = 0;
+    mem[S] = i;
+    pos[S] = -1;
+    g[S] = gd[i];
+    ++S;
+    for (int k = a; k < b && S < KMAX; ++k)
+      if (col[k] < i) {
+        mem[S] = col[k];
+        pos[S] = k;
+        g[S] = gl[k];
+        ++S;
+      }
+    for (int p = 0; p < S; ++p) tv[p] = g[p];
+    // contributions of m = i: At_(i, j) = -what at row i's entry of j
+    for (int p = 1; p < S; ++p) tv[p] = fmaf(-g[0], what[pos[p]], tv[p]);
+    // m = a lower neighbour: At_(m, i) through rev, At_(m, j) by a search of row m
+    for (int q = 1; q < S; ++q) {
+      const int m = mem[q];
+      if (rev[pos[q]] >= 0) tv[0] = fmaf(-g[q], what[rev[pos[q]]], tv[0]);
+      for (int t = rowptr[m]; t < rowptr[m + 1]; ++t) {
+        const int j = col[t];
+        if (j >= i) continue;
+        for (int p = 1; p < S; ++p)
+          if (mem[p] == j) {
+            tv[p] = fmaf(-g[q], what[t], tv[p]);
+            break;
+          }
+      }
+    }
+    const float gii = fmaxf(g[0], 1e-6f);
+    float li = -2.f * logf(gii);
+    for (int p = 0; p < S; ++p) li = fmaf(g[p], tv[p], li);
+    lsum += (double)li;
+    dgd[i] = scale * (2.f * tv[0] - 2.f / gii);
+    for (int k = a; k < b; ++k) dgl[k] = 0.f;
+    for (int p = 1; p < S; ++p) dgl[pos[p]] = scale * 2.f * tv[p];
+  }
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = lsum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    part[blockIdx.x] = t;
   }
 }
 
@@ -731,11 +809,20 @@ int forward(lv_ctx* c, const LearnSystem& S) {
   return lv_cuda_check(c, cudaGetLastError(), "learned: forward");
 }
 
-// loss (into L->loss[0]) and dGt (L->dgd, L->dgl) for K probes in L->zp
+// loss (into L->loss[0]) and dGt (L->dgd, L->dgl): the Hutchinson estimate
+// with K probes in L->zp, or the exact FSAI (Kaporin) objective for K = 0
 int loss_grad_G(lv_ctx* c, const LearnSystem& S, int K) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
   const int n = S.n, b = lv_blocks(n, TPB);
+  if (K == 0) {
+    const int nbl = std::min(PART_BLOCKS, b);
+    k_kaporin<<<nbl, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->gd, L->gl, 1.0f / (float)n, L->dgd, L->dgl,
+                                  L->partL);
+    k_sum_loss<<<1, 32, 0, s>>>(L->partL, nbl, 1.0 / (double)n, L->loss);
+    c->launches += 2;
+    return lv_cuda_check(c, cudaGetLastError(), "learned: Kaporin loss");
+  }
   k_gt<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->rev, L->gd, L->gl, L->zp, L->y);
   k_at<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->what, L->y, L->t);
   k_g<<<b, TPB, 0, s>>>(n, K, S.rowptr, S.col, L->gd, L->gl, L->t, L->u);
@@ -902,7 +989,7 @@ int lv_learn_clear_systems(lv_ctx* c) {
 // when probes is NULL).  grad may be NULL.
 int lv_learn_loss_grad(lv_ctx* c, int32_t sys, const float* probes, int32_t K, uint64_t seed, double* loss,
                        float* grad) {
-  if (!c || K < 1 || K > MAXPROBES) return LV_ERR_BAD_ARGUMENT;
+  if (!c || K < 0 || K > MAXPROBES) return LV_ERR_BAD_ARGUMENT;
   if (int rc = ensure_state(c)) return rc;
   LearnState* L = c->learn;
   LearnSystem S;
@@ -916,9 +1003,9 @@ int lv_learn_loss_grad(lv_ctx* c, int32_t sys, const float* probes, int32_t K, u
   cudaStream_t s = c->stream;
   if (int rc = prepare(c, S)) return rc;
   if (int rc = forward(c, S)) return rc;
-  if (probes)
+  if (K > 0 && probes)
     cudaMemcpyAsync(L->zp, probes, sizeof(float) * (size_t)K * S.n, cudaMemcpyHostToDevice, s);
-  else
+  else if (K > 0)
     k_probes<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, K, seed, L->zp);
   if (int rc = loss_grad_G(c, S, K)) return rc;
   if (int rc = backward(c, S)) return rc;
@@ -930,7 +1017,7 @@ int lv_learn_loss_grad(lv_ctx* c, int32_t sys, const float* probes, int32_t K, u
 // Adam on the training systems (round robin), K Rademacher probes per step.
 int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed, float* losses) {
   if (c) c->factor_valid = false;
-  if (!c || steps < 0 || K < 1 || K > MAXPROBES || !(lr > 0)) return LV_ERR_BAD_ARGUMENT;
+  if (!c || steps < 0 || K < 0 || K > MAXPROBES || !(lr > 0)) return LV_ERR_BAD_ARGUMENT;
   if (int rc = ensure_state(c)) return rc;
   LearnState* L = c->learn;
   if (L->systems.empty()) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "no training systems (lv_learn_add_system)");
@@ -942,7 +1029,7 @@ int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed,
     const LearnSystem& S = L->systems[st % L->systems.size()];
     if (int rc = prepare(c, S)) return rc;
     if (int rc = forward(c, S)) return rc;
-    k_probes<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, K, seed + 7919ull * (unsigned long long)st, L->zp);
+    if (K > 0) k_probes<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, K, seed + 7919ull * (unsigned long long)st, L->zp);
     if (int rc = loss_grad_G(c, S, K)) return rc;
     if (int rc = backward(c, S)) return rc;
     L->adam_t += 1;

@@ -1,5 +1,6 @@
 """CPU reference of the learned preconditioner (test oracle): the same
-message-passing network, readout and Hutchinson loss as the GPU kernels,
+message-passing network, readout and losses (Hutchinson and the FSAI /
+Kaporin objective) as the GPU kernels,
 written with torch autograd in FP64.  The inputs of the layers' matrix
 products are rounded to bfloat16 as the tensor-core kernels do; everything
 else is FP64, so forward values and gradients agree with the GPU to the
@@ -44,18 +45,44 @@ def prepare(rowptr, col, w, diag, adiag):
     X[:, 1] = (diag / adiag).astype(np.float32)
     s = np.zeros(n, np.float32)
     m = np.zeros(n, np.float32)
+    sl = np.zeros(n, np.float32)
+    ml = np.zeros(n, np.float32)
+    nl = np.zeros(n, np.float32)
     for i in range(n):
         a, b = rowptr[i], rowptr[i + 1]
         s[i] = np.float32(0)
         for k in range(a, b):
             s[i] = np.float32(s[i] + what[k])
+            if col[k] < i:
+                sl[i] = np.float32(sl[i] + what[k])
+                ml[i] = max(ml[i], what[k])
+                nl[i] += 1
         m[i] = what[a:b].max() if b > a else 0.0
     X[:, 2] = s
     X[:, 3] = m
     X[:, 4] = (np.diff(rowptr).astype(np.float32)) * np.float32(0.125)
+    X[:, 5] = sl
+    X[:, 6] = nl * np.float32(0.125)
+    X[:, 7] = ml
     T = lambda a: torch.from_numpy(np.asarray(a, np.float64))
+    # triples (entry of m, weight, entry of j) of tr(Gt What Gt^T) = sum_i sum_{m,j in S_i} Gt_im what_mj Gt_ij,
+    # entries indexed into cat([gd, gl]) (gd: 0..n-1, gl: n + CSR position)
+    tm, tw, tj = [], [], []
+    pos = {}
+    for i in range(n):
+        for k in range(rowptr[i], rowptr[i + 1]):
+            pos[(i, int(col[k]))] = k
+    for i in range(n):
+        mem = [(i, i)] + [(int(col[k]), n + k) for k in range(rowptr[i], rowptr[i + 1]) if col[k] < i]
+        for (m_, em) in mem:
+            for (j_, ej) in mem:
+                if m_ != j_ and (m_, j_) in pos:
+                    tm.append(em)
+                    tw.append(what[pos[(m_, j_)]])
+                    tj.append(ej)
     return dict(n=n, ri=torch.from_numpy(ri), col=torch.from_numpy(col.astype(np.int64)), what=T(what), dh=T(dh),
-                X=T(X))
+                X=T(X), tm=torch.tensor(tm, dtype=torch.int64), tw=T(np.asarray(tw, np.float32)),
+                tj=torch.tensor(tj, dtype=torch.int64))
 
 
 def agg(G, H):
@@ -107,13 +134,26 @@ def loss(G, params, probes):
     return tot / (len(probes) * G["n"])
 
 
+def loss_kaporin(G, params):
+    """(1/n) [tr(Gt At Gt^T) - 2 sum log Gt_ii], At = I - What."""
+    gd, gl = factor(G, params)
+    e = torch.cat([gd, gl])
+    tr = (e * e).sum() - (e[G["tm"]] * G["tw"] * e[G["tj"]]).sum()
+    return (tr - 2.0 * torch.log(gd).sum()) / G["n"]
+
+
 def loss_and_grad(rowptr, col, w, diag, adiag, params, probes):
+    """probes None: the Kaporin objective; else the Hutchinson loss."""
     G = prepare(rowptr, col, w, diag, adiag)
     p = torch.tensor(np.asarray(params, np.float64), requires_grad=True)
+    if probes is None:
+        L = loss_kaporin(G, p)
+        L.backward()
+        return float(L.detach()), p.grad.numpy().copy()
     z = [torch.from_numpy(np.asarray(q, np.float64)) for q in probes]
     L = loss(G, p, z)
     L.backward()
-    return float(L), p.grad.numpy().copy()
+    return float(L.detach()), p.grad.numpy().copy()
 
 
 def forward_values(rowptr, col, w, diag, adiag, params):

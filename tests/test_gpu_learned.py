@@ -101,6 +101,27 @@ def test_gradient_matches_autograd(lv, oracle, mk):
     assert cos > 0.999, cos
 
 
+@pytest.mark.parametrize("mk", [lambda: W.taylor_green(32), lambda: W.cavity(32)])
+def test_kaporin_gradient_matches_autograd(lv, oracle, mk):
+    """The exact FSAI (Kaporin) objective (probes = 0) and its gradient."""
+    flow = mk()
+    g, L = _grid(lv, oracle, flow)
+    pr = _params(L, g, 6, scale=0.3)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    loss = C.c_double()
+    grad = np.zeros(len(pr), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_loss_grad(g._ctx, -1, None, 0, 0, C.byref(loss), fp(grad)) == 0
+    rl, rg = LR.loss_and_grad(rowptr, col, w, diag, adiag, pr, None)
+    assert abs(loss.value - rl) <= 1e-4 * max(1.0, abs(rl)), (loss.value, rl)
+    for name, (o, s) in LR.OFF.items():
+        a, b = grad[o:o + s].astype(np.float64), rg[o:o + s]
+        nb = np.linalg.norm(b)
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-6, (name, np.linalg.norm(a - b), nb)
+    cos = grad.astype(np.float64) @ rg / (np.linalg.norm(grad) * np.linalg.norm(rg))
+    assert cos > 0.999, cos
+
+
 def _harvest(lv, oracle, flow, seeds):
     """A grid per seed, operator assembled and snapshot for training; returns the last grid."""
     from lvgpu import populate as pop
