@@ -214,7 +214,9 @@ def run_ours(args, world, rank, local):
     L = lv._lib.load()
     fl = flow()
     g = setup_grid(lv, fl)
-    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
+    # warm-up with the Jacobi mixed solver: its iteration count is the
+    # learned solver's fallback reference
+    solver = lv.PressureSolver(g, method="mixed_ir" if args.solver == "learned_pcg" else args.solver, tol=1e-8)
     stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
     # warm-up steps also snapshot the pressure operators the learned
@@ -223,7 +225,7 @@ def run_ours(args, world, rank, local):
         gpu_step(lv, g, solver, fl, snapshot=True)
     g.synchronize()
     t_tr = time.perf_counter()
-    train_steps = 0 if args.no_compare else args.train_steps
+    train_steps = args.train_steps if (args.solver == "learned_pcg" or not args.no_compare) else 0
     losses = np.zeros(max(train_steps, 1), np.float32)
     assert L.lv_learn_init(g._ctx, 1234) == 0
     if train_steps:
@@ -234,6 +236,10 @@ def run_ours(args, world, rank, local):
                   "lr": args.train_lr,
                   "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
                   "loss_last": float(losses[-10:].mean())}
+
+    solver = lv.PressureSolver(g, method=args.solver, tol=1e-8)
+    gpu_step(lv, g, solver, fl)  # one untimed step with the timed solver
+    g.synchronize()
 
     # ---- timed region: K steps, device time from events on the library's stream,
     # an L2 flush (512 MiB write) between steps outside the events
@@ -321,26 +327,43 @@ def run_ours(args, world, rank, local):
     # algorithmic bytes per unit (per particle): FP64 PCG iteration
     # (8+4)*nnz + 4N + 4*8N + 3*8N with nnz = F + N (diagonal included);
     # clip + geometry 16N + 28F + 28N
-    pcg_bytes = iters * (12 * (F + N) + 4 * N + 56 * N)
+    # per CG iteration, the bytes a streaming implementation moves: FP64
+    # Jacobi-PCG 12 B per nonzero (value + column) + 60 B per row (vectors);
+    # FP32 inner CG 8 B per nonzero + 28 B per row, and the learned M^-1 about
+    # 10 more nonzeros per row.  The register-resident kernels keep the matrix
+    # on chip, so these are upper bounds of their DRAM traffic.
+    if args.solver == "jacobi_pcg":
+        per_it = 12 * (F + N) + 60 * N
+    else:
+        per_it = 8 * (F + N) + 28 * N + (80 * N if args.solver == "learned_pcg" else 0)
+    pcg_bytes = iters * per_it
     clip_bytes = kt["clip"][0] * (16 * N + 28 * F + 28 * N)
     fams = {"pcg": pcg_bytes, "clip": clip_bytes}
     dom = max(("pcg", "clip"), key=lambda k: kt[k][1])
     dom_ms = kt[dom][1]
     dom_launches = max(kt[dom][0], 1)
     achieved = (fams[dom] / dom_launches) / ((dom_ms / dom_launches) / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    traffic = read_traffic(WORKLOAD, dom)
+    if dom == "pcg":
+        if args.solver == "jacobi_pcg":
+            kname = "k_pcg_reg<2>" if N <= 2 * 128 * 2 * 152 else "k_pcg"
+        else:
+            kname = "k_fcg<1>" if N <= 152 * 512 else ("k_fcg<2>" if N <= 152 * 1024 else "k_lpcg_str")
+    else:
+        kname = "k_clip"
+    traffic = read_traffic(WORKLOAD, dom, kname)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
-        "config": {"workload": WORKLOAD, "particles": N, "solver": "jacobi_pcg fp64 tol 1e-8, 10 sweeps/step",
+        "config": {"workload": WORKLOAD, "particles": N,
+                   "solver": SOLVER_DESC[args.solver] + ", tol 1e-8 (FP64 residual), 10 sweeps/step",
                    "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": f"replicas x{world}",
                    "l2": "512 MiB buffer written between timed steps (the 256x256 state, ~15 MB, fits in L2)"},
         "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1]) / args.steps,
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
                      "solves": solves, "solvers": comparison},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},
-        "roofline": {"kernel": "k_pcg" if dom == "pcg" else "k_clip", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "peak_source": peak_src},
         "clocks": clocks,
@@ -353,16 +376,23 @@ def run_ours(args, world, rank, local):
     return line
 
 
-def read_traffic(workload, family):
+SOLVER_DESC = {
+    "jacobi_pcg": "jacobi_pcg fp64",
+    "mixed_ir": "mixed_ir: fp32 jacobi CG inside fp64 refinement",
+    "learned_pcg": "learned_pcg: fp32 CG preconditioned by the trained factor inside fp64 refinement",
+}
+
+
+def read_traffic(workload, family, kernel):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
-    of the family's kernel on this workload, from the committed ncu summary
-    table profiles/traffic.txt (columns: family workload bytes_per_launch ...)."""
+    of the kernel on this workload, from the committed ncu summary table
+    profiles/traffic.txt (columns: family workload bytes_per_launch kernel ...)."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
     for ln in open(path):
         f = ln.split()
-        if len(f) >= 3 and not ln.startswith("#") and f[0] == family and f[1] == workload:
+        if len(f) >= 4 and not ln.startswith("#") and f[0] == family and f[1] == workload and f[3] == kernel:
             return float(f[2])
     return None
 
@@ -450,6 +480,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
     ap.add_argument("--nx", type=int, default=256, help="lattice side (the workload is 256; others for profiling)")
+    ap.add_argument("--solver", default="learned_pcg", choices=["jacobi_pcg", "mixed_ir", "learned_pcg"],
+                    help="pressure solver of the timed steps")
     ap.add_argument("--train-steps", type=int, default=400, help="Adam steps of the learned preconditioner")
     ap.add_argument("--train-probes", type=int, default=0, help="0: FSAI/Kaporin objective; K: Hutchinson, K probes")
     ap.add_argument("--train-lr", type=float, default=5e-3)
