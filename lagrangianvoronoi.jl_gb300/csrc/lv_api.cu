@@ -281,6 +281,9 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.f32b = dalloc<float>(c, cap, &ok);
   sv.part = dalloc<double>(c, 8 * 4096, &ok);
   sv.fslots = dalloc<unsigned long long>(c, LV_FCG_SLOT_WORDS, &ok);
+  sv.rhs_tf = dalloc<double>(c, ell, &ok);
+  sv.rhs_dmz = dalloc<double2>(c, ell, &ok);
+  sv.rhs_te = dalloc<double>(c, ell, &ok);
   sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);
   sv.iters = dalloc<int>(c, LV_IT_SIZE, &ok);
@@ -625,7 +628,7 @@ int lv_pressure_operator(lv_ctx* c, double dt) {
 int lv_pressure_rhs(lv_ctx* c, double dt, int32_t gp_step, const double* vbc) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   Timer t(c, 2);
-  return lv_phys_rhs(c, dt, gp_step, vbc);
+  return lv_phys_rhs(c, dt, gp_step, vbc, 1);
 }
 
 int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
@@ -634,7 +637,7 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;
   for (int it = 1; it <= niter; ++it) {
-    rc = lv_phys_rhs(c, dt, it > 1, vbc);
+    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1);
     if (rc) return rc;
     rc = lv_solver_solve(c, c->s.P, nullptr, it - 1);
     if (rc) return rc;

@@ -102,6 +102,10 @@ struct SolverDev {
   double* dstats;     // device-side stats
   int64_t nnz_cap;
   unsigned long long* fslots;  // flag-published reduction words (lv_fcg.cu)
+  // sweep-invariant RHS terms of refresh!, slot-major like the mesh faces
+  double* rhs_tf;    // (lrr/dt) dot(v_i - v_j, m - y) per face
+  double2* rhs_dmz;  // m - midpoint(x_i, y) per face
+  double* rhs_te;    // dot(dS, vbc - v_i)/dt per boundary edge
   // explicit learned M^-1 on the two-hop pattern (lv_fcg.cu, allocated on first use)
   int *mcnt = nullptr, *mcol = nullptr;
   float *mval = nullptr, *mdiag = nullptr;
@@ -179,7 +183,8 @@ int lv_phys_viscous(lv_ctx* c, double dt, int av);
 int lv_phys_friction(lv_ctx* c, const double* vwall, double dt);
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc);
+// prepare = 1 evaluates the sweep-invariant terms (first sweep of find_pressure!)
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare);
 int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
 
 // ---- learned preconditioner (lv_learn.cu)

@@ -102,27 +102,31 @@ __global__ void k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
 
 // ------------------------------------------------------------- RHS refresh
 
-// refresh!(solver, dt, gp_step, vbc) first loop (pressure.jl:167-187):
-// b, the warm start P and the pressure gradient GP.
-__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
+// refresh!(solver, dt, gp_step, vbc) (pressure.jl:162-201): b, the warm
+// start P and the pressure gradient GP.  It splits into the terms that stay fixed over
+// the fixed-point sweeps of find_pressure! (v, the mesh and the walls do not
+// change between them) and those that follow P.  k_rhs_prep evaluates the
+// fixed ones once per find_pressure! with the reference's expressions:
+//   tf  = (lrr/dt) dot(v_i - v_j, m - y)        per face
+//   dmz = m - midpoint(x_i, y)                  per face (explicit Laplacian)
+//   te  = dot(dS, vbc - v_i)/dt                 per boundary edge
+// and k_rhs / k_rhs_gp subtract or add them in the reference's order, so b and
+// GP are bit-identical to evaluating refresh! in full every sweep.
+__global__ void k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   const double2 xi = s.x[i];
-  const double Pi = s.P[i];
   const double2 vi = s.v[i];
-  double bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
-  double gpx = 0.0, gpy = 0.0;
   for (int k = 0; k < nf; ++k) {
     const size_t f = (size_t)k * cap + i;
     const int j = m.fnbr[f];
     const double lrr = m.flrr[f];
     const double2 mm = m.fm[f], y = m.fy[f];
     const double2 vj = s.v[j];
-    bi -= (lrr / dt) * ((vi.x - vj.x) * (mm.x - y.x) + (vi.y - vj.y) * (mm.y - y.y));
-    const double c = lrr * (Pi - s.P[j]);
-    gpx = gpx - c * (mm.x - xi.x);
-    gpy = gpy - c * (mm.y - xi.y);
+    sv.rhs_tf[f] = (lrr / dt) * ((vi.x - vj.x) * (mm.x - y.x) + (vi.y - vj.y) * (mm.y - y.y));
+    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+    sv.rhs_dmz[f] = make_double2(mm.x - zx, mm.y - zy);
   }
   if (nf < ne) {
     for (int k = 0; k < ne; ++k) {
@@ -138,7 +142,34 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, dou
         case LV_BDARY_DOWN: wx = vbc_ud.z; wy = vbc_ud.w; break;
         default: wx = vbc_rl.z; wy = vbc_rl.w; break;
       }
-      bi -= (dSx * (wx - vi.x) + dSy * (wy - vi.y)) / dt;
+      sv.rhs_te[f] = (dSx * (wx - vi.x) + dSy * (wy - vi.y)) / dt;
+    }
+  }
+}
+
+// refresh! first loop (pressure.jl:167-186) with the fixed terms of k_rhs_prep
+__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
+  const double2 xi = s.x[i];
+  const double Pi = s.P[i];
+  double bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
+  double gpx = 0.0, gpy = 0.0;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double lrr = m.flrr[f];
+    const double2 mm = m.fm[f];
+    bi -= sv.rhs_tf[f];
+    const double c = lrr * (Pi - s.P[j]);
+    gpx = gpx - c * (mm.x - xi.x);
+    gpy = gpy - c * (mm.y - xi.y);
+  }
+  if (nf < ne) {
+    for (int k = 0; k < ne; ++k) {
+      const size_t f = (size_t)k * cap + i;
+      if (m.elab[f] < 0) bi -= sv.rhs_te[f];
     }
   }
   sv.b[i] = bi;
@@ -152,17 +183,15 @@ __global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i];
-  const double2 xi = s.x[i];
   const double2 gi = s.GP[i];
   double bi = sv.b[i];
   for (int k = 0; k < nf; ++k) {
     const size_t f = (size_t)k * cap + i;
     const int j = m.fnbr[f];
     const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
+    const double2 dmz = sv.rhs_dmz[f];
     const double2 gj = s.GP[j];
-    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
-    bi += lrr * ((gi.x - gj.x) * (mm.x - zx) + (gi.y - gj.y) * (mm.y - zy));
+    bi += lrr * ((gi.x - gj.x) * dmz.x + (gi.y - gj.y) * dmz.y);
   }
   sv.b[i] = bi;
 }
@@ -584,15 +613,18 @@ int lv_phys_pressure_step(lv_ctx* c, double dt) {
   return LV_OK;
 }
 
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc) {
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare) {
   if (int rc = need_mesh(c)) return rc;
-  double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (vbc)
-    for (int k = 0; k < 8; ++k) w[k] = vbc[k];
-  // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
-  double4 ud = make_double4(w[0], w[1], w[4], w[5]);
-  double4 rl = make_double4(w[2], w[3], w[6], w[7]);
-  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt, ud, rl);
+  if (prepare) {
+    double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (vbc)
+      for (int k = 0; k < 8; ++k) w[k] = vbc[k];
+    // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
+    double4 ud = make_double4(w[0], w[1], w[4], w[5]);
+    double4 rl = make_double4(w[2], w[3], w[6], w[7]);
+    LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl);
+  }
+  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt);
   if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n);
   return LV_OK;
 }
