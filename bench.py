@@ -197,7 +197,8 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
             L.lv_kernel_time(g._ctx, f, C.byref(nl), C.byref(t), 1)
             ms[name] = t.value
         L.lv_kernel_timing(g._ctx, 0)
-        out[method] = {"solve_ms_per_step": (ms["pcg"] + ms["rhs"]) / steps,
+        out[method] = {"solve_ms_per_step": (ms["pcg"] + ms["rhs"] + ms["learn"]) / steps,
+                       "factor_ms_per_step": ms["learn"] / steps,
                        "pcg_kernel_ms_per_step": ms["pcg"] / steps,
                        "cg_iters_per_step": (i1.value - i0.value) / steps,
                        "us_per_iteration": 1e3 * ms["pcg"] / max(i1.value - i0.value, 1)}
@@ -362,7 +363,7 @@ def run_ours(args, world, rank, local):
                    "solver": SOLVER_DESC[args.solver] + ", tol 1e-8 (FP64 residual), 10 sweeps/step",
                    "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": f"replicas x{world}",
                    "l2": "512 MiB buffer written between timed steps (the 256x256 state, ~15 MB, fits in L2)"},
-        "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1]) / args.steps,
+        "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1] + kt["learn"][1]) / args.steps,
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
                      "solves": solves, "solvers": comparison},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},

@@ -231,7 +231,8 @@ void* lv_stream(lv_ctx* ctx);
 #define LV_KF_PCG 2      /* persistent pressure-solve kernels */
 #define LV_KF_RHS 3      /* operator assembly and right-hand side */
 #define LV_KF_OPS 4      /* per-particle physics operators */
-#define LV_KF_COUNT 5
+#define LV_KF_LEARN 5    /* learned factor of the assembled operator (network forward, M^-1) */
+#define LV_KF_COUNT 6
 /* When enabled, every launch of every family is bracketed by CUDA events on
  * the context's stream (no synchronisation).  lv_kernel_time synchronises
  * and returns, for one family, the launches and total device ms since the

@@ -94,7 +94,7 @@ SIGNATURES = {
     "lv_learn_factor": (C.c_int, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "lv_pcg_solve_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i32, _vp, _pi32, _pd]),
 }
-KERNEL_FAMILIES = {"bin": 0, "clip": 1, "pcg": 2, "rhs": 3, "ops": 4}
+KERNEL_FAMILIES = {"bin": 0, "clip": 1, "pcg": 2, "rhs": 3, "ops": 4, "learn": 5}
 
 _LIB = None
 

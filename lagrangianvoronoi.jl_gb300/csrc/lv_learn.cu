@@ -214,33 +214,47 @@ __global__ void __launch_bounds__(LTPB) k_layer_fwd(int n, const float* __restri
   }
 }
 
-// readout: gd_i = 1 + H_i . rd ; gl_k = what_k sum_c ro_c H_ic H_jc (j = col_k < i)
+// readout: gd_i = 1 + H_i . rd ; gl_k = what_k sum_c ro_c H_ic H_jc (j = col_k < i).
+// Four lanes per row, eight features each: the 128-byte rows of H are read
+// coalesced and the dot products finish with two shuffles.
+constexpr int RO_LANES = 4;
+constexpr int RO_F = HID / RO_LANES;
 __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                           const float* __restrict__ what, const float* __restrict__ H, const float* __restrict__ params,
                           float* gd, float* gl) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float* rd = params + OFF_RD;
-  const float* ro = params + OFF_RO;
-  const float* hi = H + (size_t)i * HID;
-  float hro[HID];
-  float d = 1.f;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / RO_LANES, q = gt % RO_LANES;
+  const bool on = i < n;  // whole groups of four lanes share a row
+  const float* rd = params + OFF_RD + q * RO_F;
+  const float* ro = params + OFF_RO + q * RO_F;
+  float hro[RO_F];
+  float d = 0.f;
+  if (on) {
+    const float* hi = H + (size_t)i * HID + q * RO_F;
 #pragma unroll
-  for (int c = 0; c < HID; ++c) {
-    d = fmaf(hi[c], rd[c], d);
-    hro[c] = hi[c] * ro[c];
+    for (int c = 0; c < RO_F; ++c) {
+      const float h = hi[c];
+      d = fmaf(h, rd[c], d);
+      hro[c] = h * ro[c];
+    }
   }
-  gd[i] = d;
-  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+  d += __shfl_xor_sync(0xffffffffu, d, 1);
+  d += __shfl_xor_sync(0xffffffffu, d, 2);
+  if (on && q == 0) gd[i] = 1.f + d;
+  const int a = on ? rowptr[i] : 0, b = on ? rowptr[i + 1] : 0;
+  // the four lanes of a row run the same trip count and shuffle among themselves
+  const unsigned gmask = 0xFu << ((threadIdx.x & 31) & ~(RO_LANES - 1));
+  for (int k = a; k < b; ++k) {
     const int j = col[k];
     float v = 0.f;
     if (j < i) {
-      const float* hj = H + (size_t)j * HID;
+      const float* hj = H + (size_t)j * HID + q * RO_F;
 #pragma unroll
-      for (int c = 0; c < HID; ++c) v = fmaf(hro[c], hj[c], v);
-      v *= what[k];
+      for (int c = 0; c < RO_F; ++c) v = fmaf(hro[c], hj[c], v);
     }
-    gl[k] = v;
+    v += __shfl_xor_sync(gmask, v, 1);
+    v += __shfl_xor_sync(gmask, v, 2);
+    if (q == 0) gl[k] = (j < i) ? v * what[k] : 0.f;
   }
 }
 
@@ -796,7 +810,7 @@ int prepare(lv_ctx* c, const LearnSystem& S) {
 int forward(lv_ctx* c, const LearnSystem& S) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
-  const int nb = launch_blocks_tiles(S.n);
+  const int nb = std::max(1, (S.n + 63) / 64);  // every 16-row tile at once: the aggregation is latency-bound
   k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
   k_layer_fwd<FIN><<<nb, LTPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0, 0,
                                          L->Z0, L->H1);
@@ -804,7 +818,8 @@ int forward(lv_ctx* c, const LearnSystem& S) {
                                          L->Z1, L->H2);
   k_layer_fwd<HID><<<nb, LTPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2, 1,
                                          L->Z2, L->H3);
-  k_readout<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd, L->gl);
+  k_readout<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd,
+                                                           L->gl);
   c->launches += 5;
   return lv_cuda_check(c, cudaGetLastError(), "learned: forward");
 }

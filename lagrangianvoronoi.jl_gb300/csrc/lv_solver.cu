@@ -595,39 +595,13 @@ __device__ void df_grid_totals(const float2* part, int slot0, float (&tot)[NV]) 
   __syncthreads();
 }
 
-// The inner preconditioner is either Jacobi, z = D^-1 r (two grid barriers
-// per iteration), or the learned factor,
+// The streaming solver's preconditioner is either Jacobi, z = D^-1 r, or the
+// learned factor,
 //     z = D^-1/2 (Gt^T (Gt r^) + eps r^),   r^ = D^-1/2 r
-// (Gt lower-triangular on the operator's pattern), which needs two
-// neighbour exchanges (four barriers per iteration).  A learned solve whose
-// inner iterations exceed those of the last Jacobi mixed solve (*jref, kept
-// on the device) continues with Jacobi and reports the fallback.
-template <int R>
-struct RowRegsL {
-  int i[R];
-  int beg[R], cnt[R];
-  int cc[R][KR];
-  float ww[R][KR];
-  float gg[R][KR];  // Gt_(i,col) for col < i, Gt_(col,i) for col > i
-  float dg[R], dnv[R], gdd[R], dhh[R];
-  double bb[R];
-};
-
-template <int R>
-__device__ __forceinline__ void row_apply32L(const RowRegsL<R>& rr, const PCGArgs& a, const float* __restrict__ vg,
-                                             const float (&own)[R], float (&out)[R]) {
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    float acc = rr.dg[r] * own[r];
-#pragma unroll
-    for (int k = 0; k < KR; ++k)
-      if (k < rr.cnt[r]) acc = fmaf(rr.ww[r][k], own[r] - vg[rr.cc[r][k]], acc);
-    for (int k = KR; k < rr.cnt[r]; ++k)
-      acc = fmaf((float)a.w[rr.beg[r] + k], own[r] - vg[a.col[rr.beg[r] + k]], acc);
-    out[r] = acc;
-  }
-}
-
+// (Gt lower-triangular on the operator's pattern), which needs two neighbour
+// exchanges.  A learned solve whose inner iterations exceed those of the last
+// Jacobi mixed solve (*jref, kept on the device) continues with Jacobi and
+// reports the fallback.
 struct LearnArgs {
   const float* gd;
   const float* gl;
@@ -642,282 +616,6 @@ struct LearnArgs {
   int* out_method;
   int learned;    // 0: Jacobi preconditioner throughout (LV_METHOD_MIXED_IR)
 };
-
-template <int R>
-__global__ void __launch_bounds__(SP_TPB) k_lpcg_reg(PCGArgs a, LearnArgs la) {
-  __shared__ double sh[4 * 32];
-  __shared__ float2 shf[4 * 32];
-  __shared__ int s_flag[2];
-  const int n = a.n;
-  const int nb = gridDim.x;
-  const int stride = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  float2* part32 = reinterpret_cast<float2*>(a.part);
-  RowRegsL<R> rr;
-  double x[R];
-#pragma unroll
-  for (int k = 0; k < R; ++k) {
-    const int i = t0 + k * stride;
-    rr.i[k] = i;
-    const bool on = i < n;
-    rr.beg[k] = on ? a.rowptr[i] : 0;
-    rr.cnt[k] = on ? a.rowptr[i + 1] - rr.beg[k] : 0;
-#pragma unroll
-    for (int e = 0; e < KR; ++e) {
-      const bool have = e < rr.cnt[k];
-      const int kk = rr.beg[k] + e;
-      const int j = have ? a.col[kk] : 0;
-      rr.cc[k][e] = j;
-      rr.ww[k][e] = have ? (float)a.w[kk] : 0.0f;
-      // the factor exists (and is read) only in learned mode
-      float gv = 0.f;
-      if (have && la.learned) {
-        if (j < i)
-          gv = la.gl[kk];
-        else if (la.rev[kk] >= 0)
-          gv = la.gl[la.rev[kk]];
-      }
-      rr.gg[k][e] = gv;
-    }
-    rr.dg[k] = on ? (float)a.diag[i] : 0.0f;
-    rr.dnv[k] = on ? (float)a.dinv[i] : 0.0f;
-    rr.gdd[k] = (on && la.learned) ? la.gd[i] : 0.0f;
-    rr.dhh[k] = (on && la.learned) ? la.dh[i] : 0.0f;
-    rr.bb[k] = on ? a.b[i] : 0.0;
-    x[k] = on ? a.x[i] : 0.0;
-  }
-  if (*a.nonsingular == 0) {
-    double v[1] = {0.0};
-#pragma unroll
-    for (int k = 0; k < R; ++k) v[0] += rr.bb[k];
-    block_sums<1>(v, sh);
-    if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
-    if (!grid_barrier(a.bar, a.status)) return;
-    double t[1];
-    grid_totals<1>(a.part, 0, t);
-    const double mean = t[0] / (double)n;
-#pragma unroll
-    for (int k = 0; k < R; ++k)
-      if (rr.i[k] < n) rr.bb[k] -= mean;
-    if (!grid_barrier(a.bar, a.status)) return;
-  }
-  const int jref = *la.jref;
-  const int cap = jref > 0 ? jref : a.itmax;
-  bool learned = la.learned != 0;
-  int it = 0, outer = 0;
-  double bnorm2 = 0.0, rtrue2 = 0.0;
-  float r[R], z[R], p[R], q[R], d[R], rh[R];
-  // z = M^-1 r for the current mode; needs r^ exchanged (learned mode)
-  auto precond = [&]() -> bool {
-    if (!learned) {
-#pragma unroll
-      for (int k = 0; k < R; ++k) z[k] = rr.dnv[k] * r[k];
-      return true;
-    }
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      rh[k] = rr.dhh[k] * r[k];
-      if (rr.i[k] < n) la.rhat[rr.i[k]] = rh[k];
-    }
-    if (!grid_barrier(a.bar, a.status)) return false;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int i = rr.i[k];
-      float t = rr.gdd[k] * rh[k];
-#pragma unroll
-      for (int e = 0; e < KR; ++e)
-        if (e < rr.cnt[k] && rr.cc[k][e] < i) t = fmaf(rr.gg[k][e], la.rhat[rr.cc[k][e]], t);
-      for (int e = KR; e < rr.cnt[k]; ++e) {  // rows with more than KR neighbours
-        const int kk = rr.beg[k] + e, j = a.col[kk];
-        if (j < i) t = fmaf(la.gl[kk], la.rhat[j], t);
-      }
-      if (i < n) la.tbuf[i] = t;
-      z[k] = t;  // own t, kept for the transpose product
-    }
-    if (!grid_barrier(a.bar, a.status)) return false;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const int i = rr.i[k];
-      float u = rr.gdd[k] * z[k];
-#pragma unroll
-      for (int e = 0; e < KR; ++e)
-        if (e < rr.cnt[k] && rr.cc[k][e] > i) u = fmaf(rr.gg[k][e], la.tbuf[rr.cc[k][e]], u);
-      for (int e = KR; e < rr.cnt[k]; ++e) {
-        const int kk = rr.beg[k] + e, j = a.col[kk];
-        if (j > i && la.rev[kk] >= 0) u = fmaf(la.gl[la.rev[kk]], la.tbuf[j], u);
-      }
-      z[k] = rr.dhh[k] * fmaf(la.eps, rh[k], u);
-    }
-    return true;
-  };
-  for (; outer < MIR_MAX_OUTER; ++outer) {
-    double r64[R];
-    double v[2] = {0.0, 0.0};
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      const bool on = rr.i[k] < n;
-      double acc = 0.0;
-      if (on) {
-        const int i = rr.i[k];
-        acc = a.diag[i] * x[k];
-        for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) acc += a.w[e] * (x[k] - a.x[a.col[e]]);
-      }
-      r64[k] = on ? rr.bb[k] - acc : 0.0;
-      v[0] += r64[k] * r64[k];
-      v[1] += rr.bb[k] * rr.bb[k];
-    }
-    block_sums<2>(v, sh);
-    if (threadIdx.x == 0) {
-      a.part[0 * nb + blockIdx.x] = v[0];
-      a.part[1 * nb + blockIdx.x] = v[1];
-    }
-    if (!grid_barrier(a.bar, a.status)) return;
-    {
-      double t2[2];
-      grid_totals<2>(a.part, 0, t2);
-      rtrue2 = t2[0];
-      bnorm2 = t2[1];
-    }
-    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax) break;
-    const double sigma = sqrt(rtrue2);
-    const double inv_sigma = 1.0 / sigma;
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      r[k] = (float)(r64[k] * inv_sigma);
-      d[k] = 0.0f;
-      p[k] = 0.0f;
-      q[k] = 0.0f;
-    }
-    const float rho_stop = fmaxf(MIR_INNER_TOL * MIR_INNER_TOL, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
-    // z = M^-1 r, rz
-    if (!precond()) return;
-    float rz;
-    {
-      float2 v1[1] = {make_float2(0.f, 0.f)};
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        v1[0] = df_add(v1[0], df_prod(r[k], z[k]));
-        if (rr.i[k] < n) la.zbuf[rr.i[k]] = z[k];
-      }
-      df_block_sums<1>(v1, shf);
-      if (threadIdx.x == 0) part32[2 * nb + blockIdx.x] = v1[0];
-      if (!grid_barrier(a.bar, a.status)) return;
-      float t1[1];
-      df_grid_totals<1>(part32, 2, t1);
-      rz = t1[0];
-    }
-    float beta = 0.f;
-    while (true) {
-      // p = z + beta p; q = A z + beta q (= A p)
-      float az[R];
-      row_apply32L<R>(rr, a, la.zbuf, z, az);
-      float2 v1[1] = {make_float2(0.f, 0.f)};
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        p[k] = fmaf(beta, p[k], z[k]);
-        q[k] = fmaf(beta, q[k], az[k]);
-        v1[0] = df_add(v1[0], df_prod(p[k], q[k]));
-      }
-      df_block_sums<1>(v1, shf);
-      if (threadIdx.x == 0) part32[3 * nb + blockIdx.x] = v1[0];
-      if (!grid_barrier(a.bar, a.status)) return;
-      float pq[1];
-      df_grid_totals<1>(part32, 3, pq);
-      const float alpha = rz / pq[0];
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        d[k] = fmaf(alpha, p[k], d[k]);
-        r[k] = fmaf(-alpha, q[k], r[k]);
-      }
-      ++it;
-      float rr2, rzn;
-      if (!learned) {
-        // Jacobi: z = D^-1 r is local, so ||r||^2 and (r, z) share one barrier
-        float2 v2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          z[k] = rr.dnv[k] * r[k];
-          if (rr.i[k] < n) la.zbuf[rr.i[k]] = z[k];
-          v2[0] = df_add(v2[0], df_prod(r[k], r[k]));
-          v2[1] = df_add(v2[1], df_prod(r[k], z[k]));
-        }
-        df_block_sums<2>(v2, shf);
-        if (threadIdx.x == 0) {
-          part32[4 * nb + blockIdx.x] = v2[0];
-          part32[5 * nb + blockIdx.x] = v2[1];
-        }
-        if (!grid_barrier(a.bar, a.status)) return;
-        float t2[2];
-        df_grid_totals<2>(part32, 4, t2);
-        rr2 = t2[0];
-        rzn = t2[1];
-      } else {
-        float2 v2[1] = {make_float2(0.f, 0.f)};
-#pragma unroll
-        for (int k = 0; k < R; ++k) v2[0] = df_add(v2[0], df_prod(r[k], r[k]));
-        df_block_sums<1>(v2, shf);
-        if (threadIdx.x == 0) part32[4 * nb + blockIdx.x] = v2[0];
-        // the preconditioner's first exchange also publishes the ||r|| partials
-        if (!precond()) return;
-        float t1[1];
-        df_grid_totals<1>(part32, 4, t1);
-        rr2 = t1[0];
-        rzn = 0.f;
-      }
-      if (threadIdx.x == 0) {
-        const int stop = (rr2 <= rho_stop || it >= a.itmax || !(pq[0] > 0.f)) ? 1 : 0;
-        s_flag[0] = stop;
-        s_flag[1] = (learned && it >= cap && !stop) ? 1 : 0;
-      }
-      __syncthreads();
-      const int stop = s_flag[0], fall = s_flag[1];
-      __syncthreads();
-      if (stop) break;
-      if (fall) {
-        // the learned preconditioner needs more iterations than Jacobi did:
-        // continue the refinement from the current iterate with Jacobi
-        learned = false;
-        break;
-      }
-      if (learned) {
-        float2 v3[1] = {make_float2(0.f, 0.f)};
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          v3[0] = df_add(v3[0], df_prod(r[k], z[k]));
-          if (rr.i[k] < n) la.zbuf[rr.i[k]] = z[k];
-        }
-        df_block_sums<1>(v3, shf);
-        if (threadIdx.x == 0) part32[5 * nb + blockIdx.x] = v3[0];
-        if (!grid_barrier(a.bar, a.status)) return;
-        float t1[1];
-        df_grid_totals<1>(part32, 5, t1);
-        rzn = t1[0];
-      }
-      beta = rzn / rz;
-      rz = rzn;
-    }
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-      x[k] += sigma * (double)d[k];
-      if (rr.i[k] < n) a.x[rr.i[k]] = x[k];
-    }
-    if (!grid_barrier(a.bar, a.status)) return;
-  }
-#pragma unroll
-  for (int k = 0; k < R; ++k)
-    if (rr.i[k] < n) a.x[rr.i[k]] = x[k];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *a.out_iters = it;
-    *la.out_outer = outer;
-    *la.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
-    if (!la.learned) *la.jref = it;
-    a.out_d[0] = rtrue2;
-    a.out_d[1] = bnorm2;
-    a.out_d[2] = rtrue2;
-    a.counters[0] += 1;
-    a.counters[1] += it;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Streaming variant of the mixed-precision solve for systems too large for
@@ -1155,7 +853,6 @@ __global__ void k_any_nonzero(const double* v, int n, int* flag) {
 
 int g_pcg_blocks_per_sm = -1;
 int g_reg_blocks_per_sm[2] = {-1, -1};
-int g_lpcg_blocks_per_sm[2] = {-1, -1};
 int g_str_blocks_per_sm = -1;
 
 }  // namespace
@@ -1225,52 +922,18 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
   a.out_d = c->sv.dstats + 3 * slot;
   a.counters = c->sv.counters;
   cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
+  if (c->method == LV_METHOD_LEARNED_PCG && !c->factor_valid) {
+    // the network's factor for this operator (once per assembly)
+    KernelTimer kf(c, LV_KF_LEARN);
+    if (int rc = lv_learn_factor_current(c)) return rc;
+    if (int rc = lv_fcg_build_minv(c)) return rc;
+    c->factor_valid = true;
+  }
   KernelTimer kt(c, LV_KF_PCG);
   if (c->method != LV_METHOD_JACOBI_PCG) {
     const bool learned = c->method == LV_METHOD_LEARNED_PCG;
-    if (learned && !c->factor_valid) {
-      KernelTimer kf(c, LV_KF_RHS);
-      if (int rc = lv_learn_factor_current(c)) return rc;
-      if (int rc = lv_fcg_build_minv(c)) return rc;
-      c->factor_valid = true;
-    }
     // systems that fit one or two blocks per SM: flag-reduced solver
     if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);
-    if (g_lpcg_blocks_per_sm[0] < 0) {
-      int b1 = 0, b2 = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_lpcg_reg<1>, SP_TPB, 0);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_lpcg_reg<2>, SP_TPB, 0);
-      g_lpcg_blocks_per_sm[0] = b1;
-      g_lpcg_blocks_per_sm[1] = b2;
-    }
-    for (int R = 1; R <= 2; ++R) {
-      const int per_sm = std::min(g_lpcg_blocks_per_sm[R - 1], 2);
-      if (per_sm < 1) continue;
-      const int need = lv_blocks(n, SP_TPB * R);
-      if (need > c->num_sms * per_sm) continue;
-      LearnArgs la;
-      if (learned) {
-        lv_learn_factor_ptrs(c, &la.gd, &la.gl, &la.dh, &la.rev);
-        if (!la.gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
-      } else {
-        la.gd = la.gl = la.dh = nullptr;  // Jacobi mode: the kernel reads no factor
-        la.rev = nullptr;
-      }
-      la.eps = c->learn_eps;
-      la.rhat = c->sv.r32;
-      la.tbuf = c->sv.z32;
-      la.zbuf = c->sv.p32;
-      la.jref = c->sv.iters + LV_IT_JREF;
-      la.out_outer = c->sv.iters + LV_IT_OUTER + slot;
-      la.out_method = c->sv.iters + LV_IT_METHOD + slot;
-      la.learned = learned ? 1 : 0;
-      void* rargs[] = {&a, &la};
-      const void* fn = (R == 1) ? (const void*)k_lpcg_reg<1> : (const void*)k_lpcg_reg<2>;
-      cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(std::max(need, 1)), dim3(SP_TPB), rargs, 0, c->stream);
-      c->launches++;
-      if (e != cudaSuccess) return lv_cuda_check(c, e, "k_lpcg_reg cooperative launch");
-      return LV_OK;
-    }
     // larger systems: the streaming variant
     {
       LearnArgs la;
