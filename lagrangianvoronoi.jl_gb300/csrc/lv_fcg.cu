@@ -627,7 +627,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.mdiag = c->sv.mdiag;
   a.mstride = c->sv.mrows;
   a.minv_ok = learned ? c->sv.mok : c->sv.iters + LV_IT_NONSINGULAR;  // read only in learned mode
-  a.jref = c->sv.iters + LV_IT_JREF;
+  a.jref = c->sv.iters + LV_IT_JREF + slot;  // the same sweep of the last Jacobi mixed solve
   a.out_iters = c->sv.iters + slot;
   a.out_outer = c->sv.iters + LV_IT_OUTER + slot;
   a.out_method = c->sv.iters + LV_IT_METHOD + slot;

@@ -27,10 +27,9 @@
 #define LV_IT_ITERS 0          // [32] inner/CG iterations per slot
 #define LV_IT_OUTER 32         // [32] refinement steps per slot
 #define LV_IT_METHOD 64        // [32] method used per slot (learned solves)
-#define LV_IT_JREF 96          // iterations of the last Jacobi mixed solve
+#define LV_IT_JREF 128         // [32] iterations of the last Jacobi mixed solve per sweep slot
 #define LV_IT_NONSINGULAR 97   // set when some diagonal term is nonzero
-#define LV_IT_EPOCH 98         // last reduction epoch of the flag-reduced solver
-#define LV_IT_SIZE 128
+#define LV_IT_SIZE 160
 
 // Status bits set on the device with atomicOr; decoded on the host.
 #define LV_FLAG_NAN_VELOCITY 0x1

@@ -946,7 +946,7 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
       }
       la.eps = c->learn_eps;
       la.rhat = la.tbuf = la.zbuf = nullptr;
-      la.jref = c->sv.iters + LV_IT_JREF;
+      la.jref = c->sv.iters + LV_IT_JREF + slot;
       la.out_outer = c->sv.iters + LV_IT_OUTER + slot;
       la.out_method = c->sv.iters + LV_IT_METHOD + slot;
       la.learned = learned ? 1 : 0;
