@@ -189,6 +189,9 @@ lv_ctx* lv_create(const lv_params* prm) {
   g.oy = g.cminy - h;
   g.n1 = (int)floor((g.cmaxx - g.cminx) / h) + 3;
   g.n2 = (int)floor((g.cmaxy - g.cminy) / h) + 3;
+  // dx >= dx_hi implies floor(dx / h) >= n1 whatever the rounding of the quotient
+  g.dx_hi = (double)g.n1 * h * (1.0 + 1e-12);
+  g.dy_hi = (double)g.n2 * h * (1.0 + 1e-12);
   const double bigm = std::max(std::max(fabs(g.cminx), fabs(g.cmaxx)), std::max(fabs(g.cminy), fabs(g.cmaxy)));
   g.bigm = (float)(bigm * (1.0 + 1e-6));
   g.delta32 = (float)(ldexp(1.0, -22) * (bigm + std::max(g.xperiod, g.yperiod)));

@@ -101,8 +101,12 @@ __global__ void k_scan_add(int* out, int len, const int* sums, int ntiles) {
 
 // neighborlist.jl:47-52: key = floor((x - origin)/h) + 1, 1-based; returns
 // the 0-based cell index or -1 when outside, -2 when not finite.
-__device__ __forceinline__ int cell_of(const GridDev& g, double px, double py) {
+// quick: the position is a periodic image of a finite one, and positions
+// surely outside the grid skip the divisions: dx < 0 gives floor(dx/h) <= -1,
+// dx >= dx_hi gives floor(dx/h) >= n1 (most images of a periodic domain).
+__device__ __forceinline__ int cell_of(const GridDev& g, double px, double py, bool quick) {
   double dx = px - g.ox, dy = py - g.oy;
+  if (quick && (dx < 0.0 || dy < 0.0 || dx >= g.dx_hi || dy >= g.dy_hi)) return -1;
   double f1 = floor(dx / g.h), f2 = floor(dy / g.h);
   if (!(fabs(f1) < 1e15) || !(fabs(f2) < 1e15)) return -2;
   long long i1 = (long long)f1 + 1, i2 = (long long)f2 + 1;
@@ -148,7 +152,7 @@ __global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int
   for (int k = 0; k < nim; ++k) {
     double qx, qy;
     image_pos(g, k, p.x, p.y, qx, qy);
-    int c = cell_of(g, qx, qy);
+    int c = cell_of(g, qx, qy, k > 0);
     if (c == -2) {
       atomicOr(status, LV_FLAG_NONFINITE);
       return;
@@ -166,7 +170,7 @@ __global__ void k_bin_scatter(GridDev g, const double2* __restrict__ x, int n, c
   for (int k = 0; k < nim; ++k) {
     double qx, qy;
     image_pos(g, k, p.x, p.y, qx, qy);
-    int c = cell_of(g, qx, qy);
+    int c = cell_of(g, qx, qy, k > 0);
     if (c < 0) continue;
     int slot = cstart[c] + atomicAdd(&cursor[c], 1);
     if (slot < item_cap)
