@@ -343,6 +343,17 @@ def run_ours(args, world, rank, local):
     pcg_bytes = iters * per_it
     clip_bytes = kt["clip"][0] * (16 * N + 28 * F + 28 * N)
     fams = {"pcg": pcg_bytes, "clip": clip_bytes}
+    # compulsory bytes of the whole step (per kernel family, the per-unit
+    # counts above): re-bin 32N and clip 16N + 28F + 28N per remesh; CSR
+    # assembly 28F + 68N + 12 nnz per find_pressure; RHS 28F + 80N per sweep;
+    # the CG iterations; ten other face passes of 28F + 40N
+    remeshes = kt["clip"][0]
+    step_bytes = (remeshes * (32 * N + 16 * N + 28 * F + 28 * N)
+                  + args.steps * (28 * F + 68 * N + 12 * (F + N))
+                  + solves * (28 * F + 80 * N)
+                  + pcg_bytes
+                  + args.steps * 10 * (28 * F + 40 * N))
+    step_gbs = step_bytes / (dev_ms / 1e3) / 1e9
     dom = max(("pcg", "clip"), key=lambda k: kt[k][1])
     dom_ms = kt[dom][1]
     dom_launches = max(kt[dom][0], 1)
@@ -367,6 +378,8 @@ def run_ours(args, world, rank, local):
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
                      "solves": solves, "solvers": comparison},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},
+        "full_step_roofline": {"bytes_per_step": step_bytes / args.steps, "achieved": step_gbs, "peak": hbm_peak,
+                               "unit": "GB/s", "frac": step_gbs / hbm_peak},
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                      "peak_source": peak_src},

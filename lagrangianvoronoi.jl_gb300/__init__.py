@@ -30,6 +30,7 @@ __all__ = [
     "ideal_eos", "stiffened_eos", "find_rho", "gravity_step", "find_pressure", "pressure_step", "find_D",
     "viscous_step", "bdary_friction", "find_dv", "relaxation_step", "multiphase_projection", "populate_jittered",
     "populate_rect", "populate_hex", "populate_circ", "populate_rand", "populate_vogel", "populate_lloyd", "run",
+    "export_grid", "export_points",
     "LvError", "BDARY_UP", "BDARY_RIGHT", "BDARY_DOWN", "BDARY_LEFT", "LV_MAX_EDGES", "wall_velocity_table",
 ]
 
@@ -354,15 +355,4 @@ def populate_lloyd(grid, niterations=100, seed=1, charfun=None):
         remesh(grid)
 
 
-def run(sim, dt, t_end, step, nframes=100, postproc=None):
-    """run!(sim, dt, t_end, step!; nframes, postproc!) (src/simulation.jl:35-94)
-    without file output: calls step(sim, t) every dt and postproc(sim, t) every
-    k_frame steps."""
-    k_frame = max(int(round(t_end / (nframes * dt))) if nframes > 0 else 1 << 62, 1)
-    t, k = 0.0, 0
-    while t < t_end:
-        k += 1
-        step(sim, t)
-        if k % k_frame == 0 and postproc is not None:
-            postproc(sim, t)
-        t += dt
+from .vtkio import export_grid, export_points, run  # noqa: E402  (src/IO.jl, src/simulation.jl)
