@@ -221,6 +221,20 @@ int lv_learn_factor(lv_ctx* ctx, float* gdiag, float* glower, float* features);
 /* MultiphaseSolver / multiphase_projection! (relaxation.jl:137-206). */
 int lv_multiphase_projection(lv_ctx* ctx, double quality_threshold, lv_solve_stats* stats);
 
+/* Post-processing on the current mesh (host arrays in and out).
+ * nearest_polygon (voronoigrid.jl:154-178): out[m] = 0-based index of the
+ * nearest seed of each points[m][2] (-1 when the cell path meets none). */
+int lv_nearest_polygon(lv_ctx* ctx, int32_t m, const double* points, int32_t* out);
+/* movingls (movingls.jl:52-86) with gaussian_kernel: Taylor coefficients of
+ * the per-polygon values[n] at polygons polys[m] (NULL: all, m = n), order 1
+ * linear (2 coefficients), 2 quadratic (5), 3 cubic (9), moving radius h;
+ * coeffs[m][2|5|9] in power_vector order (movingls.jl:26-36). */
+int lv_movingls(lv_ctx* ctx, int32_t order, int32_t m, const int32_t* polys, const double* values, double h,
+                double* coeffs);
+/* point_value (movingls.jl:140-146): values[n] interpolated at points[m][2]
+ * from the nearest polygon's linear expansion (h = cell size). */
+int lv_point_value(lv_ctx* ctx, int32_t m, const double* points, const double* values, double* out);
+
 /* The CUDA stream (cudaStream_t) every call of this context is ordered on;
  * callers may record events or enqueue their own work on it. */
 void* lv_stream(lv_ctx* ctx);

@@ -30,7 +30,8 @@ __all__ = [
     "ideal_eos", "stiffened_eos", "find_rho", "gravity_step", "find_pressure", "pressure_step", "find_D",
     "viscous_step", "bdary_friction", "find_dv", "relaxation_step", "multiphase_projection", "populate_jittered",
     "populate_rect", "populate_hex", "populate_circ", "populate_rand", "populate_vogel", "populate_lloyd", "run",
-    "export_grid", "export_points",
+    "export_grid", "export_points", "LinearExpansion", "QuadraticExpansion", "CubicExpansion", "gaussian_kernel",
+    "power_vector", "poly_eval", "nearest_polygon", "movingls", "point_value", "integral",
     "LvError", "BDARY_UP", "BDARY_RIGHT", "BDARY_DOWN", "BDARY_LEFT", "LV_MAX_EDGES", "wall_velocity_table",
 ]
 
@@ -356,3 +357,5 @@ def populate_lloyd(grid, niterations=100, seed=1, charfun=None):
 
 
 from .vtkio import export_grid, export_points, run  # noqa: E402  (src/IO.jl, src/simulation.jl)
+from .movingls import (LinearExpansion, QuadraticExpansion, CubicExpansion, gaussian_kernel,  # noqa: E402
+                       power_vector, poly_eval, nearest_polygon, movingls, point_value, integral)

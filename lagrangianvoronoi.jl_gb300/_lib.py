@@ -74,6 +74,9 @@ SIGNATURES = {
     "lv_solve": (C.c_int, [_vp, _pd, _pd, _pst]),
     "lv_operator_apply": (C.c_int, [_vp, _pd, _pd]),
     "lv_multiphase_projection": (C.c_int, [_vp, _d, _pst]),
+    "lv_nearest_polygon": (C.c_int, [_vp, _i32, _pd, _pi32]),
+    "lv_movingls": (C.c_int, [_vp, _i32, _i32, _pi32, _pd, _d, _pd]),
+    "lv_point_value": (C.c_int, [_vp, _i32, _pd, _pd, _pd]),
     "lv_get_timings": (C.c_int, [_vp, _pd, _i32]),
     "lv_reset_timings": (C.c_int, [_vp]),
     "lv_launch_count": (_i64, [_vp]),

@@ -22,6 +22,7 @@ UNITS = {
     "lv_solver.cu": [],
     "lv_learn.cu": [],
     "lv_fcg.cu": [],
+    "lv_post.cu": ["--fmad=false"],
 }
 
 

@@ -1308,4 +1308,166 @@ int lvref_multiphase_projection(void* h, double quality_threshold, double tol, i
   return 0;
 }
 
+// ------------------------------------------------------------ moving least squares
+
+// The reference's cell path in full: every offset of the (2 n - 1)^2 range
+// (neighborlist.jl:29-41, swapped n1/n2 bounds), ordered as build_path
+// orders its prefix, cut after the first node with rr > bound.
+static std::vector<PathNode> path_upto(const Grid& g, double bound) {
+  std::vector<PathNode> all;
+  for (int64_t i2 = 1 - g.n1; i2 <= g.n1 - 1; ++i2)
+    for (int64_t i1 = 1 - g.n2; i1 <= g.n2 - 1; ++i1) {
+      int64_t a = std::max<int64_t>(0, std::llabs(i1) - 1), c = std::max<int64_t>(0, std::llabs(i2) - 1);
+      double rr = (g.h * g.h) * (double)(a * a + c * c);
+      all.push_back({i1, i2, i1 * i1 + i2 * i2, rr});
+    }
+  std::stable_sort(all.begin(), all.end(), [](const PathNode& p, const PathNode& q) { return p.keysq < q.keysq; });
+  std::stable_sort(all.begin(), all.end(), [](const PathNode& p, const PathNode& q) { return p.rr < q.rr; });
+  std::vector<PathNode> out;
+  for (const auto& nd : all) {
+    out.push_back(nd);
+    if (nd.rr > bound) break;
+  }
+  return out;
+}
+
+// voronoigrid.jl:154-178; -1 when no polygon is met
+static int nearest_polygon(const Grid& g, const std::vector<PathNode>& path, V2 x) {
+  int64_t k1, k2;
+  if (!findkey(g, x, k1, k2)) return -1;
+  double rr_best = INFINITY;
+  int i_best = -1;
+  for (const auto& nd : path) {
+    if (nd.rr > rr_best) break;
+    const int64_t c1 = k1 + nd.i1, c2 = k2 + nd.i2;
+    if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) continue;
+    for (int32_t i : g.cells[(c1 - 1) + g.n1 * (c2 - 1)]) {
+      const double prr = norm_squared(g.x[i] - x);
+      if (prr < rr_best) {
+        rr_best = prr;
+        i_best = i;
+      }
+    }
+  }
+  return i_best;
+}
+
+// power_vector (movingls.jl:26-36) for 2, 5 or 9 coefficients
+static int power_vector(int nc, V2 d, double* pv) {
+  pv[0] = d.x;
+  pv[1] = d.y;
+  if (nc >= 5) {
+    pv[2] = d.x * d.x;
+    pv[3] = d.x * d.y;
+    pv[4] = d.y * d.y;
+  }
+  if (nc >= 9) {
+    pv[5] = (d.x * d.x) * d.x;
+    pv[6] = (d.x * d.x) * d.y;
+    pv[7] = (d.x * d.y) * d.y;
+    pv[8] = (d.y * d.y) * d.y;
+  }
+  return nc;
+}
+
+// R \ a: the explicit 2x2 formula, Gaussian elimination with partial
+// pivoting otherwise
+static void small_solve(int nc, double* R, double* a) {
+  if (nc == 2) {
+    const double d = R[0] * R[3] - R[2] * R[1];  // R column-major: R[k + nc*l]
+    const double b0 = a[0], b1 = a[1];
+    a[0] = (R[3] * b0 - R[2] * b1) / d;
+    a[1] = (R[0] * b1 - R[1] * b0) / d;
+    return;
+  }
+  for (int k = 0; k < nc; ++k) {
+    int piv = k;
+    for (int r = k + 1; r < nc; ++r)
+      if (std::fabs(R[r + nc * k]) > std::fabs(R[piv + nc * k])) piv = r;
+    if (piv != k) {
+      for (int c = 0; c < nc; ++c) std::swap(R[k + nc * c], R[piv + nc * c]);
+      std::swap(a[k], a[piv]);
+    }
+    for (int r = k + 1; r < nc; ++r) {
+      const double f = R[r + nc * k] / R[k + nc * k];
+      for (int c = k; c < nc; ++c) R[r + nc * c] -= f * R[k + nc * c];
+      a[r] -= f * a[k];
+    }
+  }
+  for (int k = nc - 1; k >= 0; --k) {
+    double t = a[k];
+    for (int c = k + 1; c < nc; ++c) t -= R[k + nc * c] * a[c];
+    a[k] = t / R[k + nc * k];
+  }
+}
+
+// movingls (movingls.jl:52-86) with gaussian_kernel (:22-24), for polygon i
+// and the per-polygon values f
+static void movingls(const Grid& g, const std::vector<PathNode>& path, int nc, int i, const double* f, double h,
+                     double* out) {
+  double a[9] = {0}, R[81] = {0}, pv[9];
+  const V2 px = g.x[i];
+  const double fp = f[i];
+  int64_t k1, k2;
+  if (findkey(g, px, k1, k2)) {
+    for (const auto& nd : path) {
+      if (nd.rr > h) break;
+      const int64_t c1 = k1 + nd.i1, c2 = k2 + nd.i2;
+      if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) continue;
+      for (int32_t j : g.cells[(c1 - 1) + g.n1 * (c2 - 1)]) {
+        const V2 y = px + get_arrow(g, g.x[j], px);
+        if (veq(px, y)) continue;
+        const double r = norm(px - y);
+        if (r < h) {
+          const double q = r / h;
+          const double ker = std::exp(-0.5 * (q * q)) / std::sqrt((2.0 * M_PI) * (h * h));
+          power_vector(nc, y - px, pv);
+          const double s = ker * (f[j] - fp);
+          for (int k = 0; k < nc; ++k) a[k] += s * pv[k];
+          for (int l = 0; l < nc; ++l)
+            for (int k = 0; k < nc; ++k) R[k + nc * l] += (ker * pv[k]) * pv[l];
+        }
+      }
+    }
+  }
+  small_solve(nc, R, a);
+  for (int k = 0; k < nc; ++k) out[k] = a[k];
+}
+
+int lvref_nearest_polygon(void* hdl, int m, const double* pts, int32_t* out) {
+  const Grid& g = *static_cast<Grid*>(hdl);
+  const auto path = path_upto(g, INFINITY);
+  for (int q = 0; q < m; ++q) out[q] = nearest_polygon(g, path, V2{pts[2 * q], pts[2 * q + 1]});
+  return 0;
+}
+
+// order 1, 2, 3: linear, quadratic, cubic; polys NULL: every polygon
+int lvref_movingls(void* hdl, int order, int m, const int32_t* polys, const double* f, double h, double* coeffs) {
+  const Grid& g = *static_cast<Grid*>(hdl);
+  const int nc = order == 1 ? 2 : (order == 2 ? 5 : 9);
+  const auto path = path_upto(g, h);
+  for (int q = 0; q < m; ++q) movingls(g, path, nc, polys ? polys[q] : q, f, h, coeffs + (size_t)nc * q);
+  return 0;
+}
+
+// point_value (movingls.jl:140-146): nearest polygon, linear expansion with h = grid.h
+int lvref_point_value(void* hdl, int m, const double* pts, const double* f, double* out) {
+  const Grid& g = *static_cast<Grid*>(hdl);
+  const auto pnear = path_upto(g, INFINITY);
+  const auto pls = path_upto(g, g.h);
+  for (int q = 0; q < m; ++q) {
+    const V2 x{pts[2 * q], pts[2 * q + 1]};
+    const int i = nearest_polygon(g, pnear, x);
+    if (i < 0) {
+      out[q] = NAN;
+      continue;
+    }
+    double L[2];
+    movingls(g, pls, 2, i, f, g.h, L);
+    const V2 d = x - g.x[i];
+    out[q] = f[i] + (L[0] * d.x + L[1] * d.y);
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -78,6 +78,9 @@ def lib():
             "lvref_find_pressure": (C.c_int, [vp, d, C.c_int, pd, C.c_int, d, C.c_int, C.POINTER(SolveStats)]),
             "lvref_solve": (C.c_int, [vp, pd, pd, C.c_int, d, C.c_int, C.POINTER(SolveStats)]),
             "lvref_multiphase_projection": (C.c_int, [vp, d, d, C.c_int, C.POINTER(SolveStats)]),
+            "lvref_nearest_polygon": (C.c_int, [vp, C.c_int, pd, pi32]),
+            "lvref_movingls": (C.c_int, [vp, C.c_int, C.c_int, pi32, pd, d, pd]),
+            "lvref_point_value": (C.c_int, [vp, C.c_int, pd, pd, pd]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -257,6 +260,30 @@ class OracleGrid:
         st = SolveStats()
         lib().lvref_multiphase_projection(self.h, quality_threshold, tol, itmax, C.byref(st))
         return st.iterations, st.converged
+
+
+    # post-processing (voronoigrid.jl:154-178, movingls.jl:52-146)
+    def nearest_polygon(self, pts):
+        pts = np.ascontiguousarray(np.asarray(pts, np.float64).reshape(-1, 2))
+        out = np.zeros(len(pts), np.int32)
+        lib().lvref_nearest_polygon(self.h, len(pts), _p(pts), _p(out, C.c_int32))
+        return out
+
+    def movingls(self, order, values, h, polys=None):
+        nc = {1: 2, 2: 5, 3: 9}[order]
+        f = np.ascontiguousarray(values, dtype=np.float64)
+        m = self.n if polys is None else len(polys)
+        pl = None if polys is None else np.ascontiguousarray(polys, dtype=np.int32)
+        out = np.zeros((m, nc))
+        lib().lvref_movingls(self.h, order, m, _p(pl, C.c_int32), _p(f), float(h), _p(out))
+        return out
+
+    def point_value(self, pts, values):
+        pts = np.ascontiguousarray(np.asarray(pts, np.float64).reshape(-1, 2))
+        f = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.zeros(len(pts))
+        lib().lvref_point_value(self.h, len(pts), _p(pts), _p(f), _p(out))
+        return out
 
 
 def clip_polygon(px, y, label, edges, labels, cap=64):
