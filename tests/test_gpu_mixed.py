@@ -89,10 +89,11 @@ def test_mixed_ir_steps(lv, oracle, name, mk):
 
 
 @pytest.mark.parametrize("method", ["mixed_ir", "learned_pcg"])
-@pytest.mark.parametrize("mk", [lambda: W.cavity(320), lambda: W.taylor_green(320)])
+@pytest.mark.parametrize("mk", [lambda: W.cavity(420), lambda: W.taylor_green(420)])
 def test_large_system_streaming(lv, oracle, method, mk):
-    """Systems above the register-resident capacity (here 102,400 rows) use
-    the streaming kernel; the FP64 residual still meets the tolerance."""
+    """Systems above the register-resident capacity of k_fcg (152 blocks x
+    512 threads x 2 rows; here 176,400 rows) use the streaming kernel; the
+    FP64 residual still meets the tolerance."""
     flow = mk()
     g, og = _setup(lv, oracle, flow)
     L = lv._lib.load()
