@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     double v[3] = {0.0, 0.0, 0.0};
     for (int i = t0; i < n; i += stride) {
       double acc = a.adiag[i] * a.x[i];
-      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.x[a.col[k]];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * __ldcg(a.x + a.col[k]);
       const double bi = a.b[i] - bmean;
       const double ri = bi - acc;
       const double zi = a.dinv[i] * ri;
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
       for (int i = t0; i < n; i += stride) {
         const double zi = a.z[i];
         double acc = a.adiag[i] * zi;
-        for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.z[a.col[k]];
+        for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * __ldcg(a.z + a.col[k]);
         const double pi = zi + beta * a.p[i];
         const double qi = acc + beta * a.q[i];
         a.p[i] = pi;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     double v[1] = {0.0};
     for (int i = t0; i < n; i += stride) {
       double acc = a.adiag[i] * a.x[i];
-      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * a.x[a.col[k]];
+      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) acc -= a.w[k] * __ldcg(a.x + a.col[k]);
       const double ri = (a.b[i] - bmean) - acc;
       v[0] += ri * ri;
     }
@@ -310,6 +310,8 @@ struct RowRegs {
   double adg[R], dnv[R], bb[R];
 };
 
+// Values other blocks wrote during this kernel are read with __ldcg (L2, not
+// the non-coherent L1 / read-only paths).
 template <int R>
 __device__ __forceinline__ void row_apply(const RowRegs<R>& rr, const PCGArgs& a, const double* __restrict__ vg,
                                           const double (&own)[R], double (&out)[R]) {
@@ -318,8 +320,8 @@ __device__ __forceinline__ void row_apply(const RowRegs<R>& rr, const PCGArgs& a
     double acc = rr.adg[r] * own[r];
 #pragma unroll
     for (int k = 0; k < KR; ++k)
-      if (k < rr.cnt[r]) acc -= rr.ww[r][k] * vg[rr.cc[r][k]];
-    for (int k = KR; k < rr.cnt[r]; ++k) acc -= a.w[rr.beg[r] + k] * vg[a.col[rr.beg[r] + k]];
+      if (k < rr.cnt[r]) acc -= rr.ww[r][k] * __ldcg(vg + rr.cc[r][k]);
+    for (int k = KR; k < rr.cnt[r]; ++k) acc -= a.w[rr.beg[r] + k] * __ldcg(vg + a.col[rr.beg[r] + k]);
     out[r] = acc;
   }
 }
@@ -635,7 +637,7 @@ __device__ __forceinline__ float apply32_row(int i, const int* __restrict__ rowp
                                              const float* __restrict__ w32, float dg, const float* __restrict__ v) {
   const float vi = v[i];
   float acc = dg * vi;
-  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fmaf(w32[k], vi - v[col[k]], acc);
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fmaf(w32[k], vi - __ldcg(v + col[k]), acc);
   return acc;
 }
 
@@ -677,7 +679,7 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
       float t = la.gd[i] * sa.rh[i];
       for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
         const int j = a.col[k];
-        if (j < i) t = fmaf(la.gl[k], sa.rh[j], t);
+        if (j < i) t = fmaf(la.gl[k], __ldcg(sa.rh + j), t);
       }
       sa.t[i] = t;
     }
@@ -686,7 +688,7 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
       float u = la.gd[i] * sa.t[i];
       for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
         const int j = a.col[k];
-        if (j > i && la.rev[k] >= 0) u = fmaf(la.gl[la.rev[k]], sa.t[j], u);
+        if (j > i && la.rev[k] >= 0) u = fmaf(la.gl[la.rev[k]], __ldcg(sa.t + j), u);
       }
       sa.z[i] = la.dh[i] * fmaf(la.eps, sa.rh[i], u);
     }
@@ -697,7 +699,7 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
     for (int i = t0; i < n; i += stride) {
       const double xi = a.x[i];
       double acc = a.diag[i] * xi;
-      for (int e = a.rowptr[i]; e < a.rowptr[i + 1]; ++e) acc += a.w[e] * (xi - a.x[a.col[e]]);
+      for (int e = a.rowptr[i]; e < a.rowptr[i + 1]; ++e) acc += a.w[e] * (xi - __ldcg(a.x + a.col[e]));
       const double bi = a.b[i] - bmean;
       const double ri = bi - acc;
       sa.r64[i] = ri;
