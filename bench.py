@@ -232,11 +232,13 @@ def run_ours(args, world, rank, local):
     train_steps = args.train_steps if (args.solver == "learned_pcg" or not args.no_compare) else 0
     losses = np.zeros(max(train_steps, 1), np.float32)
     assert L.lv_learn_init(g._ctx, 1234) == 0
+    assert L.lv_learn_set_pattern(g._ctx, args.learn_hops) == 0
     if train_steps:
         assert L.lv_learn_train(g._ctx, train_steps, args.train_lr, args.train_probes, 99,
                                 losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
     train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps,
                   "objective": "fsai-kaporin" if args.train_probes == 0 else f"hutchinson x{args.train_probes}",
+                  "pattern": "lower triangle" if args.learn_hops == 1 else "lower triangle + two-hop",
                   "lr": args.train_lr,
                   "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
                   "loss_last": float(losses[-10:].mean())}
@@ -502,6 +504,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=400, help="Adam steps of the learned preconditioner")
     ap.add_argument("--train-probes", type=int, default=0, help="0: FSAI/Kaporin objective; K: Hutchinson, K probes")
     ap.add_argument("--train-lr", type=float, default=5e-3)
+    ap.add_argument("--learn-hops", type=int, default=1, choices=[1, 2],
+                    help="pattern of the learned factor: 1 the operator's lower triangle, 2 with two-hop neighbours")
     args = ap.parse_args()
     set_size(args.nx)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

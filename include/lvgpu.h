@@ -214,6 +214,16 @@ int lv_learn_train(lv_ctx* ctx, int32_t steps, float lr, int32_t probes, uint64_
  * probes[K][n] or Rademacher probes from seed; grad[num_params] may be NULL. */
 int lv_learn_loss_grad(lv_ctx* ctx, int32_t sys, const float* probes, int32_t K, uint64_t seed, double* loss,
                        float* grad);
+/* Pattern of the learned factor: hops = 1, the operator's lower triangle (the
+ * default); hops = 2, also the lower neighbours at distance two (their entries
+ * Gt_ij = pw_ij sum ro2 H_i H_j with the path weight pw_ij).  The two-hop
+ * pattern trains with the FSAI objective only (probes = 0). */
+int lv_learn_set_pattern(lv_ctx* ctx, int32_t hops);
+int32_t lv_learn_get_pattern(lv_ctx* ctx);
+/* Two-hop part of the factor of the assembled operator: rowptr2[n+1],
+ * col2[nnz2] (both triangles) and g2[nnz2] (lower entries, zero elsewhere);
+ * with NULL arrays only *nnz2 is returned. */
+int lv_learn_factor2(lv_ctx* ctx, int64_t* nnz2, int64_t* rowptr2, int32_t* col2, float* g2);
 /* Factor of the assembled operator: gdiag[n], glower[nnz] (CSR positions with
  * col < row, zero elsewhere) and the node features[n][16]; any may be NULL. */
 int lv_learn_factor(lv_ctx* ctx, float* gdiag, float* glower, float* features);

@@ -74,6 +74,9 @@ SIGNATURES = {
     "lv_solve": (C.c_int, [_vp, _pd, _pd, _pst]),
     "lv_operator_apply": (C.c_int, [_vp, _pd, _pd]),
     "lv_multiphase_projection": (C.c_int, [_vp, _d, _pst]),
+    "lv_learn_set_pattern": (C.c_int, [_vp, _i32]),
+    "lv_learn_get_pattern": (C.c_int32, [_vp]),
+    "lv_learn_factor2": (C.c_int, [_vp, _pi64, _pi64, _pi32, C.POINTER(C.c_float)]),
     "lv_nearest_polygon": (C.c_int, [_vp, _i32, _pd, _pi32]),
     "lv_movingls": (C.c_int, [_vp, _i32, _i32, _pi32, _pd, _d, _pd]),
     "lv_point_value": (C.c_int, [_vp, _i32, _pd, _pd, _pd]),

@@ -25,7 +25,7 @@ constexpr int FCG_TPB = 512;
 constexpr int FCG_NW = FCG_TPB / 32;
 constexpr int FKR = 8;    // operator entries per row held in registers
 constexpr int FKM = 12;   // preconditioner off-diagonal entries per row held in registers
-constexpr int MMAX = 64;  // preconditioner off-diagonal entries per row (storage slots)
+constexpr int MMAX = 96;  // preconditioner off-diagonal entries per row (storage slots)
 constexpr long long FCG_SPIN_LIMIT = 4000000000LL;  // cycles (about 2 s)
 constexpr float FCG_UPDATE_DROP = 1e-5f;  // FP32 residual reduction per refinement step
 constexpr int FCG_MAX_UPDATES = 200;
@@ -447,11 +447,16 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   }
 }
 
-// M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2 on the two-hop pattern, one thread
-// per row i: (Gt^T Gt)_ij = sum_k Gt_ki Gt_kj over k in {i} and the upper
-// neighbours of i, j over {k} and the lower neighbours of k.
+// M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2, one thread per row i:
+// (Gt^T Gt)_ij = sum_k Gt_ki Gt_kj over k in {i} and the rows whose pattern
+// holds i (the upper neighbours of i, and with the two-hop pattern its upper
+// two-hop neighbours), j over the pattern of row k (k, its lower neighbours
+// and lower two-hop neighbours).  Two hops of Gt give M^-1 two (one-hop
+// pattern) or four (two-hop pattern) hops.
 __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                              const float* __restrict__ gd, const float* __restrict__ gl, const int* __restrict__ rev,
+                             const int* __restrict__ rowptr2, const int* __restrict__ col2,
+                             const float* __restrict__ gl2, const int* __restrict__ rev2,
                              const float* __restrict__ dh, float eps, int stride, int* mcnt, int* mcol, float* mval,
                              float* mdiag, int* ok) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -479,23 +484,25 @@ __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* _
       overflow = true;
     }
   };
-  const int b0 = rowptr[i], b1 = rowptr[i + 1];
-  // k = i: Gt_ii and row i of Gt (j < i)
-  {
-    const float gii = gd[i];
-    add(i, gii * gii);
-    for (int kk = b0; kk < b1; ++kk)
-      if (col[kk] < i) add(col[kk], gii * gl[kk]);
-  }
-  // k = upper neighbour u of i: Gt_ui = gl[rev[kk]]
-  for (int kk = b0; kk < b1; ++kk) {
+  // row k of Gt times Gt_ki
+  auto row_k = [&](int k, float gki) {
+    add(k, gki * gd[k]);
+    for (int k2 = rowptr[k]; k2 < rowptr[k + 1]; ++k2)
+      if (col[k2] < k) add(col[k2], gki * gl[k2]);
+    if (rowptr2)
+      for (int e = rowptr2[k]; e < rowptr2[k + 1]; ++e)
+        if (col2[e] < k) add(col2[e], gki * gl2[e]);
+  };
+  row_k(i, gd[i]);
+  for (int kk = rowptr[i]; kk < rowptr[i + 1]; ++kk) {
     const int u = col[kk];
-    if (u <= i || rev[kk] < 0) continue;
-    const float gui = gl[rev[kk]];
-    add(u, gui * gd[u]);
-    for (int k2 = rowptr[u]; k2 < rowptr[u + 1]; ++k2)
-      if (col[k2] < u) add(col[k2], gui * gl[k2]);
+    if (u > i && rev[kk] >= 0) row_k(u, gl[rev[kk]]);
   }
+  if (rowptr2)
+    for (int e = rowptr2[i]; e < rowptr2[i + 1]; ++e) {
+      const int u = col2[e];
+      if (u > i && rev2[e] >= 0) row_k(u, gl2[rev2[e]]);
+    }
   const float di = dh[i];
   for (int s = 0; s < m; ++s) {
     mcol[(size_t)s * stride + i] = cols[s];
@@ -574,15 +581,16 @@ int lv_fcg_build_minv(lv_ctx* c) {
   const int n = c->n;
   if (n > lv_fcg_capacity(c)) return LV_OK;  // the streaming solver applies the factor itself
   if (int rc = ensure_minv(c)) return rc;
-  const float *gd, *gl, *dh;
-  const int* rev;
+  const float *gd, *gl, *dh, *gl2;
+  const int *rev, *rowptr2, *col2, *rev2;
   lv_learn_factor_ptrs(c, &gd, &gl, &dh, &rev);
+  lv_learn_factor2_ptrs(c, &rowptr2, &col2, &gl2, &rev2);
   if (!gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
   const int one = 1;
   cudaMemcpyAsync(c->sv.mok, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-  k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, dh, c->learn_eps,
-                                                          c->sv.mrows, c->sv.mcnt, c->sv.mcol, c->sv.mval,
-                                                          c->sv.mdiag, c->sv.mok);
+  k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, rowptr2, col2, gl2,
+                                                          rev2, dh, c->learn_eps, c->sv.mrows, c->sv.mcnt,
+                                                          c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok);
   LV_LAUNCH_CHECK(c, "k_build_minv");
   return LV_OK;
 }

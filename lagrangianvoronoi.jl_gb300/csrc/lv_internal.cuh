@@ -190,6 +190,8 @@ int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
 // ---- learned preconditioner (lv_learn.cu)
 int lv_learn_factor_current(lv_ctx* c);
 void lv_learn_factor_ptrs(lv_ctx* c, const float** gd, const float** gl, const float** dh, const int** rev);
+// two-hop part of the factor (all NULL with the one-hop pattern)
+void lv_learn_factor2_ptrs(lv_ctx* c, const int** rowptr2, const int** col2, const float** gl2, const int** rev2);
 void lv_learn_free(lv_ctx* c);
 
 // ---- solver (lv_solver.cu)

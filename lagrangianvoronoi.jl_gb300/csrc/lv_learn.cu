@@ -12,6 +12,9 @@
 //   H3    = H2 + relu([H2, Agg H2] W2 + b2)        (3 layers, hidden width 32)
 //   Gt_ii = 1 + H3_i . rd
 //   Gt_ij = what_ij sum_c ro_c H3_ic H3_jc          for j < i, j ~ i
+//   Gt_ij = pw_ij sum_c ro2_c H3_ic H3_jc           for j < i at distance two
+//                                                   (two-hop pattern, optional)
+// with the path weight pw_ij = sum_k what_ik what_kj over common neighbours.
 //
 // The matrix products of the layers (forward [N x 32|64] x [32|64 x 32],
 // backward dX = dZ W^T and dW = X^T dZ) run on the tensor cores as
@@ -47,7 +50,9 @@ constexpr int OFF_W2 = OFF_B1 + HID;
 constexpr int OFF_B2 = OFF_W2 + KC * HID;
 constexpr int OFF_RD = OFF_B2 + HID;
 constexpr int OFF_RO = OFF_RD + HID;
-constexpr int NPARAM = OFF_RO + HID;
+constexpr int OFF_RO2 = OFF_RO + HID;  // readout of the two-hop entries
+constexpr int NPARAM = OFF_RO2 + HID;
+constexpr int Q2MAX = 40;  // two-hop (not one-hop) neighbours kept per row
 constexpr int WBF_W0 = 0, WBF_W1 = KC0 * HID, WBF_W2 = KC0 * HID + KC * HID, NWBF = KC0 * HID + 2 * KC * HID;
 constexpr int LTPB = 128;  // 4 warps, 16 rows each per tile
 constexpr int MAXPROBES = 8;
@@ -116,6 +121,83 @@ __global__ void k_lprep(int n, const int* __restrict__ rowptr, const int* __rest
   x[7] = ml;
 #pragma unroll
   for (int f = 8; f < FIN; ++f) x[f] = 0.f;
+}
+
+// Two-hop pattern Q (j at distance exactly two from i, both triangles) as a
+// CSR with the path weights pw_ij = sum_k what_ik what_kj and the transposed
+// positions rev2; neighbours of neighbours in CSR order, at most Q2MAX per row.
+__device__ int hop2_collect(int i, const int* __restrict__ rowptr, const int* __restrict__ col,
+                            const float* __restrict__ what, int* qj, float* qw, int* overflow) {
+  const int a = rowptr[i], b = rowptr[i + 1];
+  int m = 0;
+  for (int k1 = a; k1 < b; ++k1) {
+    const int k = col[k1];
+    const float wik = what[k1];
+    for (int k2 = rowptr[k]; k2 < rowptr[k + 1]; ++k2) {
+      const int j = col[k2];
+      if (j == i) continue;
+      bool one_hop = false;
+      for (int t = a; t < b; ++t)
+        if (col[t] == j) {
+          one_hop = true;
+          break;
+        }
+      if (one_hop) continue;
+      int s = 0;
+      while (s < m && qj[s] != j) ++s;
+      if (s < m) {
+        qw[s] = fmaf(wik, what[k2], qw[s]);
+      } else if (m < Q2MAX) {
+        qj[m] = j;
+        qw[m] = wik * what[k2];
+        ++m;
+      } else {
+        *overflow = 1;
+      }
+    }
+  }
+  return m;
+}
+
+__global__ void k_hop2_count(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const float* __restrict__ what, int* cnt, int* overflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int qj[Q2MAX];
+  float qw[Q2MAX];
+  int ov = 0;
+  cnt[i] = hop2_collect(i, rowptr, col, what, qj, qw, &ov);
+  if (ov) atomicOr(overflow, 1);
+}
+
+__global__ void k_hop2_fill(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                            const float* __restrict__ what, const int* __restrict__ rowptr2, int* col2, float* pw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int qj[Q2MAX];
+  float qw[Q2MAX];
+  int ov = 0;
+  const int m = hop2_collect(i, rowptr, col, what, qj, qw, &ov);
+  const int o = rowptr2[i];
+  for (int s = 0; s < m; ++s) {
+    col2[o + s] = qj[s];
+    pw[o + s] = qw[s];
+  }
+}
+
+__global__ void k_hop2_rev(int n, const int* __restrict__ rowptr2, const int* __restrict__ col2, int* rev2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int e = rowptr2[i]; e < rowptr2[i + 1]; ++e) {
+    const int j = col2[e];
+    int r = -1;
+    for (int t = rowptr2[j]; t < rowptr2[j + 1]; ++t)
+      if (col2[t] == i) {
+        r = t;
+        break;
+      }
+    rev2[e] = r;
+  }
 }
 
 // ---------------------------------------------------------------- forward
@@ -258,6 +340,38 @@ __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __re
   }
 }
 
+// two-hop readout: gl2_e = pw_e sum_c ro2_c H_ic H_jc (j = col2_e < i), four lanes per row
+__global__ void k_readout2(int n, const int* __restrict__ rowptr2, const int* __restrict__ col2,
+                           const float* __restrict__ pw, const float* __restrict__ H,
+                           const float* __restrict__ params, float* gl2) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / RO_LANES, q = gt % RO_LANES;
+  const bool on = i < n;
+  const float* ro2 = params + OFF_RO2 + q * RO_F;
+  float hro[RO_F];
+#pragma unroll
+  for (int c = 0; c < RO_F; ++c) hro[c] = 0.f;
+  if (on) {
+    const float* hi = H + (size_t)i * HID + q * RO_F;
+#pragma unroll
+    for (int c = 0; c < RO_F; ++c) hro[c] = hi[c] * ro2[c];
+  }
+  const int a = on ? rowptr2[i] : 0, b = on ? rowptr2[i + 1] : 0;
+  const unsigned gmask = 0xFu << ((threadIdx.x & 31) & ~(RO_LANES - 1));
+  for (int e = a; e < b; ++e) {
+    const int j = col2[e];
+    float v = 0.f;
+    if (j < i) {
+      const float* hj = H + (size_t)j * HID + q * RO_F;
+#pragma unroll
+      for (int c = 0; c < RO_F; ++c) v = fmaf(hro[c], hj[c], v);
+    }
+    v += __shfl_xor_sync(gmask, v, 1);
+    v += __shfl_xor_sync(gmask, v, 2);
+    if (q == 0) gl2[e] = (j < i) ? v * pw[e] : 0.f;
+  }
+}
+
 // ---------------------------------------------------------------- loss
 
 __device__ __forceinline__ float probe_value(unsigned long long seed, int p, int i) {
@@ -373,39 +487,51 @@ __global__ void k_gradG(int n, int K, const int* __restrict__ rowptr, const int*
 // whose minimiser on the pattern is the FSAI factor (each row solves
 // At[S,S] g = e_i / g_ii).  tv_j = (Gt At)_ij = g_j - sum_{m in S, m ~ j}
 // g_m what(m, j) for j in S; dL/dGt_ij = (2 tv_j - [j = i] 2 / Gt_ii) / n.
-constexpr int KMAX = LV_MAX_EDGES + 1;
+constexpr int KMAX = 1 + LV_MAX_EDGES + Q2MAX;
 __global__ void k_kaporin(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                          const int* __restrict__ rev, const float* __restrict__ what, const float* __restrict__ gd,
-                          const float* __restrict__ gl, float scale, float* dgd, float* dgl, double* part) {
+                          const float* __restrict__ what, const float* __restrict__ gd, const float* __restrict__ gl,
+                          const int* __restrict__ rowptr2, const int* __restrict__ col2,
+                          const float* __restrict__ gl2, float scale, float* dgd, float* dgl, float* dgl2,
+                          double* part) {
   __shared__ double sh[32];
   double lsum = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int a = rowptr[i], b = rowptr[i + 1];
-    int mem[KMAX], pos[KMAX];  // member rows and their CSR position in row i (-1: i itself)
+    // members of row i's pattern: i, its lower neighbours (kind 1) and its
+    // lower two-hop neighbours (kind 2), with their entry positions
+    int mem[KMAX], pos[KMAX], kind[KMAX];
     float g[KMAX], tv[KMAX];
     int S = 0;
     mem[S] = i;
     pos[S] = -1;
+    kind[S] = 0;
     g[S] = gd[i];
     ++S;
     for (int k = a; k < b && S < KMAX; ++k)
       if (col[k] < i) {
         mem[S] = col[k];
         pos[S] = k;
+        kind[S] = 1;
         g[S] = gl[k];
         ++S;
       }
+    if (rowptr2)
+      for (int e = rowptr2[i]; e < rowptr2[i + 1] && S < KMAX; ++e)
+        if (col2[e] < i) {
+          mem[S] = col2[e];
+          pos[S] = e;
+          kind[S] = 2;
+          g[S] = gl2[e];
+          ++S;
+        }
     for (int p = 0; p < S; ++p) tv[p] = g[p];
-    // contributions of m = i: At_(i, j) = -what at row i's entry of j
-    for (int p = 1; p < S; ++p) tv[p] = fmaf(-g[0], what[pos[p]], tv[p]);
-    // m = a lower neighbour: At_(m, i) through rev, At_(m, j) by a search of row m
-    for (int q = 1; q < S; ++q) {
+    // tv_p -= g_q what(m_q -> m_p) for every member q and neighbour m_p of m_q
+    for (int q = 0; q < S; ++q) {
       const int m = mem[q];
-      if (rev[pos[q]] >= 0) tv[0] = fmaf(-g[q], what[rev[pos[q]]], tv[0]);
       for (int t = rowptr[m]; t < rowptr[m + 1]; ++t) {
         const int j = col[t];
-        if (j >= i) continue;
-        for (int p = 1; p < S; ++p)
+        if (j > i) continue;  // members are <= i
+        for (int p = 0; p < S; ++p)
           if (mem[p] == j) {
             tv[p] = fmaf(-g[q], what[t], tv[p]);
             break;
@@ -418,7 +544,12 @@ __global__ void k_kaporin(int n, const int* __restrict__ rowptr, const int* __re
     lsum += (double)li;
     dgd[i] = scale * (2.f * tv[0] - 2.f / gii);
     for (int k = a; k < b; ++k) dgl[k] = 0.f;
-    for (int p = 1; p < S; ++p) dgl[pos[p]] = scale * 2.f * tv[p];
+    if (rowptr2)
+      for (int e = rowptr2[i]; e < rowptr2[i + 1]; ++e) dgl2[e] = 0.f;
+    for (int p = 1; p < S; ++p) {
+      if (kind[p] == 1) dgl[pos[p]] = scale * 2.f * tv[p];
+      else dgl2[pos[p]] = scale * 2.f * tv[p];
+    }
   }
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = lsum;
@@ -432,16 +563,19 @@ __global__ void k_kaporin(int n, const int* __restrict__ rowptr, const int* __re
 
 // ---------------------------------------------------------------- backward
 
-// dH_i from the readout; block partials of d rd (32) and d ro (32)
+// dH_i from the readout; block partials of d rd, d ro and d ro2 (32 each)
 __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                               const int* __restrict__ rev, const float* __restrict__ what, const float* __restrict__ H,
                               const float* __restrict__ params, const float* __restrict__ dgd,
-                              const float* __restrict__ dgl, float* dH, float* part) {
+                              const float* __restrict__ dgl, const int* __restrict__ rowptr2,
+                              const int* __restrict__ col2, const int* __restrict__ rev2,
+                              const float* __restrict__ pw, const float* __restrict__ dgl2, float* dH, float* part) {
   const float* rd = params + OFF_RD;
   const float* ro = params + OFF_RO;
-  float prd[HID], pro[HID];
+  const float* ro2 = params + OFF_RO2;
+  float prd[HID], pro[HID], pro2[HID];
 #pragma unroll
-  for (int c = 0; c < HID; ++c) prd[c] = pro[c] = 0.f;
+  for (int c = 0; c < HID; ++c) prd[c] = pro[c] = pro2[c] = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float* hi = H + (size_t)i * HID;
     float dh[HID];
@@ -467,6 +601,22 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
 #pragma unroll
       for (int c = 0; c < HID; ++c) dh[c] = fmaf(coef * ro[c], hj[c], dh[c]);
     }
+    if (rowptr2)
+      for (int e = rowptr2[i]; e < rowptr2[i + 1]; ++e) {
+        const int j = col2[e];
+        float coef;
+        const float* hj = H + (size_t)j * HID;
+        if (j < i) {
+          coef = dgl2[e] * pw[e];
+#pragma unroll
+          for (int c = 0; c < HID; ++c) pro2[c] = fmaf(coef * hi[c], hj[c], pro2[c]);
+        } else {
+          const int re = rev2[e];
+          coef = re >= 0 ? dgl2[re] * pw[re] : 0.f;
+        }
+#pragma unroll
+        for (int c = 0; c < HID; ++c) dh[c] = fmaf(coef * ro2[c], hj[c], dh[c]);
+      }
     float* o = dH + (size_t)i * HID;
 #pragma unroll
     for (int c = 0; c < HID; ++c) o[c] = dh[c];
@@ -474,25 +624,28 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
   // block reduction in a fixed order: warp shuffles, then warps in order
 #pragma unroll
   for (int c = 0; c < HID; ++c) {
-    float a = prd[c], b = pro[c];
+    float a = prd[c], b = pro[c], d = pro2[c];
     for (int off = 16; off > 0; off >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, off);
       b += __shfl_down_sync(0xffffffffu, b, off);
+      d += __shfl_down_sync(0xffffffffu, d, off);
     }
     prd[c] = a;
     pro[c] = b;
+    pro2[c] = d;
   }
-  __shared__ float swarp[8][2 * HID];
+  __shared__ float swarp[8][3 * HID];
   if ((threadIdx.x & 31) == 0)
     for (int c = 0; c < HID; ++c) {
       swarp[threadIdx.x >> 5][c] = prd[c];
       swarp[threadIdx.x >> 5][HID + c] = pro[c];
+      swarp[threadIdx.x >> 5][2 * HID + c] = pro2[c];
     }
   __syncthreads();
-  if (threadIdx.x < 2 * HID) {
+  if (threadIdx.x < 3 * HID) {
     float t = 0.f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += swarp[w][threadIdx.x];
-    part[(size_t)blockIdx.x * 2 * HID + threadIdx.x] = t;
+    part[(size_t)blockIdx.x * 3 * HID + threadIdx.x] = t;
   }
 }
 
@@ -708,6 +861,10 @@ struct LearnState {
   float *zp, *y, *t, *u, *r, *v, *s;
   float *partW, *partb, *partR;
   double *partL, *loss;
+  // two-hop pattern (hops == 2), built per system in prepare()
+  int hops = 1;
+  int *rowptr2 = nullptr, *col2 = nullptr, *rev2 = nullptr, *q_overflow = nullptr;
+  float *pw = nullptr, *gl2 = nullptr, *dgl2 = nullptr;
   std::vector<LearnSystem> systems;
   std::vector<void*> allocs;
   bool factor_ready = false;
@@ -762,7 +919,7 @@ int ensure_state(lv_ctx* c) {
   for (float** p : {&L->zp, &L->y, &L->t, &L->u, &L->r, &L->v, &L->s}) *p = lalloc<float>(L, cap * MAXPROBES);
   L->partW = lalloc<float>(L, (size_t)PART_BLOCKS * KC * HID);
   L->partb = lalloc<float>(L, (size_t)PART_BLOCKS * HID);
-  L->partR = lalloc<float>(L, (size_t)PART_BLOCKS * 2 * HID);
+  L->partR = lalloc<float>(L, (size_t)PART_BLOCKS * 3 * HID);
   L->partL = lalloc<double>(L, PART_BLOCKS);
   L->loss = lalloc<double>(L, 4);
   bool ok = L->params && L->loss && L->partR && L->s;
@@ -772,6 +929,21 @@ int ensure_state(lv_ctx* c) {
     return lv_fail(c, LV_ERR_CUDA, "learned preconditioner: out of device memory");
   }
   c->learn = L;
+  return LV_OK;
+}
+
+int ensure_hop2(lv_ctx* c) {
+  LearnState* L = c->learn;
+  if (L->rowptr2) return LV_OK;
+  const size_t cap = L->cap, q = (size_t)Q2MAX * L->cap;
+  L->rowptr2 = lalloc<int>(L, cap + 1);
+  L->col2 = lalloc<int>(L, q);
+  L->rev2 = lalloc<int>(L, q);
+  L->q_overflow = lalloc<int>(L, 1);
+  L->pw = lalloc<float>(L, q);
+  L->gl2 = lalloc<float>(L, q);
+  L->dgl2 = lalloc<float>(L, q);
+  if (!L->dgl2) return lv_fail(c, LV_ERR_CUDA, "learned preconditioner: out of device memory (two-hop pattern)");
   return LV_OK;
 }
 
@@ -787,6 +959,7 @@ void init_params(LearnState* L, unsigned long long seed, cudaStream_t s) {
   fill(OFF_W2, KC, KC * HID, 0.5f);
   fill(OFF_RD, HID, HID, 0.01f);
   fill(OFF_RO, HID, HID, 0.01f);
+  fill(OFF_RO2, HID, HID, 0.01f);
   cudaMemcpyAsync(L->params, p.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(L->m1, 0, sizeof(float) * NPARAM, s);
   cudaMemsetAsync(L->m2, 0, sizeof(float) * NPARAM, s);
@@ -804,6 +977,15 @@ int prepare(lv_ctx* c, const LearnSystem& S) {
   k_lprep_dh<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.adiag, L->dh);
   k_lprep<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, S.w, S.diag, S.adiag, L->dh, L->what, L->rev, L->X);
   c->launches += 2;
+  if (L->hops == 2) {
+    if (int rc = ensure_hop2(c)) return rc;
+    int* cnt = reinterpret_cast<int*>(L->dgl2);  // scratch for the counts
+    k_hop2_count<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, cnt, L->q_overflow);
+    if (int rc = lv_scan_int(c, cnt, L->rowptr2, S.n)) return rc;
+    k_hop2_fill<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->rowptr2, L->col2, L->pw);
+    k_hop2_rev<<<lv_blocks(S.n, TPB), TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->rev2);
+    c->launches += 3;
+  }
   return lv_cuda_check(c, cudaGetLastError(), "learned: prepare");
 }
 
@@ -820,6 +1002,11 @@ int forward(lv_ctx* c, const LearnSystem& S) {
                                          L->Z2, L->H3);
   k_readout<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd,
                                                            L->gl);
+  if (L->hops == 2) {
+    k_readout2<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, L->H3, L->params,
+                                                              L->gl2);
+    c->launches++;
+  }
   c->launches += 5;
   return lv_cuda_check(c, cudaGetLastError(), "learned: forward");
 }
@@ -832,8 +1019,10 @@ int loss_grad_G(lv_ctx* c, const LearnSystem& S, int K) {
   const int n = S.n, b = lv_blocks(n, TPB);
   if (K == 0) {
     const int nbl = std::min(PART_BLOCKS, b);
-    k_kaporin<<<nbl, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->gd, L->gl, 1.0f / (float)n, L->dgd, L->dgl,
-                                  L->partL);
+    const bool h2 = L->hops == 2;
+    k_kaporin<<<nbl, TPB, 0, s>>>(n, S.rowptr, S.col, L->what, L->gd, L->gl, h2 ? L->rowptr2 : nullptr,
+                                  h2 ? L->col2 : nullptr, h2 ? L->gl2 : nullptr, 1.0f / (float)n, L->dgd, L->dgl,
+                                  h2 ? L->dgl2 : nullptr, L->partL);
     k_sum_loss<<<1, 32, 0, s>>>(L->partL, nbl, 1.0 / (double)n, L->loss);
     c->launches += 2;
     return lv_cuda_check(c, cudaGetLastError(), "learned: Kaporin loss");
@@ -856,9 +1045,11 @@ int backward(lv_ctx* c, const LearnSystem& S) {
   cudaStream_t s = c->stream;
   const int n = S.n;
   const int nbr = std::min(PART_BLOCKS, lv_blocks(n, TPB));
-  k_readout_bwd<<<nbr, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->H3, L->params, L->dgd, L->dgl, L->dH3,
-                                    L->partR);
-  k_sum_parts<<<1, 64, 0, s>>>(L->partR, nbr, 2 * HID, L->grad + OFF_RD);
+  const bool h2 = L->hops == 2;
+  k_readout_bwd<<<nbr, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->H3, L->params, L->dgd, L->dgl,
+                                    h2 ? L->rowptr2 : nullptr, h2 ? L->col2 : nullptr, h2 ? L->rev2 : nullptr,
+                                    h2 ? L->pw : nullptr, h2 ? L->dgl2 : nullptr, L->dH3, L->partR);
+  k_sum_parts<<<1, 3 * HID, 0, s>>>(L->partR, nbr, 3 * HID, L->grad + OFF_RD);
   const int nb = launch_blocks_tiles(n);
   // layer 2: Hin = H2, dHout = dH3
   k_layer_bwd<HID><<<nb, LTPB, 0, s>>>(n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->Z2, L->dH3, L->dHdir,
@@ -926,6 +1117,15 @@ void lv_learn_factor_ptrs(lv_ctx* c, const float** gd, const float** gl, const f
   *gl = L ? L->gl : nullptr;
   *dh = L ? L->dh : nullptr;
   *rev = L ? L->rev : nullptr;
+}
+
+void lv_learn_factor2_ptrs(lv_ctx* c, const int** rowptr2, const int** col2, const float** gl2, const int** rev2) {
+  LearnState* L = c->learn;
+  const bool h2 = L && L->hops == 2 && L->rowptr2;
+  *rowptr2 = h2 ? L->rowptr2 : nullptr;
+  *col2 = h2 ? L->col2 : nullptr;
+  *gl2 = h2 ? L->gl2 : nullptr;
+  *rev2 = h2 ? L->rev2 : nullptr;
 }
 
 extern "C" {
@@ -1007,6 +1207,8 @@ int lv_learn_loss_grad(lv_ctx* c, int32_t sys, const float* probes, int32_t K, u
   if (!c || K < 0 || K > MAXPROBES) return LV_ERR_BAD_ARGUMENT;
   if (int rc = ensure_state(c)) return rc;
   LearnState* L = c->learn;
+  if (K > 0 && L->hops == 2)
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "the Hutchinson objective supports the one-hop pattern only");
   LearnSystem S;
   if (sys < 0) {
     if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
@@ -1035,6 +1237,8 @@ int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed,
   if (!c || steps < 0 || K < 0 || K > MAXPROBES || !(lr > 0)) return LV_ERR_BAD_ARGUMENT;
   if (int rc = ensure_state(c)) return rc;
   LearnState* L = c->learn;
+  if (K > 0 && L->hops == 2)
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "the Hutchinson objective supports the one-hop pattern only");
   if (L->systems.empty()) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "no training systems (lv_learn_add_system)");
   cudaStream_t s = c->stream;
   std::vector<double> hl(steps > 0 ? steps : 1);
@@ -1062,6 +1266,41 @@ int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed,
   }
   L->factor_ready = true;
   return lv_cuda_check(c, cudaStreamSynchronize(s), "lv_learn_train");
+}
+
+// Pattern of the learned factor: 1 = the operator's lower triangle, 2 = also
+// the lower two-hop neighbours.
+int lv_learn_set_pattern(lv_ctx* c, int32_t hops) {
+  if (!c || (hops != 1 && hops != 2)) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = ensure_state(c)) return rc;
+  c->learn->hops = hops;
+  c->factor_valid = false;
+  if (hops == 2) return ensure_hop2(c);
+  return LV_OK;
+}
+
+int32_t lv_learn_get_pattern(lv_ctx* c) { return (c && c->learn) ? c->learn->hops : 1; }
+
+// The two-hop part of the current factor: the two-hop pattern as a CSR
+// (rowptr2[n+1], col2[nnz2]) and its values g2[nnz2] (lower entries, zero
+// elsewhere); with NULL arrays only *nnz2 is returned.
+int lv_learn_factor2(lv_ctx* c, int64_t* nnz2, int64_t* rowptr2, int32_t* col2, float* g2) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
+  if (int rc = ensure_state(c)) return rc;
+  LearnState* L = c->learn;
+  if (L->hops != 2) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "the factor has the one-hop pattern");
+  if (int rc = lv_learn_factor_current(c)) return rc;
+  const int n = c->n;
+  std::vector<int> rp(n + 1);
+  cudaMemcpyAsync(rp.data(), L->rowptr2, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
+  if (nnz2) *nnz2 = rp[n];
+  if (rowptr2)
+    for (int i = 0; i <= n; ++i) rowptr2[i] = rp[i];
+  if (col2) cudaMemcpyAsync(col2, L->col2, sizeof(int) * rp[n], cudaMemcpyDeviceToHost, c->stream);
+  if (g2) cudaMemcpyAsync(g2, L->gl2, sizeof(float) * rp[n], cudaMemcpyDeviceToHost, c->stream);
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_factor2");
 }
 
 // The factor Gt of the current operator: gdiag[n] and glower[nnz] (entries of

@@ -609,6 +609,10 @@ struct LearnArgs {
   const float* gl;
   const float* dh;
   const int* rev;
+  const int* rowptr2;  // two-hop part of the factor (NULL with the one-hop pattern)
+  const int* col2;
+  const float* gl2;
+  const int* rev2;
   float eps;
   float* rhat;  // exchange buffers
   float* tbuf;
@@ -681,6 +685,11 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
         const int j = a.col[k];
         if (j < i) t = fmaf(la.gl[k], __ldcg(sa.rh + j), t);
       }
+      if (la.rowptr2)
+        for (int e = la.rowptr2[i]; e < la.rowptr2[i + 1]; ++e) {
+          const int j = la.col2[e];
+          if (j < i) t = fmaf(la.gl2[e], __ldcg(sa.rh + j), t);
+        }
       sa.t[i] = t;
     }
     if (!grid_barrier(a.bar, a.status)) return false;
@@ -690,6 +699,11 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
         const int j = a.col[k];
         if (j > i && la.rev[k] >= 0) u = fmaf(la.gl[la.rev[k]], __ldcg(sa.t + j), u);
       }
+      if (la.rowptr2)
+        for (int e = la.rowptr2[i]; e < la.rowptr2[i + 1]; ++e) {
+          const int j = la.col2[e];
+          if (j > i && la.rev2[e] >= 0) u = fmaf(la.gl2[la.rev2[e]], __ldcg(sa.t + j), u);
+        }
       sa.z[i] = la.dh[i] * fmaf(la.eps, sa.rh[i], u);
     }
     return true;
@@ -941,10 +955,11 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
       LearnArgs la;
       if (learned) {
         lv_learn_factor_ptrs(c, &la.gd, &la.gl, &la.dh, &la.rev);
+        lv_learn_factor2_ptrs(c, &la.rowptr2, &la.col2, &la.gl2, &la.rev2);
         if (!la.gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
       } else {
-        la.gd = la.gl = la.dh = nullptr;
-        la.rev = nullptr;
+        la.gd = la.gl = la.dh = la.gl2 = nullptr;
+        la.rev = la.rowptr2 = la.col2 = la.rev2 = nullptr;
       }
       la.eps = c->learn_eps;
       la.rhat = la.tbuf = la.zbuf = nullptr;

@@ -14,7 +14,7 @@ KC0, KC = 2 * FIN, 2 * HID
 OFF = {}
 _o = 0
 for name, size in (("W0", KC0 * HID), ("b0", HID), ("W1", KC * HID), ("b1", HID), ("W2", KC * HID), ("b2", HID),
-                   ("rd", HID), ("ro", HID)):
+                   ("rd", HID), ("ro", HID), ("ro2", HID)):
     OFF[name] = (_o, size)
     _o += size
 NPARAM = _o
@@ -34,7 +34,42 @@ def unpack(p):
     return out
 
 
-def prepare(rowptr, col, w, diag, adiag):
+def hop2(rowptr, col, what):
+    """The two-hop pattern (j at distance exactly two, both triangles) in the
+    GPU's enumeration order, with path weights pw_ij = sum_k what_ik what_kj
+    (FP32 products, FP32 fused accumulation) and transposed positions."""
+    n = len(rowptr) - 1
+    rows, cols, pws = [], [], []
+    rp = [0]
+    for i in range(n):
+        a, b = rowptr[i], rowptr[i + 1]
+        nb1 = set(int(c) for c in col[a:b])
+        qj, qw = [], []
+        for k1 in range(a, b):
+            k = int(col[k1])
+            for k2 in range(rowptr[k], rowptr[k + 1]):
+                j = int(col[k2])
+                if j == i or j in nb1:
+                    continue
+                prod = np.float64(what[k1]) * np.float64(what[k2])
+                if j in qj:
+                    s_ = qj.index(j)
+                    qw[s_] = np.float32(prod + np.float64(qw[s_]))
+                else:
+                    qj.append(j)
+                    qw.append(np.float32(prod))
+        rows += [i] * len(qj)
+        cols += qj
+        pws += qw
+        rp.append(len(cols))
+    rp = np.array(rp, np.int64)
+    cols = np.array(cols, np.int64)
+    pos = {(int(r), int(c)): e for e, (r, c) in enumerate(zip(rows, cols))}
+    rev = np.array([pos.get((int(c), int(r)), -1) for r, c in zip(rows, cols)], np.int64)
+    return rp, np.array(rows, np.int64), cols, np.array(pws, np.float32), rev
+
+
+def prepare(rowptr, col, w, diag, adiag, hops=1):
     """what, dh, features as the GPU computes them (FP32), as float64 tensors."""
     n = len(diag)
     ri = np.repeat(np.arange(n), np.diff(rowptr))
@@ -65,8 +100,14 @@ def prepare(rowptr, col, w, diag, adiag):
     X[:, 6] = nl * np.float32(0.125)
     X[:, 7] = ml
     T = lambda a: torch.from_numpy(np.asarray(a, np.float64))
+    nnz = len(col)
+    if hops == 2:
+        rp2, ri2, col2, pw, rev2 = hop2(rowptr, col, what)
+    else:
+        rp2, ri2, col2, pw, rev2 = (np.zeros(n + 1, np.int64), np.zeros(0, np.int64), np.zeros(0, np.int64),
+                                    np.zeros(0, np.float32), np.zeros(0, np.int64))
     # triples (entry of m, weight, entry of j) of tr(Gt What Gt^T) = sum_i sum_{m,j in S_i} Gt_im what_mj Gt_ij,
-    # entries indexed into cat([gd, gl]) (gd: 0..n-1, gl: n + CSR position)
+    # entries indexed into cat([gd, gl, gl2]) (gd: 0..n-1, gl: n + CSR position, gl2: n + nnz + two-hop position)
     tm, tw, tj = [], [], []
     pos = {}
     for i in range(n):
@@ -74,6 +115,7 @@ def prepare(rowptr, col, w, diag, adiag):
             pos[(i, int(col[k]))] = k
     for i in range(n):
         mem = [(i, i)] + [(int(col[k]), n + k) for k in range(rowptr[i], rowptr[i + 1]) if col[k] < i]
+        mem += [(int(col2[e]), n + nnz + e) for e in range(rp2[i], rp2[i + 1]) if col2[e] < i]
         for (m_, em) in mem:
             for (j_, ej) in mem:
                 if m_ != j_ and (m_, j_) in pos:
@@ -82,7 +124,8 @@ def prepare(rowptr, col, w, diag, adiag):
                     tj.append(ej)
     return dict(n=n, ri=torch.from_numpy(ri), col=torch.from_numpy(col.astype(np.int64)), what=T(what), dh=T(dh),
                 X=T(X), tm=torch.tensor(tm, dtype=torch.int64), tw=T(np.asarray(tw, np.float32)),
-                tj=torch.tensor(tj, dtype=torch.int64))
+                tj=torch.tensor(tj, dtype=torch.int64), hops=hops, rp2=rp2, ri2=torch.from_numpy(ri2),
+                col2=torch.from_numpy(col2), pw=T(pw))
 
 
 def agg(G, H):
@@ -105,6 +148,12 @@ def factor(G, params):
     lower = G["col"] < G["ri"]
     gl = G["what"] * ((H3[G["ri"]] * H3[G["col"]]) @ P["ro"])
     gl = torch.where(lower, gl, torch.zeros_like(gl))
+    if G["hops"] == 2:
+        lower2 = G["col2"] < G["ri2"]
+        gl2 = G["pw"] * ((H3[G["ri2"]] * H3[G["col2"]]) @ P["ro2"])
+        G["gl2"] = torch.where(lower2, gl2, torch.zeros_like(gl2))
+    else:
+        G["gl2"] = torch.zeros(0, dtype=torch.float64)
     return gd, gl
 
 
@@ -137,14 +186,14 @@ def loss(G, params, probes):
 def loss_kaporin(G, params):
     """(1/n) [tr(Gt At Gt^T) - 2 sum log Gt_ii], At = I - What."""
     gd, gl = factor(G, params)
-    e = torch.cat([gd, gl])
+    e = torch.cat([gd, gl, G["gl2"]])
     tr = (e * e).sum() - (e[G["tm"]] * G["tw"] * e[G["tj"]]).sum()
     return (tr - 2.0 * torch.log(gd).sum()) / G["n"]
 
 
-def loss_and_grad(rowptr, col, w, diag, adiag, params, probes):
+def loss_and_grad(rowptr, col, w, diag, adiag, params, probes, hops=1):
     """probes None: the Kaporin objective; else the Hutchinson loss."""
-    G = prepare(rowptr, col, w, diag, adiag)
+    G = prepare(rowptr, col, w, diag, adiag, hops)
     p = torch.tensor(np.asarray(params, np.float64), requires_grad=True)
     if probes is None:
         L = loss_kaporin(G, p)
@@ -156,8 +205,10 @@ def loss_and_grad(rowptr, col, w, diag, adiag, params, probes):
     return float(L.detach()), p.grad.numpy().copy()
 
 
-def forward_values(rowptr, col, w, diag, adiag, params):
-    G = prepare(rowptr, col, w, diag, adiag)
+def forward_values(rowptr, col, w, diag, adiag, params, hops=1):
+    G = prepare(rowptr, col, w, diag, adiag, hops)
     with torch.no_grad():
         gd, gl = factor(G, torch.tensor(np.asarray(params, np.float64)))
+    if hops == 2:
+        return gd.numpy(), gl.numpy(), G["X"].numpy(), (G["rp2"], G["col2"].numpy(), G["gl2"].numpy())
     return gd.numpy(), gl.numpy(), G["X"].numpy()

@@ -53,8 +53,9 @@ def _params(L, g, seed, scale=1.0):
     # make the readout non-trivial so every parameter gets a gradient
     o, s = LR.OFF["rd"]
     pr[o:o + s] *= 30.0 * scale
-    o, s = LR.OFF["ro"]
-    pr[o:o + s] *= 30.0 * scale
+    for name in ("ro", "ro2"):
+        o, s = LR.OFF[name]
+        pr[o:o + s] *= 30.0 * scale
     assert L.lv_learn_set_params(g._ctx, pr.ctypes.data_as(C.POINTER(C.c_float))) == 0
     return pr
 
@@ -122,6 +123,62 @@ def test_kaporin_gradient_matches_autograd(lv, oracle, mk):
     assert cos > 0.999, cos
 
 
+def _factor2(lv, g, L):
+    nnz2 = C.c_int64()
+    assert L.lv_learn_factor2(g._ctx, C.byref(nnz2), None, None, None) == 0
+    rp2 = np.zeros(g.n + 1, np.int64)
+    col2 = np.zeros(nnz2.value, np.int32)
+    g2 = np.zeros(nnz2.value, np.float32)
+    assert L.lv_learn_factor2(g._ctx, None, lv._lib.ptr(rp2, C.c_int64), lv._lib.ptr(col2, C.c_int32),
+                              g2.ctypes.data_as(C.POINTER(C.c_float))) == 0
+    return rp2, col2, g2
+
+
+@pytest.mark.parametrize("mk", [lambda: W.taylor_green(24), lambda: W.cavity(24)])
+def test_two_hop_forward_matches_reference(lv, oracle, mk):
+    """The two-hop pattern (enumeration order, path weights) and its readout."""
+    flow = mk()
+    g, L = _grid(lv, oracle, flow)
+    assert L.lv_learn_set_pattern(g._ctx, 2) == 0
+    pr = _params(L, g, 12)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    n, nnz = g.n, len(col)
+    gd = np.zeros(n, np.float32)
+    gl = np.zeros(nnz, np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_factor(g._ctx, fp(gd), fp(gl), None) == 0
+    rp2, col2, g2 = _factor2(lv, g, L)
+    rgd, rgl, _, (rrp2, rcol2, rg2) = LR.forward_values(rowptr, col, w, diag, adiag, pr, hops=2)
+    assert np.array_equal(rp2, rrp2) and np.array_equal(col2, rcol2)
+    assert np.max(np.abs(gd - rgd)) <= 2e-3 * max(1.0, np.max(np.abs(rgd)))
+    assert np.max(np.abs(g2 - rg2)) <= 2e-3 * max(1e-3, np.max(np.abs(rg2)))
+    assert np.max(np.abs(rg2)) > 1e-5  # the two-hop readout is exercised
+    # symmetric pattern: (i, j) present iff (j, i) is
+    rows = np.repeat(np.arange(n), np.diff(rp2))
+    assert set(zip(rows.tolist(), col2.tolist())) == set(zip(col2.tolist(), rows.tolist()))
+
+
+@pytest.mark.parametrize("mk", [lambda: W.taylor_green(24), lambda: W.cavity(24)])
+def test_two_hop_kaporin_gradient_matches_autograd(lv, oracle, mk):
+    flow = mk()
+    g, L = _grid(lv, oracle, flow)
+    assert L.lv_learn_set_pattern(g._ctx, 2) == 0
+    pr = _params(L, g, 6, scale=0.3)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    loss = C.c_double()
+    grad = np.zeros(len(pr), np.float32)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    assert L.lv_learn_loss_grad(g._ctx, -1, None, 0, 0, C.byref(loss), fp(grad)) == 0
+    rl, rg = LR.loss_and_grad(rowptr, col, w, diag, adiag, pr, None, hops=2)
+    assert abs(loss.value - rl) <= 1e-4 * max(1.0, abs(rl)), (loss.value, rl)
+    for name, (o, s) in LR.OFF.items():
+        a, b = grad[o:o + s].astype(np.float64), rg[o:o + s]
+        nb = np.linalg.norm(b)
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-6, (name, np.linalg.norm(a - b), nb)
+    # the Hutchinson objective is refused with the two-hop pattern
+    assert L.lv_learn_loss_grad(g._ctx, -1, None, 2, 1, C.byref(loss), None) != 0
+
+
 def _harvest(lv, oracle, flow, seeds):
     """A grid per seed, operator assembled and snapshot for training; returns the last grid."""
     from lvgpu import populate as pop
@@ -181,3 +238,18 @@ def test_training_lowers_loss_and_iterations(lv, oracle):
     it_l, meth = res["learned_pcg"]
     assert meth == 2, "the trained factor fell back to Jacobi"
     assert it_l < it_j, res
+    # the two-hop pattern, trained the same way, needs fewer still
+    assert L.lv_learn_set_pattern(trainer._ctx, 2) == 0
+    assert L.lv_learn_init(trainer._ctx, 7) == 0
+    assert L.lv_learn_train(trainer._ctx, steps, 3e-3, 0, 1, fp(losses)) == 0
+    assert L.lv_learn_get_params(trainer._ctx, fp(pr)) == 0
+    assert L.lv_learn_set_pattern(g._ctx, 2) == 0
+    assert L.lv_learn_set_params(g._ctx, fp(pr)) == 0
+    lv.PressureSolver(g, method="learned_pcg", tol=1e-8).configure()
+    xg = np.zeros(g.n)
+    st = lv.LvSolveStats()
+    assert L.lv_solve(g._ctx, lv._lib.ptr(b), lv._lib.ptr(xg), C.byref(st)) == 0
+    rel = np.linalg.norm(b - og.operator_apply(xg)) / np.linalg.norm(b)
+    assert st.converged == 1 and rel <= 1.5e-8, rel
+    print("two-hop learned inner iterations:", st.iterations, st.method)
+    assert st.method == 2 and st.iterations < it_l, (st.iterations, it_l)
