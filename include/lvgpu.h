@@ -104,6 +104,10 @@ int32_t lv_num_particles(const lv_ctx* ctx);
 /* Upload / download one field of all n particles (see lv_field). */
 int lv_set_field(lv_ctx* ctx, int32_t field, const double* host);
 int lv_get_field(lv_ctx* ctx, int32_t field, double* host);
+/* Several fields in one call with one synchronisation (fields[count],
+ * host arrays data[count] laid out as for lv_set_field / lv_get_field). */
+int lv_set_fields(lv_ctx* ctx, int32_t count, const int32_t* fields, const double* const* data);
+int lv_get_fields(lv_ctx* ctx, int32_t count, const int32_t* fields, double* const* data);
 /* Device pointer of a field (for zero-copy interop); NULL if unknown. */
 void* lv_field_device_ptr(lv_ctx* ctx, int32_t field);
 

@@ -128,6 +128,37 @@ class VoronoiGrid:
         _check(self, _lib.load().lv_get_field(self._ctx, fid, _lib.ptr(a)))
         return a.reshape(self.n, k) if k > 1 else a
 
+    def get_many(self, names, out=None):
+        """Several fields in one call (one synchronisation); `out` may hold
+        preallocated float64 arrays of the right shapes."""
+        L = _lib.load()
+        arrays = []
+        for k, name in enumerate(names):
+            fid, w = _lib.FIELDS[name]
+            a = out[k] if out is not None else np.empty((self.n, w) if w > 1 else self.n, dtype=np.float64)
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.n * w
+            arrays.append(a)
+        ids = np.array([_lib.FIELDS[nm][0] for nm in names], np.int32)
+        ptrs = (C.c_void_p * len(names))(*[a.ctypes.data for a in arrays])
+        _check(self, L.lv_get_fields(self._ctx, len(names), _lib.ptr(ids, C.c_int32), ptrs))
+        return arrays
+
+    def set_many(self, fields):
+        """Several fields {name: array} in one call (one synchronisation)."""
+        self._flush()
+        L = _lib.load()
+        names = list(fields)
+        arrays = []
+        for name in names:
+            fid, w = _lib.FIELDS[name]
+            a = np.ascontiguousarray(fields[name], dtype=np.float64)
+            if a.size != self.n * w:
+                raise ValueError(f"{name}: expected {self.n * w} values, got {a.size}")
+            arrays.append(a)
+        ids = np.array([_lib.FIELDS[nm][0] for nm in names], np.int32)
+        ptrs = (C.c_void_p * len(names))(*[a.ctypes.data for a in arrays])
+        _check(self, L.lv_set_fields(self._ctx, len(names), _lib.ptr(ids, C.c_int32), ptrs))
+
     def set(self, name, values):
         fid, k = _lib.FIELDS[name]
         a = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64),

@@ -49,6 +49,8 @@ SIGNATURES = {
     "lv_num_particles": (_i32, [_vp]),
     "lv_set_field": (C.c_int, [_vp, _i32, _pd]),
     "lv_get_field": (C.c_int, [_vp, _i32, _pd]),
+    "lv_set_fields": (C.c_int, [_vp, _i32, _pi32, C.POINTER(C.c_void_p)]),
+    "lv_get_fields": (C.c_int, [_vp, _i32, _pi32, C.POINTER(C.c_void_p)]),
     "lv_field_device_ptr": (_vp, [_vp, _i32]),
     "lv_remesh": (C.c_int, [_vp]),
     "lv_remesh_async": (C.c_int, [_vp]),

@@ -128,6 +128,10 @@ __global__ void k_split_phase(const double* __restrict__ src, int* dst, int n) {
   if (i < n) dst[i] = (int)src[i];
 }
 
+// Queue one field transfer on the context's stream (no synchronisation).
+int queue_set_field(lv_ctx* c, int32_t f, const double* h);
+int queue_get_field(lv_ctx* c, int32_t f, double* h, std::vector<int>* phase_tmp);
+
 }  // namespace
 
 KernelTimer::KernelTimer(lv_ctx* cc, int f) : c(cc), fam(f) {
@@ -375,8 +379,48 @@ static double2* dptr2(lv_ctx* c, int f) {
   }
 }
 
+int lv_set_fields(lv_ctx* c, int32_t count, const int32_t* fields, const double* const* data) {
+  if (!c || count < 0 || (count > 0 && (!fields || !data))) return LV_ERR_BAD_ARGUMENT;
+  for (int k = 0; k < count; ++k) {
+    if (!data[k]) return LV_ERR_BAD_ARGUMENT;
+    if (int rc = queue_set_field(c, fields[k], data[k])) return rc;
+  }
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_set_fields");
+}
+
+int lv_get_fields(lv_ctx* c, int32_t count, const int32_t* fields, double* const* data) {
+  if (!c || count < 0 || (count > 0 && (!fields || !data))) return LV_ERR_BAD_ARGUMENT;
+  std::vector<std::vector<int>> ph(count);
+  for (int k = 0; k < count; ++k) {
+    if (!data[k]) return LV_ERR_BAD_ARGUMENT;
+    if (int rc = queue_get_field(c, fields[k], data[k], &ph[k])) return rc;
+  }
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  for (int k = 0; k < count; ++k)
+    for (size_t i = 0; i < ph[k].size(); ++i) data[k][i] = ph[k][i];
+  return lv_cuda_check(c, e, "lv_get_fields");
+}
+
 int lv_set_field(lv_ctx* c, int32_t f, const double* h) {
   if (!c || !h) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = queue_set_field(c, f, h)) return rc;
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_set_field");
+}
+
+int lv_get_field(lv_ctx* c, int32_t f, double* h) {
+  if (!c || !h) return LV_ERR_BAD_ARGUMENT;
+  std::vector<int> ph;
+  if (int rc = queue_get_field(c, f, h, &ph)) return rc;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  for (size_t i = 0; i < ph.size(); ++i) h[i] = ph[i];
+  return lv_cuda_check(c, e, "lv_get_field");
+}
+
+}  // extern "C"
+
+namespace {
+
+int queue_set_field(lv_ctx* c, int32_t f, const double* h) {
   const size_t n = c->n;
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
@@ -404,12 +448,12 @@ int lv_set_field(lv_ctx* c, int32_t f, const double* h) {
   } else {
     return lv_fail(c, LV_ERR_BAD_ARGUMENT, "unknown field");
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return lv_cuda_check(c, e, "lv_set_field");
 }
 
-int lv_get_field(lv_ctx* c, int32_t f, double* h) {
-  if (!c || !h) return LV_ERR_BAD_ARGUMENT;
+// phase (int32 on the device) lands in *phase_tmp, converted by the caller
+// after the synchronisation
+int queue_get_field(lv_ctx* c, int32_t f, double* h, std::vector<int>* phase_tmp) {
   const size_t n = c->n;
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
@@ -421,17 +465,17 @@ int lv_get_field(lv_ctx* c, int32_t f, double* h) {
     e = cudaMemcpy2DAsync(h, 32, c->s.Da, 16, 16, n, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpy2DAsync(h + 2, 32, c->s.Db, 16, 16, n, cudaMemcpyDeviceToHost, s);
   } else if (f == LV_FIELD_PHASE) {
-    std::vector<int> tmp(n);
-    e = cudaMemcpyAsync(tmp.data(), c->s.phase, 4 * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    for (size_t i = 0; i < n; ++i) h[i] = tmp[i];
-    return lv_cuda_check(c, e, "lv_get_field");
+    phase_tmp->resize(n);
+    e = cudaMemcpyAsync(phase_tmp->data(), c->s.phase, 4 * n, cudaMemcpyDeviceToHost, s);
   } else {
     return lv_fail(c, LV_ERR_BAD_ARGUMENT, "unknown field");
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return lv_cuda_check(c, e, "lv_get_field");
 }
+
+}  // namespace
+
+extern "C" {
 
 void* lv_field_device_ptr(lv_ctx* c, int32_t f) {
   if (!c) return nullptr;

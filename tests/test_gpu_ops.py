@@ -134,3 +134,22 @@ def test_destroyed_mesh_is_reported(lv, oracle):
         lv.move(g, flow.dt)
         g.synchronize()
     assert e.value.code == 2
+
+
+def test_batched_field_transfers(lv, oracle):
+    """lv_set_fields / lv_get_fields move several fields with one synchronisation
+    and agree with the one-field calls."""
+    from lvgpu import populate as pop
+    flow = W.taylor_green(16)
+    g = H.make_gpu(lv, flow, H.seeds(pop, flow))
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal((g.n, 2))
+    P = rng.standard_normal(g.n)
+    ph = (rng.random(g.n) < 0.5).astype(float)
+    g.set_many({"v": v, "P": P, "phase": ph})
+    got = g.get_many(["v", "P", "phase", "area"])
+    assert np.array_equal(got[0], v) and np.array_equal(got[1], P) and np.array_equal(got[2], ph)
+    assert np.array_equal(got[3], g["area"])
+    out = [np.empty((g.n, 2)), np.empty(g.n)]
+    res = g.get_many(["v", "P"], out=out)
+    assert res[0] is out[0] and np.array_equal(out[1], P)
