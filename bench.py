@@ -360,7 +360,11 @@ def run_ours(args, world, rank, local):
         if args.solver == "jacobi_pcg":
             kname = "k_pcg_reg<2>" if N <= 2 * 128 * 2 * 152 else "k_pcg"
         else:
-            kname = "k_fcg<1>" if N <= 152 * 512 else ("k_fcg<2>" if N <= 152 * 1024 else "k_lpcg_str")
+            # the learned solve runs the staged instantiation when the per-block
+            # images fit shared memory (they do for these workloads)
+            staged = "true" if args.solver == "learned_pcg" else "false"
+            kname = (f"k_fcg<1,{staged}>" if N <= 152 * 512 else
+                     (f"k_fcg<2,{staged}>" if N <= 152 * 1024 else "k_lpcg_str"))
     else:
         kname = "k_clip"
     traffic = read_traffic(WORKLOAD, dom, kname)

@@ -270,6 +270,13 @@ int lv_kernel_time(lv_ctx* ctx, int32_t family, int64_t* launches, double* ms, i
 /* Cumulative pressure-solver counters since creation: linear solves and CG
  * iterations (inner iterations for the mixed-precision solver); synchronises. */
 int lv_solver_counters(lv_ctx* ctx, int64_t* solves, int64_t* iterations);
+/* Diagnostic of the learned solve for systems that fit one block per SM:
+ * the largest halo (rows outside a block that the block's rows reference)
+ * over the blocks of the last built factor, or 0 when that solve moves
+ * M^-1 r between blocks instead of computing it on the halo (halo mode off
+ * through LVGPU_FCG_HALO=0, a halo above 1536 rows, or a larger system);
+ * synchronises. */
+int lv_solver_halo(lv_ctx* ctx, int32_t* max_rows);
 
 /* Per-kernel-family device times in ms accumulated since the last reset:
  * out[0] mesh, [1] operators, [2] pressure solve, [3] other.  Returns the

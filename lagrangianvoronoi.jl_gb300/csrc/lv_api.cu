@@ -793,6 +793,14 @@ int lv_kernel_time(lv_ctx* c, int32_t fam, int64_t* launches, double* ms, int32_
   return LV_OK;
 }
 
+int lv_solver_halo(lv_ctx* c, int32_t* max_rows) {
+  if (!c || !max_rows) return LV_ERR_BAD_ARGUMENT;
+  int m = 0;
+  if (int rc = lv_fcg_halo_info(c, &m)) return rc;
+  *max_rows = m;
+  return LV_OK;
+}
+
 int lv_solver_counters(lv_ctx* c, int64_t* solves, int64_t* iterations) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   long long h[2] = {0, 0};

@@ -17,6 +17,9 @@
 // exchanges (nexchange: per-block flags, each block waits only for the blocks
 // whose rows it reads).  A Jacobi iteration costs one exchange and one phase,
 // a learned one two exchanges and one phase.
+#include <cstddef>
+#include <cstdlib>
+
 #include "lv_internal.cuh"
 
 namespace {
@@ -31,6 +34,14 @@ constexpr float FCG_UPDATE_DROP = 1e-5f;  // FP32 residual reduction per refinem
 constexpr int FCG_MAX_UPDATES = 200;
 
 constexpr int RG_WORDS = 4;  // partial-sum words per block and phase
+constexpr int FCG_RPB_MAX = FCG_TPB * 2;  // rows per block at most (two per thread)
+constexpr int FCG_HMAX = 1536;            // staged mode: halo rows per block
+constexpr int STG_EXTMAX = 2048;          // staged mode: r values a block gathers per iteration
+constexpr int STG_MAXG = FCG_RPB_MAX / 32 + FCG_HMAX / 32;  // row groups of 32
+constexpr int STG_PMAX = FCG_RPB_MAX + FCG_HMAX;  // staged mode: rows whose u a block computes
+constexpr int STG_ENTRIES = 24576;  // staged mode: M^-1 entries per block (padded per group)
+constexpr int STG_SLOTS = 32;       // staged mode: M^-1 off-diagonal entries per row at most
+constexpr int STG_HASH = 8192;      // hash slots of the image builder
 constexpr int FLAG_STRIDE = 32;  // exchange flags sit on separate 128-byte lines (packed flags halve the speed)
 constexpr int FCG_MAX_BLOCKS = 1024;
 
@@ -39,6 +50,40 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+
+// Per-block image of the staged learned solve, built once per factor by
+// k_stage_build and copied to shared memory at launch.  The rows whose u the
+// block computes (its own rows and its halo: the rows outside the block that
+// its operator rows reference) take positions ordered by their M^-1 entry
+// count, longest first; thread t applies positions t, t + 512, ...  Positions
+// form groups of 32, stored slot-major within a group and padded to the
+// group's longest row (one warp reads one slot of 32 rows without bank
+// conflicts; the ordering keeps the padding small).  Column indices point into
+// the block's r staging: own rows first, then the ext rows gathered from
+// other blocks.
+struct StageImage {
+  int npos, ne, nh, total;  // positions, ext rows, halo rows, entries
+  int goff[STG_MAXG];       // first entry of each group
+  int gsl[STG_MAXG];        // slots of each group
+  int ext[STG_EXTMAX];      // rows gathered from other blocks each iteration
+  float pmd[STG_PMAX];      // per position: M^-1 diagonal
+  float pdnv[STG_PMAX];     // per position: Jacobi scale
+  unsigned short pridx[STG_PMAX];  // per position: the row's r in the staging
+  unsigned short puidx[STG_PMAX];  // per position: the row's u in shared memory
+  unsigned char pm[STG_PMAX];      // per position: off-diagonal entries
+  float sval[STG_ENTRIES];
+  unsigned short sidx[STG_ENTRIES];
+};
+static_assert(offsetof(StageImage, sval) % 16 == 0 && offsetof(StageImage, sidx) % 16 == 0, "16-byte copies");
+
+// Shared memory of the staged mode: r of the own rows then of the ext rows,
+// u of the own rows then of the halo rows, the image.
+struct StageSmem {
+  float r[FCG_RPB_MAX + STG_EXTMAX];
+  float u[FCG_RPB_MAX + FCG_HMAX];
+  StageImage img;
+};
+static_assert(offsetof(StageSmem, img) % 16 == 0, "16-byte copies");
 
 struct FcgArgs {
   int n, nb, rows_per_block;
@@ -65,6 +110,11 @@ struct FcgArgs {
   const float* mdiag;
   int mstride;
   const int* minv_ok;
+  // staged mode (learned): each block also computes u = M^-1 r on its halo,
+  // so that only r crosses blocks; the operator's columns are remapped to
+  // the shared-memory u of the own and halo rows
+  const StageImage* stage;
+  const int* remap;
   int* jref;
   int* out_iters;
   int* out_outer;
@@ -225,12 +275,30 @@ struct FRows {
   double bb[R];
 };
 
-template <int R>
+// HALO: the staged instantiation (learned solves whose image fits shared
+// memory); the other one is free of its code and holds M^-1 in registers.
+template <int R, bool HALO>
 __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   const int n = a.n;
   const int rb0 = blockIdx.x * a.rows_per_block;
   const int rb1 = min(n, rb0 + a.rows_per_block);
   const bool learned0 = a.learned != 0 && *a.minv_ok != 0;
+  extern __shared__ __align__(16) unsigned char fcg_dyn[];
+  StageSmem& ss = *reinterpret_cast<StageSmem*>(fcg_dyn);
+  if constexpr (HALO) {
+    // the block's image into shared memory: the fixed part, then the used entries
+    const StageImage& gi = a.stage[blockIdx.x];
+    const int total = gi.total;
+    const int4* src = reinterpret_cast<const int4*>(&gi);
+    int4* dst = reinterpret_cast<int4*>(&ss.img);
+    for (int q = threadIdx.x; q < (int)(offsetof(StageImage, sval) / 16); q += FCG_TPB) dst[q] = src[q];
+    const int4* sv = reinterpret_cast<const int4*>(gi.sval);
+    int4* dv = reinterpret_cast<int4*>(ss.img.sval);
+    for (int q = threadIdx.x; q < total / 4; q += FCG_TPB) dv[q] = sv[q];
+    const int4* si = reinterpret_cast<const int4*>(gi.sidx);
+    int4* di = reinterpret_cast<int4*>(ss.img.sidx);
+    for (int q = threadIdx.x; q < total / 8; q += FCG_TPB) di[q] = si[q];
+  }
   FRows<R> rr;
   double x[R];
 #pragma unroll
@@ -244,17 +312,19 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
 #pragma unroll
     for (int e = 0; e < FKR; ++e) {
       const bool have = e < rr.cnt[k];
-      rr.cc[k][e] = have ? a.col[rr.beg[k] + e] : 0;
+      rr.cc[k][e] = have ? (HALO ? a.remap[rr.beg[k] + e] : a.col[rr.beg[k] + e]) : 0;
       rr.ww[k][e] = have ? (float)a.w[rr.beg[k] + e] : 0.f;
     }
     rr.dg[k] = on ? (float)a.diag[i] : 0.f;
     rr.dnv[k] = on ? (float)a.dinv[i] : 0.f;
     rr.mn[k] = (on && learned0) ? a.mcnt[i] : 0;
+    if constexpr (!HALO) {
 #pragma unroll
-    for (int e = 0; e < FKM; ++e) {
-      const bool have = e < rr.mn[k];
-      rr.mc[k][e] = have ? a.mcol[(size_t)e * a.mstride + i] : 0;
-      rr.mv[k][e] = have ? a.mval[(size_t)e * a.mstride + i] : 0.f;
+      for (int e = 0; e < FKM; ++e) {
+        const bool have = e < rr.mn[k];
+        rr.mc[k][e] = have ? a.mcol[(size_t)e * a.mstride + i] : 0;
+        rr.mv[k][e] = have ? a.mval[(size_t)e * a.mstride + i] : 0.f;
+      }
     }
     rr.md[k] = (on && learned0) ? a.mdiag[i] : 0.f;
     rr.bb[k] = on ? a.b[i] : 0.0;
@@ -275,8 +345,13 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     for (int k = 0; k < R; ++k) {
       if (!rr.on[k]) continue;
       for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) mark(a.col[e]);
-      for (int e = 0; e < rr.mn[k]; ++e) mark(a.mcol[(size_t)e * a.mstride + rr.i[k]]);
+      if constexpr (!HALO)
+        for (int e = 0; e < rr.mn[k]; ++e) mark(a.mcol[(size_t)e * a.mstride + rr.i[k]]);
     }
+    // staged mode: the owners of the gathered rows (these include the halo
+    // rows and the columns of every staged M^-1 row)
+    if constexpr (HALO)
+      for (int q = threadIdx.x; q < ss.img.ne; q += FCG_TPB) mark(ss.img.ext[q]);
   }
   unsigned ep = 0;  // phases completed in this launch
   unsigned xe = 0;  // neighbour exchanges completed in this launch
@@ -298,16 +373,23 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   int it = 0, updates = 0;
   double bnorm2 = 0.0, rtrue2 = 0.0;
   float r[R], u[R], w[R], p[R], s[R], d[R];
-  // out = A v with the neighbours' values from buf (FP32 difference form)
+  // out = A v with the neighbours' values from buf (FP32 difference form);
+  // in the staged mode from shared memory through the remapped columns
   auto spmv = [&](const float* buf, const float(&own)[R], float(&out)[R]) {
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       float acc = rr.dg[k] * own[k];
 #pragma unroll
       for (int e = 0; e < FKR; ++e)
-        if (e < rr.cnt[k]) acc = fmaf(rr.ww[k][e], own[k] - __ldcg(buf + rr.cc[k][e]), acc);
-      for (int e = FKR; e < rr.cnt[k]; ++e)
-        acc = fmaf((float)a.w[rr.beg[k] + e], own[k] - __ldcg(buf + a.col[rr.beg[k] + e]), acc);
+        if (e < rr.cnt[k]) {
+          const float vj = HALO ? ss.u[rr.cc[k][e]] : __ldcg(buf + rr.cc[k][e]);
+          acc = fmaf(rr.ww[k][e], own[k] - vj, acc);
+        }
+      for (int e = FKR; e < rr.cnt[k]; ++e) {
+        const int q = rr.beg[k] + e;
+        const float vj = HALO ? ss.u[a.remap[q]] : __ldcg(buf + a.col[q]);
+        acc = fmaf((float)a.w[q], own[k] - vj, acc);
+      }
       out[k] = acc;
     }
   };
@@ -328,15 +410,89 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   };
   // u = M^-1 r (the learned preconditioner needs r from the neighbours)
   auto precond = [&]() -> bool {
-    if (learned) {
+    if constexpr (HALO) {
+      // r crosses blocks (global and staged); u of the own and the halo rows
+      // lands in shared memory, each halo row computed exactly as its owner
+      // computes it (same entries, same order)
+      const int rpb = a.rows_per_block;
+      const int lane = threadIdx.x & 31;
 #pragma unroll
       for (int k = 0; k < R; ++k)
-        if (rr.on[k]) a.rbuf[rr.i[k]] = r[k];
+        if (rr.on[k]) {
+          a.rbuf[rr.i[k]] = r[k];
+          ss.r[threadIdx.x + k * FCG_TPB] = r[k];
+        }
       if (!nexchange(a, ++xe, s_mask)) return false;
-      mapply(a.rbuf, r, u);
-    } else {
+      const int ne = ss.img.ne;
+      constexpr int NQ = STG_EXTMAX / FCG_TPB;
+      float ev[NQ];
 #pragma unroll
-      for (int k = 0; k < R; ++k) u[k] = rr.dnv[k] * r[k];
+      for (int q = 0; q < NQ; ++q) {
+        const int e = threadIdx.x + q * FCG_TPB;
+        ev[q] = e < ne ? __ldcg(a.rbuf + ss.img.ext[e]) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int e = threadIdx.x + q * FCG_TPB;
+        if (e < ne) ss.r[rpb + e] = ev[q];
+      }
+      __syncthreads();
+      // u at this thread's positions p = t + k 512: u_i = md_i r_i + the
+      // row's slots in order (a halo row exactly as its owner computes it),
+      // or the Jacobi scale times r_i.  The loads of four
+      // slots are issued together (padding slots point at a valid index with
+      // value 0 and are not added).
+      auto row_apply = [&](int g, int m, float md, float ri) {
+        const int base = ss.img.goff[g] + lane;
+        const int sl = ss.img.gsl[g];
+        float t = md * ri;
+        int q = 0;
+        for (; q + 4 <= sl; q += 4) {
+          float v[4], xr[4];
+#pragma unroll
+          for (int z = 0; z < 4; ++z) {
+            v[z] = ss.img.sval[base + (q + z) * 32];
+            xr[z] = ss.r[ss.img.sidx[base + (q + z) * 32]];
+          }
+#pragma unroll
+          for (int z = 0; z < 4; ++z)
+            if (q + z < m) t = fmaf(v[z], xr[z], t);
+        }
+        for (; q < sl; ++q)
+          if (q < m) t = fmaf(ss.img.sval[base + q * 32], ss.r[ss.img.sidx[base + q * 32]], t);
+        return t;
+      };
+      constexpr int KP = STG_PMAX / FCG_TPB;
+      const int npos = ss.img.npos;
+      float acc[KP];
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        const int p = threadIdx.x + k * FCG_TPB;
+        acc[k] = 0.f;
+        if (p < npos) {
+          const float ri = ss.r[ss.img.pridx[p]];
+          acc[k] = learned ? row_apply(p >> 5, ss.img.pm[p], ss.img.pmd[p], ri) : ss.img.pdnv[p] * ri;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < KP; ++k) {
+        const int p = threadIdx.x + k * FCG_TPB;
+        if (p < npos) ss.u[ss.img.puidx[p]] = acc[k];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < R; ++k) u[k] = rr.on[k] ? ss.u[threadIdx.x + k * FCG_TPB] : 0.f;  // zeros past the block's end
+    } else {
+      if (learned) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          if (rr.on[k]) a.rbuf[rr.i[k]] = r[k];
+        if (!nexchange(a, ++xe, s_mask)) return false;
+        mapply(a.rbuf, r, u);
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k) u[k] = rr.dnv[k] * r[k];
+      }
     }
     return true;
   };
@@ -400,10 +556,12 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     const float rho_upd = fmaxf(FCG_UPDATE_DROP * FCG_UPDATE_DROP, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
     if (!(ok = precond())) break;
     while (true) {
+      if constexpr (!HALO) {
 #pragma unroll
-      for (int k = 0; k < R; ++k)
-        if (rr.on[k]) a.ubuf[rr.i[k]] = u[k];
-      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+        for (int k = 0; k < R; ++k)
+          if (rr.on[k]) a.ubuf[rr.i[k]] = u[k];
+        if (!(ok = nexchange(a, ++xe, s_mask))) break;
+      }
       spmv(a.ubuf, u, w);
       float v3[3] = {0.f, 0.f, 0.f}, t3[3];
 #pragma unroll
@@ -513,7 +671,244 @@ __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* _
   if (overflow) atomicAnd(ok, 0);
 }
 
+// The staged image of solve block b (rows [b rpb, (b+1) rpb)), one block of
+// STG_BUILD_TPB threads per solve block.  An open-addressing hash in shared
+// memory numbers the rows outside the block: first the halo (the operator's
+// columns), then the rest of the ext rows (the M^-1 columns of the own and the
+// halo rows).  Then it writes the image and remaps every operator nonzero of
+// the block's rows to the shared-memory u of the staged solve (own row j:
+// j - b rpb; halo row: rpb + halo slot).  stat[0] is cleared when an image
+// does not fit; stat[1..3] collect the largest halo, ext and entry counts.
+constexpr int STG_BUILD_TPB = 512;
+constexpr size_t STG_BUILD_SMEM = (size_t)STG_HASH * (4 + 2 + 2) + (size_t)FCG_HMAX * 4 + (size_t)STG_PMAX * 4;
+
+__device__ __forceinline__ unsigned stg_hash(int j) { return ((unsigned)j * 2654435761u) >> 19; }
+
+__global__ void __launch_bounds__(STG_BUILD_TPB) k_stage_build(int n, int rpb, const int* __restrict__ rowptr,
+                                                               const int* __restrict__ col,
+                                                               const int* __restrict__ mcnt,
+                                                               const int* __restrict__ mcol,
+                                                               const float* __restrict__ mval,
+                                                               const float* __restrict__ mdiag,
+                                                               const double* __restrict__ dinv, int mstride,
+                                                               StageImage* images, int* remap, int* stat) {
+  static_assert(STG_HASH == 8192, "stg_hash yields 13 bits");
+  extern __shared__ __align__(16) unsigned char stg_dyn[];
+  int* keys = reinterpret_cast<int*>(stg_dyn);
+  short* hsl = reinterpret_cast<short*>(keys + STG_HASH);
+  short* esl = hsl + STG_HASH;
+  int* hrow = reinterpret_cast<int*>(esl + STG_HASH);
+  int* prow = hrow + FCG_HMAX;  // sorted position -> unsorted (own rows, then halo rows)
+  __shared__ int s_nh, s_ne, s_bad, s_total;
+  __shared__ int s_gsl[STG_MAXG], s_goff[STG_MAXG];
+  __shared__ int s_hist[STG_SLOTS + 1];
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int lane = t & 31, wid = t >> 5;
+  StageImage& im = images[b];
+  const int rb0 = b * rpb, rb1 = min(n, rb0 + rpb);
+  const int nown = max(0, rb1 - rb0);
+  for (int h = t; h < STG_HASH; h += STG_BUILD_TPB) {
+    keys[h] = -1;
+    hsl[h] = -1;
+    esl[h] = -1;
+  }
+  for (int h = t; h <= STG_SLOTS; h += STG_BUILD_TPB) s_hist[h] = 0;
+  if (t == 0) {
+    s_nh = 0;
+    s_ne = 0;
+    s_bad = 0;
+  }
+  __syncthreads();
+  auto outside = [&](int j) { return j < rb0 || j >= rb1; };
+  auto insert = [&](int j, bool halo) {
+    unsigned h = stg_hash(j);
+    for (int p = 0; p < STG_HASH; ++p, h = (h + 1) & (STG_HASH - 1)) {
+      const int old = atomicCAS(&keys[h], -1, j);
+      if (old == -1) {
+        esl[h] = (short)min(atomicAdd(&s_ne, 1), 32767);
+        if (halo) {
+          const int x = atomicAdd(&s_nh, 1);
+          hsl[h] = (short)min(x, 32767);
+          if (x < FCG_HMAX) hrow[x] = j;
+        }
+        return;
+      }
+      if (old == j) return;
+    }
+    s_bad = 1;
+  };
+  auto find = [&](int j) {
+    unsigned h = stg_hash(j);
+    for (int p = 0; p < STG_HASH; ++p, h = (h + 1) & (STG_HASH - 1)) {
+      const int k = keys[h];
+      if (k == j) return (int)h;
+      if (k == -1) break;
+    }
+    return -1;
+  };
+  // the halo: operator columns outside the block
+  for (int l = t; l < nown; l += STG_BUILD_TPB)
+    for (int e = rowptr[rb0 + l]; e < rowptr[rb0 + l + 1]; ++e)
+      if (outside(col[e])) insert(col[e], true);
+  __syncthreads();
+  const int nh = s_nh;
+  // the rest of the ext rows: M^-1 columns of the own and the halo rows
+  for (int l = t; l < nown; l += STG_BUILD_TPB) {
+    const int i = rb0 + l;
+    for (int q = 0; q < mcnt[i]; ++q) {
+      const int j = mcol[(size_t)q * mstride + i];
+      if (outside(j)) insert(j, false);
+    }
+  }
+  for (int x = t; x < min(nh, FCG_HMAX); x += STG_BUILD_TPB) {
+    const int i = hrow[x];
+    for (int q = 0; q < mcnt[i]; ++q) {
+      const int j = mcol[(size_t)q * mstride + i];
+      if (outside(j)) insert(j, false);
+    }
+  }
+  __syncthreads();
+  const int ne = s_ne;
+  const int npos = nown + nh, ng = (npos + 31) / 32;
+  if (s_bad || nh > FCG_HMAX || ne > STG_EXTMAX || ng > STG_MAXG) {
+    if (t == 0) atomicAnd(stat, 0);
+    return;
+  }
+  // the row at unsorted position p (own rows, then halo rows)
+  auto pos_row = [&](int p) { return p < nown ? rb0 + p : hrow[p - nown]; };
+  // positions ordered by entry count, longest first (counting sort)
+  for (int p = t; p < npos; p += STG_BUILD_TPB) {
+    const int m = mcnt[pos_row(p)];
+    if (m > STG_SLOTS)
+      s_bad = 1;
+    else
+      atomicAdd(&s_hist[m], 1);
+  }
+  __syncthreads();
+  if (t == 0) {
+    int off = 0;
+    for (int m = STG_SLOTS; m >= 0; --m) {
+      const int c = s_hist[m];
+      s_hist[m] = off;
+      off += c;
+    }
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (t == 0) atomicAnd(stat, 0);
+    return;
+  }
+  for (int p = t; p < npos; p += STG_BUILD_TPB) prow[atomicAdd(&s_hist[mcnt[pos_row(p)]], 1)] = p;
+  __syncthreads();
+  // the row at sorted position q (-1: padding)
+  auto srow = [&](int q) { return q < npos ? pos_row(prow[q]) : -1; };
+  // groups of 32 positions: slots = the longest row
+  for (int g = wid; g < ng; g += STG_BUILD_TPB / 32) {
+    const int i = srow(g * 32 + lane);
+    int m = i >= 0 ? mcnt[i] : 0;
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (lane == 0) s_gsl[g] = m;
+  }
+  __syncthreads();
+  if (t == 0) {
+    int off = 0;
+    for (int g = 0; g < ng; ++g) {
+      s_goff[g] = off;
+      off += s_gsl[g] * 32;
+    }
+    s_total = off;
+    if (off > STG_ENTRIES) s_bad = 1;
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (t == 0) atomicAnd(stat, 0);
+    return;
+  }
+  // the staging index of column j (own rows first, then the ext rows)
+  auto sidx = [&](int j) -> int {
+    if (!outside(j)) return j - rb0;
+    const int h = find(j);
+    return h < 0 ? 0 : rpb + esl[h];
+  };
+  for (int h = t; h < STG_HASH; h += STG_BUILD_TPB)
+    if (keys[h] >= 0) im.ext[esl[h]] = keys[h];
+  for (int q = t; q < npos; q += STG_BUILD_TPB) {
+    const int p = prow[q];
+    const int i = pos_row(p);
+    im.pridx[q] = (unsigned short)sidx(i);
+    im.puidx[q] = (unsigned short)(p < nown ? p : rpb + (p - nown));
+    im.pm[q] = (unsigned char)mcnt[i];
+    im.pmd[q] = mdiag[i];
+    im.pdnv[q] = (float)dinv[i];
+  }
+  for (int q = t; q < ng * 32; q += STG_BUILD_TPB) {
+    const int i = srow(q);
+    const int m = i >= 0 ? mcnt[i] : 0;
+    const int base = s_goff[q >> 5] + (q & 31);
+    for (int z = 0; z < s_gsl[q >> 5]; ++z) {
+      const bool have = z < m;
+      im.sidx[base + z * 32] = (unsigned short)(have ? sidx(mcol[(size_t)z * mstride + i]) : 0);
+      im.sval[base + z * 32] = have ? mval[(size_t)z * mstride + i] : 0.f;
+    }
+  }
+  // the operator's columns, remapped to the staged u
+  for (int l = t; l < nown; l += STG_BUILD_TPB)
+    for (int e = rowptr[rb0 + l]; e < rowptr[rb0 + l + 1]; ++e) {
+      const int j = col[e];
+      int r = j - rb0;
+      if (outside(j)) {
+        const int h = find(j);
+        r = h < 0 ? 0 : rpb + hsl[h];
+      }
+      remap[e] = r;
+    }
+  for (int g = t; g < ng; g += STG_BUILD_TPB) {
+    im.goff[g] = s_goff[g];
+    im.gsl[g] = s_gsl[g];
+  }
+  if (t == 0) {
+    im.npos = npos;
+    im.ne = ne;
+    im.nh = nh;
+    im.total = s_total;
+    atomicMax(stat + 1, nh);
+    atomicMax(stat + 2, ne);
+    atomicMax(stat + 3, s_total);
+  }
+}
+
 int g_fcg_blocks_per_sm[2] = {-1, -1};
+int g_fcg_halo_blocks_per_sm[2] = {-1, -1};
+
+// blocks and rows per thread of the flag-reduced solve of n rows: one block
+// per SM while one row per thread suffices, else two rows per thread, then
+// two blocks per SM
+void fcg_shape(const lv_ctx* c, int n, int* nb, int* R) {
+  *nb = c->num_sms;
+  *R = 1;
+  if (n > *nb * FCG_TPB) *R = 2;
+  if (n > *nb * FCG_TPB * 2) *nb = std::min(c->num_sms * 2, FCG_MAX_BLOCKS);
+}
+
+// whether the staged mode's shared memory leaves nb blocks co-resident
+bool stage_fits(const lv_ctx* c, int nb, int R) {
+  if (g_fcg_halo_blocks_per_sm[0] < 0) {
+    int b1 = 0, b2 = 0;
+    const int bytes = (int)sizeof(StageSmem);
+    if (cudaFuncSetAttribute(k_fcg<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_fcg<1, true>, FCG_TPB, bytes);
+    if (cudaFuncSetAttribute(k_fcg<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_fcg<2, true>, FCG_TPB, bytes);
+    cudaGetLastError();
+    if (cudaFuncSetAttribute(k_stage_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STG_BUILD_SMEM) !=
+        cudaSuccess)
+      b1 = b2 = 0;
+    cudaGetLastError();
+    g_fcg_halo_blocks_per_sm[0] = b1;
+    g_fcg_halo_blocks_per_sm[1] = b2;
+  }
+  return g_fcg_halo_blocks_per_sm[R - 1] * c->num_sms >= nb;
+}
 
 
 
@@ -524,8 +919,8 @@ int g_fcg_blocks_per_sm[2] = {-1, -1};
 int lv_fcg_capacity(lv_ctx* c) {
   if (g_fcg_blocks_per_sm[0] < 0) {
     int b1 = 0, b2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_fcg<1>, FCG_TPB, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_fcg<2>, FCG_TPB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_fcg<1, false>, FCG_TPB, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_fcg<2, false>, FCG_TPB, 0);
     g_fcg_blocks_per_sm[0] = b1;
     g_fcg_blocks_per_sm[1] = b2;
   }
@@ -543,19 +938,30 @@ static int ensure_minv(lv_ctx* c) {
   cudaFree(sv.mval);
   cudaFree(sv.mdiag);
   cudaFree(sv.mok);
+  cudaFree(sv.stage);
+  cudaFree(sv.remap);
+  cudaFree(sv.stage_stat);
   sv.mcnt = nullptr;
   sv.mcol = nullptr;
   sv.mval = nullptr;
   sv.mdiag = nullptr;
   sv.mok = nullptr;
+  sv.stage = nullptr;
+  sv.remap = sv.stage_stat = nullptr;
+  sv.stage_ready = false;
   sv.mrows = 0;
+  const int maxb = std::min(c->num_sms * 2, FCG_MAX_BLOCKS);
   bool ok = cudaMalloc(&sv.mcnt, sizeof(int) * rows) == cudaSuccess;
   ok = ok && cudaMalloc(&sv.mcol, sizeof(int) * (size_t)MMAX * rows) == cudaSuccess;
   ok = ok && cudaMalloc(&sv.mval, sizeof(float) * (size_t)MMAX * rows) == cudaSuccess;
   ok = ok && cudaMalloc(&sv.mdiag, sizeof(float) * rows) == cudaSuccess;
   ok = ok && cudaMalloc(&sv.mok, sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMalloc(&sv.stage, sizeof(StageImage) * (size_t)maxb) == cudaSuccess;
+  ok = ok && cudaMalloc(&sv.remap, sizeof(int) * (size_t)LV_MAX_EDGES * rows) == cudaSuccess;
+  ok = ok && cudaMalloc(&sv.stage_stat, sizeof(int) * 4) == cudaSuccess;
   if (!ok) return lv_fail(c, LV_ERR_CUDA, "allocation of the learned preconditioner matrix failed");
   cudaMemsetAsync(sv.mok, 0, sizeof(int), c->stream);
+  cudaMemsetAsync(sv.stage_stat, 0, sizeof(int) * 4, c->stream);
   sv.mrows = rows;
   return LV_OK;
 }
@@ -567,12 +973,24 @@ void lv_fcg_free(lv_ctx* c) {
   cudaFree(sv.mval);
   cudaFree(sv.mdiag);
   cudaFree(sv.mok);
+  cudaFree(sv.stage);
+  cudaFree(sv.remap);
+  cudaFree(sv.stage_stat);
   sv.mcnt = nullptr;
   sv.mcol = nullptr;
   sv.mval = nullptr;
   sv.mdiag = nullptr;
   sv.mok = nullptr;
+  sv.stage = nullptr;
+  sv.remap = sv.stage_stat = nullptr;
+  sv.stage_ready = false;
   sv.mrows = 0;
+}
+
+// Largest per-block halo of the last built factor (0: staged mode off).
+int lv_fcg_halo_info(lv_ctx* c, int* max_rows) {
+  *max_rows = c->sv.stage_ready ? c->sv.stage_max[0] : 0;
+  return LV_OK;
 }
 
 // Builds the explicit learned M^-1 from the current factor (after
@@ -592,6 +1010,28 @@ int lv_fcg_build_minv(lv_ctx* c) {
                                                           rev2, dh, c->learn_eps, c->sv.mrows, c->sv.mcnt,
                                                           c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok);
   LV_LAUNCH_CHECK(c, "k_build_minv");
+  // the staged image of every solve block, for the shape lv_fcg_solve
+  // launches; the host learns whether every image fit (one synchronisation
+  // per factor)
+  const char* env = getenv("LVGPU_FCG_HALO");
+  c->fcg_halo = !(env && env[0] == '0');
+  c->sv.stage_ready = false;
+  int nb, R;
+  fcg_shape(c, n, &nb, &R);
+  if (c->fcg_halo && stage_fits(c, nb, R) && nb <= std::min(c->num_sms * 2, FCG_MAX_BLOCKS)) {
+    const int init[4] = {1, 0, 0, 0};
+    cudaMemcpyAsync(c->sv.stage_stat, init, sizeof(init), cudaMemcpyHostToDevice, c->stream);
+    k_stage_build<<<nb, STG_BUILD_TPB, STG_BUILD_SMEM, c->stream>>>(
+        n, (n + nb - 1) / nb, c->sv.rowptr, c->sv.col, c->sv.mcnt, c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.dinv,
+        c->sv.mrows, static_cast<StageImage*>(c->sv.stage), c->sv.remap, c->sv.stage_stat);
+    LV_LAUNCH_CHECK(c, "k_stage_build");
+    int st[4] = {0, 0, 0, 0}, mok = 0;
+    cudaMemcpyAsync(st, c->sv.stage_stat, sizeof(st), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(&mok, c->sv.mok, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (int rc = lv_cuda_check(c, cudaStreamSynchronize(c->stream), "k_stage_build")) return rc;
+    c->sv.stage_ready = st[0] != 0 && mok != 0;
+    for (int q = 0; q < 3; ++q) c->sv.stage_max[q] = st[q + 1];
+  }
   return LV_OK;
 }
 
@@ -602,11 +1042,8 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   const int capn = lv_fcg_capacity(c);
   if (n > capn || n < 1) return LV_ERR_BAD_ARGUMENT;
   if (learned && !c->sv.mcnt) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a preconditioner");
-  // one block per SM while one row per thread suffices, else two rows per
-  // thread, then two blocks per SM
-  int nb = c->num_sms, R = 1;
-  if (n > nb * FCG_TPB) R = 2;
-  if (n > nb * FCG_TPB * 2) nb = std::min(c->num_sms * 2, FCG_MAX_BLOCKS);
+  int nb, R;
+  fcg_shape(c, n, &nb, &R);
   if (g_fcg_blocks_per_sm[R - 1] * c->num_sms < nb) return LV_ERR_BAD_ARGUMENT;
   FcgArgs a;
   a.n = n;
@@ -635,6 +1072,9 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.mdiag = c->sv.mdiag;
   a.mstride = c->sv.mrows;
   a.minv_ok = learned ? c->sv.mok : c->sv.iters + LV_IT_NONSINGULAR;  // read only in learned mode
+  const bool halo = learned && c->sv.stage_ready && stage_fits(c, nb, R);
+  a.stage = static_cast<const StageImage*>(c->sv.stage);
+  a.remap = c->sv.remap;
   a.jref = c->sv.iters + LV_IT_JREF + slot;  // the same sweep of the last Jacobi mixed solve
   a.out_iters = c->sv.iters + slot;
   a.out_outer = c->sv.iters + LV_IT_OUTER + slot;
@@ -644,8 +1084,10 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   cudaMemsetAsync(c->sv.bar + 2, 0, sizeof(unsigned), c->stream);
   cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * FLAG_STRIDE * nb, c->stream);
   void* args[] = {&a};
-  const void* fn = R == 1 ? (const void*)k_fcg<1> : (const void*)k_fcg<2>;
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(FCG_TPB), args, 0, c->stream);
+  const void* fn = halo ? (R == 1 ? (const void*)k_fcg<1, true> : (const void*)k_fcg<2, true>)
+                        : (R == 1 ? (const void*)k_fcg<1, false> : (const void*)k_fcg<2, false>);
+  const size_t dyn = halo ? sizeof(StageSmem) : 0;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(FCG_TPB), args, dyn, c->stream);
   c->launches++;
   if (e != cudaSuccess) return lv_cuda_check(c, e, "k_fcg cooperative launch");
   return LV_OK;

@@ -111,6 +111,13 @@ struct SolverDev {
   float *mval = nullptr, *mdiag = nullptr;
   int* mok = nullptr;
   int mrows = 0;
+  // staged learned solve (lv_fcg.cu): per-block images, the operator's
+  // columns remapped to shared-memory slots, build status [ok, max halo,
+  // max ext, max entries]; whether the images of the current factor fit
+  void* stage = nullptr;
+  int *remap = nullptr, *stage_stat = nullptr;
+  bool stage_ready = false;
+  int stage_max[3] = {0, 0, 0};
 };
 
 struct LearnState;  // learned preconditioner (lv_learn.cu)
@@ -139,6 +146,7 @@ struct lv_ctx {
   double* mp_buf = nullptr;  // multiphase projection vectors (allocated on first use)
   LearnState* learn = nullptr;
   bool factor_valid = false;  // learned factor matches the assembled operator and parameters
+  bool fcg_halo = true;  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
@@ -205,6 +213,7 @@ int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
 int lv_fcg_capacity(lv_ctx* c);
 int lv_fcg_build_minv(lv_ctx* c);
 int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned);
+int lv_fcg_halo_info(lv_ctx* c, int* max_rows);
 void lv_fcg_free(lv_ctx* c);
 
 #define LV_LAUNCH_CHECK(c, what)                                   \

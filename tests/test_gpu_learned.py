@@ -253,3 +253,60 @@ def test_training_lowers_loss_and_iterations(lv, oracle):
     assert st.converged == 1 and rel <= 1.5e-8, rel
     print("two-hop learned inner iterations:", st.iterations, st.method)
     assert st.method == 2 and st.iterations < it_l, (st.iterations, it_l)
+
+
+@pytest.mark.parametrize("nx", [64, 256, 300])
+def test_halo_mode_is_bit_identical(lv, monkeypatch, nx):
+    """The learned one-block-per-SM solve in its staged mode (each block
+    computes M^-1 r on its halo from shared memory: one neighbour exchange per
+    iteration) gives the same iterate, bit for bit, and the same iteration
+    count as with u exchanged between blocks (two exchanges): every halo value
+    is computed exactly as its owner computes it.  64^2, 256^2 (one row per
+    thread, halos above 512 rows) and 300^2 (two rows per thread); an
+    untrained and a perturbed network; and a learned solve that falls back to
+    Jacobi (the reference count from a loose mixed solve is exceeded)."""
+    from lvgpu import populate as pop
+    flow = W.taylor_green(nx)
+    x = H.seeds(pop, flow, 5, jitter=0.25)
+    g = H.make_gpu(lv, flow, x)
+    for k, v in W.initial_fields(flow, g["x"], g["area"]).items():
+        g[k] = v
+    lv.stiffened_eos(g, flow.gamma, flow.P0)
+    L = lv._lib.load()
+    assert L.lv_pressure_operator(g._ctx, flow.dt) == 0
+    rng = np.random.default_rng(1)
+    b = rng.standard_normal(g.n)
+    b -= b.mean()
+
+    def solve(method, tol):
+        lv.PressureSolver(g, method=method, tol=tol).configure()
+        xg = np.zeros(g.n)
+        st = lv.LvSolveStats()
+        assert L.lv_solve(g._ctx, lv._lib.ptr(b), lv._lib.ptr(xg), C.byref(st)) == 0
+        return xg, st
+
+    for scale, prior_tol in ((None, None), (0.3, None), (0.3, 1e-2)):
+        out = {}
+        for halo in ("0", "1"):
+            monkeypatch.setenv("LVGPU_FCG_HALO", halo)
+            if prior_tol is not None:
+                solve("mixed_ir", prior_tol)  # sets the Jacobi reference count
+            else:
+                solve("mixed_ir", 1e-8)
+            if scale is None:
+                assert L.lv_learn_init(g._ctx, 5) == 0  # invalidates the factor: rebuilt in this mode
+            else:
+                _params(L, g, 5, scale=scale)
+            xg, st = solve("learned_pcg", 1e-8)
+            assert st.converged == 1, (scale, prior_tol, halo, st.iterations)
+            hr = C.c_int32()
+            assert L.lv_solver_halo(g._ctx, C.byref(hr)) == 0
+            if halo == "0":
+                assert hr.value == 0
+            else:
+                assert hr.value > (512 if nx >= 256 else 0), hr.value
+            out[halo] = (xg, st.iterations, st.method)
+        if prior_tol is not None:
+            assert out["1"][2] == 1, "expected the fallback to Jacobi"
+        assert out["0"][1:] == out["1"][1:], (scale, prior_tol, out["0"][1:], out["1"][1:])
+        assert np.array_equal(out["0"][0], out["1"][0]), (scale, prior_tol)
