@@ -362,7 +362,7 @@ def run_ours(args, world, rank, local):
         else:
             # the learned solve runs the staged instantiation when the per-block
             # images fit shared memory (they do for these workloads)
-            staged = "true" if args.solver == "learned_pcg" else "false"
+            staged = 1 if args.solver == "learned_pcg" else 0
             kname = (f"k_fcg<1,{staged}>" if N <= 152 * 512 else
                      (f"k_fcg<2,{staged}>" if N <= 152 * 1024 else "k_lpcg_str"))
     else:
