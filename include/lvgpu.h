@@ -257,7 +257,7 @@ void* lv_stream(lv_ctx* ctx);
 #define LV_KF_BIN 0      /* cell-list re-binning (count, scan, scatter, order) */
 #define LV_KF_CLIP 1     /* Voronoi clipping + geometry + faces (k_clip) */
 #define LV_KF_PCG 2      /* persistent pressure-solve kernels */
-#define LV_KF_RHS 3      /* operator assembly and right-hand side */
+#define LV_KF_RHS 3      /* operator assembly, right-hand side and initial guess of each sweep */
 #define LV_KF_OPS 4      /* per-particle physics operators */
 #define LV_KF_LEARN 5    /* learned factor of the assembled operator (network forward, M^-1) */
 #define LV_KF_COUNT 6

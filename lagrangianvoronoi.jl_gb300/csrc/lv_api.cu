@@ -271,6 +271,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.dinv = dalloc<double>(c, cap, &ok);
   sv.b = dalloc<double>(c, cap, &ok);
   sv.xs = dalloc<double>(c, cap, &ok);
+  sv.pprev = dalloc<double>(c, cap, &ok);
   sv.r = dalloc<double>(c, 2 * (size_t)cap, &ok);
   sv.z = dalloc<double>(c, cap, &ok);
   sv.p = dalloc<double>(c, 2 * (size_t)cap, &ok);
@@ -683,9 +684,16 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
   Timer t(c, 2);
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;
+  const char* env = getenv("LVGPU_SWEEP_GUESS");
+  c->sweep_guess = !(env && env[0] == '0');
   for (int it = 1; it <= niter; ++it) {
     rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1);
     if (rc) return rc;
+    if (c->sweep_guess) {
+      KernelTimer kt(c, LV_KF_RHS);  // prepares the sweep's system, like the right-hand side
+      rc = lv_solver_sweep_guess(c, c->s.P, it);
+      if (rc) return rc;
+    }
     rc = lv_solver_solve(c, c->s.P, nullptr, it - 1);
     if (rc) return rc;
   }

@@ -94,6 +94,7 @@ struct SolverDev {
   double* w;    // [nnz_cap]
   float* w32;   // FP32 copy for the mixed-precision inner solve
   double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
+  double* pprev;      // pressure before the previous sweep's solve (sweep line search)
   float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
   long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
@@ -146,6 +147,7 @@ struct lv_ctx {
   double* mp_buf = nullptr;  // multiphase projection vectors (allocated on first use)
   LearnState* learn = nullptr;
   bool factor_valid = false;  // learned factor matches the assembled operator and parameters
+  bool sweep_guess = true;  // line search of the sweep's initial guess (LVGPU_SWEEP_GUESS=0 turns it off)
   bool fcg_halo = true;  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
@@ -206,6 +208,7 @@ void lv_learn_free(lv_ctx* c);
 int lv_solver_assemble(lv_ctx* c, double dt);
 int lv_solver_solve(lv_ctx* c, double* dst_P, lv_solve_stats* st_dev_or_null, int stats_slot);
 int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev);
+int lv_solver_sweep_guess(lv_ctx* c, double* P, int it);
 int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
 
 // ---- flag-reduced mixed-precision solver (lv_fcg.cu)

@@ -1181,16 +1181,57 @@ int lvref_operator_apply(void* h, const double* xin, double* y) {
   return 0;
 }
 
+// The GPU solver's initial guess of sweep it >= 2 (not part of the
+// reference, whose MINRES starts from the previous sweep's P): the previous
+// solution moved along d = P_{it-1} - P_{it-2} by the exact A-norm line
+// search omega = (b - A P, d) / (d, A d), with b projected to zero mean when
+// the operator is singular; omega outside (-2, 2) or undefined gives the
+// plain warm start.
+void sweep_guess(const Grid& g, std::vector<double>& x, std::vector<double>& prev, int it) {
+  const int n = g.n;
+  if (it >= 2) {
+    std::vector<double> d(n), Ad(n);
+    for (int i = 0; i < n; ++i) d[i] = x[i] - prev[i];
+    op_mul(g, d.data(), Ad.data());
+    double bd = bdot(g.b.data(), d.data(), n), pad = bdot(x.data(), Ad.data(), n), dad = bdot(d.data(), Ad.data(), n);
+    bool singular = true;
+    for (int i = 0; i < n; ++i)
+      if (g.diag[i] != 0.0) {
+        singular = false;
+        break;
+      }
+    if (singular && n > 0) {
+      double sb = 0.0, sd = 0.0;
+      for (int i = 0; i < n; ++i) {
+        sb += g.b[i];
+        sd += d[i];
+      }
+      bd -= sb * sd / n;
+    }
+    double om = dad > 0.0 ? (bd - pad) / dad : 0.0;
+    if (!(om > -2.0 && om < 2.0)) om = 0.0;
+    for (int i = 0; i < n; ++i) {
+      prev[i] = x[i];
+      x[i] += om * d[i];
+    }
+  } else {
+    prev = x;
+  }
+}
+
 // find_pressure! (pressure.jl:215-224).  method 0: MINRES (atol = rtol = tol),
-// method 1: Jacobi-PCG with ||r|| <= tol*||b||.  stats[niter] receives one
-// record per fixed-point sweep.
+// method 1: Jacobi-PCG with ||r|| <= tol*||b||, method 2: the same PCG from
+// the GPU solver's line-searched initial guess (sweep_guess).  stats[niter]
+// receives one record per fixed-point sweep.
 int lvref_find_pressure(void* h, double dt, int niter, const double* vbc, int method, double tol, int itmax,
                         SolveStats* stats) {
   Grid* g = static_cast<Grid*>(h);
   refresh_operator(*g, dt);
+  std::vector<double> prev;
   for (int it = 1; it <= niter; ++it) {
     refresh_rhs(*g, dt, it > 1, vbc);
     std::vector<double> x = g->Psol;
+    if (method == 2) sweep_guess(*g, x, prev, it);
     SolveStats st{};
     if (method == 0)
       minres_solve(*g, g->b, x, tol, tol, itmax, &st);

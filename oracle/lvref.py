@@ -242,10 +242,12 @@ class OracleGrid:
         lib().lvref_operator_apply(self.h, _p(x), _p(y))
         return y
 
-    def find_pressure(self, dt, niter=10, vbc=None, method="pcg", tol=1e-8, itmax=10000):
+    def find_pressure(self, dt, niter=10, vbc=None, method="pcg", tol=1e-8, itmax=10000, guess=False):
+        """guess: with method "pcg", start sweeps >= 2 from the GPU solver's
+        line-searched guess instead of the previous sweep's P."""
         stats = (SolveStats * niter)()
         v = None if vbc is None else np.ascontiguousarray(np.asarray(vbc, np.float64).reshape(8))
-        m = 0 if method == "minres" else 1
+        m = 0 if method == "minres" else (2 if guess else 1)
         lib().lvref_find_pressure(self.h, dt, niter, _p(v), m, tol, itmax, stats)
         return [(s.iterations, s.converged, s.rel_residual) for s in stats]
 

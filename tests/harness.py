@@ -1,5 +1,7 @@
 """Builds matched GPU / oracle grids from the same seeds and applies the
 reference's operations to both."""
+import os
+
 import numpy as np
 
 import workloads as W
@@ -9,6 +11,11 @@ ORDER_FIELDS = ["x", "v", "e", "P", "rho", "c2", "dv", "mass", "momentum", "ener
 
 def seeds(pop, flow, seed=12345, jitter=0.1):
     return pop.jittered_lattice(flow.xlims, flow.ylims, flow.nx, flow.ny, jitter, seed)
+
+
+def sweep_guess_on():
+    """Whether the GPU's find_pressure starts sweeps from the line-searched guess."""
+    return os.environ.get("LVGPU_SWEEP_GUESS", "1") != "0"
 
 
 def make_gpu(lv, flow, x):
@@ -58,7 +65,9 @@ def apply(lv, flow, target, op, kw, is_gpu, solver=None, tol=1e-8):
         vbc = wall_table(flow)
         if is_gpu:
             return lv.find_pressure(solver, dt, 10, boundary_velocity=flow.walls or None)
-        return target.find_pressure(dt, 10, vbc, method="pcg", tol=tol)
+        # the oracle starts the sweeps as the GPU does (line-searched guess
+        # unless LVGPU_SWEEP_GUESS=0)
+        return target.find_pressure(dt, 10, vbc, method="pcg", tol=tol, guess=sweep_guess_on())
     if op == "pressure_step":
         return lv.pressure_step(target, dt) if is_gpu else target.pressure_step(dt)
     if op == "find_D":

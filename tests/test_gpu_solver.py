@@ -129,13 +129,18 @@ def test_pcg_solution(lv, oracle, mk):
     assert np.linalg.norm(d) <= 1e-5 * max(np.linalg.norm(xr - (xr.mean() if singular else 0)), 1e-30)
 
 
+@pytest.mark.parametrize("guess", ["0", "1"])
 @pytest.mark.parametrize("mk", FLOWS)
-def test_find_pressure_sweeps(lv, oracle, mk):
+def test_find_pressure_sweeps(lv, oracle, mk, guess, monkeypatch):
+    """The sweeps match the oracle's sweep for sweep, iteration counts
+    included: with the plain warm start (the previous sweep's P) and with the
+    line-searched guess."""
+    monkeypatch.setenv("LVGPU_SWEEP_GUESS", guess)
     flow = mk()
     g, og = _setup(lv, oracle, flow)
     solver = lv.PressureSolver(g, tol=1e-8)
     st = lv.find_pressure(solver, flow.dt, 10, boundary_velocity=flow.walls or None)
-    ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8)
+    ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8, guess=guess == "1")
     assert all(s[1] for s in st), st
     assert all(s[2] <= 1.5e-8 for s in st), st
     P, Pr = g["P"], og.get("P")
@@ -145,3 +150,30 @@ def test_find_pressure_sweeps(lv, oracle, mk):
     assert np.linalg.norm(P - Pr) <= 1e-5 * np.linalg.norm(Pr)
     for rec, refrec in zip(st, ref):
         assert abs(rec[0] - refrec[0]) <= max(3, 0.05 * refrec[0]), (st, ref)
+
+
+@pytest.mark.parametrize("mk", FLOWS)
+def test_find_pressure_sweep_guess(lv, oracle, mk, monkeypatch):
+    """With the line-searched initial guess (the default) every sweep still
+    meets the FP64 residual 1e-8, P agrees with the oracle's plain sweeps to
+    the solver tolerance, and the sweeps need no more CG iterations in total
+    than with the plain warm start (the guess never increases the A-norm of
+    the initial error; CG's count can still move by an iteration or two)."""
+    flow = mk()
+    runs = {}
+    for guess in ("0", "1"):
+        monkeypatch.setenv("LVGPU_SWEEP_GUESS", guess)
+        g, og = _setup(lv, oracle, flow)
+        solver = lv.PressureSolver(g, tol=1e-8)
+        runs[guess] = (g, og, lv.find_pressure(solver, flow.dt, 10, boundary_velocity=flow.walls or None))
+    g, og, st = runs["1"]
+    ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8)
+    assert all(s[1] for s in st), st
+    assert all(s[2] <= 1.5e-8 for s in st), st
+    P, Pr = g["P"], og.get("P")
+    if flow.name in ("gresho", "cavity"):
+        P, Pr = P - P.mean(), Pr - Pr.mean()
+    assert np.linalg.norm(P - Pr) <= 1e-5 * np.linalg.norm(Pr)
+    it_guess = sum(s[0] for s in st)
+    it_plain = sum(s[0] for s in runs["0"][2])
+    assert it_guess <= 1.02 * it_plain + 2, (it_guess, it_plain, st, runs["0"][2])
