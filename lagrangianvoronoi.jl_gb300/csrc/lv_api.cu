@@ -272,6 +272,10 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.b = dalloc<double>(c, cap, &ok);
   sv.xs = dalloc<double>(c, cap, &ok);
   sv.pprev = dalloc<double>(c, cap, &ok);
+  sv.bprev = dalloc<double>(c, cap, &ok);
+  sv.sgd32 = dalloc<float>(c, cap, &ok);
+  sv.sgpart = dalloc<double>(c, 4 * ((size_t)cap / 256 + 2), &ok);
+  sv.sgomega = dalloc<double>(c, 1, &ok);
   sv.r = dalloc<double>(c, 2 * (size_t)cap, &ok);
   sv.z = dalloc<double>(c, cap, &ok);
   sv.p = dalloc<double>(c, 2 * (size_t)cap, &ok);
@@ -687,7 +691,7 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
   const char* env = getenv("LVGPU_SWEEP_GUESS");
   c->sweep_guess = !(env && env[0] == '0');
   for (int it = 1; it <= niter; ++it) {
-    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1);
+    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1, c->sweep_guess && it > 1);
     if (rc) return rc;
     if (c->sweep_guess) {
       KernelTimer kt(c, LV_KF_RHS);  // prepares the sweep's system, like the right-hand side

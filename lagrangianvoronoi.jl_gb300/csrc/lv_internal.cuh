@@ -94,7 +94,10 @@ struct SolverDev {
   double* w;    // [nnz_cap]
   float* w32;   // FP32 copy for the mixed-precision inner solve
   double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
-  double* pprev;      // pressure before the previous sweep's solve (sweep line search)
+  // initial guess of find_pressure's sweeps (lv_sweep_sums): P and b before
+  // the previous sweep's solve, d = P - prev in FP32, block partials, omega
+  double *pprev, *bprev, *sgpart, *sgomega;
+  float* sgd32;
   float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
   long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
@@ -166,6 +169,76 @@ struct lv_ctx {
   } kev[LV_KF_COUNT];
 };
 
+// Initial guess of find_pressure's sweep k >= 2 (the solve of A P_k = b_k
+// starts from P_{k-1} + omega d, d = P_{k-1} - P_{k-2}): omega is the exact
+// line search in the A-norm of the error, (b_k - A P_{k-1}, d) / (d, A d),
+// with b_k - A P_{k-1} = (b_k - b_{k-1}) + the previous solve's residual,
+// which the solver left below its tolerance and is dropped.  The numerator is
+// summed in FP64, (d, A d) in FP32 (only its relative size matters); for a
+// singular operator b_k - b_{k-1} is taken projected to zero mean.  Called
+// by every thread of the right-hand side's second pass (blockDim.x == 256,
+// one row per thread, `on` = row in range) once b_k is known: block partials
+// into sv.sgpart, the last block to finish adds them in block order and
+// writes omega to *sv.sgomega (counter: zero before, zero again after).
+constexpr int LV_SG_TPB = 256;
+__device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, const double* __restrict__ P, int i, bool on,
+                                              double bi, int n) {
+  const bool singular = sv.iters[LV_IT_NONSINGULAR] == 0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // (db, d) (d, Ad) sum db, sum d
+  if (on) {
+    const double di = P[i] - sv.pprev[i];
+    const double db = bi - sv.bprev[i];
+    const float d32 = sv.sgd32[i];
+    float ad = sv.d32[i] * d32;
+    const int e0 = sv.rowptr[i], e1 = sv.rowptr[i + 1];
+    for (int e = e0; e < e1; ++e) ad = ad + sv.w32[e] * (d32 - sv.sgd32[sv.col[e]]);
+    acc[0] = db * di;
+    acc[1] = (double)(d32 * ad);
+    acc[2] = db;
+    acc[3] = di;
+  }
+  __shared__ double sh[4][LV_SG_TPB / 32];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nsum = singular ? 4 : 2;
+  for (int q = 0; q < nsum; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[q][wid] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nsum) {
+    double v = 0.0;
+    for (int k = 0; k < LV_SG_TPB / 32; ++k) v += sh[threadIdx.x][k];
+    sv.sgpart[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  unsigned* counter = sv.bar + 3;
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int q = 0; q < nsum; ++q) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += LV_SG_TPB) v += __ldcg(sv.sgpart + (size_t)q * gridDim.x + b);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[q][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < nsum; ++q)
+      for (int k = 0; k < LV_SG_TPB / 32; ++k) tot[q] += sh[q][k];
+    double num = tot[0];
+    if (singular) num -= tot[2] * tot[3] / (double)n;
+    double om = tot[1] > 0.0 ? num / tot[1] : 0.0;
+    if (!(om > -2.0 && om < 2.0)) om = 0.0;  // also NaN
+    *sv.sgomega = om;
+    *counter = 0u;
+  }
+}
+
 // Brackets the launches of one kernel family with CUDA events when kernel
 // timing is on (lv_api.cu).
 struct KernelTimer {
@@ -194,7 +267,8 @@ int lv_phys_friction(lv_ctx* c, const double* vwall, double dt);
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
 // prepare = 1 evaluates the sweep-invariant terms (first sweep of find_pressure!)
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare);
+// guess != 0: also the sums of the sweep's initial guess (sweep >= 2)
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess = 0);
 int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
 
 // ---- learned preconditioner (lv_learn.cu)

@@ -148,12 +148,15 @@ __global__ void k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt
 }
 
 // refresh! first loop (pressure.jl:167-186) with the fixed terms of k_rhs_prep
-__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt) {
+// guess != 0: also d = P - pprev in FP32 for the sweep's initial guess
+// (lv_sweep_sums)
+__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   const double2 xi = s.x[i];
   const double Pi = s.P[i];
+  if (guess) sv.sgd32[i] = (float)(Pi - sv.pprev[i]);
   double bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
   double gpx = 0.0, gpy = 0.0;
   for (int k = 0; k < nf; ++k) {
@@ -179,21 +182,27 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt) {
 }
 
 // refresh! second loop (pressure.jl:189-201): explicit part of the Laplacian.
-__global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n) {
+// guess != 0: then the sums of the sweep's initial guess (lv_sweep_sums; all
+// threads of the block take part, so rows past n do not return early).
+__global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int cap = m.cap, nf = m.nfaces[i];
-  const double2 gi = s.GP[i];
-  double bi = sv.b[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 dmz = sv.rhs_dmz[f];
-    const double2 gj = s.GP[j];
-    bi += lrr * ((gi.x - gj.x) * dmz.x + (gi.y - gj.y) * dmz.y);
+  const bool on = i < n;
+  double bi = 0.0;
+  if (on) {
+    const int cap = m.cap, nf = m.nfaces[i];
+    const double2 gi = s.GP[i];
+    bi = sv.b[i];
+    for (int k = 0; k < nf; ++k) {
+      const size_t f = (size_t)k * cap + i;
+      const int j = m.fnbr[f];
+      const double lrr = m.flrr[f];
+      const double2 dmz = sv.rhs_dmz[f];
+      const double2 gj = s.GP[j];
+      bi += lrr * ((gi.x - gj.x) * dmz.x + (gi.y - gj.y) * dmz.y);
+    }
+    sv.b[i] = bi;
   }
-  sv.b[i] = bi;
+  if (guess) lv_sweep_sums(sv, s.P, i, on, bi, n);
 }
 
 // ---------------------------------------------------------- viscosity, D
@@ -613,7 +622,7 @@ int lv_phys_pressure_step(lv_ctx* c, double dt) {
   return LV_OK;
 }
 
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare) {
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess) {
   if (int rc = need_mesh(c)) return rc;
   if (prepare) {
     double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -624,8 +633,10 @@ int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepar
     double4 rl = make_double4(w[2], w[3], w[6], w[7]);
     LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl);
   }
-  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt);
-  if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n);
+  static_assert(TPB == LV_SG_TPB, "the sweep-guess sums assume 256 threads per block");
+  guess = guess && gp_step;  // the guess sums ride on the second pass (sweeps >= 2)
+  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt, guess);
+  if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n, guess);
   return LV_OK;
 }
 

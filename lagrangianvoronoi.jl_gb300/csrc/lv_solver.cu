@@ -885,6 +885,10 @@ int lv_solver_assemble(lv_ctx* c, double dt) {
   LV_LAUNCH_CHECK(c, "k_half_rho");
   k_assemble<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s, c->m, c->sv, n, dt, hr);
   LV_LAUNCH_CHECK(c, "k_assemble");
+  // FP32 copies of the operator (the streaming mixed solver, the sweep guess)
+  k_to_f32<<<lv_blocks(n, TPB), TPB, 0, s>>>(n, c->sv.rowptr, c->sv.w, c->sv.diag, c->sv.dinv, c->sv.w32, c->sv.d32,
+                                              c->sv.dinv32);
+  LV_LAUNCH_CHECK(c, "k_to_f32");
   // singular operator <=> every diagonal term is zero (c2 = Inf everywhere)
   cudaMemsetAsync(c->sv.iters + LV_IT_NONSINGULAR, 0, sizeof(int), s);
   k_any_nonzero<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->sv.diag, n, c->sv.iters + LV_IT_NONSINGULAR);
@@ -905,129 +909,25 @@ int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev) {
 // ---------------------------------------------------------------- sweep guess
 //
 // find_pressure's sweeps solve A P_k = b_k with the same operator and a
-// right-hand side that follows P; each solve starts from the previous sweep's
-// P.  Before sweep k >= 2 the start is moved along d = P_{k-1} - P_{k-2} by
-// the exact line search in the A-norm of the error,
-//   omega = (b_k - A P_{k-1}, d) / (d, A d),
-// which never increases that error (omega = 0 is the plain warm start).  The
-// solution the solver returns is the same to its tolerance.  b is taken
-// projected to zero mean when the operator is singular (the solver solves
-// with the projected b).  The five sums run in a fixed order, so the guess is
-// reproducible.
-constexpr int SG_BLOCKS = 256, SG_TPB = 256, SG_SUMS = 5;
+// right-hand side that follows P.  Sweep k >= 2 starts from P_{k-1} + omega
+// (P_{k-1} - P_{k-2}), omega from lv_sweep_sums (the right-hand side's second
+// pass); every sweep then saves P and b for the next one.
 
-// The five sums (b,d) (P,Ad) (d,Ad) sum b, sum d (the last two only for a
-// singular operator), block partials into part; the last block to finish
-// adds the partials in block order and writes omega to part[SG_SUMS *
-// SG_BLOCKS] (counter: zero before the launch, zero again after it).
-// d = P - prev (FP64), stored so that the row pass gathers one value per
-// neighbour
-__global__ void k_sweep_diff(int n, const double* __restrict__ P, const double* __restrict__ prev, double* d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) d[i] = P[i] - prev[i];
-}
-
-constexpr int SG_UNROLL = 8;  // neighbours whose loads are issued together
-
-__global__ void __launch_bounds__(SG_TPB) k_sweep_dots(int n, const int* __restrict__ rowptr,
-                                                       const int* __restrict__ col, const double* __restrict__ w,
-                                                       const double* __restrict__ diag, const double* __restrict__ b,
-                                                       const double* __restrict__ P,
-                                                       const double* __restrict__ d, const int* nonsingular,
-                                                       double* part, unsigned* counter) {
-  const bool singular = *nonsingular == 0;
-  double acc[SG_SUMS] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int i = blockIdx.x * SG_TPB + threadIdx.x; i < n; i += SG_BLOCKS * SG_TPB) {
-    const double di = d[i];
-    double ad = diag[i] * di;
-    const int e0 = rowptr[i], e1 = rowptr[i + 1];
-    for (int e = e0; e < e1; e += SG_UNROLL) {
-      double wv[SG_UNROLL], dj[SG_UNROLL];
-#pragma unroll
-      for (int u = 0; u < SG_UNROLL; ++u) {
-        const bool in = e + u < e1;
-        wv[u] = in ? w[e + u] : 0.0;
-        dj[u] = in ? d[col[e + u]] : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < SG_UNROLL; ++u)
-        if (e + u < e1) ad += wv[u] * (di - dj[u]);
-    }
-    acc[0] += b[i] * di;
-    acc[1] += P[i] * ad;
-    acc[2] += di * ad;
-    if (singular) {
-      acc[3] += b[i];
-      acc[4] += di;
-    }
-  }
-  __shared__ double sh[SG_SUMS][SG_TPB / 32];
-  __shared__ bool s_last;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nsum = singular ? SG_SUMS : 3;
-  for (int q = 0; q < nsum; ++q) {
-    double v = acc[q];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[q][wid] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < nsum) {
-    double v = 0.0;
-    for (int k = 0; k < SG_TPB / 32; ++k) v += sh[threadIdx.x][k];
-    part[threadIdx.x * SG_BLOCKS + blockIdx.x] = v;
-    __threadfence();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == SG_BLOCKS - 1;
-  __syncthreads();
-  if (!s_last) return;
-  // the last block: every block's partials, in block order
-  __threadfence();
-  static_assert(SG_TPB == SG_BLOCKS, "one partial per thread");
-  for (int q = 0; q < nsum; ++q) {
-    double v = __ldcg(part + q * SG_BLOCKS + threadIdx.x);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[q][wid] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double tot[SG_SUMS] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int q = 0; q < nsum; ++q)
-      for (int k = 0; k < SG_TPB / 32; ++k) tot[q] += sh[q][k];
-    double bd = tot[0];
-    if (singular) bd -= tot[3] * tot[4] / (double)n;
-    const double dad = tot[2];
-    double om = (dad > 0.0) ? (bd - tot[1]) / dad : 0.0;
-    if (!(om > -2.0 && om < 2.0)) om = 0.0;  // also NaN
-    part[SG_SUMS * SG_BLOCKS] = om;
-    *counter = 0u;
-  }
-}
-
-// P <- P + omega d (shift != 0), prev <- P (before the update)
-__global__ void k_sweep_apply(int n, double* P, double* prev, const double* __restrict__ d, const double* omega,
-                              int shift) {
+// P <- P + omega (P - prev) (shift != 0); prev <- P, bprev <- b (before the update)
+__global__ void k_sweep_apply(int n, double* P, double* prev, double* bprev, const double* __restrict__ b,
+                              const double* omega, int shift) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double p = P[i];
-  if (shift) P[i] = p + *omega * d[i];
+  if (shift) P[i] = p + *omega * (p - prev[i]);
   prev[i] = p;
+  bprev[i] = b[i];
 }
 
 int lv_solver_sweep_guess(lv_ctx* c, double* P, int it) {
   if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
   const int n = c->n;
-  double* d = c->sv.q;  // scratch between solves
-  if (it >= 2) {
-    k_sweep_diff<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, d);
-    LV_LAUNCH_CHECK(c, "k_sweep_diff");
-    k_sweep_dots<<<SG_BLOCKS, SG_TPB, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, c->sv.w, c->sv.diag, c->sv.b, P, d,
-                                                      c->sv.iters + LV_IT_NONSINGULAR, c->sv.part, c->sv.bar + 3);
-    LV_LAUNCH_CHECK(c, "k_sweep_dots");
-  }
-  k_sweep_apply<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, d, c->sv.part + SG_SUMS * SG_BLOCKS,
+  k_sweep_apply<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, c->sv.bprev, c->sv.b, c->sv.sgomega,
                                                           it >= 2 ? 1 : 0);
   LV_LAUNCH_CHECK(c, "k_sweep_apply");
   return LV_OK;
@@ -1098,10 +998,7 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
       la.out_outer = c->sv.iters + LV_IT_OUTER + slot;
       la.out_method = c->sv.iters + LV_IT_METHOD + slot;
       la.learned = learned ? 1 : 0;
-      StreamArgs sa;
-      k_to_f32<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, c->sv.rowptr, c->sv.w, c->sv.diag, c->sv.dinv, c->sv.w32,
-                                                           c->sv.d32, c->sv.dinv32);
-      c->launches++;
+      StreamArgs sa;  // the FP32 copies were made when the operator was assembled
       sa.w32 = c->sv.w32;
       sa.dg32 = c->sv.d32;
       sa.dinv32 = c->sv.dinv32;

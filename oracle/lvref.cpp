@@ -1183,17 +1183,22 @@ int lvref_operator_apply(void* h, const double* xin, double* y) {
 
 // The GPU solver's initial guess of sweep it >= 2 (not part of the
 // reference, whose MINRES starts from the previous sweep's P): the previous
-// solution moved along d = P_{it-1} - P_{it-2} by the exact A-norm line
-// search omega = (b - A P, d) / (d, A d), with b projected to zero mean when
-// the operator is singular; omega outside (-2, 2) or undefined gives the
-// plain warm start.
-void sweep_guess(const Grid& g, std::vector<double>& x, std::vector<double>& prev, int it) {
+// solution moved along d = P_{it-1} - P_{it-2} by omega = (b_it - b_{it-1},
+// d) / (d, A d), the exact A-norm line search up to the previous solve's
+// residual, with b_it - b_{it-1} projected to zero mean when the operator is
+// singular; omega outside (-2, 2) or undefined gives the plain warm start.
+// prev and bprev receive P and b of this sweep.
+void sweep_guess(const Grid& g, std::vector<double>& x, std::vector<double>& prev, std::vector<double>& bprev,
+                 int it) {
   const int n = g.n;
   if (it >= 2) {
-    std::vector<double> d(n), Ad(n);
-    for (int i = 0; i < n; ++i) d[i] = x[i] - prev[i];
+    std::vector<double> d(n), Ad(n), db(n);
+    for (int i = 0; i < n; ++i) {
+      d[i] = x[i] - prev[i];
+      db[i] = g.b[i] - bprev[i];
+    }
     op_mul(g, d.data(), Ad.data());
-    double bd = bdot(g.b.data(), d.data(), n), pad = bdot(x.data(), Ad.data(), n), dad = bdot(d.data(), Ad.data(), n);
+    double num = bdot(db.data(), d.data(), n), den = bdot(d.data(), Ad.data(), n);
     bool singular = true;
     for (int i = 0; i < n; ++i)
       if (g.diag[i] != 0.0) {
@@ -1203,20 +1208,19 @@ void sweep_guess(const Grid& g, std::vector<double>& x, std::vector<double>& pre
     if (singular && n > 0) {
       double sb = 0.0, sd = 0.0;
       for (int i = 0; i < n; ++i) {
-        sb += g.b[i];
+        sb += db[i];
         sd += d[i];
       }
-      bd -= sb * sd / n;
+      num -= sb * sd / n;
     }
-    double om = dad > 0.0 ? (bd - pad) / dad : 0.0;
+    double om = den > 0.0 ? num / den : 0.0;
     if (!(om > -2.0 && om < 2.0)) om = 0.0;
-    for (int i = 0; i < n; ++i) {
-      prev[i] = x[i];
-      x[i] += om * d[i];
-    }
+    prev = x;
+    for (int i = 0; i < n; ++i) x[i] += om * d[i];
   } else {
     prev = x;
   }
+  bprev = g.b;
 }
 
 // find_pressure! (pressure.jl:215-224).  method 0: MINRES (atol = rtol = tol),
@@ -1227,11 +1231,11 @@ int lvref_find_pressure(void* h, double dt, int niter, const double* vbc, int me
                         SolveStats* stats) {
   Grid* g = static_cast<Grid*>(h);
   refresh_operator(*g, dt);
-  std::vector<double> prev;
+  std::vector<double> prev, bprev;
   for (int it = 1; it <= niter; ++it) {
     refresh_rhs(*g, dt, it > 1, vbc);
     std::vector<double> x = g->Psol;
-    if (method == 2) sweep_guess(*g, x, prev, it);
+    if (method == 2) sweep_guess(*g, x, prev, bprev, it);
     SolveStats st{};
     if (method == 0)
       minres_solve(*g, g->b, x, tol, tol, itmax, &st);
