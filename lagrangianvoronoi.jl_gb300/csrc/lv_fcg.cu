@@ -611,14 +611,16 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
 // two-hop neighbours), j over the pattern of row k (k, its lower neighbours
 // and lower two-hop neighbours).  Two hops of Gt give M^-1 two (one-hop
 // pattern) or four (two-hop pattern) hops.
+// only: rows whose flag is set (nullptr: every row)
 __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                              const float* __restrict__ gd, const float* __restrict__ gl, const int* __restrict__ rev,
                              const int* __restrict__ rowptr2, const int* __restrict__ col2,
                              const float* __restrict__ gl2, const int* __restrict__ rev2,
                              const float* __restrict__ dh, float eps, int stride, int* mcnt, int* mcol, float* mval,
-                             float* mdiag, int* ok) {
+                             float* mdiag, int* ok, const int* __restrict__ only) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (only && !only[i]) return;
   int cols[MMAX];
   float vals[MMAX];
   int m = 0;
@@ -877,6 +879,77 @@ __global__ void __launch_bounds__(STG_BUILD_TPB) k_stage_build(int n, int rpb, c
   }
 }
 
+// The one-hop M^-1 rows with the entries in registers (up to MREG, compared
+// and placed by unrolled loops instead of a local-memory array); the same
+// entries, values and order as k_build_minv.  A row with more entries is
+// flagged in `over` and built by k_build_minv afterwards.
+constexpr int MREG = 24;
+__global__ void __launch_bounds__(128) k_build_minv_reg(int n, const int* __restrict__ rowptr,
+                                                        const int* __restrict__ col, const float* __restrict__ gd,
+                                                        const float* __restrict__ gl, const int* __restrict__ rev,
+                                                        const float* __restrict__ dh, float eps, int stride, int* mcnt,
+                                                        int* mcol, float* mval, float* mdiag, int* over) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int cols[MREG];
+  float vals[MREG];
+#pragma unroll
+  for (int s = 0; s < MREG; ++s) {
+    cols[s] = -1;
+    vals[s] = 0.f;
+  }
+  int m = 0;
+  float dsum = 0.f;
+  bool full = false;
+  auto add = [&](int j, float v) {
+    if (j == i) {
+      dsum += v;
+      return;
+    }
+    bool found = false;
+#pragma unroll
+    for (int s = 0; s < MREG; ++s)
+      if (cols[s] == j) {
+        vals[s] += v;
+        found = true;
+      }
+    if (!found) {
+      if (m < MREG) {
+#pragma unroll
+        for (int s = 0; s < MREG; ++s)
+          if (s == m) {
+            cols[s] = j;
+            vals[s] = v;
+          }
+        ++m;
+      } else {
+        full = true;
+      }
+    }
+  };
+  auto row_k = [&](int k, float gki) {
+    add(k, gki * gd[k]);
+    for (int k2 = rowptr[k]; k2 < rowptr[k + 1]; ++k2)
+      if (col[k2] < k) add(col[k2], gki * gl[k2]);
+  };
+  row_k(i, gd[i]);
+  for (int kk = rowptr[i]; kk < rowptr[i + 1]; ++kk) {
+    const int u = col[kk];
+    if (u > i && rev[kk] >= 0) row_k(u, gl[rev[kk]]);
+  }
+  over[i] = full ? 1 : 0;
+  if (full) return;
+  const float di = dh[i];
+#pragma unroll
+  for (int s = 0; s < MREG; ++s)
+    if (s < m) {
+      mcol[(size_t)s * stride + i] = cols[s];
+      mval[(size_t)s * stride + i] = di * vals[s] * dh[cols[s]];
+    }
+  mcnt[i] = m;
+  mdiag[i] = di * (dsum + eps) * di;
+}
+
 int g_fcg_blocks_per_sm[2] = {-1, -1};
 int g_fcg_halo_blocks_per_sm[2] = {-1, -1};
 
@@ -1006,10 +1079,24 @@ int lv_fcg_build_minv(lv_ctx* c) {
   if (!gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
   const int one = 1;
   cudaMemcpyAsync(c->sv.mok, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
-  k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, rowptr2, col2, gl2,
-                                                          rev2, dh, c->learn_eps, c->sv.mrows, c->sv.mcnt,
-                                                          c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok);
-  LV_LAUNCH_CHECK(c, "k_build_minv");
+  if (rowptr2) {
+    k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, rowptr2, col2,
+                                                            gl2, rev2, dh, c->learn_eps, c->sv.mrows, c->sv.mcnt,
+                                                            c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok, nullptr);
+    LV_LAUNCH_CHECK(c, "k_build_minv");
+  } else {
+    // rows of up to MREG entries in registers, the rest (flagged) as before
+    int* over = c->sv.remap;  // scratch: the staged image build rewrites it below
+    k_build_minv_reg<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, dh,
+                                                                c->learn_eps, c->sv.mrows, c->sv.mcnt, c->sv.mcol,
+                                                                c->sv.mval, c->sv.mdiag, over);
+    LV_LAUNCH_CHECK(c, "k_build_minv_reg");
+    k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, nullptr, nullptr,
+                                                            nullptr, nullptr, dh, c->learn_eps, c->sv.mrows,
+                                                            c->sv.mcnt, c->sv.mcol, c->sv.mval, c->sv.mdiag,
+                                                            c->sv.mok, over);
+    LV_LAUNCH_CHECK(c, "k_build_minv");
+  }
   // the staged image of every solve block, for the shape lv_fcg_solve
   // launches; the host learns whether every image fit (one synchronisation
   // per factor)

@@ -219,14 +219,47 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
 #pragma unroll
   for (int f = 0; f < FH; ++f) own[f] = 0.f;
   if (row < n) {
-    const float* hr = Hin + (size_t)row * KH + half * FH;
+    static_assert(FH % 4 == 0, "16-byte feature chunks");
+    const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
 #pragma unroll
-    for (int f = 0; f < FH; ++f) own[f] = hr[f];
-    for (int k = rowptr[row]; k < rowptr[row + 1]; ++k) {
-      const float wv = what[k];
-      const float* hj = Hin + (size_t)col[k] * KH + half * FH;
+    for (int f = 0; f < FH / 4; ++f) {
+      const float4 v = hr[f];
+      own[4 * f] = v.x;
+      own[4 * f + 1] = v.y;
+      own[4 * f + 2] = v.z;
+      own[4 * f + 3] = v.w;
+    }
+    // two neighbours per round, their loads issued together; the sum runs
+    // over the neighbours in order
+    const int k1 = rowptr[row + 1];
+    for (int k = rowptr[row]; k < k1; k += 2) {
+      const bool two = k + 1 < k1;
+      const int ja = col[k], jb = two ? col[k + 1] : ja;
+      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
+      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
+      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
+      float4 va[FH / 4], vb[FH / 4];
 #pragma unroll
-      for (int f = 0; f < FH; ++f) agg[f] = fmaf(wv, hj[f], agg[f]);
+      for (int f = 0; f < FH / 4; ++f) {
+        va[f] = ha[f];
+        vb[f] = hb[f];
+      }
+#pragma unroll
+      for (int f = 0; f < FH / 4; ++f) {
+        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
+        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
+        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
+        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
+      }
+      if (two) {
+#pragma unroll
+        for (int f = 0; f < FH / 4; ++f) {
+          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
+          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
+          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
+          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
+        }
+      }
     }
   }
   float* t = tile + r * (2 * KH);
