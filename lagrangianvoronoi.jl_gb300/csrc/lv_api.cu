@@ -274,8 +274,10 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.pprev = dalloc<double>(c, cap, &ok);
   sv.bprev = dalloc<double>(c, cap, &ok);
   sv.sgd32 = dalloc<float>(c, cap, &ok);
-  sv.sgpart = dalloc<double>(c, 4 * ((size_t)cap / 256 + 2), &ok);
-  sv.sgomega = dalloc<double>(c, 1, &ok);
+  sv.sgpart = dalloc<double>(c, LV_SG_SUMS * ((size_t)cap / 256 + 2), &ok);
+  sv.sgomega = dalloc<double>(c, 2, &ok);
+  sv.dinc = nullptr;
+  sv.dinc_slots = 0;
   sv.r = dalloc<double>(c, 2 * (size_t)cap, &ok);
   sv.z = dalloc<double>(c, cap, &ok);
   sv.p = dalloc<double>(c, 2 * (size_t)cap, &ok);
@@ -318,6 +320,7 @@ int lv_destroy(lv_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   lv_learn_free(c);
   lv_fcg_free(c);
+  cudaFree(c->sv.dinc);
   for (void* p : c->allocs) cudaFree(p);
   if (c->status_host) cudaFreeHost(c->status_host);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -690,16 +693,40 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
   if (rc) return rc;
   const char* env = getenv("LVGPU_SWEEP_GUESS");
   c->sweep_guess = !(env && env[0] == '0');
+  SolverDev& sv = c->sv;
+  if (c->sweep_guess && niter > sv.dinc_slots) {
+    // one FP32 vector per sweep for the sweeps' changes (kept for the next call)
+    cudaFree(sv.dinc);
+    sv.dinc = nullptr;
+    sv.dinc_slots = 0;
+    c->sg_valid = 0;
+    if (cudaMalloc(&sv.dinc, sizeof(float) * (size_t)niter * c->cap) != cudaSuccess)
+      return lv_fail(c, LV_ERR_CUDA, "allocation of the sweep-guess history failed");
+    sv.dinc_slots = niter;
+  }
+  if (c->sg_n != c->n) c->sg_valid = 0;
+  const size_t cap = (size_t)c->cap;
   for (int it = 1; it <= niter; ++it) {
-    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1, c->sweep_guess && it > 1);
+    // the previous call's change of this sweep, while it is still there
+    const float* D = (c->sweep_guess && it <= c->sg_valid) ? sv.dinc + (size_t)(it - 1) * cap : nullptr;
+    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1, c->sweep_guess ? 1 : 0, D);
     if (rc) return rc;
     if (c->sweep_guess) {
       KernelTimer kt(c, LV_KF_RHS);  // prepares the sweep's system, like the right-hand side
-      rc = lv_solver_sweep_guess(c, c->s.P, it);
+      // this call's change of the previous sweep replaces the old one
+      float* store = it >= 2 ? sv.dinc + (size_t)(it - 2) * cap : nullptr;
+      rc = lv_solver_sweep_guess(c, c->s.P, it, D, store);
       if (rc) return rc;
     }
     rc = lv_solver_solve(c, c->s.P, nullptr, it - 1);
     if (rc) return rc;
+  }
+  if (c->sweep_guess && niter >= 1) {
+    KernelTimer kt(c, LV_KF_RHS);
+    rc = lv_solver_sweep_store(c, c->s.P, sv.dinc + (size_t)(niter - 1) * cap);
+    if (rc) return rc;
+    c->sg_valid = niter;
+    c->sg_n = c->n;
   }
   if (stats) {
     rc = lv_solver_fetch_stats(c, stats, niter);

@@ -71,6 +71,7 @@ struct StageImage {
   unsigned short pridx[STG_PMAX];  // per position: the row's r in the staging
   unsigned short puidx[STG_PMAX];  // per position: the row's u in shared memory
   unsigned char pm[STG_PMAX];      // per position: off-diagonal entries
+  int hrow[FCG_HMAX];              // halo rows (global) by halo slot, for the FP64 residual
   float sval[STG_ENTRIES];
   unsigned short sidx[STG_ENTRIES];
 };
@@ -522,12 +523,53 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     }
     double r64[R];
     double v[2] = {0.0, 0.0}, t2[2];
+    if constexpr (HALO) {
+      // x of the own rows and of the halo in shared memory (the float
+      // staging is free between iterations), gathered like u
+      double* xo = reinterpret_cast<double*>(ss.u);
+      double* xh = reinterpret_cast<double*>(ss.r);
+      static_assert(sizeof(ss.u) >= sizeof(double) * FCG_RPB_MAX && sizeof(ss.r) >= sizeof(double) * FCG_HMAX,
+                    "FP64 staging fits the float staging");
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        if (rr.on[k]) xo[threadIdx.x + k * FCG_TPB] = x[k];
+      const int nh = ss.img.nh;
+      double xv[FCG_HMAX / FCG_TPB];
+#pragma unroll
+      for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
+        const int h = threadIdx.x + q * FCG_TPB;
+        xv[q] = h < nh ? __ldcg(a.x + ss.img.hrow[h]) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
+        const int h = threadIdx.x + q * FCG_TPB;
+        if (h < nh) xh[h] = xv[q];
+      }
+      __syncthreads();
+    }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       double acc = 0.0;
       if (rr.on[k]) {
         acc = a.diag[rr.i[k]] * x[k];
-        for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) acc += a.w[e] * (x[k] - __ldcg(a.x + a.col[e]));
+        if constexpr (HALO) {
+          // columns remapped to own rows (< rows_per_block) and halo slots
+          const double* xo = reinterpret_cast<const double*>(ss.u);
+          const double* xh = reinterpret_cast<const double*>(ss.r);
+          const int rpb = a.rows_per_block;
+#pragma unroll
+          for (int e = 0; e < FKR; ++e)
+            if (e < rr.cnt[k]) {
+              const int cc = rr.cc[k][e];
+              acc += a.w[rr.beg[k] + e] * (x[k] - (cc < rpb ? xo[cc] : xh[cc - rpb]));
+            }
+          for (int e = FKR; e < rr.cnt[k]; ++e) {
+            const int cc = a.remap[rr.beg[k] + e];
+            acc += a.w[rr.beg[k] + e] * (x[k] - (cc < rpb ? xo[cc] : xh[cc - rpb]));
+          }
+        } else {
+          for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) acc += a.w[e] * (x[k] - __ldcg(a.x + a.col[e]));
+        }
       }
       r64[k] = rr.on[k] ? rr.bb[k] - acc : 0.0;
       v[0] += r64[k] * r64[k];
@@ -834,6 +876,7 @@ __global__ void __launch_bounds__(STG_BUILD_TPB) k_stage_build(int n, int rpb, c
   };
   for (int h = t; h < STG_HASH; h += STG_BUILD_TPB)
     if (keys[h] >= 0) im.ext[esl[h]] = keys[h];
+  for (int x = t; x < nh; x += STG_BUILD_TPB) im.hrow[x] = hrow[x];
   for (int q = t; q < npos; q += STG_BUILD_TPB) {
     const int p = prow[q];
     const int i = pos_row(p);

@@ -95,9 +95,12 @@ struct SolverDev {
   float* w32;   // FP32 copy for the mixed-precision inner solve
   double *diag, *adiag, *dinv, *b, *xs, *r, *z, *p, *q, *tmp;
   // initial guess of find_pressure's sweeps (lv_sweep_sums): P and b before
-  // the previous sweep's solve, d = P - prev in FP32, block partials, omega
+  // the previous sweep's solve, d1 = P - pprev in FP32, block partials, the
+  // coefficients c1, c2; dinc: the change of each sweep of the last call
+  // (FP32, sweeps x cap, allocated with the first call that uses it)
   double *pprev, *bprev, *sgpart, *sgomega;
-  float* sgd32;
+  float *sgd32, *dinc;
+  int dinc_slots;
   float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
   long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
@@ -150,7 +153,9 @@ struct lv_ctx {
   double* mp_buf = nullptr;  // multiphase projection vectors (allocated on first use)
   LearnState* learn = nullptr;
   bool factor_valid = false;  // learned factor matches the assembled operator and parameters
-  bool sweep_guess = true;  // line search of the sweep's initial guess (LVGPU_SWEEP_GUESS=0 turns it off)
+  bool sweep_guess = true;  // Galerkin initial guess of the sweeps (LVGPU_SWEEP_GUESS=0 turns it off)
+  int sg_valid = 0;         // sweeps of the last find_pressure whose changes sv.dinc holds
+  int sg_n = 0;             // the particle count they belong to
   bool fcg_halo = true;  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
@@ -169,38 +174,54 @@ struct lv_ctx {
   } kev[LV_KF_COUNT];
 };
 
-// Initial guess of find_pressure's sweep k >= 2 (the solve of A P_k = b_k
-// starts from P_{k-1} + omega d, d = P_{k-1} - P_{k-2}): omega is the exact
-// line search in the A-norm of the error, (b_k - A P_{k-1}, d) / (d, A d),
-// with b_k - A P_{k-1} = (b_k - b_{k-1}) + the previous solve's residual,
-// which the solver left below its tolerance and is dropped.  The numerator is
-// summed in FP64, (d, A d) in FP32 (only its relative size matters); for a
-// singular operator b_k - b_{k-1} is taken projected to zero mean.  Called
-// by every thread of the right-hand side's second pass (blockDim.x == 256,
-// one row per thread, `on` = row in range) once b_k is known: block partials
-// into sv.sgpart, the last block to finish adds them in block order and
-// writes omega to *sv.sgomega (counter: zero before, zero again after).
+// Initial guess of find_pressure's sweep k: the solve of A P_k = b_k starts
+// from P + c1 d1 + c2 D, the Galerkin projection of its error onto the span
+// of two directions in the A-norm (exact minimisation of that error over the
+// span; c = 0 is the plain warm start from P):
+//   d1 = P - pprev, the last sweep's change (sweeps k >= 2);
+//   D  = the change of sweep k in the previous call (sweeps the previous call
+//        ran; the sweeps of consecutive time steps follow similar paths).
+// The residual of the start is res = b_k - A P: for k >= 2 it equals
+// (b_k - b_{k-1}) + the previous solve's residual, which the solver left
+// below its tolerance and is dropped; for k = 1 (a new operator) it is
+// evaluated.  For a singular operator res is taken projected to zero mean.
+// (res, d1) and (res, D) are summed in FP64, the Gram entries (d, A d) in
+// FP32 (only their relative size matters).  Called by every thread of the
+// right-hand side's pass (blockDim.x == 256, `on` = row in range): block
+// partials into sv.sgpart, the last block to finish adds them in block order
+// and writes c1, c2 to sv.sgomega[0..1] (counter: zero before, zero after).
 constexpr int LV_SG_TPB = 256;
-__device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, const double* __restrict__ P, int i, bool on,
-                                              double bi, int n) {
+constexpr int LV_SG_SUMS = 8;
+__device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, int i, bool on, double res, double d1,
+                                              const float* __restrict__ D, bool has1, bool has2, int n) {
   const bool singular = sv.iters[LV_IT_NONSINGULAR] == 0;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // (db, d) (d, Ad) sum db, sum d
+  // (res,d1) (res,D) (d1,Ad1) (d1,AD) (D,AD) sum res, sum d1, sum D
+  double acc[LV_SG_SUMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   if (on) {
-    const double di = P[i] - sv.pprev[i];
-    const double db = bi - sv.bprev[i];
-    const float d32 = sv.sgd32[i];
-    float ad = sv.d32[i] * d32;
+    const float f1 = has1 ? sv.sgd32[i] : 0.f;
+    const float f2 = has2 ? D[i] : 0.f;
+    const float dg = sv.d32[i];
+    float a1 = dg * f1, a2 = dg * f2;
     const int e0 = sv.rowptr[i], e1 = sv.rowptr[i + 1];
-    for (int e = e0; e < e1; ++e) ad = ad + sv.w32[e] * (d32 - sv.sgd32[sv.col[e]]);
-    acc[0] = db * di;
-    acc[1] = (double)(d32 * ad);
-    acc[2] = db;
-    acc[3] = di;
+    for (int e = e0; e < e1; ++e) {
+      const int j = sv.col[e];
+      const float w = sv.w32[e];
+      if (has1) a1 = a1 + w * (f1 - sv.sgd32[j]);
+      if (has2) a2 = a2 + w * (f2 - D[j]);
+    }
+    acc[0] = res * d1;
+    acc[1] = res * (double)f2;
+    acc[2] = (double)(f1 * a1);
+    acc[3] = (double)(f1 * a2);
+    acc[4] = (double)(f2 * a2);
+    acc[5] = res;
+    acc[6] = d1;
+    acc[7] = (double)f2;
   }
-  __shared__ double sh[4][LV_SG_TPB / 32];
+  __shared__ double sh[LV_SG_SUMS][LV_SG_TPB / 32];
   __shared__ bool s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int nsum = singular ? 4 : 2;
+  const int nsum = singular ? LV_SG_SUMS : 5;
   for (int q = 0; q < nsum; ++q) {
     double v = acc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -227,14 +248,29 @@ __device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, const double*
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double tot[4] = {0.0, 0.0, 0.0, 0.0};
+    double t[LV_SG_SUMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int q = 0; q < nsum; ++q)
-      for (int k = 0; k < LV_SG_TPB / 32; ++k) tot[q] += sh[q][k];
-    double num = tot[0];
-    if (singular) num -= tot[2] * tot[3] / (double)n;
-    double om = tot[1] > 0.0 ? num / tot[1] : 0.0;
-    if (!(om > -2.0 && om < 2.0)) om = 0.0;  // also NaN
-    *sv.sgomega = om;
+      for (int k = 0; k < LV_SG_TPB / 32; ++k) t[q] += sh[q][k];
+    double r1 = t[0], r2 = t[1];
+    if (singular) {
+      r1 -= t[5] * t[6] / (double)n;
+      r2 -= t[5] * t[7] / (double)n;
+    }
+    const double a11 = t[2], a12 = t[3], a22 = t[4];
+    double c1 = 0.0, c2 = 0.0;
+    const bool u1 = has1 && a11 > 0.0, u2 = has2 && a22 > 0.0;
+    const double det = a11 * a22 - a12 * a12;
+    if (u1 && u2 && det > 1e-6 * a11 * a22) {  // else a nearly dependent pair
+      c1 = (r1 * a22 - r2 * a12) / det;
+      c2 = (a11 * r2 - a12 * r1) / det;
+    } else if (u1 && (!u2 || r1 * r1 / a11 >= r2 * r2 / a22)) {
+      c1 = r1 / a11;  // the better single direction (larger decrease of the error)
+    } else if (u2) {
+      c2 = r2 / a22;
+    }
+    if (!(c1 > -4.0 && c1 < 4.0 && c2 > -4.0 && c2 < 4.0)) c1 = c2 = 0.0;  // also NaN
+    sv.sgomega[0] = c1;
+    sv.sgomega[1] = c2;
     *counter = 0u;
   }
 }
@@ -267,8 +303,11 @@ int lv_phys_friction(lv_ctx* c, const double* vwall, double dt);
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
 // prepare = 1 evaluates the sweep-invariant terms (first sweep of find_pressure!)
-// guess != 0: also the sums of the sweep's initial guess (sweep >= 2)
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess = 0);
+// guess: also the sums of the sweep's initial guess (lv_sweep_sums) on the
+// first (gp_step = 0) or the second pass; D: the previous call's change of this
+// sweep (nullptr: none)
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess = 0,
+                const float* D = nullptr);
 int lv_phys_multiphase(lv_ctx* c, double quality_threshold, lv_solve_stats* st);
 
 // ---- learned preconditioner (lv_learn.cu)
@@ -282,7 +321,10 @@ void lv_learn_free(lv_ctx* c);
 int lv_solver_assemble(lv_ctx* c, double dt);
 int lv_solver_solve(lv_ctx* c, double* dst_P, lv_solve_stats* st_dev_or_null, int stats_slot);
 int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev);
-int lv_solver_sweep_guess(lv_ctx* c, double* P, int it);
+// moves P to the sweep's start (c1, c2 from lv_sweep_sums), stores the last
+// sweep's change into `store` (nullptr: none), saves P and b
+int lv_solver_sweep_guess(lv_ctx* c, double* P, int it, const float* D, float* store);
+int lv_solver_sweep_store(lv_ctx* c, const double* P, float* store);
 int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
 
 // ---- flag-reduced mixed-precision solver (lv_fcg.cu)

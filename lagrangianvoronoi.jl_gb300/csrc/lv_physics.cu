@@ -147,44 +147,60 @@ __global__ void k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt
   }
 }
 
-// refresh! first loop (pressure.jl:167-186) with the fixed terms of k_rhs_prep
-// guess != 0: also d = P - pprev in FP32 for the sweep's initial guess
-// (lv_sweep_sums)
-__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess) {
+// refresh! first loop (pressure.jl:167-186) with the fixed terms of k_rhs_prep.
+// guess 1: also d1 = P - pprev in FP32 for the sweep's initial guess; guess 2
+// (sweep 1): the sums of the initial guess with the residual b - A P and the
+// previous call's change D (lv_sweep_sums; all threads of the block take
+// part, so rows past n do not return early).
+__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess, const float* D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
-  const double2 xi = s.x[i];
-  const double Pi = s.P[i];
-  if (guess) sv.sgd32[i] = (float)(Pi - sv.pprev[i]);
-  double bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
-  double gpx = 0.0, gpy = 0.0;
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f];
-    bi -= sv.rhs_tf[f];
-    const double c = lrr * (Pi - s.P[j]);
-    gpx = gpx - c * (mm.x - xi.x);
-    gpy = gpy - c * (mm.y - xi.y);
-  }
-  if (nf < ne) {
-    for (int k = 0; k < ne; ++k) {
+  const bool on = i < n;
+  double bi = 0.0, Pi = 0.0;
+  if (on) {
+    const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
+    const double2 xi = s.x[i];
+    Pi = s.P[i];
+    if (guess == 1) sv.sgd32[i] = (float)(Pi - sv.pprev[i]);
+    bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
+    double gpx = 0.0, gpy = 0.0;
+    for (int k = 0; k < nf; ++k) {
       const size_t f = (size_t)k * cap + i;
-      if (m.elab[f] < 0) bi -= sv.rhs_te[f];
+      const int j = m.fnbr[f];
+      const double lrr = m.flrr[f];
+      const double2 mm = m.fm[f];
+      bi -= sv.rhs_tf[f];
+      const double c = lrr * (Pi - s.P[j]);
+      gpx = gpx - c * (mm.x - xi.x);
+      gpy = gpy - c * (mm.y - xi.y);
     }
+    if (nf < ne) {
+      for (int k = 0; k < ne; ++k) {
+        const size_t f = (size_t)k * cap + i;
+        if (m.elab[f] < 0) bi -= sv.rhs_te[f];
+      }
+    }
+    sv.b[i] = bi;
+    sv.xs[i] = Pi;
+    const double mi = s.mass[i];
+    s.GP[i] = make_double2(gpx / mi, gpy / mi);
   }
-  sv.b[i] = bi;
-  sv.xs[i] = Pi;
-  const double mi = s.mass[i];
-  s.GP[i] = make_double2(gpx / mi, gpy / mi);
+  if (guess == 2) {
+    double res = 0.0;
+    if (on) {
+      // b - A P with the operator's difference form
+      double ap = sv.diag[i] * Pi;
+      for (int e = sv.rowptr[i]; e < sv.rowptr[i + 1]; ++e) ap += sv.w[e] * (Pi - s.P[sv.col[e]]);
+      res = bi - ap;
+    }
+    lv_sweep_sums(sv, i, on, res, 0.0, D, false, true, n);
+  }
 }
 
 // refresh! second loop (pressure.jl:189-201): explicit part of the Laplacian.
-// guess != 0: then the sums of the sweep's initial guess (lv_sweep_sums; all
-// threads of the block take part, so rows past n do not return early).
-__global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess) {
+// guess != 0: then the sums of the sweep's initial guess with the directions
+// d1 and D (nullptr: none) and the residual b_k - b_{k-1} (lv_sweep_sums;
+// all threads of the block take part, so rows past n do not return early).
+__global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess, const float* D) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool on = i < n;
   double bi = 0.0;
@@ -202,7 +218,11 @@ __global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess) 
     }
     sv.b[i] = bi;
   }
-  if (guess) lv_sweep_sums(sv, s.P, i, on, bi, n);
+  if (guess) {
+    const double res = on ? bi - sv.bprev[i] : 0.0;
+    const double d1 = on ? s.P[i] - sv.pprev[i] : 0.0;
+    lv_sweep_sums(sv, i, on, res, d1, D, true, D != nullptr, n);
+  }
 }
 
 // ---------------------------------------------------------- viscosity, D
@@ -622,7 +642,7 @@ int lv_phys_pressure_step(lv_ctx* c, double dt) {
   return LV_OK;
 }
 
-int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess) {
+int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepare, int guess, const float* D) {
   if (int rc = need_mesh(c)) return rc;
   if (prepare) {
     double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -634,9 +654,11 @@ int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepar
     LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl);
   }
   static_assert(TPB == LV_SG_TPB, "the sweep-guess sums assume 256 threads per block");
-  guess = guess && gp_step;  // the guess sums ride on the second pass (sweeps >= 2)
-  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt, guess);
-  if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n, guess);
+  // the guess sums ride on the second pass (sweeps >= 2), on the first pass
+  // of sweep 1 when there is a direction (the previous call's change)
+  const int g1 = !guess ? 0 : (gp_step ? 1 : (D ? 2 : 0));
+  LAUNCH_F(LV_KF_RHS, k_rhs, c->s, c->m, c->sv, c->n, dt, g1, D);
+  if (gp_step) LAUNCH_F(LV_KF_RHS, k_rhs_gp, c->s, c->m, c->sv, c->n, guess, D);
   return LV_OK;
 }
 

@@ -909,27 +909,44 @@ int lv_solver_apply(lv_ctx* c, const double* x_dev, double* y_dev) {
 // ---------------------------------------------------------------- sweep guess
 //
 // find_pressure's sweeps solve A P_k = b_k with the same operator and a
-// right-hand side that follows P.  Sweep k >= 2 starts from P_{k-1} + omega
-// (P_{k-1} - P_{k-2}), omega from lv_sweep_sums (the right-hand side's second
-// pass); every sweep then saves P and b for the next one.
+// right-hand side that follows P.  Each sweep starts from P + c1 d1 + c2 D
+// (lv_sweep_sums computes c1, c2 on the right-hand side's pass); every sweep
+// saves P and b for the next one, and the change P - pprev of the sweep
+// before it.
 
-// P <- P + omega (P - prev) (shift != 0); prev <- P, bprev <- b (before the update)
+// store <- P - prev (the last sweep's change; store may be nullptr); with
+// shift: P <- P + c1 (P - prev) + c2 D; then prev <- P, bprev <- b (the
+// values before the shift)
 __global__ void k_sweep_apply(int n, double* P, double* prev, double* bprev, const double* __restrict__ b,
-                              const double* omega, int shift) {
+                              const float* __restrict__ D, float* store, const double* coef, int shift) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double p = P[i];
-  if (shift) P[i] = p + *omega * (p - prev[i]);
+  const double p = P[i], pv = prev[i];
+  if (store) store[i] = (float)(p - pv);
+  if (shift) P[i] = p + coef[0] * (p - pv) + coef[1] * (D ? (double)D[i] : 0.0);
   prev[i] = p;
   bprev[i] = b[i];
 }
 
-int lv_solver_sweep_guess(lv_ctx* c, double* P, int it) {
+// store <- P - prev after the last sweep of a call
+__global__ void k_sweep_store(int n, const double* __restrict__ P, const double* __restrict__ prev, float* store) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) store[i] = (float)(P[i] - prev[i]);
+}
+
+int lv_solver_sweep_guess(lv_ctx* c, double* P, int it, const float* D, float* store) {
   if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
   const int n = c->n;
-  k_sweep_apply<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, c->sv.bprev, c->sv.b, c->sv.sgomega,
-                                                          it >= 2 ? 1 : 0);
+  const int shift = (it >= 2 || D) ? 1 : 0;
+  k_sweep_apply<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, c->sv.bprev, c->sv.b, D, store,
+                                                          c->sv.sgomega, shift);
   LV_LAUNCH_CHECK(c, "k_sweep_apply");
+  return LV_OK;
+}
+
+int lv_solver_sweep_store(lv_ctx* c, const double* P, float* store) {
+  k_sweep_store<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(c->n, P, c->sv.pprev, store);
+  LV_LAUNCH_CHECK(c, "k_sweep_store");
   return LV_OK;
 }
 

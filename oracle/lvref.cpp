@@ -104,6 +104,10 @@ struct Grid {
   std::vector<std::vector<int32_t>> op_nbr;
   std::vector<std::vector<double>> op_w;
   std::vector<double> b, Psol;
+  // the change of each find_pressure sweep in the last call with the GPU
+  // solver's initial guess (method 2), stored in FP32 as the GPU does
+  std::vector<std::vector<double>> sweep_inc;
+  int sweep_n = 0;
   std::vector<V2> GP;
   int status = ST_OK;
 };
@@ -1181,67 +1185,102 @@ int lvref_operator_apply(void* h, const double* xin, double* y) {
   return 0;
 }
 
-// The GPU solver's initial guess of sweep it >= 2 (not part of the
-// reference, whose MINRES starts from the previous sweep's P): the previous
-// solution moved along d = P_{it-1} - P_{it-2} by omega = (b_it - b_{it-1},
-// d) / (d, A d), the exact A-norm line search up to the previous solve's
-// residual, with b_it - b_{it-1} projected to zero mean when the operator is
-// singular; omega outside (-2, 2) or undefined gives the plain warm start.
-// prev and bprev receive P and b of this sweep.
+// The GPU solver's initial guess of a sweep (not part of the reference,
+// whose MINRES starts from the previous sweep's P): the start x moves to
+// x + c1 d1 + c2 D, the Galerkin projection of the error onto span{d1, D} in
+// the A-norm, d1 = x - prev (the last sweep's change, sweeps >= 2), D = the
+// change of this sweep in the previous call (if it ran this sweep).  res =
+// b - A x is evaluated on sweep 1 and taken as b - bprev on the others (the
+// previous solve's residual, below its tolerance, is dropped); projected to
+// zero mean when the operator is singular.  A nearly dependent pair (det <=
+// 1e-6 a11 a22) keeps the single direction that lowers the error more;
+// coefficients outside (-4, 4) or undefined give the plain warm start.
+// prev and bprev receive x and b before the move.
 void sweep_guess(const Grid& g, std::vector<double>& x, std::vector<double>& prev, std::vector<double>& bprev,
-                 int it) {
+                 const std::vector<double>* D, int it) {
   const int n = g.n;
-  if (it >= 2) {
-    std::vector<double> d(n), Ad(n), db(n);
+  const bool has1 = it >= 2, has2 = D != nullptr;
+  std::vector<double> res(n), d1(n, 0.0);
+  if (has1) {
     for (int i = 0; i < n; ++i) {
-      d[i] = x[i] - prev[i];
-      db[i] = g.b[i] - bprev[i];
+      d1[i] = x[i] - prev[i];
+      res[i] = g.b[i] - bprev[i];
     }
-    op_mul(g, d.data(), Ad.data());
-    double num = bdot(db.data(), d.data(), n), den = bdot(d.data(), Ad.data(), n);
-    bool singular = true;
-    for (int i = 0; i < n; ++i)
-      if (g.diag[i] != 0.0) {
-        singular = false;
-        break;
-      }
-    if (singular && n > 0) {
-      double sb = 0.0, sd = 0.0;
-      for (int i = 0; i < n; ++i) {
-        sb += db[i];
-        sd += d[i];
-      }
-      num -= sb * sd / n;
-    }
-    double om = den > 0.0 ? num / den : 0.0;
-    if (!(om > -2.0 && om < 2.0)) om = 0.0;
-    prev = x;
-    for (int i = 0; i < n; ++i) x[i] += om * d[i];
   } else {
-    prev = x;
+    std::vector<double> Ax(n);
+    op_mul(g, x.data(), Ax.data());
+    for (int i = 0; i < n; ++i) res[i] = g.b[i] - Ax[i];
   }
+  prev = x;
   bprev = g.b;
+  if (!has1 && !has2) return;
+  bool singular = true;
+  for (int i = 0; i < n; ++i)
+    if (g.diag[i] != 0.0) {
+      singular = false;
+      break;
+    }
+  if (singular && n > 0) {
+    double sr = 0.0;
+    for (int i = 0; i < n; ++i) sr += res[i];
+    for (int i = 0; i < n; ++i) res[i] -= sr / n;
+  }
+  std::vector<double> A1(n, 0.0), A2(n, 0.0);
+  double r1 = 0.0, r2 = 0.0, a11 = 0.0, a12 = 0.0, a22 = 0.0;
+  if (has1) {
+    op_mul(g, d1.data(), A1.data());
+    r1 = bdot(res.data(), d1.data(), n);
+    a11 = bdot(d1.data(), A1.data(), n);
+  }
+  if (has2) {
+    op_mul(g, D->data(), A2.data());
+    r2 = bdot(res.data(), D->data(), n);
+    a22 = bdot(D->data(), A2.data(), n);
+    if (has1) a12 = bdot(d1.data(), A2.data(), n);
+  }
+  double c1 = 0.0, c2 = 0.0;
+  const bool u1 = has1 && a11 > 0.0, u2 = has2 && a22 > 0.0;
+  const double det = a11 * a22 - a12 * a12;
+  if (u1 && u2 && det > 1e-6 * a11 * a22) {
+    c1 = (r1 * a22 - r2 * a12) / det;
+    c2 = (a11 * r2 - a12 * r1) / det;
+  } else if (u1 && (!u2 || r1 * r1 / a11 >= r2 * r2 / a22)) {
+    c1 = r1 / a11;
+  } else if (u2) {
+    c2 = r2 / a22;
+  }
+  if (!(c1 > -4.0 && c1 < 4.0 && c2 > -4.0 && c2 < 4.0)) c1 = c2 = 0.0;
+  for (int i = 0; i < n; ++i) x[i] += c1 * d1[i] + (has2 ? c2 * (*D)[i] : 0.0);
 }
 
 // find_pressure! (pressure.jl:215-224).  method 0: MINRES (atol = rtol = tol),
 // method 1: Jacobi-PCG with ||r|| <= tol*||b||, method 2: the same PCG from
-// the GPU solver's line-searched initial guess (sweep_guess).  stats[niter]
+// the GPU solver's Galerkin initial guess (sweep_guess).  stats[niter]
 // receives one record per fixed-point sweep.
 int lvref_find_pressure(void* h, double dt, int niter, const double* vbc, int method, double tol, int itmax,
                         SolveStats* stats) {
   Grid* g = static_cast<Grid*>(h);
   refresh_operator(*g, dt);
   std::vector<double> prev, bprev;
+  if ((int)g->sweep_n != g->n) g->sweep_inc.clear();
   for (int it = 1; it <= niter; ++it) {
     refresh_rhs(*g, dt, it > 1, vbc);
     std::vector<double> x = g->Psol;
-    if (method == 2) sweep_guess(*g, x, prev, bprev, it);
+    if (method == 2) sweep_guess(*g, x, prev, bprev, it <= (int)g->sweep_inc.size() ? &g->sweep_inc[it - 1] : nullptr, it);
     SolveStats st{};
     if (method == 0)
       minres_solve(*g, g->b, x, tol, tol, itmax, &st);
     else
       pcg_solve(*g, g->b, x, tol, itmax, &st);
     if (stats) stats[it - 1] = st;
+    if (method == 2) {
+      // this sweep's change, for the same sweep of the next call
+      std::vector<double> dd(g->n);
+      for (int i = 0; i < g->n; ++i) dd[i] = (double)(float)(x[i] - g->P[i]);
+      if ((int)g->sweep_inc.size() < it) g->sweep_inc.resize(it);
+      g->sweep_inc[it - 1] = dd;
+      g->sweep_n = g->n;
+    }
     for (int i = 0; i < g->n; ++i) g->P[i] = x[i];
   }
   return 0;

@@ -243,8 +243,9 @@ class OracleGrid:
         return y
 
     def find_pressure(self, dt, niter=10, vbc=None, method="pcg", tol=1e-8, itmax=10000, guess=False):
-        """guess: with method "pcg", start sweeps >= 2 from the GPU solver's
-        line-searched guess instead of the previous sweep's P."""
+        """guess: with method "pcg", start each sweep from the GPU solver's
+        Galerkin guess (the span of the last sweep's change and the previous
+        call's change of the same sweep) instead of the previous sweep's P."""
         stats = (SolveStats * niter)()
         v = None if vbc is None else np.ascontiguousarray(np.asarray(vbc, np.float64).reshape(8))
         m = 0 if method == "minres" else (2 if guess else 1)
