@@ -253,16 +253,19 @@ def run_ours(args, world, rank, local):
                   "loss_last": float(losses[-10:].mean())}
 
     solver = lv.PressureSolver(g, method=args.solver, tol=1e-8)
-    gpu_step(lv, g, solver, fl)  # one untimed step with the timed solver
-    g.synchronize()
-    # the state the timed steps start from: the instrumented pass and the
-    # end-to-end pass restart from it, so all three measure the same steps
+    # the state the passes start from: each pass restores it, forgets the
+    # sweep-guess history and runs one untimed step with the timed solver, so
+    # the timed, the instrumented and the end-to-end passes run the same steps
     state = g.get_many(STATE_FIELDS)
 
     def restore():
         g.set_many(dict(zip(STATE_FIELDS, state)))
         lv.remesh(g)
+        assert L.lv_solver_forget(g._ctx) == 0
+        gpu_step(lv, g, solver, fl)
         g.synchronize()
+
+    restore()
 
     # ---- timed region: K steps, device time from events on the library's stream,
     # an L2 flush (512 MiB write) between steps outside the events; no per-family

@@ -277,6 +277,11 @@ int lv_solver_counters(lv_ctx* ctx, int64_t* solves, int64_t* iterations);
  * through LVGPU_FCG_HALO=0, a halo above 1536 rows, or a larger system);
  * synchronises. */
 int lv_solver_halo(lv_ctx* ctx, int32_t* max_rows);
+/* The sweeps of lv_find_pressure start from a Galerkin guess that uses the
+ * previous call's change of each sweep (LVGPU_SWEEP_GUESS=0 turns the guess
+ * off).  lv_solver_forget forgets that history, e.g. after the state was
+ * replaced (a restart from a checkpoint): the next call starts like the first. */
+int lv_solver_forget(lv_ctx* ctx);
 
 /* Per-kernel-family device times in ms accumulated since the last reset:
  * out[0] mesh, [1] operators, [2] pressure solve, [3] other.  Returns the

@@ -832,6 +832,12 @@ int lv_kernel_time(lv_ctx* c, int32_t fam, int64_t* launches, double* ms, int32_
   return LV_OK;
 }
 
+int lv_solver_forget(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  c->sg_valid = 0;
+  return LV_OK;
+}
+
 int lv_solver_halo(lv_ctx* c, int32_t* max_rows) {
   if (!c || !max_rows) return LV_ERR_BAD_ARGUMENT;
   int m = 0;
