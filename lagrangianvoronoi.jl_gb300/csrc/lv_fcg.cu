@@ -206,30 +206,40 @@ __device__ bool fphase(const FcgArgs& a, unsigned ph, const T (&v)[NV], T (&tot)
   }
   __syncthreads();
   if (!s_ok) return false;
-  // 2. every block's words, read once: thread t reads block t's
-  T acc[NV];
+  // 2. every block's words, read once: thread t reads block t's; only the
+  // warps that hold words add (the FP64 pipe of this GPU is narrow), and one
+  // thread forms the totals for the whole block
+  __shared__ T s_tot[NV];
+  const int nwr = (a.nb + 31) >> 5;  // warps holding words
+  if (wid < nwr) {
+    T acc[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) acc[k] = T(0);
-  if ((int)threadIdx.x < a.nb) {
-    unsigned wd[NWD];
+    for (int k = 0; k < NV; ++k) acc[k] = T(0);
+    if ((int)threadIdx.x < a.nb) {
+      unsigned wd[NWD];
 #pragma unroll
-    for (int q = 0; q < NWD; ++q) wd[q] = __ldcg(words + (size_t)q * a.nb + threadIdx.x);
+      for (int q = 0; q < NWD; ++q) wd[q] = __ldcg(words + (size_t)q * a.nb + threadIdx.x);
 #pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = Words<T>::get(wd + k * Words<T>::N);
+      for (int k = 0; k < NV; ++k) acc[k] = Words<T>::get(wd + k * Words<T>::N);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      acc[k] = allsum(acc[k]);
+      if (lane == 0) shw2[k * 32 + wid] = acc[k];
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    acc[k] = allsum(acc[k]);
-    if (lane == 0) shw2[k * 32 + wid] = acc[k];
+    for (int k = 0; k < NV; ++k) {
+      T t = T(0);
+      for (int q = 0; q < nwr; ++q) t += shw2[k * 32 + q];
+      s_tot[k] = t;
+    }
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    T t = T(0);
-#pragma unroll
-    for (int q = 0; q < FCG_NW; ++q) t += shw2[k * 32 + q];
-    tot[k] = t;
-  }
+  for (int k = 0; k < NV; ++k) tot[k] = s_tot[k];
   return true;
 }
 
@@ -363,7 +373,10 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
 #pragma unroll
     for (int k = 0; k < R; ++k) v[0] += rr.bb[k];
     ok = fphase<1, double>(a, ++ep, v, t);
-    const double mean = t[0] / (double)n;
+    __shared__ double s_mean;
+    if (threadIdx.x == 0) s_mean = t[0] / (double)n;  // one FP64 division per block
+    __syncthreads();
+    const double mean = s_mean;
 #pragma unroll
     for (int k = 0; k < R; ++k)
       if (rr.on[k]) rr.bb[k] -= mean;
@@ -579,8 +592,19 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     rtrue2 = t2[0];
     bnorm2 = t2[1];
     if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax || updates >= FCG_MAX_UPDATES) break;
-    sigma = sqrt(rtrue2);
-    const double inv_sigma = 1.0 / sigma;
+    // the restart's scalars once per block (the FP64 square root and
+    // divisions are many FP64 instructions on this GPU)
+    __shared__ double s_sig[2];
+    __shared__ float s_rho_upd;
+    if (threadIdx.x == 0) {
+      const double sg = sqrt(rtrue2);
+      s_sig[0] = sg;
+      s_sig[1] = 1.0 / sg;
+      s_rho_upd = fmaxf(FCG_UPDATE_DROP * FCG_UPDATE_DROP, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
+    }
+    __syncthreads();
+    sigma = s_sig[0];
+    const double inv_sigma = s_sig[1];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       r[k] = (float)(r64[k] * inv_sigma);
@@ -595,7 +619,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       learned = false;
       fall = false;
     }
-    const float rho_upd = fmaxf(FCG_UPDATE_DROP * FCG_UPDATE_DROP, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
+    const float rho_upd = s_rho_upd;
     if (!(ok = precond())) break;
     while (true) {
       if constexpr (!HALO) {
