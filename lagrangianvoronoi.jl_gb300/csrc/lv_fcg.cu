@@ -91,6 +91,9 @@ struct FcgArgs {
   const int* rowptr;
   const int* col;
   const double* w;
+  const float* w32;    // FP32 copies of w, diag, dinv (made when the operator is assembled)
+  const float* dg32;
+  const float* dinv32;
   const double* diag;  // the reference's diagonal term (mass part)
   const double* dinv;  // 1 / (diag + sum_j w_ij)
   const double* b;
@@ -324,10 +327,10 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     for (int e = 0; e < FKR; ++e) {
       const bool have = e < rr.cnt[k];
       rr.cc[k][e] = have ? (HALO ? a.remap[rr.beg[k] + e] : a.col[rr.beg[k] + e]) : 0;
-      rr.ww[k][e] = have ? (float)a.w[rr.beg[k] + e] : 0.f;
+      rr.ww[k][e] = have ? a.w32[rr.beg[k] + e] : 0.f;
     }
-    rr.dg[k] = on ? (float)a.diag[i] : 0.f;
-    rr.dnv[k] = on ? (float)a.dinv[i] : 0.f;
+    rr.dg[k] = on ? a.dg32[i] : 0.f;
+    rr.dnv[k] = on ? a.dinv32[i] : 0.f;
     rr.mn[k] = (on && learned0) ? a.mcnt[i] : 0;
     if constexpr (!HALO) {
 #pragma unroll
@@ -402,7 +405,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       for (int e = FKR; e < rr.cnt[k]; ++e) {
         const int q = rr.beg[k] + e;
         const float vj = HALO ? ss.u[a.remap[q]] : __ldcg(buf + a.col[q]);
-        acc = fmaf((float)a.w[q], own[k] - vj, acc);
+        acc = fmaf(a.w32[q], own[k] - vj, acc);
       }
       out[k] = acc;
     }
@@ -1206,6 +1209,9 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.rowptr = c->sv.rowptr;
   a.col = c->sv.col;
   a.w = c->sv.w;
+  a.w32 = c->sv.w32;
+  a.dg32 = c->sv.d32;
+  a.dinv32 = c->sv.dinv32;
   a.diag = c->sv.diag;
   a.dinv = c->sv.dinv;
   a.b = c->sv.b;
