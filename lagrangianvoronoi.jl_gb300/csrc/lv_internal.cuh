@@ -29,6 +29,7 @@
 #define LV_IT_METHOD 64        // [32] method used per slot (learned solves)
 #define LV_IT_JREF 128         // [32] iterations of the last Jacobi mixed solve per sweep slot
 #define LV_IT_NONSINGULAR 97   // set when some diagonal term is nonzero
+#define LV_IT_REDO 98          // polygons queued for the second clipping pass
 #define LV_IT_SIZE 160
 
 // Status bits set on the device with atomicOr; decoded on the host.

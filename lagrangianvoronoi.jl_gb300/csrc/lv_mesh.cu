@@ -226,6 +226,13 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 
 constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
+// edge slots of the first clipping pass: shared memory for 10 edges per
+// polygon lets six blocks share an SM (three with LV_MAX_EDGES); a polygon
+// that needs more at any point is redone by a second pass with LV_MAX_EDGES
+// slots.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2):
+// 8 slots 1.84 / 12.9, 10 slots 1.44 / 12.8, 12 slots 1.49 / 14.2, 14 slots
+// 1.52 / 16.6, all 20 slots in one pass 1.93 / 20.9.
+constexpr int ME_SMALL = 10;
 
 struct Poly {
   double* v1x;
@@ -239,6 +246,7 @@ struct Poly {
   float* r2y;
   float* d2;   // upper bound of 4 |v1 - x|^2
   int t;
+  int cap_e;   // edge slots
   __device__ __forceinline__ int at(int k) const { return k * CLIP_TPB + t; }
 };
 
@@ -340,7 +348,7 @@ __device__ int clip_exact(const Poly& P, int& ne, double px, double py, double y
   }
   const bool ynull = isnan(Yx) && isnan(Yy);
   if (!ynull && !(Xx == Yx && Xy == Yy)) {
-    if (ne >= ME) return -1;
+    if (ne >= P.cap_e) return -1;
     const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
     if (ax * by - ay * bx > 0.0) {
       set_v1(P, ne, Yx, Yy, px, py);
@@ -487,7 +495,7 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   const double Xx = (visited_last == 1) ? X0x : X1x, Xy = (visited_last == 1) ? X0y : X1y;
   const double Yx = (visited_first == 1) ? X0x : X1x, Yy = (visited_first == 1) ? X0y : X1y;
   if (Xx == Yx && Xy == Yy) return 0;
-  if (ne >= ME) return -1;
+  if (ne >= P.cap_e) return -1;
   const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
   if (ax * by - ay * bx > 0.0) {
     set_v1(P, ne, Yx, Yy, px, py);
@@ -528,25 +536,34 @@ __device__ __forceinline__ void get_arrow(const GridDev& g, double ax, double ay
   if (g.yper && fabs(vy) > 0.5 * g.yperiod) vy -= (vy > 0 ? 1.0 : -1.0) * g.yperiod;
 }
 
-__global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
-                                                   const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
-                                                   int* status) {
+// Shared-memory bytes of a block whose polygons have `cap` edge slots.
+constexpr size_t clip_smem(int cap) {
+  return (size_t)cap * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 5 * sizeof(float));
+}
+
+// One polygon per thread (i, active): the whole warp takes part, so threads
+// without a polygon pass active = false.  Returns false when the polygon
+// needed more than CAP edge slots and `retry` is set: then nothing of it is
+// written (the caller queues it for the pass with LV_MAX_EDGES slots);
+// without `retry` that case is the reference's edge overflow error.
+template <int CAP>
+__device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ path, const double2* __restrict__ x,
+                             int i, bool active, const CellsDev& cl, const MeshDev& m, int* status, bool retry) {
   extern __shared__ double smem[];
   const int t = threadIdx.x;
-  const int i = blockIdx.x * CLIP_TPB + t;
   Poly P;
   P.v1x = smem;
-  P.v1y = P.v1x + ME * CLIP_TPB;
-  P.v2x = P.v1y + ME * CLIP_TPB;
-  P.v2y = P.v2x + ME * CLIP_TPB;
-  P.lab = reinterpret_cast<int*>(P.v2y + ME * CLIP_TPB);
-  P.r1x = reinterpret_cast<float*>(P.lab + ME * CLIP_TPB);
-  P.r1y = P.r1x + ME * CLIP_TPB;
-  P.r2x = P.r1y + ME * CLIP_TPB;
-  P.r2y = P.r2x + ME * CLIP_TPB;
-  P.d2 = P.r2y + ME * CLIP_TPB;
+  P.v1y = P.v1x + CAP * CLIP_TPB;
+  P.v2x = P.v1y + CAP * CLIP_TPB;
+  P.v2y = P.v2x + CAP * CLIP_TPB;
+  P.lab = reinterpret_cast<int*>(P.v2y + CAP * CLIP_TPB);
+  P.r1x = reinterpret_cast<float*>(P.lab + CAP * CLIP_TPB);
+  P.r1y = P.r1x + CAP * CLIP_TPB;
+  P.r2x = P.r1y + CAP * CLIP_TPB;
+  P.r2y = P.r2x + CAP * CLIP_TPB;
+  P.d2 = P.r2y + CAP * CLIP_TPB;
   P.t = t;
-  const bool active = i < n;
+  P.cap_e = CAP;
 
   double px = 0.0, py = 0.0;
   int ne = 0;
@@ -648,7 +665,8 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
       prr_up = prr_upper(P, ne);
     }
   }
-  if (!active) return;
+  if (!active) return true;
+  if (flag == LV_FLAG_EDGE_OVERFLOW && retry) return false;
   if (flag) atomicOr(status, flag);
 
   // sort_edges! (IO.jl:35-48)
@@ -709,6 +727,32 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
   m.nfaces[i] = nf;
   m.area[i] = A;
   m.centroid[i] = make_double2(cx / Ac, cy / Ac);
+  return true;
+}
+
+// first pass: every polygon with CAP slots; the ones that need more are
+// appended to redo[] (redo_n counts them)
+template <int CAP>
+__global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
+                                                   const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
+                                                   int* status, int* redo, int* redo_n) {
+  const int i = blockIdx.x * CLIP_TPB + threadIdx.x;
+  if (!clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, true)) redo[atomicAdd(redo_n, 1)] = i;
+}
+
+// second pass: the queued polygons with LV_MAX_EDGES slots (a grid-stride
+// loop in whole warps)
+__global__ void __launch_bounds__(CLIP_TPB) k_clip_redo(GridDev g, const PathNodeDev* __restrict__ path,
+                                                        const double2* __restrict__ x, CellsDev cl, MeshDev m,
+                                                        int* status, const int* __restrict__ redo,
+                                                        const int* __restrict__ redo_n) {
+  const int cnt = *redo_n;
+  for (int base = blockIdx.x * CLIP_TPB; base < cnt; base += gridDim.x * CLIP_TPB) {
+    const int q = base + threadIdx.x;
+    const bool on = q < cnt;
+    clip_polygon<ME>(g, path, x, on ? redo[q] : 0, on, cl, m, status, false);
+    __syncwarp();
+  }
 }
 
 }  // namespace
@@ -748,16 +792,25 @@ int lv_mesh_remesh(lv_ctx* c) {
   k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap);
   LV_LAUNCH_CHECK(c, "k_bin_order");
   }
-  const size_t smem = (size_t)ME * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 5 * sizeof(float));
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME_SMALL));
+    cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME));
     attr_set = true;
   }
   {
     KernelTimer kt(c, LV_KF_CLIP);
-    k_clip<<<lv_blocks(n, CLIP_TPB), CLIP_TPB, smem, s>>>(c->g, c->path, c->s.x, n, c->c, c->m, c->status);
+    // the queue of polygons for the second pass lives in the solver's scratch
+    // (free during a remesh): n ints, then the count
+    int* redo = reinterpret_cast<int*>(c->sv.xs);
+    int* redo_n = c->sv.iters + LV_IT_REDO;
+    cudaMemsetAsync(redo_n, 0, sizeof(int), s);
+    k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
+                                                                                   c->m, c->status, redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip");
+    k_clip_redo<<<c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status, redo,
+                                                           redo_n);
+    LV_LAUNCH_CHECK(c, "k_clip_redo");
   }
   c->meshed = true;
   c->op_ready = false;
