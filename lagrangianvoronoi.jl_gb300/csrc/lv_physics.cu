@@ -392,7 +392,17 @@ __global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha)
 
 // relaxation_step! first loop (relaxation.jl:37-66): conservative remap of
 // mass, momentum and energy along dv with the Rusanov flux.
-__global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov) {
+// |dv| of every particle, evaluated once instead of on every face that
+// reads it (the same expression, so the same value)
+__global__ void k_norm_dv(StateDev s, int n, double* ndv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 d = s.dv[i];
+  ndv[i] = sqrt(d.x * d.x + d.y * d.y);
+}
+
+// ndv: |dv| of every particle (k_norm_dv), read when rusanov is set
+__global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov, const double* __restrict__ ndv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i];
@@ -403,7 +413,7 @@ __global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusano
   double mass = s.mass[i];
   double momx = mass * vp.x, momy = mass * vp.y;
   double energy = mass * ep;
-  const double ndvp = sqrt(dvp.x * dvp.x + dvp.y * dvp.y);
+  const double ndvp = rusanov ? ndv[i] : 0.0;
   for (int k = 0; k < nf; ++k) {
     const size_t f = (size_t)k * cap + i;
     const int j = m.fnbr[f];
@@ -428,7 +438,7 @@ __global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusano
     momy = momy + kk * (t1y - 0.5 * t2y);
     energy += kk * ((pdvmz * rp * ep - qdvmz * rq * eq) - 0.5 * (pdvpq * rp * ep + qdvpq * rq * eq));
     if (rusanov) {
-      const double ndvq = sqrt(dvq.x * dvq.x + dvq.y * dvq.y);
+      const double ndvq = ndv[j];
       const double a = jmax(ndvp, ndvq);
       const double l = m.flen[f];
       const double cr = 0.5 * dt * l * a;
@@ -698,7 +708,9 @@ int lv_phys_find_dv(lv_ctx* c, double dt, double alpha) {
 
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov) {
   if (int rc = need_mesh(c)) return rc;
-  LAUNCH(k_relax_flux, c->s, c->m, c->n, dt, rusanov);
+  double* ndv = c->sv.q;  // scratch between solves
+  if (rusanov) LAUNCH(k_norm_dv, c->s, c->n, ndv);
+  LAUNCH(k_relax_flux, c->s, c->m, c->n, dt, rusanov, ndv);
   LAUNCH(k_relax_update, c->s, c->n, dt);
   c->meshed = false;
   return lv_mesh_remesh(c);
