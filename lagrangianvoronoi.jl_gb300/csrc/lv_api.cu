@@ -258,6 +258,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   cl.ccount = dalloc<int>(c, cl.ncells, &ok);
   cl.item_cap = cap * nimages(g);
   cl.citem = dalloc<int>(c, cl.item_cap, &ok);
+  cl.bkey = dalloc<int2>(c, cl.item_cap, &ok);
   cl.cpos = dalloc<float2>(c, cl.item_cap, &ok);
 
   SolverDev& sv = c->sv;

@@ -83,9 +83,10 @@ struct MeshDev {
 struct CellsDev {
   int ncells;
   int* cstart;   // [ncells + 1]
-  int* ccount;   // [ncells] counts, then cursors
+  int* ccount;   // [ncells] counts
   int* citem;    // [item_cap]
   float2* cpos;  // [item_cap]
+  int2* bkey;    // [images][cap]: cell and rank in the cell of every copy (re-binning)
   int item_cap;
 };
 

@@ -144,7 +144,12 @@ done:
   if (sy < 0) qy = qy - g.yperiod;
 }
 
-__global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int* ccount, int* status) {
+// Counts every copy per cell and keeps, per copy k of particle i, its cell
+// and its rank among the cell's copies in key[k * cap + i] (cell -1: outside
+// the grid), so that the scatter needs neither the cell computation nor
+// atomics.
+__global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int cap, int* ccount, int2* key,
+                            int* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double2 p = x[i];
@@ -155,24 +160,22 @@ __global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int
     int c = cell_of(g, qx, qy, k > 0);
     if (c == -2) {
       atomicOr(status, LV_FLAG_NONFINITE);
+      for (; k < nim; ++k) key[(size_t)k * cap + i] = make_int2(-1, 0);
       return;
     }
-    if (c >= 0) atomicAdd(&ccount[c], 1);
+    key[(size_t)k * cap + i] = make_int2(c, c >= 0 ? atomicAdd(&ccount[c], 1) : 0);
   }
 }
 
-__global__ void k_bin_scatter(GridDev g, const double2* __restrict__ x, int n, const int* __restrict__ cstart,
-                              int* cursor, int* citem, int item_cap, int* status) {
+__global__ void k_bin_scatter(GridDev g, int n, int cap, const int2* __restrict__ key, const int* __restrict__ cstart,
+                              int* citem, int item_cap, int* status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double2 p = x[i];
   int nim = image_count(g);
   for (int k = 0; k < nim; ++k) {
-    double qx, qy;
-    image_pos(g, k, p.x, p.y, qx, qy);
-    int c = cell_of(g, qx, qy, k > 0);
-    if (c < 0) continue;
-    int slot = cstart[c] + atomicAdd(&cursor[c], 1);
+    const int2 cr = key[(size_t)k * cap + i];
+    if (cr.x < 0) continue;
+    int slot = cstart[cr.x] + cr.y;
     if (slot < item_cap)
       citem[slot] = i;
     else
@@ -781,12 +784,11 @@ int lv_mesh_remesh(lv_ctx* c) {
   {
   KernelTimer kt(c, LV_KF_BIN);
   cudaMemsetAsync(c->c.ccount, 0, sizeof(int) * nc, s);
-  k_bin_count<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->c.ccount, c->status);
+  k_bin_count<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->cap, c->c.ccount, c->c.bkey, c->status);
   LV_LAUNCH_CHECK(c, "k_bin_count");
   int rc = lv_scan_int(c, c->c.ccount, c->c.cstart, nc);
   if (rc) return rc;
-  cudaMemsetAsync(c->c.ccount, 0, sizeof(int) * nc, s);
-  k_bin_scatter<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->c.cstart, c->c.ccount, c->c.citem,
+  k_bin_scatter<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, n, c->cap, c->c.bkey, c->c.cstart, c->c.citem,
                                                     c->c.item_cap, c->status);
   LV_LAUNCH_CHECK(c, "k_bin_scatter");
   k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap);
