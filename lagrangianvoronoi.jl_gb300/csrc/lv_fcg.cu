@@ -101,7 +101,8 @@ struct FcgArgs {
   float* rbuf;
   float* ubuf;    // u exchange
   unsigned long long* slots;  // partial words [2 parities][RG_WORDS][nb] (as 32-bit words)
-  unsigned* counter;          // arrivals, zeroed before the launch
+  unsigned* counter;          // arrivals, cumulative over launches
+  unsigned* sync_base;        // [0] arrivals, [1] exchange epochs of the previous launches
   unsigned* flags;            // per-block exchange epochs, one 128-byte line each (FLAG_STRIDE words)
   int* status;
   double tol2;
@@ -139,12 +140,17 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// The arrival counter and the exchange flags are never reset: a launch
+// continues from the totals the previous one left in sync_base (read into
+// this block's shared s_base at the start), and comparisons are wrap-safe.
+__shared__ unsigned s_base[2];
+
 // thread 0: arrive and wait for phase ph; returns 0 on timeout
 __device__ __forceinline__ int arrive_wait(const FcgArgs& a, unsigned ph) {
   red_release_add(a.counter, 1u);
-  const unsigned target = ph * (unsigned)a.nb;
+  const unsigned target = s_base[0] + ph * (unsigned)a.nb;
   const long long t0 = clock64();
-  while (ld_acquire_u32(a.counter) < target) {
+  while ((int)(ld_acquire_u32(a.counter) - target) < 0) {
     if (clock64() - t0 > FCG_SPIN_LIMIT) {
       atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
       return 0;
@@ -258,12 +264,13 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
 // grid-wide phase, so one buffer per exchanged vector suffices.
 __device__ bool nexchange(const FcgArgs& a, unsigned e, const unsigned* mask) {
   __syncthreads();
-  if (threadIdx.x == 0) st_release_u32(a.flags + (size_t)blockIdx.x * FLAG_STRIDE, e);
+  const unsigned ee = s_base[1] + e;
+  if (threadIdx.x == 0) st_release_u32(a.flags + (size_t)blockIdx.x * FLAG_STRIDE, ee);
   int to = 0;
   const int t = threadIdx.x;
   if (t < a.nb && ((mask[t >> 5] >> (t & 31)) & 1u)) {
     const long long t0 = clock64();
-    while (ld_acquire_u32(a.flags + (size_t)t * FLAG_STRIDE) < e) {
+    while ((int)(ld_acquire_u32(a.flags + (size_t)t * FLAG_STRIDE) - ee) < 0) {
       if (clock64() - t0 > FCG_SPIN_LIMIT) {
         to = 1;
         atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
@@ -297,6 +304,10 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   const int rb0 = blockIdx.x * a.rows_per_block;
   const int rb1 = min(n, rb0 + a.rows_per_block);
   const bool learned0 = a.learned != 0 && *a.minv_ok != 0;
+  if (threadIdx.x == 0) {
+    s_base[0] = __ldcg(a.sync_base);
+    s_base[1] = __ldcg(a.sync_base + 1);
+  }  // visible after the first __syncthreads, before any phase or exchange
   extern __shared__ __align__(16) unsigned char fcg_dyn[];
   StageSmem& ss = *reinterpret_cast<StageSmem*>(fcg_dyn);
   if constexpr (HALO) {
@@ -662,6 +673,10 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     }
   }
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
+    // every block read the bases before its first arrival, and this is after
+    // the last phase: the next launch continues from here
+    a.sync_base[0] = s_base[0] + ep * (unsigned)a.nb;
+    a.sync_base[1] = s_base[1] + xe;
     *a.out_iters = it;
     *a.out_outer = updates;
     *a.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
@@ -1220,6 +1235,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.ubuf = c->sv.f32a;
   a.slots = c->sv.fslots;
   a.counter = c->sv.bar + 2;
+  a.sync_base = reinterpret_cast<unsigned*>(c->sv.iters + LV_IT_FCG_BASE);
   a.flags = reinterpret_cast<unsigned*>(c->sv.fslots + 8192);
   a.status = c->status;
   a.tol2 = c->tol * c->tol;
@@ -1241,14 +1257,23 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.out_method = c->sv.iters + LV_IT_METHOD + slot;
   a.out_d = c->sv.dstats + 3 * slot;
   a.counters = c->sv.counters;
-  cudaMemsetAsync(c->sv.bar + 2, 0, sizeof(unsigned), c->stream);
-  cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * FLAG_STRIDE * nb, c->stream);
+  if (c->fcg_reset) {
+    // first launch, or a launch after a failed one: the counter, the flags
+    // (all FCG_MAX_BLOCKS of them) and the bases start from zero
+    cudaMemsetAsync(a.counter, 0, sizeof(unsigned), c->stream);
+    cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * FLAG_STRIDE * FCG_MAX_BLOCKS, c->stream);
+    cudaMemsetAsync(a.sync_base, 0, sizeof(unsigned) * 2, c->stream);
+    c->fcg_reset = false;
+  }
   void* args[] = {&a};
   const void* fn = halo ? (R == 1 ? (const void*)k_fcg<1, true> : (const void*)k_fcg<2, true>)
                         : (R == 1 ? (const void*)k_fcg<1, false> : (const void*)k_fcg<2, false>);
   const size_t dyn = halo ? sizeof(StageSmem) : 0;
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(FCG_TPB), args, dyn, c->stream);
   c->launches++;
-  if (e != cudaSuccess) return lv_cuda_check(c, e, "k_fcg cooperative launch");
+  if (e != cudaSuccess) {
+    c->fcg_reset = true;
+    return lv_cuda_check(c, e, "k_fcg cooperative launch");
+  }
   return LV_OK;
 }

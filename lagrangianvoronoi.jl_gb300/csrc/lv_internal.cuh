@@ -30,6 +30,7 @@
 #define LV_IT_JREF 128         // [32] iterations of the last Jacobi mixed solve per sweep slot
 #define LV_IT_NONSINGULAR 97   // set when some diagonal term is nonzero
 #define LV_IT_REDO 98          // polygons queued for the second clipping pass
+#define LV_IT_FCG_BASE 100     // [2] arrivals and exchange epochs of the flag-reduced solver so far
 #define LV_IT_SIZE 160
 
 // Status bits set on the device with atomicOr; decoded on the host.
@@ -158,7 +159,8 @@ struct lv_ctx {
   bool sweep_guess = true;  // Galerkin initial guess of the sweeps (LVGPU_SWEEP_GUESS=0 turns it off)
   int sg_valid = 0;         // sweeps of the last find_pressure whose changes sv.dinc holds
   int sg_n = 0;             // the particle count they belong to
-  bool fcg_halo = true;  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
+  bool fcg_halo = true;
+  bool fcg_reset = true;  // clear the flag-reduced solver's counter, flags and bases before its next launch  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
