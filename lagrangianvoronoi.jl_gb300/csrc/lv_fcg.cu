@@ -765,7 +765,7 @@ __global__ void k_build_minv(int n, const int* __restrict__ rowptr, const int* _
 // the block's rows to the shared-memory u of the staged solve (own row j:
 // j - b rpb; halo row: rpb + halo slot).  stat[0] is cleared when an image
 // does not fit; stat[1..3] collect the largest halo, ext and entry counts.
-constexpr int STG_BUILD_TPB = 512;
+constexpr int STG_BUILD_TPB = 1024;
 constexpr size_t STG_BUILD_SMEM = (size_t)STG_HASH * (4 + 2 + 2) + (size_t)FCG_HMAX * 4 + (size_t)STG_PMAX * 4;
 
 __device__ __forceinline__ unsigned stg_hash(int j) { return ((unsigned)j * 2654435761u) >> 19; }
