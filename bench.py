@@ -426,7 +426,7 @@ def run_ours(args, world, rank, local):
                                "unit": "GB/s", "frac": step_gbs / hbm_peak},
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "peak_source": peak_src},
+                     "peak_source": peak_src, "note": ROOFLINE_NOTE.get(kname, "")},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -436,6 +436,15 @@ def run_ours(args, world, rank, local):
         line["cpu_baseline"] = cpu_baseline(args, sample_steps=2)
     return line
 
+
+# what bounds each dominant kernel instead of HBM (from the ncu summaries in profiles/)
+ROOFLINE_NOTE = {
+    "k_clip": "FP64-pipe bound: sm__pipe_fp64_cycles_active 65% at ~10 warps/SM (profiles/k_clip_taylor_green_1024.md);"
+              " its compulsory traffic is 212 B per polygon",
+    "k_fcg<1,1>": "synchronisation-latency bound: a grid-wide reduction and a neighbour exchange per CG iteration"
+                  " (profiles/k_fcg_taylor_green_256.md)",
+    "k_fcg<1,0>": "synchronisation-latency bound (profiles/k_fcg_taylor_green_256.md)",
+}
 
 SOLVER_DESC = {
     "jacobi_pcg": "jacobi_pcg fp64",
