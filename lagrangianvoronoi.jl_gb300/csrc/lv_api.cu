@@ -62,7 +62,7 @@ std::vector<PathNodeDev> build_path(const GridDev& g) {
   std::stable_sort(all.begin(), all.end(), [](const Node& p, const Node& q) { return p.rr < q.rr; });
   std::vector<PathNodeDev> out;
   for (const auto& nd : all) {
-    out.push_back(PathNodeDev{(int)nd.i1, (int)nd.i2, nd.rr});
+    out.push_back(PathNodeDev{(int)nd.i1, (int)nd.i2, nd.rr, (float)nd.rr, nd.rr > g.rr_max ? 1 : 0});
     if (nd.rr > g.rr_max) break;
   }
   return out;
@@ -558,6 +558,7 @@ int lv_get_faces(lv_ctx* c, int64_t* nfaces, int64_t* rowptr, int32_t* nbr, doub
   for (int i = 0; i < n; ++i) tot += nf[i];
   if (nfaces) *nfaces = tot;
   if (!rowptr && !nbr) return LV_OK;
+  if (int rc = lv_mesh_face_len(c)) return rc;
   const size_t ell = (size_t)LV_MAX_EDGES * cap;
   std::vector<int> fn(ell);
   std::vector<double> fl(ell), fle(ell);

@@ -60,6 +60,8 @@ struct GridDev {
 struct PathNodeDev {
   int di1, di2;
   double rr;
+  float rrf;   // (float)rr, for the float test against the influence bound
+  int beyond;  // rr > rr_max (only the last node of the clipping path)
 };
 
 struct StateDev {
@@ -75,11 +77,64 @@ struct MeshDev {
   double2 *ev1, *ev2;
   int* elab;
   int* fnbr;
-  double *flrr, *flen;
+  double *flrr, *flen;  // flen is filled on demand (lv_mesh_face_len)
   double2 *fm, *fy;
   double* area;
   double2* centroid;
 };
+
+// Loads of data that no thread writes during the kernel, issued where they
+// stand in the source (volatile inline PTX): the face and row loops load a
+// batch of faces (entries) this way and only then use them, so that the
+// loads are in flight together instead of one dependent round trip each.
+__device__ __forceinline__ int ld_nc(const int* p) {
+  int v;
+  asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_nc(const float* p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_nc(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double2 ld_nc(const double2* p) {
+  double2 v;
+  asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+  return v;
+}
+
+// Face lengths |v1 - v2| of polygon i's interior edges in face order, with
+// the expression of the reference's face loop.  The edges are loaded eight at
+// a time (indexes clamped to the last edge) so that their loads overlap.
+__device__ __forceinline__ void lv_face_lengths(const MeshDev& m, int i) {
+  constexpr int B = 8;
+  const int cap = m.cap, ne = m.nedges[i];
+  int nf = 0;
+  for (int k0 = 0; k0 < ne; k0 += B) {
+    int lab[B];
+    double2 a[B], b[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t e = (size_t)min(k0 + u, ne - 1) * cap + i;
+      lab[u] = ld_nc(m.elab + e);
+      a[u] = ld_nc(m.ev1 + e);
+      b[u] = ld_nc(m.ev2 + e);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u < ne && lab[u] >= 0) {
+        const double lx = a[u].x - b[u].x, ly = a[u].y - b[u].y;
+        m.flen[(size_t)nf * cap + i] = sqrt(lx * lx + ly * ly);
+        ++nf;
+      }
+    }
+  }
+}
 
 struct CellsDev {
   int ncells;
@@ -159,8 +214,9 @@ struct lv_ctx {
   bool sweep_guess = true;  // Galerkin initial guess of the sweeps (LVGPU_SWEEP_GUESS=0 turns it off)
   int sg_valid = 0;         // sweeps of the last find_pressure whose changes sv.dinc holds
   int sg_n = 0;             // the particle count they belong to
-  bool fcg_halo = true;
-  bool fcg_reset = true;  // clear the flag-reduced solver's counter, flags and bases before its next launch  // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
+  bool fcg_halo = true;    // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
+  bool fcg_reset = true;   // clear the flag-reduced solver's counter, flags and bases before its next launch
+  bool flen_valid = false;  // m.flen belongs to the current mesh
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
@@ -207,11 +263,29 @@ __device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, int i, bool o
     const float dg = sv.d32[i];
     float a1 = dg * f1, a2 = dg * f2;
     const int e0 = sv.rowptr[i], e1 = sv.rowptr[i + 1];
-    for (int e = e0; e < e1; ++e) {
-      const int j = sv.col[e];
-      const float w = sv.w32[e];
-      if (has1) a1 = a1 + w * (f1 - sv.sgd32[j]);
-      if (has2) a2 = a2 + w * (f2 - D[j]);
+    // entries eight at a time (indexes clamped to the row's last) so that
+    // their loads overlap; the sums run over the entries in order
+    constexpr int EB = 8;
+    for (int b0 = e0; b0 < e1; b0 += EB) {
+      int j[EB];
+      float w[EB], g1[EB], g2[EB];
+#pragma unroll
+      for (int u = 0; u < EB; ++u) {
+        const int e = min(b0 + u, e1 - 1);
+        j[u] = ld_nc(sv.col + e);
+        w[u] = ld_nc(sv.w32 + e);
+      }
+#pragma unroll
+      for (int u = 0; u < EB; ++u) {
+        g1[u] = has1 ? ld_nc(sv.sgd32 + j[u]) : 0.f;
+        g2[u] = has2 ? ld_nc(D + j[u]) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < EB; ++u) {
+        if (b0 + u >= e1) break;
+        if (has1) a1 = a1 + w[u] * (f1 - g1[u]);
+        if (has2) a2 = a2 + w[u] * (f2 - g2[u]);
+      }
     }
     acc[0] = res * d1;
     acc[1] = res * (double)f2;
@@ -294,6 +368,7 @@ int lv_cuda_check(lv_ctx* c, cudaError_t e, const char* what);
 
 // ---- mesh (lv_mesh.cu)
 int lv_mesh_remesh(lv_ctx* c);
+int lv_mesh_face_len(lv_ctx* c);  // fills m.flen unless it is current
 int lv_scan_int(lv_ctx* c, const int* in, int* out, int len);  // exclusive, out[len] = total
 
 // ---- physics (lv_physics.cu)

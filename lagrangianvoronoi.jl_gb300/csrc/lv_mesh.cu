@@ -253,6 +253,32 @@ struct Poly {
   __device__ __forceinline__ int at(int k) const { return k * CLIP_TPB + t; }
 };
 
+// a == b (IEEE) decided on the integer pipe: equal bit patterns of a value
+// that is not NaN, or two zeros of either sign.
+__device__ __forceinline__ bool same_value(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+  constexpr unsigned long long MAG = 0x7fffffffffffffffull;
+  return (x == y && (x & MAG) <= 0x7ff0000000000000ull) || ((x | y) & MAG) == 0ull;
+}
+
+// RN(a / 3) with one multiplication and two fused multiply-adds (Markstein,
+// IBM J. Res. Dev. 34(1), 1990): y = RN(1/3) = (1/3)(1 - 2^-54) lies within
+// half an ulp of 1/3, so q = RN(a y) lies within one ulp of a/3, the residual
+// r = a - 3q is exact in one fma, and RN(q + r y) is the correctly rounded
+// quotient.  For |a| outside [2^-900, 2^1000) (zeros, values whose residual
+// could be subnormal, infinities, NaN) the division itself.
+__device__ __forceinline__ double div3(double a) {
+  const unsigned ex = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  if (ex - 123u < 1900u) {
+    const double y = 0x1.5555555555555p-2;
+    const double q = a * y;
+    const double r = fma(-3.0, q, a);
+    return fma(r, y, q);
+  }
+  return a / 3.0;
+}
+
 __device__ __forceinline__ int signum_eps(double f) {  // polygon.jl:9-16
   return (f < -LV_SIGNUM_EPS) ? -1 : ((f > LV_SIGNUM_EPS) ? 1 : 0);
 }
@@ -350,7 +376,7 @@ __device__ int clip_exact(const Poly& P, int& ne, double px, double py, double y
     }
   }
   const bool ynull = isnan(Yx) && isnan(Yy);
-  if (!ynull && !(Xx == Yx && Xy == Yy)) {
+  if (!ynull && !(same_value(Xx, Yx) && same_value(Xy, Yy))) {
     if (ne >= P.cap_e) return -1;
     const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
     if (ax * by - ay * bx > 0.0) {
@@ -497,7 +523,7 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   // new edge from X = the crossing visited last, Y = the one visited first
   const double Xx = (visited_last == 1) ? X0x : X1x, Xy = (visited_last == 1) ? X0y : X1y;
   const double Yx = (visited_first == 1) ? X0x : X1x, Yy = (visited_first == 1) ? X0y : X1y;
-  if (Xx == Yx && Xy == Yy) return 0;
+  if (same_value(Xx, Yx) && same_value(Xy, Yy)) return 0;
   if (ne >= P.cap_e) return -1;
   const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
   if (ax * by - ay * bx > 0.0) {
@@ -612,18 +638,18 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
           done = true;
           break;
         }
-        const double rr = path[pn].rr;
-        if ((float)rr > prr_up) {  // prr_up >= prr: never earlier than the reference
+        const PathNodeDev nd = path[pn];
+        if (nd.rrf > prr_up) {  // prr_up >= prr: never earlier than the reference
           done = true;
           break;
         }
-        if (rr > g.rr_max) {
+        if (nd.beyond) {
           // the reference stops here if rr > prr, and throws otherwise
-          if (!(rr > influence_rr_exact(P, ne, px, py))) flag = LV_FLAG_MESH_DESTROYED;
+          if (!(nd.rr > influence_rr_exact(P, ne, px, py))) flag = LV_FLAG_MESH_DESTROYED;
           done = true;
           break;
         }
-        const long long c1 = k1 + path[pn].di1, c2 = k2 + path[pn].di2;
+        const long long c1 = k1 + nd.di1, c2 = k2 + nd.di2;
         if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) {
           s = se = 0;
           continue;
@@ -676,7 +702,7 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   for (int a = 0; a < ne; ++a) {
     const double lx = P.v2x[P.at(a)], ly = P.v2y[P.at(a)];
     for (int b = a + 1; b < ne; ++b) {
-      if (lx == P.v1x[P.at(b)] && ly == P.v1y[P.at(b)]) {
+      if (same_value(lx, P.v1x[P.at(b)]) && same_value(ly, P.v1y[P.at(b)])) {
         const int u = P.at(a + 1), w = P.at(b);
         double t0;
         int tl;
@@ -690,8 +716,10 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     }
   }
 
-  // area (polygon.jl:114-121), centroid (polygon.jl:210-219), faces.
-  double A = 0.0, Ac = 0.0, cx = 0.0, cy = 0.0;
+  // area (polygon.jl:114-121), centroid (polygon.jl:210-219), faces.  Both
+  // sums of the triangle areas run over the same terms in the same order, so
+  // one accumulator serves both.  The face lengths are computed on demand.
+  double A = 0.0, cx = 0.0, cy = 0.0;
   int nf = 0;
   const int cap = m.cap;
   for (int k = 0; k < ne; ++k) {
@@ -701,10 +729,9 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     const double ax = v1x - px, ay = v1y - py, bx = v2x - px, by = v2y - py;
     const double dA = 0.5 * fabs(ax * by - ay * bx);
     A += dA;
-    Ac += dA;
     const double sx = (px + v1x) + v2x, sy = (py + v1y) + v2y;
-    cx = cx + (dA * sx) / 3.0;
-    cy = cy + (dA * sy) / 3.0;
+    cx = cx + div3(dA * sx);
+    cy = cy + div3(dA * sy);
     m.ev1[(size_t)k * cap + i] = make_double2(v1x, v1y);
     m.ev2[(size_t)k * cap + i] = make_double2(v2x, v2y);
     m.elab[(size_t)k * cap + i] = lab;
@@ -720,7 +747,6 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       const size_t f = (size_t)nf * cap + i;
       m.fnbr[f] = lab;
       m.flrr[f] = sqrt(l2 / r2);
-      m.flen[f] = sqrt(lx * lx + ly * ly);
       m.fm[f] = make_double2(0.5 * (v1x + v2x), 0.5 * (v1y + v2y));
       m.fy[f] = make_double2(yx, yy);
       ++nf;
@@ -729,7 +755,7 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   m.nedges[i] = ne;
   m.nfaces[i] = nf;
   m.area[i] = A;
-  m.centroid[i] = make_double2(cx / Ac, cy / Ac);
+  m.centroid[i] = make_double2(cx / A, cy / A);
   return true;
 }
 
@@ -776,9 +802,23 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len) {
   return LV_OK;
 }
 
+__global__ void k_face_len(MeshDev m, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) lv_face_lengths(m, i);
+}
+
+int lv_mesh_face_len(lv_ctx* c) {
+  if (c->flen_valid) return LV_OK;
+  k_face_len<<<lv_blocks(c->n, 256), 256, 0, c->stream>>>(c->m, c->n);
+  LV_LAUNCH_CHECK(c, "k_face_len");
+  c->flen_valid = true;
+  return LV_OK;
+}
+
 int lv_mesh_remesh(lv_ctx* c) {
   const int n = c->n;
   if (n <= 0) return lv_fail(c, LV_ERR_NOT_MESHED, "remesh: no particles");
+  c->flen_valid = false;
   cudaStream_t s = c->stream;
   const int nc = c->c.ncells;
   {

@@ -20,6 +20,15 @@ namespace {
 
 constexpr int TPB = 256;
 
+// Face loops load FB faces at a time (slot indexes clamped to the last face)
+// so that the loads of a particle's faces overlap instead of forming one
+// chain of dependent round trips; the arithmetic then runs over the faces
+// in order, as before.
+constexpr int FB = 8;
+__device__ __forceinline__ size_t face_slot(int k, int nf, int cap, int i) {
+  return (size_t)(k < nf ? k : nf - 1) * cap + i;
+}
+
 __device__ __forceinline__ double jmax(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double jmin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double dot2(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
@@ -63,20 +72,32 @@ __global__ void k_pstep_v(StateDev s, MeshDev m, int n, double dt) {
   const double2 xi = s.x[i];
   const double Pi = s.P[i], mi = s.mass[i];
   double2 vi = s.v[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f];
-    const double c = dt / mi * lrr * (Pi - s.P[j]);
-    vi.x = vi.x + c * (mm.x - xi.x);
-    vi.y = vi.y + c * (mm.y - xi.y);
+  for (int k0 = 0; k0 < nf; k0 += FB) {
+    int j[FB];
+    double lrr[FB], pj[FB];
+    double2 mm[FB];
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+    }
+#pragma unroll
+    for (int u = 0; u < FB; ++u) pj[u] = ld_nc(s.P + j[u]);
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      if (k0 + u >= nf) break;
+      const double c = dt / mi * lrr[u] * (Pi - pj[u]);
+      vi.x = vi.x + c * (mm[u].x - xi.x);
+      vi.y = vi.y + c * (mm[u].y - xi.y);
+    }
   }
   s.v[i] = vi;
 }
 
 // pressure_step! energy pass (uses the updated velocities).
-__global__ void k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
+__global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i];
@@ -85,17 +106,32 @@ __global__ void k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
   const double2 vi = s.v[i];
   const double2 Pv = make_double2(Pi * vi.x, Pi * vi.y);
   double ei = s.e[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
-    const double Pj = s.P[j];
-    const double2 vj = s.v[j];
-    const double2 Pvj = make_double2(Pj * vj.x, Pj * vj.y);
-    const double a = (mm.x - xi.x) * Pv.x + (mm.y - xi.y) * Pv.y;
-    const double b = (mm.x - y.x) * Pvj.x + (mm.y - y.y) * Pvj.y;
-    ei -= dt * lrr / mi * (a - b);
+  constexpr int B = FB / 2;
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    int j[B];
+    double lrr[B], Pj[B];
+    double2 mm[B], y[B], vj[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+      y[u] = ld_nc(m.fy + f);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      Pj[u] = ld_nc(s.P + j[u]);
+      vj[u] = ld_nc(s.v + j[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u >= nf) break;
+      const double2 Pvj = make_double2(Pj[u] * vj[u].x, Pj[u] * vj[u].y);
+      const double a = (mm[u].x - xi.x) * Pv.x + (mm[u].y - xi.y) * Pv.y;
+      const double b = (mm[u].x - y[u].x) * Pvj.x + (mm[u].y - y[u].y) * Pvj.y;
+      ei -= dt * lrr[u] / mi * (a - b);
+    }
   }
   s.e[i] = ei;
 }
@@ -112,21 +148,35 @@ __global__ void k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
 //   te  = dot(dS, vbc - v_i)/dt                 per boundary edge
 // and k_rhs / k_rhs_gp subtract or add them in the reference's order, so b and
 // GP are bit-identical to evaluating refresh! in full every sweep.
-__global__ void k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
+__global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   const double2 xi = s.x[i];
   const double2 vi = s.v[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
-    const double2 vj = s.v[j];
-    sv.rhs_tf[f] = (lrr / dt) * ((vi.x - vj.x) * (mm.x - y.x) + (vi.y - vj.y) * (mm.y - y.y));
-    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
-    sv.rhs_dmz[f] = make_double2(mm.x - zx, mm.y - zy);
+  constexpr int B = FB / 2;
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    int j[B];
+    double lrr[B];
+    double2 mm[B], y[B], vj[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+      y[u] = ld_nc(m.fy + f);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) vj[u] = ld_nc(s.v + j[u]);
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u >= nf) break;
+      const size_t f = (size_t)(k0 + u) * cap + i;
+      sv.rhs_tf[f] = (lrr[u] / dt) * ((vi.x - vj[u].x) * (mm[u].x - y[u].x) + (vi.y - vj[u].y) * (mm[u].y - y[u].y));
+      const double zx = 0.5 * (xi.x + y[u].x), zy = 0.5 * (xi.y + y[u].y);
+      sv.rhs_dmz[f] = make_double2(mm[u].x - zx, mm[u].y - zy);
+    }
   }
   if (nf < ne) {
     for (int k = 0; k < ne; ++k) {
@@ -163,15 +213,28 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
     if (guess == 1) sv.sgd32[i] = (float)(Pi - sv.pprev[i]);
     bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
     double gpx = 0.0, gpy = 0.0;
-    for (int k = 0; k < nf; ++k) {
-      const size_t f = (size_t)k * cap + i;
-      const int j = m.fnbr[f];
-      const double lrr = m.flrr[f];
-      const double2 mm = m.fm[f];
-      bi -= sv.rhs_tf[f];
-      const double c = lrr * (Pi - s.P[j]);
-      gpx = gpx - c * (mm.x - xi.x);
-      gpy = gpy - c * (mm.y - xi.y);
+    for (int k0 = 0; k0 < nf; k0 += FB) {
+      int j[FB];
+      double lrr[FB], tf[FB], pj[FB];
+      double2 mm[FB];
+#pragma unroll
+      for (int u = 0; u < FB; ++u) {
+        const size_t f = face_slot(k0 + u, nf, cap, i);
+        j[u] = ld_nc(m.fnbr + f);
+        lrr[u] = ld_nc(m.flrr + f);
+        mm[u] = ld_nc(m.fm + f);
+        tf[u] = ld_nc(sv.rhs_tf + f);
+      }
+#pragma unroll
+      for (int u = 0; u < FB; ++u) pj[u] = ld_nc(s.P + j[u]);
+#pragma unroll
+      for (int u = 0; u < FB; ++u) {
+        if (k0 + u >= nf) break;
+        bi -= tf[u];
+        const double c = lrr[u] * (Pi - pj[u]);
+        gpx = gpx - c * (mm[u].x - xi.x);
+        gpy = gpy - c * (mm[u].y - xi.y);
+      }
     }
     if (nf < ne) {
       for (int k = 0; k < ne; ++k) {
@@ -189,7 +252,24 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
     if (on) {
       // b - A P with the operator's difference form
       double ap = sv.diag[i] * Pi;
-      for (int e = sv.rowptr[i]; e < sv.rowptr[i + 1]; ++e) ap += sv.w[e] * (Pi - s.P[sv.col[e]]);
+      const int e0 = sv.rowptr[i], e1 = sv.rowptr[i + 1];
+      for (int b0 = e0; b0 < e1; b0 += FB) {
+        int j[FB];
+        double w[FB], pj[FB];
+#pragma unroll
+        for (int u = 0; u < FB; ++u) {
+          const int e = min(b0 + u, e1 - 1);
+          j[u] = ld_nc(sv.col + e);
+          w[u] = ld_nc(sv.w + e);
+        }
+#pragma unroll
+        for (int u = 0; u < FB; ++u) pj[u] = ld_nc(s.P + j[u]);
+#pragma unroll
+        for (int u = 0; u < FB; ++u) {
+          if (b0 + u >= e1) break;
+          ap += w[u] * (Pi - pj[u]);
+        }
+      }
       res = bi - ap;
     }
     lv_sweep_sums(sv, i, on, res, 0.0, D, false, true, n);
@@ -208,13 +288,24 @@ __global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess, 
     const int cap = m.cap, nf = m.nfaces[i];
     const double2 gi = s.GP[i];
     bi = sv.b[i];
-    for (int k = 0; k < nf; ++k) {
-      const size_t f = (size_t)k * cap + i;
-      const int j = m.fnbr[f];
-      const double lrr = m.flrr[f];
-      const double2 dmz = sv.rhs_dmz[f];
-      const double2 gj = s.GP[j];
-      bi += lrr * ((gi.x - gj.x) * dmz.x + (gi.y - gj.y) * dmz.y);
+    for (int k0 = 0; k0 < nf; k0 += FB) {
+      int j[FB];
+      double lrr[FB];
+      double2 dmz[FB], gj[FB];
+#pragma unroll
+      for (int u = 0; u < FB; ++u) {
+        const size_t f = face_slot(k0 + u, nf, cap, i);
+        j[u] = ld_nc(m.fnbr + f);
+        lrr[u] = ld_nc(m.flrr + f);
+        dmz[u] = ld_nc(sv.rhs_dmz + f);
+      }
+#pragma unroll
+      for (int u = 0; u < FB; ++u) gj[u] = ld_nc(s.GP + j[u]);
+#pragma unroll
+      for (int u = 0; u < FB; ++u) {
+        if (k0 + u >= nf) break;
+        bi += lrr[u] * ((gi.x - gj[u].x) * dmz[u].x + (gi.y - gj[u].y) * dmz[u].y);
+      }
     }
     sv.b[i] = bi;
   }
@@ -234,17 +325,29 @@ __global__ void k_find_D(StateDev s, MeshDev m, int n) {
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 vi = s.v[i];
   double d11 = 0.0, d21 = 0.0, d12 = 0.0, d22 = 0.0;
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
-    const double2 vj = s.v[j];
-    const double ax = vi.x - vj.x, ay = vi.y - vj.y, bx = mm.x - y.x, by = mm.y - y.y;
-    d11 += lrr * (ax * bx);
-    d21 += lrr * (ay * bx);
-    d12 += lrr * (ax * by);
-    d22 += lrr * (ay * by);
+  for (int k0 = 0; k0 < nf; k0 += FB) {
+    int j[FB];
+    double lrr[FB];
+    double2 mm[FB], y[FB], vj[FB];
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+      y[u] = ld_nc(m.fy + f);
+    }
+#pragma unroll
+    for (int u = 0; u < FB; ++u) vj[u] = ld_nc(s.v + j[u]);
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      if (k0 + u >= nf) break;
+      const double ax = vi.x - vj[u].x, ay = vi.y - vj[u].y, bx = mm[u].x - y[u].x, by = mm[u].y - y[u].y;
+      d11 += lrr[u] * (ax * bx);
+      d21 += lrr[u] * (ay * bx);
+      d12 += lrr[u] * (ax * by);
+      d22 += lrr[u] * (ay * by);
+    }
   }
   const double A = m.area[i];
   d11 = d11 / A;
@@ -270,7 +373,7 @@ __global__ void k_stress(StateDev s, int n, double avdr, double2* Sa, double2* S
 }
 
 // viscous_step! velocity pass (diffusion.jl:41-46)
-__global__ void k_visc_v(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
+__global__ void __launch_bounds__(TPB, 2) k_visc_v(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
                          const double2* __restrict__ Sb) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -279,23 +382,39 @@ __global__ void k_visc_v(StateDev s, MeshDev m, int n, double dt, const double2*
   const double mi = s.mass[i];
   const double2 sa = Sa[i], sb = Sb[i];
   double2 vi = s.v[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f];
-    const double2 qa = Sa[j], qb = Sb[j];
-    const double c = dt * lrr / mi;
-    const double M11 = c * (sa.x - qa.x), M21 = c * (sa.y - qa.y), M12 = c * (sb.x - qb.x), M22 = c * (sb.y - qb.y);
-    const double dx = mm.x - xi.x, dy = mm.y - xi.y;
-    vi.x = vi.x - (M11 * dx + M12 * dy);
-    vi.y = vi.y - (M21 * dx + M22 * dy);
+  constexpr int B = FB / 2;
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    int j[B];
+    double lrr[B];
+    double2 mm[B], qa[B], qb[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      qa[u] = ld_nc(Sa + j[u]);
+      qb[u] = ld_nc(Sb + j[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u >= nf) break;
+      const double c = dt * lrr[u] / mi;
+      const double M11 = c * (sa.x - qa[u].x), M21 = c * (sa.y - qa[u].y), M12 = c * (sb.x - qb[u].x),
+                   M22 = c * (sb.y - qb[u].y);
+      const double dx = mm[u].x - xi.x, dy = mm[u].y - xi.y;
+      vi.x = vi.x - (M11 * dx + M12 * dy);
+      vi.y = vi.y - (M21 * dx + M22 * dy);
+    }
   }
   s.v[i] = vi;
 }
 
 // viscous_step! energy pass (diffusion.jl:47-52)
-__global__ void k_visc_e(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
+__global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
                          const double2* __restrict__ Sb) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -306,17 +425,33 @@ __global__ void k_visc_e(StateDev s, MeshDev m, int n, double dt, const double2*
   const double2 vi = s.v[i];
   const double Svx = sa.x * vi.x + sb.x * vi.y, Svy = sa.y * vi.x + sb.y * vi.y;
   double ei = s.e[i];
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
-    const double2 qa = Sa[j], qb = Sb[j];
-    const double2 vj = s.v[j];
-    const double Sqx = qa.x * vj.x + qb.x * vj.y, Sqy = qa.y * vj.x + qb.y * vj.y;
-    const double a = (mm.x - xi.x) * Svx + (mm.y - xi.y) * Svy;
-    const double b = (mm.x - y.x) * Sqx + (mm.y - y.y) * Sqy;
-    ei += dt * lrr / mi * (a - b);
+  constexpr int B = FB / 2;
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    int j[B];
+    double lrr[B];
+    double2 mm[B], y[B], qa[B], qb[B], vj[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+      mm[u] = ld_nc(m.fm + f);
+      y[u] = ld_nc(m.fy + f);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      qa[u] = ld_nc(Sa + j[u]);
+      qb[u] = ld_nc(Sb + j[u]);
+      vj[u] = ld_nc(s.v + j[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u >= nf) break;
+      const double Sqx = qa[u].x * vj[u].x + qb[u].x * vj[u].y, Sqy = qa[u].y * vj[u].x + qb[u].y * vj[u].y;
+      const double a = (mm[u].x - xi.x) * Svx + (mm[u].y - xi.y) * Svy;
+      const double b = (mm[u].x - y[u].x) * Sqx + (mm[u].y - y[u].y) * Sqy;
+      ei += dt * lrr[u] / mi * (a - b);
+    }
   }
   s.e[i] = ei;
 }
@@ -373,14 +508,24 @@ __global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha)
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double2 c = m.centroid[i];
-  double rmax = 0.0, rmin = __longlong_as_double(0x7ff0000000000000LL);
-  for (int k = 0; k < nf; ++k) {
-    const double2 y = m.fy[(size_t)k * cap + i];
-    const double dx = xi.x - y.x, dy = xi.y - y.y;
-    const double r = sqrt(dx * dx + dy * dy);
-    rmax = jmax(rmax, r);
-    rmin = jmin(rmin, r);
+  // the extreme distances are the square roots of the extreme squared
+  // distances (sqrt is correctly rounded and monotone, and jmax/jmin keep
+  // the first of equal values), so two square roots instead of one per face
+  double r2max = 0.0, r2min = __longlong_as_double(0x7ff0000000000000LL);
+  for (int k0 = 0; k0 < nf; k0 += FB) {
+    double2 y[FB];
+#pragma unroll
+    for (int u = 0; u < FB; ++u) y[u] = ld_nc(m.fy + face_slot(k0 + u, nf, cap, i));
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      if (k0 + u >= nf) break;
+      const double dx = xi.x - y[u].x, dy = xi.y - y[u].y;
+      const double r2 = dx * dx + dy * dy;
+      r2max = jmax(r2max, r2);
+      r2min = jmin(r2min, r2);
+    }
   }
+  const double rmax = sqrt(r2max), rmin = sqrt(r2min);
   const double q = rmin / rmax;
   s.quality[i] = q;
   const double2 a = s.Da[i], b = s.Db[i];
@@ -393,16 +538,18 @@ __global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha)
 // relaxation_step! first loop (relaxation.jl:37-66): conservative remap of
 // mass, momentum and energy along dv with the Rusanov flux.
 // |dv| of every particle, evaluated once instead of on every face that
-// reads it (the same expression, so the same value)
-__global__ void k_norm_dv(StateDev s, int n, double* ndv) {
+// reads it (the same expression, so the same value); lens: also the face
+// lengths of the mesh (lv_face_lengths)
+__global__ void k_norm_dv(StateDev s, MeshDev m, int n, double* ndv, int lens) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double2 d = s.dv[i];
   ndv[i] = sqrt(d.x * d.x + d.y * d.y);
+  if (lens) lv_face_lengths(m, i);
 }
 
 // ndv: |dv| of every particle (k_norm_dv), read when rusanov is set
-__global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov, const double* __restrict__ ndv) {
+__global__ void __launch_bounds__(TPB, 2) k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov, const double* __restrict__ ndv) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i];
@@ -414,38 +561,63 @@ __global__ void k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusano
   double momx = mass * vp.x, momy = mass * vp.y;
   double energy = mass * ep;
   const double ndvp = rusanov ? ndv[i] : 0.0;
-  for (int k = 0; k < nf; ++k) {
-    const size_t f = (size_t)k * cap + i;
-    const int j = m.fnbr[f];
-    if (s.phase[j] != php) continue;
-    const double lrr = m.flrr[f];
-    const double2 mm = m.fm[f], y = m.fy[f];
-    const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
-    const double rq = s.rho[j], eq = s.e[j];
-    const double2 vq = s.v[j], dvq = s.dv[j];
-    const double pqx = xi.x - y.x, pqy = xi.y - y.y;
-    const double mzx = mm.x - zx, mzy = mm.y - zy;
-    const double pdvpq = dvp.x * pqx + dvp.y * pqy;
-    const double qdvpq = dvq.x * pqx + dvq.y * pqy;
-    const double pdvmz = dvp.x * mzx + dvp.y * mzy;
-    const double qdvmz = dvq.x * mzx + dvq.y * mzy;
-    const double kk = dt * lrr;
-    mass += kk * ((pdvmz * rp - qdvmz * rq) - 0.5 * (pdvpq * rp + qdvpq * rq));
-    const double a1 = pdvmz * rp, a2 = qdvmz * rq, b1 = pdvpq * rp, b2 = qdvpq * rq;
-    const double t1x = a1 * vp.x - a2 * vq.x, t1y = a1 * vp.y - a2 * vq.y;
-    const double t2x = b1 * vp.x + b2 * vq.x, t2y = b1 * vp.y + b2 * vq.y;
-    momx = momx + kk * (t1x - 0.5 * t2x);
-    momy = momy + kk * (t1y - 0.5 * t2y);
-    energy += kk * ((pdvmz * rp * ep - qdvmz * rq * eq) - 0.5 * (pdvpq * rp * ep + qdvpq * rq * eq));
-    if (rusanov) {
-      const double ndvq = ndv[j];
-      const double a = jmax(ndvp, ndvq);
-      const double l = m.flen[f];
-      const double cr = 0.5 * dt * l * a;
-      mass += cr * (rq - rp);
-      momx = momx + cr * (rq * vq.x - rp * vp.x);
-      momy = momy + cr * (rq * vq.y - rp * vp.y);
-      energy += cr * (rq * eq - rp * ep);
+  constexpr int B = 2;  // six gathers per face
+  for (int k0 = 0; k0 < nf; k0 += B) {
+    int jb[B], phb[B];
+    double lrrb[B], lb[B], rqb[B], eqb[B], nqb[B];
+    double2 mmb[B], yb[B], vqb[B], dvqb[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      jb[u] = ld_nc(m.fnbr + f);
+      lrrb[u] = ld_nc(m.flrr + f);
+      mmb[u] = ld_nc(m.fm + f);
+      yb[u] = ld_nc(m.fy + f);
+      lb[u] = rusanov ? ld_nc(m.flen + f) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const int j = jb[u];
+      phb[u] = ld_nc(s.phase + j);
+      rqb[u] = ld_nc(s.rho + j);
+      eqb[u] = ld_nc(s.e + j);
+      vqb[u] = ld_nc(s.v + j);
+      dvqb[u] = ld_nc(s.dv + j);
+      nqb[u] = rusanov ? ld_nc(ndv + j) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      if (k0 + u >= nf) break;
+      if (phb[u] != php) continue;
+      const double lrr = lrrb[u];
+      const double2 mm = mmb[u], y = yb[u];
+      const double zx = 0.5 * (xi.x + y.x), zy = 0.5 * (xi.y + y.y);
+      const double rq = rqb[u], eq = eqb[u];
+      const double2 vq = vqb[u], dvq = dvqb[u];
+      const double pqx = xi.x - y.x, pqy = xi.y - y.y;
+      const double mzx = mm.x - zx, mzy = mm.y - zy;
+      const double pdvpq = dvp.x * pqx + dvp.y * pqy;
+      const double qdvpq = dvq.x * pqx + dvq.y * pqy;
+      const double pdvmz = dvp.x * mzx + dvp.y * mzy;
+      const double qdvmz = dvq.x * mzx + dvq.y * mzy;
+      const double kk = dt * lrr;
+      mass += kk * ((pdvmz * rp - qdvmz * rq) - 0.5 * (pdvpq * rp + qdvpq * rq));
+      const double a1 = pdvmz * rp, a2 = qdvmz * rq, b1 = pdvpq * rp, b2 = qdvpq * rq;
+      const double t1x = a1 * vp.x - a2 * vq.x, t1y = a1 * vp.y - a2 * vq.y;
+      const double t2x = b1 * vp.x + b2 * vq.x, t2y = b1 * vp.y + b2 * vq.y;
+      momx = momx + kk * (t1x - 0.5 * t2x);
+      momy = momy + kk * (t1y - 0.5 * t2y);
+      energy += kk * ((pdvmz * rp * ep - qdvmz * rq * eq) - 0.5 * (pdvpq * rp * ep + qdvpq * rq * eq));
+      if (rusanov) {
+        const double ndvq = nqb[u];
+        const double a = jmax(ndvp, ndvq);
+        const double l = lb[u];
+        const double cr = 0.5 * dt * l * a;
+        mass += cr * (rq - rp);
+        momx = momx + cr * (rq * vq.x - rp * vp.x);
+        momy = momy + cr * (rq * vq.y - rp * vp.y);
+        energy += cr * (rq * eq - rp * ep);
+      }
     }
   }
   s.mass[i] = mass;
@@ -709,7 +881,10 @@ int lv_phys_find_dv(lv_ctx* c, double dt, double alpha) {
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov) {
   if (int rc = need_mesh(c)) return rc;
   double* ndv = c->sv.q;  // scratch between solves
-  if (rusanov) LAUNCH(k_norm_dv, c->s, c->n, ndv);
+  if (rusanov) {
+    LAUNCH(k_norm_dv, c->s, c->m, c->n, ndv, c->flen_valid ? 0 : 1);
+    c->flen_valid = true;
+  }
   LAUNCH(k_relax_flux, c->s, c->m, c->n, dt, rusanov, ndv);
   LAUNCH(k_relax_update, c->s, c->n, dt);
   c->meshed = false;

@@ -202,7 +202,7 @@ std::vector<PathNodeDev> path_upto(const GridDev& g, double bound) {
   std::stable_sort(all.begin(), all.end(), [](const Node& p, const Node& q) { return p.rr < q.rr; });
   std::vector<PathNodeDev> out;
   for (const auto& nd : all) {
-    out.push_back(PathNodeDev{(int)nd.i1, (int)nd.i2, nd.rr});
+    out.push_back(PathNodeDev{(int)nd.i1, (int)nd.i2, nd.rr, (float)nd.rr, nd.rr > bound ? 1 : 0});
     if (nd.rr > bound) break;
   }
   return out;
