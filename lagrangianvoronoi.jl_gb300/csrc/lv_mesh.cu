@@ -404,6 +404,28 @@ __device__ int clip_exact(const Poly& P, int& ne, double px, double py, double y
 // FP64 rounding of the reference expression in absolute coordinates
 // (<= 4e-15 D M, M = max |coordinate|), so |f32| > that margin + 2 eps
 // decides signum(f) exactly; otherwise f is evaluated in FP64.
+//
+// FP64 work is priced per warp instruction, so it is laid out for the warp:
+// the pass over the edges only classifies (float, FP64 just for vertices
+// within the margin); the vertex values of the two crossing edges, their
+// intersection points and the float offsets of those points are then
+// computed by every lane with the same instructions, and written to the slots
+// through selects instead of branches.  The values are the same expressions
+// as the reference's, so the result is unchanged.
+__device__ __forceinline__ void put_vertex(const Poly& P, int k, bool first, double vx, double vy, float fx,
+                                           float fy) {
+  const int a = P.at(k);
+  double* X = first ? P.v1x : P.v2x;
+  double* Y = first ? P.v1y : P.v2y;
+  float* RX = first ? P.r1x : P.r2x;
+  float* RY = first ? P.r1y : P.r2y;
+  X[a] = vx;
+  Y[a] = vy;
+  RX[a] = fx;
+  RY[a] = fy;
+  if (first) P.d2[a] = d2_up(fx, fy);
+}
+
 __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm) {
   const double dfx = yx - px, dfy = yy - py;
   const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
@@ -416,34 +438,29 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   R = 0.5f * sqrtf(R) * 1.0001f;
   const float margin = 1e-6f * (D * R + D * D) + 4e-15f * D * bigm + 1e-14f;
   const float half = 0.5f * dd2;
-  // pre-pass: per-edge code 0 keep, 1 event-keep, 2 event-delete, 3 delete
+  // classification: per-edge code 0 keep, 1 event-keep, 2 event-delete, 3 delete
   unsigned long long code = 0ull;  // 2 bits per slot
   int nev = 0;
   int e0_slot = 0, e1_slot = 0, e0_s1 = 0, e0_s2 = 0, e1_s1 = 0, e1_s2 = 0;
-  double e0_f1 = 0.0, e0_f2 = 0.0, e1_f1 = 0.0, e1_f2 = 0.0;
   for (int k = 0; k < ne; ++k) {
     const int a = P.at(k);
     const float g1 = dx * P.r1x[a] + dy * P.r1y[a] - half;
     const float g2 = dx * P.r2x[a] + dy * P.r2y[a] - half;
     int s1, s2;
-    double f1 = 0.0, f2 = 0.0;
-    bool exact1 = false, exact2 = false;
     if (g1 < -margin) s1 = -1;
     else if (g1 > margin) s1 = 1;
-    else { f1 = dfx * P.v1x[a] + dfy * P.v1y[a] - c; s1 = signum_eps(f1); exact1 = true; }
+    else s1 = signum_eps(dfx * P.v1x[a] + dfy * P.v1y[a] - c);
     if (g2 < -margin) s2 = -1;
     else if (g2 > margin) s2 = 1;
-    else { f2 = dfx * P.v2x[a] + dfy * P.v2y[a] - c; s2 = signum_eps(f2); exact2 = true; }
+    else s2 = signum_eps(dfx * P.v2x[a] + dfy * P.v2y[a] - c);
     const int s12 = s1 + s2;
     unsigned cd = 0;
     if (0 <= s12 && s12 <= 1 && (s1 | s2) != 0) {
       if (nev >= 2) return 2;
-      if (!exact1) f1 = dfx * P.v1x[a] + dfy * P.v1y[a] - c;
-      if (!exact2) f2 = dfx * P.v2x[a] + dfy * P.v2y[a] - c;
       if (nev == 0) {
-        e0_slot = k; e0_s1 = s1; e0_s2 = s2; e0_f1 = f1; e0_f2 = f2;
+        e0_slot = k; e0_s1 = s1; e0_s2 = s2;
       } else {
-        e1_slot = k; e1_s1 = s1; e1_s2 = s2; e1_f1 = f1; e1_f2 = f2;
+        e1_slot = k; e1_s1 = s1; e1_s2 = s2;
       }
       ++nev;
       cd = (s12 >= 1) ? 2u : 1u;
@@ -457,30 +474,33 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
     return 0;
   }
   if (nev != 2) return 2;
-  // intersection points of the two crossing edges (from their original data)
+  // the crossing edges' vertex values and intersection points (original
+  // data).  Their vertices have s1 != s2 in sign or one zero, so f1 != f2.
   double X0x, X0y, X1x, X1y;
   {
     const int a = P.at(e0_slot);
     const double a1x = P.v1x[a], a1y = P.v1y[a], a2x = P.v2x[a], a2y = P.v2y[a];
+    const double f1 = dfx * a1x + dfy * a1y - c;
+    const double f2 = dfx * a2x + dfy * a2y - c;
+    const double inv = 1.0 / (f1 - f2);
+    X0x = inv * (f1 * a2x - f2 * a1x);
+    X0y = inv * (f1 * a2y - f2 * a1y);
+    if (e0_s1 == 0) { X0x = a1x; X0y = a1y; }
     if (e0_s2 == 0) { X0x = a2x; X0y = a2y; }
-    else if (e0_s1 == 0) { X0x = a1x; X0y = a1y; }
-    else {
-      const double inv = 1.0 / (e0_f1 - e0_f2);
-      X0x = inv * (e0_f1 * a2x - e0_f2 * a1x);
-      X0y = inv * (e0_f1 * a2y - e0_f2 * a1y);
-    }
   }
   {
     const int a = P.at(e1_slot);
     const double a1x = P.v1x[a], a1y = P.v1y[a], a2x = P.v2x[a], a2y = P.v2y[a];
+    const double f1 = dfx * a1x + dfy * a1y - c;
+    const double f2 = dfx * a2x + dfy * a2y - c;
+    const double inv = 1.0 / (f1 - f2);
+    X1x = inv * (f1 * a2x - f2 * a1x);
+    X1y = inv * (f1 * a2y - f2 * a1y);
+    if (e1_s1 == 0) { X1x = a1x; X1y = a1y; }
     if (e1_s2 == 0) { X1x = a2x; X1y = a2y; }
-    else if (e1_s1 == 0) { X1x = a1x; X1y = a1y; }
-    else {
-      const double inv = 1.0 / (e1_f1 - e1_f2);
-      X1x = inv * (e1_f1 * a2x - e1_f2 * a1x);
-      X1y = inv * (e1_f1 * a2y - e1_f2 * a1y);
-    }
   }
+  const float q0x = (float)(X0x - px), q0y = (float)(X0y - py);
+  const float q1x = (float)(X1x - px), q1y = (float)(X1y - py);
   // the reference's sequential pass over the slots with swap-delete; the
   // crossing identity (2 bits: 0 none, 1 first, 2 second in slot order)
   // travels with its slot.
@@ -511,28 +531,22 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
       ++i;
     }
   }
-  if (fs0 >= 0) {
-    if (e0_s1 == 1) set_v1(P, fs0, X0x, X0y, px, py);
-    else set_v2(P, fs0, X0x, X0y, px, py);
-  }
-  if (fs1 >= 0) {
-    if (e1_s1 == 1) set_v1(P, fs1, X1x, X1y, px, py);
-    else set_v2(P, fs1, X1x, X1y, px, py);
-  }
+  // a kept crossing edge: its outside vertex becomes the intersection point
+  if (fs0 >= 0) put_vertex(P, fs0, e0_s1 == 1, X0x, X0y, q0x, q0y);
+  if (fs1 >= 0) put_vertex(P, fs1, e1_s1 == 1, X1x, X1y, q1x, q1y);
   ne = nn;
   // new edge from X = the crossing visited last, Y = the one visited first
-  const double Xx = (visited_last == 1) ? X0x : X1x, Xy = (visited_last == 1) ? X0y : X1y;
-  const double Yx = (visited_first == 1) ? X0x : X1x, Yy = (visited_first == 1) ? X0y : X1y;
+  const bool xl0 = visited_last == 1, yf0 = visited_first == 1;
+  const double Xx = xl0 ? X0x : X1x, Xy = xl0 ? X0y : X1y;
+  const double Yx = yf0 ? X0x : X1x, Yy = yf0 ? X0y : X1y;
   if (same_value(Xx, Yx) && same_value(Xy, Yy)) return 0;
   if (ne >= P.cap_e) return -1;
+  const float rXx = xl0 ? q0x : q1x, rXy = xl0 ? q0y : q1y;
+  const float rYx = yf0 ? q0x : q1x, rYy = yf0 ? q0y : q1y;
   const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
-  if (ax * by - ay * bx > 0.0) {
-    set_v1(P, ne, Yx, Yy, px, py);
-    set_v2(P, ne, Xx, Xy, px, py);
-  } else {
-    set_v1(P, ne, Xx, Xy, px, py);
-    set_v2(P, ne, Yx, Yy, px, py);
-  }
+  const bool inv = ax * by - ay * bx > 0.0;  // reorient counter-clockwise: Y -> X
+  put_vertex(P, ne, true, inv ? Yx : Xx, inv ? Yy : Xy, inv ? rYx : rXx, inv ? rYy : rXy);
+  put_vertex(P, ne, false, inv ? Xx : Yx, inv ? Xy : Yy, inv ? rXx : rYx, inv ? rXy : rYy);
   P.lab[P.at(ne)] = label;
   ++ne;
   return 1;

@@ -985,7 +985,6 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
   a.out_iters = c->sv.iters + slot;
   a.out_d = c->sv.dstats + 3 * slot;
   a.counters = c->sv.counters;
-  cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
   if (c->method == LV_METHOD_LEARNED_PCG && !c->factor_valid) {
     // the network's factor for this operator (once per assembly)
     KernelTimer kf(c, LV_KF_LEARN);
@@ -998,6 +997,8 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     const bool learned = c->method == LV_METHOD_LEARNED_PCG;
     // systems that fit one or two blocks per SM: flag-reduced solver
     if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);
+    // the grid barriers of the cooperative solvers below start from zero
+    cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
     // larger systems: the streaming variant
     {
       LearnArgs la;
@@ -1041,6 +1042,7 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
       return LV_OK;
     }
   }
+  cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
   // small systems: register-resident pipelined CG, one barrier per iteration
   if (g_reg_blocks_per_sm[0] < 0) {
     int b1 = 0, b2 = 0;
