@@ -300,6 +300,10 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.rhs_tf = dalloc<double>(c, ell, &ok);
   sv.rhs_dmz = dalloc<double2>(c, ell, &ok);
   sv.rhs_te = dalloc<double>(c, ell, &ok);
+  sv.rhs_dm = dalloc<double2>(c, ell, &ok);
+  sv.rhs_den = dalloc<double>(c, cap, &ok);
+  sv.rhs_rden = dalloc<double>(c, cap, &ok);
+  sv.rhs_rm = dalloc<double>(c, cap, &ok);
   sv.counters = dalloc<long long>(c, 4, &ok);
   sv.bar = dalloc<unsigned>(c, 4, &ok);
   sv.iters = dalloc<int>(c, LV_IT_SIZE, &ok);

@@ -83,6 +83,26 @@ struct MeshDev {
   double2* centroid;
 };
 
+// RN(a / b) from y = RN(1/b) without a division (Markstein, IBM J. Res. Dev.
+// 34(1), 1990): q0 = RN(a y) lies within 1.5 ulp of a/b, one correction
+// q1 = RN(q0 + RN(a - b q0) y) within one ulp, and for such a q1 the residual
+// a - b q1 is exact and RN(q1 + (a - b q1) y) is the correctly rounded
+// quotient (Markstein's theorem).  For |a| outside [2^-900, 2^900) or |b|
+// outside [2^-100, 2^100) (zeros, infinities, NaN, and every case where an
+// intermediate could under- or overflow) the division itself.
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
+  if (ea - 123u < 1800u && eb - 923u < 200u) {
+    double q = a * y;
+    double r = fma(-b, q, a);
+    q = fma(r, y, q);
+    r = fma(-b, q, a);
+    return fma(r, y, q);
+  }
+  return a / b;
+}
+
 // Loads of data that no thread writes during the kernel, issued where they
 // stand in the source (volatile inline PTX): the face and row loops load a
 // batch of faces (entries) this way and only then use them, so that the
@@ -100,6 +120,11 @@ __device__ __forceinline__ float ld_nc(const float* p) {
 __device__ __forceinline__ double ld_nc(const double* p) {
   double v;
   asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float4 ld_nc(const float4* p) {
+  float4 v;
+  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
   return v;
 }
 __device__ __forceinline__ double2 ld_nc(const double2* p) {
@@ -171,6 +196,10 @@ struct SolverDev {
   double* rhs_tf;    // (lrr/dt) dot(v_i - v_j, m - y) per face
   double2* rhs_dmz;  // m - midpoint(x_i, y) per face
   double* rhs_te;    // dot(dS, vbc - v_i)/dt per boundary edge
+  double2* rhs_dm;   // m - x_i per face
+  double* rhs_den;   // rho c2 dt^2 per particle
+  double* rhs_rden;  // RN(1 / rhs_den)
+  double* rhs_rm;    // RN(1 / mass)
   // explicit learned M^-1 on the two-hop pattern (lv_fcg.cu, allocated on first use)
   int *mcnt = nullptr, *mcol = nullptr;
   float *mval = nullptr, *mdiag = nullptr;

@@ -88,26 +88,53 @@ __global__ void k_lprep(int n, const int* __restrict__ rowptr, const int* __rest
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int a = rowptr[i], b = rowptr[i + 1];
+  const float dhi = dh[i];
   float s = 0.f, m = 0.f, sl = 0.f, ml = 0.f;
   int nl = 0;
-  for (int k = a; k < b; ++k) {
-    const int j = col[k];
-    const float v = (float)w[k] * dh[i] * dh[j];
-    what[k] = v;
-    s += v;
-    m = fmaxf(m, v);
-    if (j < i) {
-      sl += v;
-      ml = fmaxf(ml, v);
-      ++nl;
+  // entries eight at a time, and each neighbour's row searched eight entries
+  // at a time (indexes clamped), so that the loads of a round overlap
+  constexpr int EB = 8;
+  for (int kb = a; kb < b; kb += EB) {
+    int jj[EB], r0[EB], r1[EB];
+    double wv[EB];
+    float dj[EB];
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int k = min(kb + u, b - 1);
+      jj[u] = ld_nc(col + k);
+      wv[u] = ld_nc(w + k);
     }
-    int r = -1;
-    for (int t = rowptr[j]; t < rowptr[j + 1]; ++t)
-      if (col[t] == i) {
-        r = t;
-        break;
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      dj[u] = ld_nc(dh + jj[u]);
+      r0[u] = ld_nc(rowptr + jj[u]);
+      r1[u] = ld_nc(rowptr + jj[u] + 1);
+    }
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int k = kb + u;
+      if (k >= b) break;
+      const int j = jj[u];
+      const float v = (float)wv[u] * dhi * dj[u];
+      what[k] = v;
+      s += v;
+      m = fmaxf(m, v);
+      if (j < i) {
+        sl += v;
+        ml = fmaxf(ml, v);
+        ++nl;
       }
-    rev[k] = r;
+      int r = -1;
+      for (int t0 = r0[u]; t0 < r1[u] && r < 0; t0 += EB) {
+        int cc[EB];
+#pragma unroll
+        for (int q = 0; q < EB; ++q) cc[q] = ld_nc(col + min(t0 + q, r1[u] - 1));
+#pragma unroll
+        for (int q = 0; q < EB; ++q)
+          if (r < 0 && t0 + q < r1[u] && cc[q] == i) r = t0 + q;
+      }
+      rev[k] = r;
+    }
   }
   float* x = X + (size_t)i * FIN;
   x[0] = 1.f;
@@ -229,35 +256,41 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
       own[4 * f + 2] = v.z;
       own[4 * f + 3] = v.w;
     }
-    // two neighbours per round, their loads issued together; the sum runs
-    // over the neighbours in order
+    // the row's neighbours eight at a time: their indexes and weights in one
+    // round of loads, their feature rows in two rounds of four (indexes
+    // clamped to the row's last); the sum runs over the neighbours in order
+    constexpr int IB = 8, HB = 4;
     const int k1 = rowptr[row + 1];
-    for (int k = rowptr[row]; k < k1; k += 2) {
-      const bool two = k + 1 < k1;
-      const int ja = col[k], jb = two ? col[k + 1] : ja;
-      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
-      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
-      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
-      float4 va[FH / 4], vb[FH / 4];
+    for (int kb = rowptr[row]; kb < k1; kb += IB) {
+      int jj[IB];
+      float ww[IB];
 #pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        va[f] = ha[f];
-        vb[f] = hb[f];
+      for (int u = 0; u < IB; ++u) {
+        const int k = min(kb + u, k1 - 1);
+        jj[u] = ld_nc(col + k);
+        ww[u] = ld_nc(what + k);
       }
 #pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
-        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
-        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
-        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
-      }
-      if (two) {
+      for (int h0 = 0; h0 < IB; h0 += HB) {
+        if (kb + h0 >= k1) break;
+        float4 hv[HB][FH / 4];
 #pragma unroll
-        for (int f = 0; f < FH / 4; ++f) {
-          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
-          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
-          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
-          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
+        for (int u = 0; u < HB; ++u) {
+          const float4* hr4 = reinterpret_cast<const float4*>(Hin + (size_t)jj[h0 + u] * KH + half * FH);
+#pragma unroll
+          for (int f = 0; f < FH / 4; ++f) hv[u][f] = ld_nc(hr4 + f);
+        }
+#pragma unroll
+        for (int u = 0; u < HB; ++u) {
+          if (kb + h0 + u >= k1) break;
+          const float w = ww[h0 + u];
+#pragma unroll
+          for (int f = 0; f < FH / 4; ++f) {
+            agg[4 * f] = fmaf(w, hv[u][f].x, agg[4 * f]);
+            agg[4 * f + 1] = fmaf(w, hv[u][f].y, agg[4 * f + 1]);
+            agg[4 * f + 2] = fmaf(w, hv[u][f].z, agg[4 * f + 2]);
+            agg[4 * f + 3] = fmaf(w, hv[u][f].w, agg[4 * f + 3]);
+          }
         }
       }
     }

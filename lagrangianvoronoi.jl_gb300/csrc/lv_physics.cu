@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double Pi = s.P[i], mi = s.mass[i];
+  const double rmi = 1.0 / mi;  // the per-face divisions by mi through div_rcp
   const double2 vi = s.v[i];
   const double2 Pv = make_double2(Pi * vi.x, Pi * vi.y);
   double ei = s.e[i];
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n
       const double2 Pvj = make_double2(Pj[u] * vj[u].x, Pj[u] * vj[u].y);
       const double a = (mm[u].x - xi.x) * Pv.x + (mm[u].y - xi.y) * Pv.y;
       const double b = (mm[u].x - y[u].x) * Pvj.x + (mm[u].y - y[u].y) * Pvj.y;
-      ei -= dt * lrr[u] / mi * (a - b);
+      ei -= div_rcp(dt * lrr[u], mi, rmi) * (a - b);
     }
   }
   s.e[i] = ei;
@@ -154,6 +155,12 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   const double2 xi = s.x[i];
   const double2 vi = s.v[i];
+  // the fixed factors of k_rhs: the divisor of the first term with its
+  // reciprocal, and the reciprocal of the mass (divisions by div_rcp)
+  const double den = s.rho[i] * s.c2[i] * (dt * dt);
+  sv.rhs_den[i] = den;
+  sv.rhs_rden[i] = 1.0 / den;
+  sv.rhs_rm[i] = 1.0 / s.mass[i];
   constexpr int B = FB / 2;
   for (int k0 = 0; k0 < nf; k0 += B) {
     int j[B];
@@ -176,6 +183,7 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
       sv.rhs_tf[f] = (lrr[u] / dt) * ((vi.x - vj[u].x) * (mm[u].x - y[u].x) + (vi.y - vj[u].y) * (mm[u].y - y[u].y));
       const double zx = 0.5 * (xi.x + y[u].x), zy = 0.5 * (xi.y + y[u].y);
       sv.rhs_dmz[f] = make_double2(mm[u].x - zx, mm[u].y - zy);
+      sv.rhs_dm[f] = make_double2(mm[u].x - xi.x, mm[u].y - xi.y);
     }
   }
   if (nf < ne) {
@@ -208,21 +216,21 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
   double bi = 0.0, Pi = 0.0;
   if (on) {
     const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
-    const double2 xi = s.x[i];
     Pi = s.P[i];
     if (guess == 1) sv.sgd32[i] = (float)(Pi - sv.pprev[i]);
-    bi = m.area[i] * Pi / (s.rho[i] * s.c2[i] * (dt * dt));
+    // area Pi / (rho c2 dt^2), with the divisor and its reciprocal from k_rhs_prep
+    bi = div_rcp(m.area[i] * Pi, sv.rhs_den[i], sv.rhs_rden[i]);
     double gpx = 0.0, gpy = 0.0;
     for (int k0 = 0; k0 < nf; k0 += FB) {
       int j[FB];
       double lrr[FB], tf[FB], pj[FB];
-      double2 mm[FB];
+      double2 dm[FB];  // m - x_i
 #pragma unroll
       for (int u = 0; u < FB; ++u) {
         const size_t f = face_slot(k0 + u, nf, cap, i);
         j[u] = ld_nc(m.fnbr + f);
         lrr[u] = ld_nc(m.flrr + f);
-        mm[u] = ld_nc(m.fm + f);
+        dm[u] = ld_nc(sv.rhs_dm + f);
         tf[u] = ld_nc(sv.rhs_tf + f);
       }
 #pragma unroll
@@ -232,8 +240,8 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
         if (k0 + u >= nf) break;
         bi -= tf[u];
         const double c = lrr[u] * (Pi - pj[u]);
-        gpx = gpx - c * (mm[u].x - xi.x);
-        gpy = gpy - c * (mm[u].y - xi.y);
+        gpx = gpx - c * dm[u].x;
+        gpy = gpy - c * dm[u].y;
       }
     }
     if (nf < ne) {
@@ -244,8 +252,8 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
     }
     sv.b[i] = bi;
     sv.xs[i] = Pi;
-    const double mi = s.mass[i];
-    s.GP[i] = make_double2(gpx / mi, gpy / mi);
+    const double mi = s.mass[i], rm = sv.rhs_rm[i];
+    s.GP[i] = make_double2(div_rcp(gpx, mi, rm), div_rcp(gpy, mi, rm));
   }
   if (guess == 2) {
     double res = 0.0;
@@ -380,6 +388,7 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_v(StateDev s, MeshDev m, int n,
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double mi = s.mass[i];
+  const double rmi = 1.0 / mi;  // the per-face divisions by mi through div_rcp
   const double2 sa = Sa[i], sb = Sb[i];
   double2 vi = s.v[i];
   constexpr int B = FB / 2;
@@ -402,7 +411,7 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_v(StateDev s, MeshDev m, int n,
 #pragma unroll
     for (int u = 0; u < B; ++u) {
       if (k0 + u >= nf) break;
-      const double c = dt * lrr[u] / mi;
+      const double c = div_rcp(dt * lrr[u], mi, rmi);
       const double M11 = c * (sa.x - qa[u].x), M21 = c * (sa.y - qa[u].y), M12 = c * (sb.x - qb[u].x),
                    M22 = c * (sb.y - qb[u].y);
       const double dx = mm[u].x - xi.x, dy = mm[u].y - xi.y;
@@ -421,6 +430,7 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n,
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double mi = s.mass[i];
+  const double rmi = 1.0 / mi;  // the per-face divisions by mi through div_rcp
   const double2 sa = Sa[i], sb = Sb[i];
   const double2 vi = s.v[i];
   const double Svx = sa.x * vi.x + sb.x * vi.y, Svy = sa.y * vi.x + sb.y * vi.y;
@@ -450,7 +460,7 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n,
       const double Sqx = qa[u].x * vj[u].x + qb[u].x * vj[u].y, Sqy = qa[u].y * vj[u].x + qb[u].y * vj[u].y;
       const double a = (mm[u].x - xi.x) * Svx + (mm[u].y - xi.y) * Svy;
       const double b = (mm[u].x - y[u].x) * Sqx + (mm[u].y - y[u].y) * Sqy;
-      ei += dt * lrr[u] / mi * (a - b);
+      ei += div_rcp(dt * lrr[u], mi, rmi) * (a - b);
     }
   }
   s.e[i] = ei;
