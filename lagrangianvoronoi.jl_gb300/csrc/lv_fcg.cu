@@ -75,7 +75,12 @@ struct StageImage {
   float sval[STG_ENTRIES];
   unsigned short sidx[STG_ENTRIES];
 };
-static_assert(offsetof(StageImage, sval) % 16 == 0 && offsetof(StageImage, sidx) % 16 == 0, "16-byte copies");
+static_assert(offsetof(StageImage, ext) % 16 == 0 && offsetof(StageImage, pmd) % 16 == 0 &&
+                  offsetof(StageImage, pdnv) % 16 == 0 && offsetof(StageImage, pridx) % 16 == 0 &&
+                  offsetof(StageImage, puidx) % 16 == 0 && offsetof(StageImage, pm) % 16 == 0 &&
+                  offsetof(StageImage, hrow) % 16 == 0 && offsetof(StageImage, sval) % 16 == 0 &&
+                  offsetof(StageImage, sidx) % 16 == 0 && sizeof(StageImage) % 16 == 0,
+              "16-byte bulk copies of every field");
 
 // Shared memory of the staged mode: r of the own rows then of the ext rows,
 // u of the own rows then of the halo rows, the image.
@@ -281,6 +286,44 @@ __device__ bool nexchange(const FcgArgs& a, unsigned e, const unsigned* mask) {
   return __syncthreads_or(to) == 0;
 }
 
+// The staged image is moved into shared memory by the bulk-copy engine
+// (cp.async.bulk, no tensor map: 16-byte aligned addresses, sizes multiples
+// of 16), completing on an mbarrier, while the threads load their rows and
+// evaluate the first FP64 residual.
+constexpr unsigned BULK_CHUNK = 16384;
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long* bar, unsigned parity) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(b), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// bytes (a multiple of 16) from src to dst in chunks, completing on bar
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const char* sp = static_cast<const char*>(src);
+  for (unsigned off = 0; off < bytes; off += BULK_CHUNK) {
+    const unsigned sz = min(BULK_CHUNK, bytes - off);
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     d + off),
+                 "l"(sp + off), "r"(sz), "r"(b)
+                 : "memory");
+  }
+}
+
 template <int R>
 struct FRows {
   int i[R];
@@ -310,20 +353,59 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
   }  // visible after the first __syncthreads, before any phase or exchange
   extern __shared__ __align__(16) unsigned char fcg_dyn[];
   StageSmem& ss = *reinterpret_cast<StageSmem*>(fcg_dyn);
+  // staged mode: the block's image in global memory; its copy in shared memory
+  // is ready once img_ready is set (until then ext and the halo rows are read
+  // from the global image)
+  const StageImage* gim = HALO ? a.stage + blockIdx.x : nullptr;
+  __shared__ __align__(8) unsigned long long s_img_bar;
+  bool img_ready = !HALO;
   if constexpr (HALO) {
-    // the block's image into shared memory: the fixed part, then the used entries
-    const StageImage& gi = a.stage[blockIdx.x];
-    const int total = gi.total;
-    const int4* src = reinterpret_cast<const int4*>(&gi);
-    int4* dst = reinterpret_cast<int4*>(&ss.img);
-    for (int q = threadIdx.x; q < (int)(offsetof(StageImage, sval) / 16); q += FCG_TPB) dst[q] = src[q];
-    const int4* sv = reinterpret_cast<const int4*>(gi.sval);
-    int4* dv = reinterpret_cast<int4*>(ss.img.sval);
-    for (int q = threadIdx.x; q < total / 4; q += FCG_TPB) dv[q] = sv[q];
-    const int4* si = reinterpret_cast<const int4*>(gi.sidx);
-    int4* di = reinterpret_cast<int4*>(ss.img.sidx);
-    for (int q = threadIdx.x; q < total / 8; q += FCG_TPB) di[q] = si[q];
+    if (threadIdx.x == 0) {
+      // the used prefix of every field (each field starts on a 16-byte
+      // boundary; sizes rounded up to 16 bytes stay inside the field)
+      const int4 hd = *reinterpret_cast<const int4*>(gim);  // npos, ne, nh, total
+      const unsigned npos = (unsigned)hd.x, ne = (unsigned)hd.y, nh = (unsigned)hd.z, total = (unsigned)hd.w;
+      auto up16 = [](unsigned b) { return (b + 15u) & ~15u; };
+      const unsigned hdr = (unsigned)offsetof(StageImage, ext);
+      const unsigned sz[9] = {hdr,           up16(ne * 4u),   up16(npos * 4u), up16(npos * 4u), up16(npos * 2u),
+                              up16(npos * 2u), up16(npos),   up16(nh * 4u),   total * 4u};
+      const size_t off[9] = {0,
+                             offsetof(StageImage, ext),
+                             offsetof(StageImage, pmd),
+                             offsetof(StageImage, pdnv),
+                             offsetof(StageImage, pridx),
+                             offsetof(StageImage, puidx),
+                             offsetof(StageImage, pm),
+                             offsetof(StageImage, hrow),
+                             offsetof(StageImage, sval)};
+      unsigned bytes = total * 2u;
+      for (int f = 0; f < 9; ++f) bytes += sz[f];
+      mbar_init(&s_img_bar);
+      mbar_expect_tx(&s_img_bar, bytes);
+      const char* src = reinterpret_cast<const char*>(gim);
+      char* dst = reinterpret_cast<char*>(&ss.img);
+      for (int f = 0; f < 9; ++f)
+        if (sz[f]) bulk_g2s(dst + off[f], src + off[f], sz[f], &s_img_bar);
+      if (total) bulk_g2s(ss.img.sidx, gim->sidx, total * 2u, &s_img_bar);
+    }
   }
+  // every thread waits for the image (bounded; on a timeout the copies get a
+  // second bounded wait before the block may exit); the block agrees on the result
+  auto img_wait = [&]() -> bool {
+    bool fail = false;
+    const long long t0 = clock64();
+    while (!mbar_try(&s_img_bar, 0u)) {
+      if (clock64() - t0 > FCG_SPIN_LIMIT) {
+        fail = true;
+        atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
+        const long long t1 = clock64();
+        while (!mbar_try(&s_img_bar, 0u) && clock64() - t1 < FCG_SPIN_LIMIT) {
+        }
+        break;
+      }
+    }
+    return __syncthreads_or(fail) == 0;
+  };
   FRows<R> rr;
   double x[R];
 #pragma unroll
@@ -366,17 +448,21 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       const int bj = j / rpb;
       if (bj != me) atomicOr(&s_mask[bj >> 5], 1u << (bj & 31));
     };
+    if constexpr (!HALO) {
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-      if (!rr.on[k]) continue;
-      for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) mark(a.col[e]);
-      if constexpr (!HALO)
+      for (int k = 0; k < R; ++k) {
+        if (!rr.on[k]) continue;
+        for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) mark(a.col[e]);
         for (int e = 0; e < rr.mn[k]; ++e) mark(a.mcol[(size_t)e * a.mstride + rr.i[k]]);
+      }
     }
-    // staged mode: the owners of the gathered rows (these include the halo
-    // rows and the columns of every staged M^-1 row)
-    if constexpr (HALO)
-      for (int q = threadIdx.x; q < ss.img.ne; q += FCG_TPB) mark(ss.img.ext[q]);
+    // staged mode: the owners of the gathered rows (these include every
+    // operator column outside the block, i.e. the halo rows, and the columns
+    // of every staged M^-1 row)
+    if constexpr (HALO) {
+      const int ne = gim->ne;
+      for (int q = threadIdx.x; q < ne; q += FCG_TPB) mark(gim->ext[q]);
+    }
   }
   unsigned ep = 0;  // phases completed in this launch
   unsigned xe = 0;  // neighbour exchanges completed in this launch
@@ -442,6 +528,10 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       // r crosses blocks (global and staged); u of the own and the halo rows
       // lands in shared memory, each halo row computed exactly as its owner
       // computes it (same entries, same order)
+      if (!img_ready) {
+        if (!img_wait()) return false;
+        img_ready = true;
+      }
       const int rpb = a.rows_per_block;
       const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -560,12 +650,13 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
 #pragma unroll
       for (int k = 0; k < R; ++k)
         if (rr.on[k]) xo[threadIdx.x + k * FCG_TPB] = x[k];
-      const int nh = ss.img.nh;
+      const StageImage* im = img_ready ? &ss.img : gim;  // the halo rows, staged or global
+      const int nh = im->nh;
       double xv[FCG_HMAX / FCG_TPB];
 #pragma unroll
       for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
         const int h = threadIdx.x + q * FCG_TPB;
-        xv[q] = h < nh ? __ldcg(a.x + ss.img.hrow[h]) : 0.0;
+        xv[q] = h < nh ? __ldcg(a.x + im->hrow[h]) : 0.0;
       }
 #pragma unroll
       for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
@@ -672,6 +763,8 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       if (!(ok = precond())) break;
     }
   }
+  // no bulk copy may still be in flight when the block exits
+  if (!img_ready) img_wait();
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
     // every block read the bases before its first arrival, and this is after
     // the last phase: the next launch continues from here

@@ -256,41 +256,35 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
       own[4 * f + 2] = v.z;
       own[4 * f + 3] = v.w;
     }
-    // the row's neighbours eight at a time: their indexes and weights in one
-    // round of loads, their feature rows in two rounds of four (indexes
-    // clamped to the row's last); the sum runs over the neighbours in order
-    constexpr int IB = 8, HB = 4;
+    // two neighbours per round, their loads issued together; the sum runs
+    // over the neighbours in order
     const int k1 = rowptr[row + 1];
-    for (int kb = rowptr[row]; kb < k1; kb += IB) {
-      int jj[IB];
-      float ww[IB];
+    for (int k = rowptr[row]; k < k1; k += 2) {
+      const bool two = k + 1 < k1;
+      const int ja = col[k], jb = two ? col[k + 1] : ja;
+      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
+      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
+      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
+      float4 va[FH / 4], vb[FH / 4];
 #pragma unroll
-      for (int u = 0; u < IB; ++u) {
-        const int k = min(kb + u, k1 - 1);
-        jj[u] = ld_nc(col + k);
-        ww[u] = ld_nc(what + k);
+      for (int f = 0; f < FH / 4; ++f) {
+        va[f] = ha[f];
+        vb[f] = hb[f];
       }
 #pragma unroll
-      for (int h0 = 0; h0 < IB; h0 += HB) {
-        if (kb + h0 >= k1) break;
-        float4 hv[HB][FH / 4];
+      for (int f = 0; f < FH / 4; ++f) {
+        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
+        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
+        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
+        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
+      }
+      if (two) {
 #pragma unroll
-        for (int u = 0; u < HB; ++u) {
-          const float4* hr4 = reinterpret_cast<const float4*>(Hin + (size_t)jj[h0 + u] * KH + half * FH);
-#pragma unroll
-          for (int f = 0; f < FH / 4; ++f) hv[u][f] = ld_nc(hr4 + f);
-        }
-#pragma unroll
-        for (int u = 0; u < HB; ++u) {
-          if (kb + h0 + u >= k1) break;
-          const float w = ww[h0 + u];
-#pragma unroll
-          for (int f = 0; f < FH / 4; ++f) {
-            agg[4 * f] = fmaf(w, hv[u][f].x, agg[4 * f]);
-            agg[4 * f + 1] = fmaf(w, hv[u][f].y, agg[4 * f + 1]);
-            agg[4 * f + 2] = fmaf(w, hv[u][f].z, agg[4 * f + 2]);
-            agg[4 * f + 3] = fmaf(w, hv[u][f].w, agg[4 * f + 3]);
-          }
+        for (int f = 0; f < FH / 4; ++f) {
+          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
+          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
+          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
+          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
         }
       }
     }
