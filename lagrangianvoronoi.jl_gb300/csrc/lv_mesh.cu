@@ -229,13 +229,14 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 
 constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
-// edge slots of the first clipping pass: shared memory for 10 edges per
-// polygon lets six blocks share an SM (three with LV_MAX_EDGES); a polygon
+// edge slots of the first clipping pass: shared memory for 9 edges per
+// polygon lets seven blocks share an SM (three with LV_MAX_EDGES); a polygon
 // that needs more at any point is redone by a second pass with LV_MAX_EDGES
-// slots.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2):
-// 8 slots 1.84 / 12.9, 10 slots 1.44 / 12.8, 12 slots 1.49 / 14.2, 14 slots
-// 1.52 / 16.6, all 20 slots in one pass 1.93 / 20.9.
-constexpr int ME_SMALL = 10;
+// slots.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
+// before the warp-uniform clip: 8 slots 1.84 / 12.9, 10 slots 1.44 / 12.8,
+// 12 slots 1.49 / 14.2, 14 slots 1.52 / 16.6, all 20 slots in one pass
+// 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16.
+constexpr int ME_SMALL = 9;
 
 struct Poly {
   double* v1x;
@@ -708,14 +709,16 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       prr_up = prr_upper(P, ne);
     }
   }
-  if (!active) return true;
-  if (flag == LV_FLAG_EDGE_OVERFLOW && retry) return false;
-  if (flag) atomicOr(status, flag);
+  // a polygon that overflowed the first pass's slots is not written (requeued)
+  const bool requeue = active && flag == LV_FLAG_EDGE_OVERFLOW && retry;
+  const bool emit = active && !requeue;
+  if (emit && flag) atomicOr(status, flag);
 
   // sort_edges! (IO.jl:35-48)
-  for (int a = 0; a < ne; ++a) {
+  const int ne_own = emit ? ne : 0;
+  for (int a = 0; a < ne_own; ++a) {
     const double lx = P.v2x[P.at(a)], ly = P.v2y[P.at(a)];
-    for (int b = a + 1; b < ne; ++b) {
+    for (int b = a + 1; b < ne_own; ++b) {
       if (same_value(lx, P.v1x[P.at(b)]) && same_value(ly, P.v1y[P.at(b)])) {
         const int u = P.at(a + 1), w = P.at(b);
         double t0;
@@ -730,44 +733,83 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     }
   }
 
-  // area (polygon.jl:114-121), centroid (polygon.jl:210-219), faces.  Both
-  // sums of the triangle areas run over the same terms in the same order, so
-  // one accumulator serves both.  The face lengths are computed on demand.
-  double A = 0.0, cx = 0.0, cy = 0.0;
-  int nf = 0;
+  // area (polygon.jl:114-121), centroid (polygon.jl:210-219), faces.  The
+  // per-edge work of the warp's polygons is one flat list of (polygon, edge)
+  // pairs, 32 per round, so every lane has an edge in every round instead of
+  // idling once its own polygon is done.  An edge's terms of the sums go back
+  // into its slot and each lane then adds its own polygon's terms in edge
+  // order (both sums of the triangle areas run over the same terms in the
+  // same order, so one accumulator serves both).  Face f of a polygon is its
+  // f-th edge with a neighbour label.  The face lengths are computed on demand.
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wbase = threadIdx.x - lane;
+  unsigned fmask = 0u;  // edges with a neighbour (at most LV_MAX_EDGES bits)
+  for (int k = 0; k < ne_own; ++k)
+    if (P.lab[P.at(k)] >= 0) fmask |= 1u << k;
+  int incl = ne_own;  // inclusive prefix of the edge counts over the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
   const int cap = m.cap;
-  for (int k = 0; k < ne; ++k) {
-    const int a = P.at(k);
-    const double v1x = P.v1x[a], v1y = P.v1y[a], v2x = P.v2x[a], v2y = P.v2y[a];
-    const int lab = P.lab[a];
-    const double ax = v1x - px, ay = v1y - py, bx = v2x - px, by = v2y - py;
-    const double dA = 0.5 * fabs(ax * by - ay * bx);
-    A += dA;
-    const double sx = (px + v1x) + v2x, sy = (py + v1y) + v2y;
-    cx = cx + div3(dA * sx);
-    cy = cy + div3(dA * sy);
-    m.ev1[(size_t)k * cap + i] = make_double2(v1x, v1y);
-    m.ev2[(size_t)k * cap + i] = make_double2(v2x, v2y);
-    m.elab[(size_t)k * cap + i] = lab;
-    if (lab >= 0) {
-      const double2 xq = x[lab];
-      double vx, vy;
-      get_arrow(g, xq.x, xq.y, px, py, vx, vy);
-      const double yx = px + vx, yy = py + vy;
-      const double lx = v1x - v2x, ly = v1y - v2y;
-      const double l2 = lx * lx + ly * ly;
-      const double rx = px - yx, ry = py - yy;
-      const double r2 = rx * rx + ry * ry;
-      const size_t f = (size_t)nf * cap + i;
-      m.fnbr[f] = lab;
-      m.flrr[f] = sqrt(l2 / r2);
-      m.fm[f] = make_double2(0.5 * (v1x + v2x), 0.5 * (v1y + v2y));
-      m.fy[f] = make_double2(yx, yy);
-      ++nf;
+  for (int q0 = 0; q0 < total; q0 += 32) {
+    const int q = q0 + lane;
+    // the owner lane: the first whose inclusive prefix exceeds q
+    int lo = 0, hi = 31;
+#pragma unroll
+    for (int st = 0; st < 5; ++st) {
+      const int mid = (lo + hi) >> 1;
+      if (__shfl_sync(FULL, incl, mid) > q) hi = mid;
+      else lo = mid + 1;
+    }
+    const int t = min(lo, 31);
+    const int k = q - (__shfl_sync(FULL, incl, t) - __shfl_sync(FULL, ne_own, t));
+    const double tpx = __shfl_sync(FULL, px, t), tpy = __shfl_sync(FULL, py, t);
+    const int ti = __shfl_sync(FULL, i, t);
+    const unsigned tfm = __shfl_sync(FULL, fmask, t);
+    if (q < total) {
+      const int a = k * CLIP_TPB + wbase + t;
+      const double v1x = P.v1x[a], v1y = P.v1y[a], v2x = P.v2x[a], v2y = P.v2y[a];
+      const int lab = P.lab[a];
+      const double ax = v1x - tpx, ay = v1y - tpy, bx = v2x - tpx, by = v2y - tpy;
+      const double dA = 0.5 * fabs(ax * by - ay * bx);
+      const double sx = (tpx + v1x) + v2x, sy = (tpy + v1y) + v2y;
+      P.v1x[a] = dA;
+      P.v1y[a] = div3(dA * sx);
+      P.v2x[a] = div3(dA * sy);
+      m.ev1[(size_t)k * cap + ti] = make_double2(v1x, v1y);
+      m.ev2[(size_t)k * cap + ti] = make_double2(v2x, v2y);
+      m.elab[(size_t)k * cap + ti] = lab;
+      if (lab >= 0) {
+        const double2 xq = x[lab];
+        double vx, vy;
+        get_arrow(g, xq.x, xq.y, tpx, tpy, vx, vy);
+        const double yx = tpx + vx, yy = tpy + vy;
+        const double lx = v1x - v2x, ly = v1y - v2y;
+        const double l2 = lx * lx + ly * ly;
+        const double rx = tpx - yx, ry = tpy - yy;
+        const double r2 = rx * rx + ry * ry;
+        const size_t f = (size_t)__popc(tfm & ((1u << k) - 1u)) * cap + ti;
+        m.fnbr[f] = lab;
+        m.flrr[f] = sqrt(l2 / r2);
+        m.fm[f] = make_double2(0.5 * (v1x + v2x), 0.5 * (v1y + v2y));
+        m.fy[f] = make_double2(yx, yy);
+      }
     }
   }
+  __syncwarp();
+  if (!emit) return !requeue;
+  double A = 0.0, cx = 0.0, cy = 0.0;
+  for (int k = 0; k < ne; ++k) {
+    const int a = P.at(k);
+    A += P.v1x[a];
+    cx = cx + P.v1y[a];
+    cy = cy + P.v2x[a];
+  }
   m.nedges[i] = ne;
-  m.nfaces[i] = nf;
+  m.nfaces[i] = __popc(fmask);
   m.area[i] = A;
   m.centroid[i] = make_double2(cx / A, cy / A);
   return true;
@@ -851,6 +893,8 @@ int lv_mesh_remesh(lv_ctx* c) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME_SMALL));
+    cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME));
     attr_set = true;
   }
