@@ -288,6 +288,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   sv.tmp = dalloc<double>(c, tmp_n, &ok);
   sv.dinv32 = dalloc<float>(c, cap, &ok);
   sv.r32 = dalloc<float>(c, cap, &ok);
+  sv.rtag = dalloc<unsigned long long>(c, cap, &ok);
   sv.z32 = dalloc<float>(c, cap, &ok);
   sv.p32 = dalloc<float>(c, cap, &ok);
   sv.q32 = dalloc<float>(c, cap, &ok);

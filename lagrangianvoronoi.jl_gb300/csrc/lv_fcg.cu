@@ -45,6 +45,21 @@ constexpr int STG_HASH = 8192;      // hash slots of the image builder
 constexpr int FLAG_STRIDE = 32;  // exchange flags sit on separate 128-byte lines (packed flags halve the speed)
 constexpr int FCG_MAX_BLOCKS = 1024;
 
+// Tagged values: the high word is the exchange's epoch with the top bit set
+// (zeroed memory never matches), the low word the float's bits.  An aligned
+// 64-bit access is single-copy atomic, so a word whose tag is current also
+// holds the current value: no flag and no fence are needed.
+__device__ __forceinline__ unsigned rtag_of(unsigned ee) { return ee | 0x80000000u; }
+__device__ __forceinline__ void st_tagged(unsigned long long* p, unsigned tag, float v) {
+  const unsigned long long w = ((unsigned long long)tag << 32) | __float_as_uint(v);
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(w) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -105,6 +120,7 @@ struct FcgArgs {
   double* x;  // FP64 iterate, also the exchange buffer of the outer residual
   float* rbuf;
   float* ubuf;    // u exchange
+  unsigned long long* rtag;  // staged mode: the r exchange as tagged words
   unsigned long long* slots;  // partial words [2 parities][RG_WORDS][nb] (as 32-bit words)
   unsigned* counter;          // arrivals, cumulative over launches
   unsigned* sync_base;        // [0] arrivals, [1] exchange epochs of the previous launches
@@ -534,21 +550,45 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       }
       const int rpb = a.rows_per_block;
       const int lane = threadIdx.x & 31;
+      // the exchange: every row's r as a word tagged with this exchange's
+      // epoch; a reader takes an ext row's word once its tag is current
+      // (bounded), so it waits on the data itself, not on a flag and then
+      // the data.  Consecutive exchanges are separated by a grid-wide phase,
+      // so no word is overwritten before every reader has taken it.
+      const unsigned tag = rtag_of(s_base[1] + (++xe));
 #pragma unroll
       for (int k = 0; k < R; ++k)
         if (rr.on[k]) {
-          a.rbuf[rr.i[k]] = r[k];
+          st_tagged(a.rtag + rr.i[k], tag, r[k]);
           ss.r[threadIdx.x + k * FCG_TPB] = r[k];
         }
-      if (!nexchange(a, ++xe, s_mask)) return false;
       const int ne = ss.img.ne;
       constexpr int NQ = STG_EXTMAX / FCG_TPB;
       float ev[NQ];
+      unsigned long long wv[NQ];
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         const int e = threadIdx.x + q * FCG_TPB;
-        ev[q] = e < ne ? __ldcg(a.rbuf + ss.img.ext[e]) : 0.f;
+        wv[q] = e < ne ? ld_relaxed_u64(a.rtag + ss.img.ext[e]) : ((unsigned long long)tag << 32);
       }
+      int late = 0;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int e = threadIdx.x + q * FCG_TPB;
+        if ((unsigned)(wv[q] >> 32) != tag) {
+          const long long t0 = clock64();
+          do {
+            wv[q] = ld_relaxed_u64(a.rtag + ss.img.ext[e]);
+            if (clock64() - t0 > FCG_SPIN_LIMIT) {
+              late = 1;
+              atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
+              break;
+            }
+          } while ((unsigned)(wv[q] >> 32) != tag);
+        }
+        ev[q] = __uint_as_float((unsigned)wv[q]);
+      }
+      if (__syncthreads_or(late)) return false;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         const int e = threadIdx.x + q * FCG_TPB;
@@ -1325,6 +1365,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.b = c->sv.b;
   a.x = x;
   a.rbuf = c->sv.r32;
+  a.rtag = c->sv.rtag;
   a.ubuf = c->sv.f32a;
   a.slots = c->sv.fslots;
   a.counter = c->sv.bar + 2;
@@ -1356,6 +1397,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
     cudaMemsetAsync(a.counter, 0, sizeof(unsigned), c->stream);
     cudaMemsetAsync(a.flags, 0, sizeof(unsigned) * FLAG_STRIDE * FCG_MAX_BLOCKS, c->stream);
     cudaMemsetAsync(a.sync_base, 0, sizeof(unsigned) * 2, c->stream);
+    cudaMemsetAsync(a.rtag, 0, sizeof(unsigned long long) * (size_t)c->cap, c->stream);
     c->fcg_reset = false;
   }
   void* args[] = {&a};

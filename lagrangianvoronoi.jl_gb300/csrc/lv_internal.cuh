@@ -185,6 +185,7 @@ struct SolverDev {
   float *sgd32, *dinc;
   int dinc_slots;
   float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
+  unsigned long long* rtag;  // staged solve: r of every row tagged with its exchange's epoch
   long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
   double* part;       // reduction partials [4][maxblocks]
   unsigned* bar;      // grid barrier {count, generation}
