@@ -825,17 +825,22 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
   if (!clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, true)) redo[atomicAdd(redo_n, 1)] = i;
 }
 
-// second pass: the queued polygons with LV_MAX_EDGES slots (a grid-stride
-// loop in whole warps)
+// second pass: the queued polygons with LV_MAX_EDGES slots.  The queue is
+// short, so its polygons are dealt round-robin over all resident blocks
+// (queue entry t * gridDim.x + b to thread t of block b): every SM gets some,
+// and the pass lasts about one polygon's clipping instead of a block's share.
 __global__ void __launch_bounds__(CLIP_TPB) k_clip_redo(GridDev g, const PathNodeDev* __restrict__ path,
                                                         const double2* __restrict__ x, CellsDev cl, MeshDev m,
                                                         int* status, const int* __restrict__ redo,
                                                         const int* __restrict__ redo_n) {
   const int cnt = *redo_n;
-  for (int base = blockIdx.x * CLIP_TPB; base < cnt; base += gridDim.x * CLIP_TPB) {
-    const int q = base + threadIdx.x;
+  const int per_round = gridDim.x * CLIP_TPB;
+  for (int base = 0; base < cnt; base += per_round) {
+    if (base + (int)blockIdx.x >= cnt) break;  // nothing for this block (uniform)
+    const int q = base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x;
     const bool on = q < cnt;
-    clip_polygon<ME>(g, path, x, on ? redo[q] : 0, on, cl, m, status, false);
+    // warps without a polygon skip the call (uniform per warp: q grows with the lane)
+    if (__any_sync(0xffffffffu, on)) clip_polygon<ME>(g, path, x, on ? redo[q] : 0, on, cl, m, status, false);
     __syncwarp();
   }
 }
@@ -908,8 +913,9 @@ int lv_mesh_remesh(lv_ctx* c) {
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
                                                                                    c->m, c->status, redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip");
-    k_clip_redo<<<c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status, redo,
-                                                           redo_n);
+    // three 20-slot blocks fit an SM
+    k_clip_redo<<<3 * c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status,
+                                                               redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip_redo");
   }
   c->meshed = true;
