@@ -211,7 +211,7 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 // GPU, so full warps of independent polygons use the FP64 pipe best).  The
 // polygon lives in shared memory in the reference's edge order.  Besides the
 // FP64 edges each slot keeps float offsets of both vertices from the seed
-// and a float upper bound of 4|v1 - x|^2, so that:
+// (from which a float upper bound of 4|v1 - x|^2 is formed), so that:
 //  * a candidate's fate is decided in float whenever that is provably
 //    exact: "cannot cut" (all vertices strictly inside the half-plane with a
 //    margin covering every rounding) is skipped, and vertex signs away from
@@ -230,12 +230,14 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
 // edge slots of the first clipping pass: shared memory for 9 edges per
-// polygon lets seven blocks share an SM (three with LV_MAX_EDGES); a polygon
-// that needs more at any point is redone by a second pass with LV_MAX_EDGES
-// slots.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
+// polygon (52 bytes a slot) lets seven blocks share an SM (three with
+// LV_MAX_EDGES); a polygon that needs more at any point is redone by a second
+// pass with LV_MAX_EDGES slots, spread over every SM.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
 // before the warp-uniform clip: 8 slots 1.84 / 12.9, 10 slots 1.44 / 12.8,
 // 12 slots 1.49 / 14.2, 14 slots 1.52 / 16.6, all 20 slots in one pass
-// 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16.
+// 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16; with
+// the second pass spread over every SM: 9 slots 1.123 / 9.58, 8 slots (eight
+// blocks per SM) 1.140 / 9.08.
 constexpr int ME_SMALL = 9;
 
 struct Poly {
@@ -248,7 +250,6 @@ struct Poly {
   float* r1y;
   float* r2x;  // v2 - x (float)
   float* r2y;
-  float* d2;   // upper bound of 4 |v1 - x|^2
   int t;
   int cap_e;   // edge slots
   __device__ __forceinline__ int at(int k) const { return k * CLIP_TPB + t; }
@@ -295,7 +296,6 @@ __device__ __forceinline__ void set_v1(const Poly& P, int k, double vx, double v
   const float fx = (float)(vx - px), fy = (float)(vy - py);
   P.r1x[a] = fx;
   P.r1y[a] = fy;
-  P.d2[a] = d2_up(fx, fy);
 }
 
 __device__ __forceinline__ void set_v2(const Poly& P, int k, double vx, double vy, double px, double py) {
@@ -317,12 +317,11 @@ __device__ __forceinline__ void copy_slot(const Poly& P, int dst, int src) {
   P.r1y[a] = P.r1y[l];
   P.r2x[a] = P.r2x[l];
   P.r2y[a] = P.r2y[l];
-  P.d2[a] = P.d2[l];
 }
 
 __device__ __forceinline__ float prr_upper(const Poly& P, int ne) {
   float m = 0.0f;
-  for (int k = 0; k < ne; ++k) m = fmaxf(m, P.d2[P.at(k)]);
+  for (int k = 0; k < ne; ++k) m = fmaxf(m, d2_up(P.r1x[P.at(k)], P.r1y[P.at(k)]));
   return m;
 }
 
@@ -424,7 +423,6 @@ __device__ __forceinline__ void put_vertex(const Poly& P, int k, bool first, dou
   Y[a] = vy;
   RX[a] = fx;
   RY[a] = fy;
-  if (first) P.d2[a] = d2_up(fx, fy);
 }
 
 __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm) {
@@ -435,7 +433,7 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   const float dd2 = dx * dx + dy * dy;
   const float D = sqrtf(dd2) * 1.0001f;
   float R = 0.0f;
-  for (int k = 0; k < ne; ++k) R = fmaxf(R, P.d2[P.at(k)]);
+  for (int k = 0; k < ne; ++k) R = fmaxf(R, d2_up(P.r1x[P.at(k)], P.r1y[P.at(k)]));
   R = 0.5f * sqrtf(R) * 1.0001f;
   const float margin = 1e-6f * (D * R + D * D) + 4e-15f * D * bigm + 1e-14f;
   const float half = 0.5f * dd2;
@@ -582,7 +580,7 @@ __device__ __forceinline__ void get_arrow(const GridDev& g, double ax, double ay
 
 // Shared-memory bytes of a block whose polygons have `cap` edge slots.
 constexpr size_t clip_smem(int cap) {
-  return (size_t)cap * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 5 * sizeof(float));
+  return (size_t)cap * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 4 * sizeof(float));
 }
 
 // One polygon per thread (i, active): the whole warp takes part, so threads
@@ -605,7 +603,6 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   P.r1y = P.r1x + CAP * CLIP_TPB;
   P.r2x = P.r1y + CAP * CLIP_TPB;
   P.r2y = P.r2x + CAP * CLIP_TPB;
-  P.d2 = P.r2y + CAP * CLIP_TPB;
   P.t = t;
   P.cap_e = CAP;
 
