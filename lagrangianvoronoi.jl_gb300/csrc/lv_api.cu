@@ -697,6 +697,7 @@ int lv_pressure_rhs(lv_ctx* c, double dt, int32_t gp_step, const double* vbc) {
 int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
   if (!c || niter < 0 || niter > 31) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 31]");
   Timer t(c, 2);
+  c->sg_pending = false;  // a start queued by a call that failed is void
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;
   const char* env = getenv("LVGPU_SWEEP_GUESS");
@@ -843,6 +844,7 @@ int lv_kernel_time(lv_ctx* c, int32_t fam, int64_t* launches, double* ms, int32_
 int lv_solver_forget(lv_ctx* c) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   c->sg_valid = 0;
+  c->sg_pending = false;
   return LV_OK;
 }
 

@@ -141,6 +141,14 @@ struct FcgArgs {
   // the shared-memory u of the own and halo rows
   const StageImage* stage;
   const int* remap;
+  // the sweep's start, queued by the sweep guess (0: none; 1: keep P and b
+  // for the next sweep; 2: also start from P + c0 (P - pprev) + c1 D)
+  int sg_mode;
+  double* pprev;
+  double* bprev;
+  const float* sgD;
+  float* sgstore;
+  const double* sgcoef;
   int* jref;
   int* out_iters;
   int* out_outer;
@@ -453,6 +461,29 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     rr.bb[k] = on ? a.b[i] : 0.0;
     x[k] = on ? a.x[i] : 0.0;
   }
+  // the sweep's start: the own rows shift now; the halo rows are shifted
+  // where the first residual gathers them; P (unshifted) goes to pprev and the
+  // shifted x to P once every block has gathered (after the first phase)
+  double pold[R];
+  const double sgc0 = a.sg_mode == 2 ? a.sgcoef[0] : 0.0, sgc1 = a.sg_mode == 2 ? a.sgcoef[1] : 0.0;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    pold[k] = x[k];
+    if (a.sg_mode && rr.on[k]) {
+      const int i = rr.i[k];
+      const double pv = a.pprev[i];
+      if (a.sgstore) a.sgstore[i] = (float)(x[k] - pv);
+      if (a.sg_mode == 2) x[k] = sweep_shift(x[k], pv, a.sgD ? (double)a.sgD[i] : 0.0, sgc0, sgc1);
+      a.bprev[i] = a.b[i];
+    }
+  }
+  bool first_res = true;
+  // x of row j as the first residual sees it (shifted when the start is)
+  auto x_at = [&](int j) -> double {
+    const double p = __ldcg(a.x + j);
+    if (!first_res || a.sg_mode != 2) return p;
+    return sweep_shift(p, __ldcg(a.pprev + j), a.sgD ? (double)__ldcg(a.sgD + j) : 0.0, sgc0, sgc1);
+  };
   // blocks owning the columns of this block's rows (operator and M^-1)
   __shared__ unsigned s_mask[FCG_MAX_BLOCKS / 32];
   for (int t = threadIdx.x; t < FCG_MAX_BLOCKS / 32; t += FCG_TPB) s_mask[t] = 0u;
@@ -696,7 +727,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
 #pragma unroll
       for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
         const int h = threadIdx.x + q * FCG_TPB;
-        xv[q] = h < nh ? __ldcg(a.x + im->hrow[h]) : 0.0;
+        xv[q] = h < nh ? x_at(im->hrow[h]) : 0.0;
       }
 #pragma unroll
       for (int q = 0; q < FCG_HMAX / FCG_TPB; ++q) {
@@ -726,7 +757,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
             acc += a.w[rr.beg[k] + e] * (x[k] - (cc < rpb ? xo[cc] : xh[cc - rpb]));
           }
         } else {
-          for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) acc += a.w[e] * (x[k] - __ldcg(a.x + a.col[e]));
+          for (int e = rr.beg[k]; e < rr.beg[k] + rr.cnt[k]; ++e) acc += a.w[e] * (x[k] - x_at(a.col[e]));
         }
       }
       r64[k] = rr.on[k] ? rr.bb[k] - acc : 0.0;
@@ -734,6 +765,18 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
       v[1] += rr.bb[k] * rr.bb[k];
     }
     if (!(ok = fphase<2, double>(a, ++ep, v, t2))) break;
+    if (first_res) {
+      // every block has gathered its halo of the unshifted P
+      first_res = false;
+      if (a.sg_mode) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          if (rr.on[k]) {
+            a.pprev[rr.i[k]] = pold[k];
+            if (a.sg_mode == 2) a.x[rr.i[k]] = x[k];
+          }
+      }
+    }
     rtrue2 = t2[0];
     bnorm2 = t2[1];
     if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax || updates >= FCG_MAX_UPDATES) break;
@@ -1366,6 +1409,18 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.x = x;
   a.rbuf = c->sv.r32;
   a.rtag = c->sv.rtag;
+  a.sg_mode = 0;
+  a.pprev = c->sv.pprev;
+  a.bprev = c->sv.bprev;
+  a.sgD = nullptr;
+  a.sgstore = nullptr;
+  a.sgcoef = c->sv.sgomega;
+  if (c->sg_pending && c->sg_P == x) {
+    a.sg_mode = c->sg_shift ? 2 : 1;
+    a.sgD = c->sg_D;
+    a.sgstore = c->sg_store;
+    c->sg_pending = false;
+  }
   a.ubuf = c->sv.f32a;
   a.slots = c->sv.fslots;
   a.counter = c->sv.bar + 2;

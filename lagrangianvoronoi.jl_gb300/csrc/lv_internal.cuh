@@ -103,6 +103,12 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   return a / b;
 }
 
+// The sweep's start P + c0 (P - pprev) + c1 D, rounded operation by
+// operation (no contraction) so that every kernel that forms it agrees.
+__device__ __forceinline__ double sweep_shift(double p, double pv, double d, double c0, double c1) {
+  return __dadd_rn(__dadd_rn(p, __dmul_rn(c0, __dsub_rn(p, pv))), __dmul_rn(c1, d));
+}
+
 // Loads of data that no thread writes during the kernel, issued where they
 // stand in the source (volatile inline PTX): the face and row loops load a
 // batch of faces (entries) this way and only then use them, so that the
@@ -242,6 +248,13 @@ struct lv_ctx {
   LearnState* learn = nullptr;
   bool factor_valid = false;  // learned factor matches the assembled operator and parameters
   bool sweep_guess = true;  // Galerkin initial guess of the sweeps (LVGPU_SWEEP_GUESS=0 turns it off)
+  // the sweep's start, queued by lv_solver_sweep_guess and applied by the next
+  // solve of that vector: inside the flag-reduced solver, else by k_sweep_apply
+  bool sg_pending = false;
+  int sg_shift = 0;
+  double* sg_P = nullptr;
+  const float* sg_D = nullptr;
+  float* sg_store = nullptr;
   int sg_valid = 0;         // sweeps of the last find_pressure whose changes sv.dinc holds
   int sg_n = 0;             // the particle count they belong to
   bool fcg_halo = true;    // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
@@ -441,6 +454,7 @@ int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count);
 int lv_fcg_capacity(lv_ctx* c);
 int lv_fcg_build_minv(lv_ctx* c);
 int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned);
+int lv_solver_flush_shift(lv_ctx* c);  // applies a queued sweep start (k_sweep_apply)
 int lv_fcg_halo_info(lv_ctx* c, int* max_rows);
 void lv_fcg_free(lv_ctx* c);
 

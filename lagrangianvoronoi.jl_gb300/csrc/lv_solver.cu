@@ -923,7 +923,7 @@ __global__ void k_sweep_apply(int n, double* P, double* prev, double* bprev, con
   if (i >= n) return;
   const double p = P[i], pv = prev[i];
   if (store) store[i] = (float)(p - pv);
-  if (shift) P[i] = p + coef[0] * (p - pv) + coef[1] * (D ? (double)D[i] : 0.0);
+  if (shift) P[i] = sweep_shift(p, pv, D ? (double)D[i] : 0.0, coef[0], coef[1]);
   prev[i] = p;
   bprev[i] = b[i];
 }
@@ -934,17 +934,31 @@ __global__ void k_sweep_store(int n, const double* __restrict__ P, const double*
   if (i < n) store[i] = (float)(P[i] - prev[i]);
 }
 
+// queues the start of sweep `it` for the next solve of P (lv_solver_solve
+// applies it: the flag-reduced solver inside its first residual, the other
+// solvers through k_sweep_apply)
 int lv_solver_sweep_guess(lv_ctx* c, double* P, int it, const float* D, float* store) {
   if (!c->op_ready) return lv_fail(c, LV_ERR_NOT_MESHED, "the pressure operator has not been assembled");
-  const int n = c->n;
-  const int shift = (it >= 2 || D) ? 1 : 0;
-  k_sweep_apply<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(n, P, c->sv.pprev, c->sv.bprev, c->sv.b, D, store,
-                                                          c->sv.sgomega, shift);
+  if (int rc = lv_solver_flush_shift(c)) return rc;
+  c->sg_pending = true;
+  c->sg_shift = (it >= 2 || D) ? 1 : 0;
+  c->sg_P = P;
+  c->sg_D = D;
+  c->sg_store = store;
+  return LV_OK;
+}
+
+int lv_solver_flush_shift(lv_ctx* c) {
+  if (!c->sg_pending) return LV_OK;
+  c->sg_pending = false;
+  k_sweep_apply<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(c->n, c->sg_P, c->sv.pprev, c->sv.bprev, c->sv.b,
+                                                             c->sg_D, c->sg_store, c->sv.sgomega, c->sg_shift);
   LV_LAUNCH_CHECK(c, "k_sweep_apply");
   return LV_OK;
 }
 
 int lv_solver_sweep_store(lv_ctx* c, const double* P, float* store) {
+  if (int rc = lv_solver_flush_shift(c)) return rc;
   k_sweep_store<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(c->n, P, c->sv.pprev, store);
   LV_LAUNCH_CHECK(c, "k_sweep_store");
   return LV_OK;
@@ -992,11 +1006,17 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     if (int rc = lv_fcg_build_minv(c)) return rc;
     c->factor_valid = true;
   }
+  // a queued sweep start of x: the flag-reduced solver applies it itself
+  const bool fcg_path = c->method != LV_METHOD_JACOBI_PCG && n <= lv_fcg_capacity(c);
+  if (c->sg_pending && (!fcg_path || c->sg_P != x)) {
+    KernelTimer ks(c, LV_KF_RHS);
+    if (int rc = lv_solver_flush_shift(c)) return rc;
+  }
   KernelTimer kt(c, LV_KF_PCG);
   if (c->method != LV_METHOD_JACOBI_PCG) {
     const bool learned = c->method == LV_METHOD_LEARNED_PCG;
     // systems that fit one or two blocks per SM: flag-reduced solver
-    if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);
+    if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);  // applies a queued start of x itself
     // the grid barriers of the cooperative solvers below start from zero
     cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
     // larger systems: the streaming variant
