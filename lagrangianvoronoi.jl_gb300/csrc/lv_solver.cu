@@ -35,7 +35,10 @@ __global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n) {
 }
 
 // refresh!(A, grid, dt) (pressure.jl:104-117) into CSR.
-__global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt, const double* __restrict__ hr) {
+// Also the FP32 copies of w, diag and dinv (the mixed solvers and the sweep
+// guess) and the flag of a nonsingular operator (some diagonal term != 0).
+__global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt, const double* __restrict__ hr,
+                           int* nonsingular) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i];
@@ -50,11 +53,16 @@ __global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt
     const double w = m.flrr[f] * (hi + hr[j]);
     sv.col[base + k] = j;
     sv.w[base + k] = w;
+    sv.w32[base + k] = (float)w;
     ad += w;
   }
+  const double dinv = 1.0 / ad;
   sv.diag[i] = diag;
   sv.adiag[i] = ad;
-  sv.dinv[i] = 1.0 / ad;
+  sv.dinv[i] = dinv;
+  sv.d32[i] = (float)diag;
+  sv.dinv32[i] = (float)dinv;
+  if (diag != 0.0) atomicOr(nonsingular, 1);
 }
 
 __global__ void k_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col, const double* __restrict__ w,
@@ -159,7 +167,7 @@ struct PCGArgs {
   int* status;
   double tol2;
   int itmax;
-  const int* nonsingular;  // set by k_any_nonzero when some diagonal term is nonzero
+  const int* nonsingular;  // set by k_assemble when some diagonal term is nonzero
   const double* diag;      // the reference's diagonal term (mixed solver only)
   int* out_iters;
   double* out_d;  // [rr, bb, true rr]
@@ -852,20 +860,6 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
   }
 }
 
-__global__ void k_to_f32(int n, const int* __restrict__ rowptr, const double* __restrict__ w,
-                         const double* __restrict__ diag, const double* __restrict__ dinv, float* w32, float* dg32,
-                         float* dinv32) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) w32[k] = (float)w[k];
-  dg32[i] = (float)diag[i];
-  dinv32[i] = (float)dinv[i];
-}
-
-__global__ void k_any_nonzero(const double* v, int n, int* flag) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && v[i] != 0.0) atomicOr(flag, 1);
-}
 
 int g_pcg_blocks_per_sm = -1;
 int g_reg_blocks_per_sm[2] = {-1, -1};
@@ -883,16 +877,10 @@ int lv_solver_assemble(lv_ctx* c, double dt) {
   double* hr = c->sv.tmp + 2 * (size_t)c->cap;  // scratch past the scan sums
   k_half_rho<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s.rho, hr, n);
   LV_LAUNCH_CHECK(c, "k_half_rho");
-  k_assemble<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s, c->m, c->sv, n, dt, hr);
-  LV_LAUNCH_CHECK(c, "k_assemble");
-  // FP32 copies of the operator (the streaming mixed solver, the sweep guess)
-  k_to_f32<<<lv_blocks(n, TPB), TPB, 0, s>>>(n, c->sv.rowptr, c->sv.w, c->sv.diag, c->sv.dinv, c->sv.w32, c->sv.d32,
-                                              c->sv.dinv32);
-  LV_LAUNCH_CHECK(c, "k_to_f32");
   // singular operator <=> every diagonal term is zero (c2 = Inf everywhere)
   cudaMemsetAsync(c->sv.iters + LV_IT_NONSINGULAR, 0, sizeof(int), s);
-  k_any_nonzero<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->sv.diag, n, c->sv.iters + LV_IT_NONSINGULAR);
-  LV_LAUNCH_CHECK(c, "k_any_nonzero");
+  k_assemble<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s, c->m, c->sv, n, dt, hr, c->sv.iters + LV_IT_NONSINGULAR);
+  LV_LAUNCH_CHECK(c, "k_assemble");
   c->op_ready = true;
   c->factor_valid = false;
   return LV_OK;
