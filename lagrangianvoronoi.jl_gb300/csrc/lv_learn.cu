@@ -298,62 +298,179 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
   __syncwarp();
 }
 
-// Z = [Hin, Agg Hin] W + b;  Hout = (res ? Hin : 0) + relu(Z)
+// ---------------------------------------------------------------- forward on tcgen05
+//
+// Z = [Hin, Agg Hin] W + b;  Hout = (res ? Hin : 0) + relu(Z), in 128-row
+// tiles on the fifth-generation tensor cores.  The tile's A operand
+// (128 x K BF16) and W (K x 32 BF16, as its transpose: N x K) sit in shared
+// memory in the canonical no-swizzle K-major layout: core matrices of 8 rows
+// x 16 bytes, 128 bytes apart along K (LBO) and K x 16 bytes apart along the
+// rows (SBO).  One thread issues K/16 tcgen05.mma (kind::f16, M = 128, N = 32,
+// FP32 accumulation in tensor memory) and commits them to an mbarrier; each
+// warp then reads its 32 rows of D with tcgen05.ld (thread = row, 32 columns)
+// and writes Z and Hout as contiguous rows.
+constexpr int TC_ROWS = 128;
+constexpr int TC_TPB = 128;  // 4 warps of 32 rows
+constexpr unsigned TC_COLS = 32;  // tensor-memory columns (the minimum allocation)
+constexpr long long TC_SPIN_LIMIT = 4000000000LL;  // cycles (about 2 s)
+
+// byte offset of element (r, k) of a K-major operand with K columns
+__device__ __forceinline__ int umma_off(int r, int k, int K) {
+  return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+// shared-memory matrix descriptor: start >> 4 [0,14), LBO >> 4 [16,30),
+// SBO >> 4 [32,46), version 1 [46,48), no swizzle
+__device__ __forceinline__ unsigned long long umma_desc(const void* p, unsigned lbo, unsigned sbo) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  return (unsigned long long)((a & 0x3FFFFu) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
+         ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: D F32 [4,6), A BF16 [7,10), B BF16
+// [10,13), both K-major, N >> 3 [17,23), M >> 4 [24,29)
+constexpr unsigned TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(HID >> 3) << 17) |
+                              ((unsigned)(TC_ROWS >> 4) << 24);
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ bool tc_bar_try(unsigned bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ bool tc_bar_wait(unsigned bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!tc_bar_try(bar, parity))
+    if (clock64() - t0 > TC_SPIN_LIMIT) return false;
+  return true;
+}
+
 template <int KH>
-__global__ void __launch_bounds__(LTPB) k_layer_fwd(int n, const float* __restrict__ Hin,
-                                                   const int* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const float* __restrict__ what, const __nv_bfloat16* __restrict__ W,
-                                                   const float* __restrict__ bias, int res, float* Z, float* Hout) {
+__global__ void __launch_bounds__(TC_TPB) k_layer_fwd(int n, const float* __restrict__ Hin,
+                                                      const int* __restrict__ rowptr, const int* __restrict__ col,
+                                                      const float* __restrict__ what,
+                                                      const __nv_bfloat16* __restrict__ W,
+                                                      const float* __restrict__ bias, int res, float* Z, float* Hout,
+                                                      int* status) {
   constexpr int K = 2 * KH;
-  __shared__ __nv_bfloat16 sW[K * HID];
-  __shared__ float sT[4][16 * K];
-  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) sW[t] = W[t];
-  __syncthreads();
+  static_assert(K % 16 == 0, "K in steps of 16");
+  __shared__ __align__(1024) unsigned char sA[TC_ROWS * K * 2];
+  __shared__ __align__(1024) unsigned char sB[HID * K * 2];
+  __shared__ __align__(16) float sT[4][16 * K];
+  __shared__ __align__(8) unsigned long long s_bar;
+  __shared__ unsigned s_tmem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tq = lane & 3;
-  float* tile = sT[warp];
-  const int ntiles = (n + 15) / 16;
-  for (int tl = blockIdx.x * 4 + warp; tl < ntiles; tl += gridDim.x * 4) {
-    const int row0 = tl * 16;
-    fill_xcat<KH>(tile, row0, n, Hin, rowptr, col, what);
-    float acc[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
-#pragma unroll
-    for (int ks = 0; ks < K / 16; ++ks) {
-      const int k0 = ks * 16;
-      uint32_t af[4];
-      af[0] = pack_bf16(tile[g * K + k0 + 2 * tq], tile[g * K + k0 + 2 * tq + 1]);
-      af[1] = pack_bf16(tile[(g + 8) * K + k0 + 2 * tq], tile[(g + 8) * K + k0 + 2 * tq + 1]);
-      af[2] = pack_bf16(tile[g * K + k0 + 2 * tq + 8], tile[g * K + k0 + 2 * tq + 9]);
-      af[3] = pack_bf16(tile[(g + 8) * K + k0 + 2 * tq + 8], tile[(g + 8) * K + k0 + 2 * tq + 9]);
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int n0 = nt * 8;
-        uint32_t bfr[2];
-        bfr[0] = pack_bf16(bf(sW, (k0 + 2 * tq) * HID + n0 + g), bf(sW, (k0 + 2 * tq + 1) * HID + n0 + g));
-        bfr[1] = pack_bf16(bf(sW, (k0 + 2 * tq + 8) * HID + n0 + g), bf(sW, (k0 + 2 * tq + 9) * HID + n0 + g));
-        mma_bf16(acc[nt], af, bfr);
-      }
-    }
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int row = row0 + g + ((e >= 2) ? 8 : 0);
-        const int c = nt * 8 + 2 * tq + (e & 1);
-        if (row < n) {
-          const float z = acc[nt][e] + bias[c];
-          Z[(size_t)row * HID + c] = z;
-          const float h0 = res ? Hin[(size_t)row * KH + c] : 0.f;
-          Hout[(size_t)row * HID + c] = h0 + fmaxf(z, 0.f);
-        }
-      }
-    }
-    __syncwarp();
+  const unsigned bar = (unsigned)__cvta_generic_to_shared(&s_bar);
+  // W^T into the B layout: element (n, k) = W[k][n]
+  for (int t = threadIdx.x; t < K * HID; t += TC_TPB)
+    *reinterpret_cast<__nv_bfloat16*>(sB + umma_off(t % HID, t / HID, K)) = W[t];
+  if (warp == 0) {
+    const unsigned holder = (unsigned)__cvta_generic_to_shared(&s_tmem);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(holder), "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B, for the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = s_tmem;
+  const unsigned long long bdesc0 = umma_desc(sB, 128, K * 16);
+  const unsigned long long adesc0 = umma_desc(sA, 128, K * 16);
+  const int ntiles = (n + TC_ROWS - 1) / TC_ROWS;
+  unsigned parity = 0;
+  bool ok = true;
+  for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
+    const int row0 = tl * TC_ROWS;
+    // A: each warp its 32 rows, 16 at a time through its FP32 staging tile;
+    // lane (r, half) converts half of row r's K features
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int rl = warp * 32 + h * 16;
+      fill_xcat<KH>(sT[warp], row0 + rl, n, Hin, rowptr, col, what);
+      const int r = lane & 15, k0 = (lane >> 4) * (K / 2);
+      const float* tr = sT[warp] + r * K;
+#pragma unroll
+      for (int k = k0; k < k0 + K / 2; k += 2)
+        *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, k, K)) = pack_bf16(tr[k], tr[k + 1]);
+      __syncwarp();
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A, for the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int ks = 0; ks < K / 16; ++ks) {
+        // K = 16 per instruction: two core matrices along K (256 bytes)
+        const unsigned long long ad = adesc0 + (unsigned long long)((ks * 256) >> 4);
+        const unsigned long long bd = bdesc0 + (unsigned long long)((ks * 256) >> 4);
+        const unsigned acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                tmem),
+            "l"(ad), "l"(bd), "r"(TC_IDESC), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                   : "memory");
+    }
+    // the products (bounded wait; on a timeout a second bounded wait lets the
+    // instructions in flight finish before the block gives up)
+    const bool done = tc_bar_wait(bar, parity);
+    if (!__syncthreads_and(done)) {
+      if (threadIdx.x == 0) atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
+      tc_bar_wait(bar, parity);
+      ok = false;
+      break;
+    }
+    parity ^= 1u;
+    tc_fence_after();
+    uint32_t d[HID];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
+          "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15]),
+          "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]), "=r"(d[22]), "=r"(d[23]),
+          "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]), "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
+        : "r"(tmem + ((unsigned)(warp * 32) << 16)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int row = row0 + warp * 32 + lane;
+    if (row < n) {
+      float4* zr = reinterpret_cast<float4*>(Z + (size_t)row * HID);
+      float4* hr = reinterpret_cast<float4*>(Hout + (size_t)row * HID);
+      const float4* hin = reinterpret_cast<const float4*>(Hin + (size_t)row * KH);
+#pragma unroll
+      for (int c4 = 0; c4 < HID / 4; ++c4) {
+        float z[4], h[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) z[e] = __uint_as_float(d[4 * c4 + e]) + bias[4 * c4 + e];
+        float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (res) h0 = hin[c4];  // res: KH == HID
+        h[0] = h0.x + fmaxf(z[0], 0.f);
+        h[1] = h0.y + fmaxf(z[1], 0.f);
+        h[2] = h0.z + fmaxf(z[2], 0.f);
+        h[3] = h0.w + fmaxf(z[3], 0.f);
+        zr[c4] = make_float4(z[0], z[1], z[2], z[3]);
+        hr[c4] = make_float4(h[0], h[1], h[2], h[3]);
+      }
+    }
+    // every warp has read D and the tensor cores are done with A before the
+    // next tile writes them
+    tc_fence_before();
+    __syncthreads();
+  }
+  tc_fence_after();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
 }
 
 // readout: gd_i = 1 + H_i . rd ; gl_k = what_k sum_c ro_c H_ic H_jc (j = col_k < i).
@@ -1052,14 +1169,16 @@ int prepare(lv_ctx* c, const LearnSystem& S) {
 int forward(lv_ctx* c, const LearnSystem& S) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
-  const int nb = std::max(1, (S.n + 63) / 64);  // every 16-row tile at once: the aggregation is latency-bound
+  // 128-row tiles, all at once while they fit four blocks per SM (the
+  // aggregation is latency-bound), else a persistent loop
+  const int nb = std::max(1, std::min((S.n + TC_ROWS - 1) / TC_ROWS, 4 * c->num_sms));
   k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
-  k_layer_fwd<FIN><<<nb, LTPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0, 0,
-                                         L->Z0, L->H1);
-  k_layer_fwd<HID><<<nb, LTPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1, 1,
-                                         L->Z1, L->H2);
-  k_layer_fwd<HID><<<nb, LTPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2, 1,
-                                         L->Z2, L->H3);
+  k_layer_fwd<FIN><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0,
+                                           0, L->Z0, L->H1, c->status);
+  k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1,
+                                           1, L->Z1, L->H2, c->status);
+  k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2,
+                                           1, L->Z2, L->H3, c->status);
   k_readout<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd,
                                                            L->gl);
   if (L->hops == 2) {
