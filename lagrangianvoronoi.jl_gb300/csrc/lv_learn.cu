@@ -16,9 +16,10 @@
 //                                                   (two-hop pattern, optional)
 // with the path weight pw_ij = sum_k what_ik what_kj over common neighbours.
 //
-// The matrix products of the layers (forward [N x 32|64] x [32|64 x 32],
-// backward dX = dZ W^T and dW = X^T dZ) run on the tensor cores as
-// mma.sync m16n8k16 with BF16 operands and FP32 accumulation; everything else
+// The matrix products of the layers run on the tensor cores with BF16
+// operands and FP32 accumulation: the forward [N x 32|64] x [32|64 x 32] (the
+// factor of every timestep) as tcgen05.mma into tensor memory, the training's
+// backward dX = dZ W^T and dW = X^T dZ as mma.sync m16n8k16; everything else
 // is FP32.  Training minimises either the exact FSAI (Kaporin) objective
 //     (1/N) [ tr(Gt At Gt^T) - 2 sum_i log Gt_ii ]
 // (Kolotilina & Yeremin, SIAM J. Matrix Anal. Appl. 14, 1993; Kaporin,
