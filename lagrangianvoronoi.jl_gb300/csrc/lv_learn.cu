@@ -311,7 +311,7 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
 // warp then reads its 32 rows of D with tcgen05.ld (thread = row, 32 columns)
 // and writes Z and Hout as contiguous rows.
 constexpr int TC_ROWS = 128;
-constexpr int TC_TPB = 128;  // 4 warps of 32 rows
+constexpr int TC_TPB = 256;  // 8 warps: 16 rows each for the operand, a quarter of the lanes and half the columns of D each
 constexpr unsigned TC_COLS = 32;  // tensor-memory columns (the minimum allocation)
 constexpr long long TC_SPIN_LIMIT = 4000000000LL;  // cycles (about 2 s)
 
@@ -349,8 +349,71 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned bar, unsigned parity) {
   return true;
 }
 
+// fill_xcat into the A operand: the warp's 16 rows [Hin, Agg Hin] as BF16
+// pairs at their K-major core-matrix positions (rows past n are zeros)
 template <int KH>
-__global__ void __launch_bounds__(TC_TPB) k_layer_fwd(int n, const float* __restrict__ Hin,
+__device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const float* __restrict__ Hin,
+                               const int* __restrict__ rowptr, const int* __restrict__ col,
+                               const float* __restrict__ what) {
+  constexpr int K = 2 * KH, FH = KH / 2;
+  const int lane = threadIdx.x & 31;
+  const int r = lane & 15, half = lane >> 4;
+  const int row = row0 + rl + r;
+  float agg[FH], own[FH];
+#pragma unroll
+  for (int f = 0; f < FH; ++f) agg[f] = own[f] = 0.f;
+  if (row < n) {
+    const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
+#pragma unroll
+    for (int f = 0; f < FH / 4; ++f) {
+      const float4 v = hr[f];
+      own[4 * f] = v.x;
+      own[4 * f + 1] = v.y;
+      own[4 * f + 2] = v.z;
+      own[4 * f + 3] = v.w;
+    }
+    // two neighbours per round, their loads issued together; the sum runs
+    // over the neighbours in order
+    const int k1 = rowptr[row + 1];
+    for (int k = rowptr[row]; k < k1; k += 2) {
+      const bool two = k + 1 < k1;
+      const int ja = col[k], jb = two ? col[k + 1] : ja;
+      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
+      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
+      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
+      float4 va[FH / 4], vb[FH / 4];
+#pragma unroll
+      for (int f = 0; f < FH / 4; ++f) {
+        va[f] = ha[f];
+        vb[f] = hb[f];
+      }
+#pragma unroll
+      for (int f = 0; f < FH / 4; ++f) {
+        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
+        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
+        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
+        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
+      }
+      if (two) {
+#pragma unroll
+        for (int f = 0; f < FH / 4; ++f) {
+          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
+          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
+          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
+          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < FH; f += 2) {
+    *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, half * FH + f, K)) = pack_bf16(own[f], own[f + 1]);
+    *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, KH + half * FH + f, K)) = pack_bf16(agg[f], agg[f + 1]);
+  }
+}
+
+template <int KH>
+__global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __restrict__ Hin,
                                                       const int* __restrict__ rowptr, const int* __restrict__ col,
                                                       const float* __restrict__ what,
                                                       const __nv_bfloat16* __restrict__ W,
@@ -360,7 +423,6 @@ __global__ void __launch_bounds__(TC_TPB) k_layer_fwd(int n, const float* __rest
   static_assert(K % 16 == 0, "K in steps of 16");
   __shared__ __align__(1024) unsigned char sA[TC_ROWS * K * 2];
   __shared__ __align__(1024) unsigned char sB[HID * K * 2];
-  __shared__ __align__(16) float sT[4][16 * K];
   __shared__ __align__(8) unsigned long long s_bar;
   __shared__ unsigned s_tmem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -390,19 +452,8 @@ __global__ void __launch_bounds__(TC_TPB) k_layer_fwd(int n, const float* __rest
   bool ok = true;
   for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
     const int row0 = tl * TC_ROWS;
-    // A: each warp its 32 rows, 16 at a time through its FP32 staging tile;
-    // lane (r, half) converts half of row r's K features
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int rl = warp * 32 + h * 16;
-      fill_xcat<KH>(sT[warp], row0 + rl, n, Hin, rowptr, col, what);
-      const int r = lane & 15, k0 = (lane >> 4) * (K / 2);
-      const float* tr = sT[warp] + r * K;
-#pragma unroll
-      for (int k = k0; k < k0 + K / 2; k += 2)
-        *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, k, K)) = pack_bf16(tr[k], tr[k + 1]);
-      __syncwarp();
-    }
+    // A: each warp its 16 rows
+    fill_xcat_umma<KH>(sA, warp * 16, row0, n, Hin, rowptr, col, what);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A, for the tensor cores
     tc_fence_before();
     __syncthreads();
@@ -434,26 +485,28 @@ __global__ void __launch_bounds__(TC_TPB) k_layer_fwd(int n, const float* __rest
     }
     parity ^= 1u;
     tc_fence_after();
-    uint32_t d[HID];
+    // warp w: lanes 32 (w % 4) .. + 31 (its quarter of tensor memory),
+    // columns 16 (w / 4) .. + 15
+    constexpr int DC = HID / 2;
+    const int quarter = warp & 3, cb = (warp >> 2) * DC;
+    uint32_t d[DC];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
         : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]),
-          "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15]),
-          "=r"(d[16]), "=r"(d[17]), "=r"(d[18]), "=r"(d[19]), "=r"(d[20]), "=r"(d[21]), "=r"(d[22]), "=r"(d[23]),
-          "=r"(d[24]), "=r"(d[25]), "=r"(d[26]), "=r"(d[27]), "=r"(d[28]), "=r"(d[29]), "=r"(d[30]), "=r"(d[31])
-        : "r"(tmem + ((unsigned)(warp * 32) << 16)));
+          "=r"(d[8]), "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+        : "r"(tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)cb));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    const int row = row0 + warp * 32 + lane;
+    const int row = row0 + quarter * 32 + lane;
     if (row < n) {
-      float4* zr = reinterpret_cast<float4*>(Z + (size_t)row * HID);
-      float4* hr = reinterpret_cast<float4*>(Hout + (size_t)row * HID);
-      const float4* hin = reinterpret_cast<const float4*>(Hin + (size_t)row * KH);
+      float4* zr = reinterpret_cast<float4*>(Z + (size_t)row * HID + cb);
+      float4* hr = reinterpret_cast<float4*>(Hout + (size_t)row * HID + cb);
+      const float4* hin = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + cb);
 #pragma unroll
-      for (int c4 = 0; c4 < HID / 4; ++c4) {
+      for (int c4 = 0; c4 < DC / 4; ++c4) {
         float z[4], h[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) z[e] = __uint_as_float(d[4 * c4 + e]) + bias[4 * c4 + e];
+        for (int e = 0; e < 4; ++e) z[e] = __uint_as_float(d[4 * c4 + e]) + bias[cb + 4 * c4 + e];
         float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (res) h0 = hin[c4];  // res: KH == HID
         h[0] = h0.x + fmaxf(z[0], 0.f);
@@ -1171,7 +1224,7 @@ int forward(lv_ctx* c, const LearnSystem& S) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
   // 128-row tiles, all at once while they fit four blocks per SM (the
-  // aggregation is latency-bound), else a persistent loop
+  // aggregation is latency-bound), else a persistent loop over the tiles
   const int nb = std::max(1, std::min((S.n + TC_ROWS - 1) / TC_ROWS, 4 * c->num_sms));
   k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
   k_layer_fwd<FIN><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0,
