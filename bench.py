@@ -439,8 +439,8 @@ def run_ours(args, world, rank, local):
 
 # what bounds each dominant kernel instead of HBM (from the ncu summaries in profiles/)
 ROOFLINE_NOTE = {
-    "k_clip": "FP64-pipe bound: sm__pipe_fp64_cycles_active 65% at ~10 warps/SM (profiles/k_clip_taylor_green_1024.md);"
-              " its compulsory traffic is 212 B per polygon",
+    "k_clip": "FP64-pipe and FP64-latency bound: sm__pipe_fp64_cycles_active 62% at ~12 warps/SM, 13 of 32 lanes"
+              " active per instruction (profiles/k_clip_taylor_green_1024.md); its compulsory traffic is 212 B per polygon",
     "k_fcg<1,1>": "synchronisation-latency bound: a grid-wide reduction and a neighbour exchange per CG iteration"
                   " (profiles/k_fcg_taylor_green_256.md)",
     "k_fcg<1,0>": "synchronisation-latency bound (profiles/k_fcg_taylor_green_256.md)",
