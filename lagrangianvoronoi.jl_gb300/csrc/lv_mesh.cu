@@ -336,10 +336,33 @@ __device__ double influence_rr_exact(const Poly& P, int ne, double px, double py
   return rr;
 }
 
+// The new edge (X, Y) of a clip, oriented counter-clockwise about the seed
+// and appended in the next slot (polygon.jl:88-95).
+__device__ __forceinline__ void append_edge(const Poly& P, int& ne, double Xx, double Xy, double Yx, double Yy,
+                                            double px, double py, int label) {
+  const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
+  if (ax * by - ay * bx > 0.0) {
+    set_v1(P, ne, Yx, Yy, px, py);
+    set_v2(P, ne, Xx, Xy, px, py);
+  } else {
+    set_v1(P, ne, Xx, Xy, px, py);
+    set_v2(P, ne, Yx, Yy, px, py);
+  }
+  P.lab[P.at(ne)] = label;
+  ++ne;
+}
+
+// the points of a new edge that found no free slot
+struct PendingEdge {
+  double xx, xy, yx, yy;
+};
+
 // polygon.jl:51-97 verbatim in FP64, with FastVector's swap-delete
 // (fastvector.jl:44-50).  Returns 1 when a new edge was added, 0 otherwise,
-// -1 on overflow; nev counts crossing events.
-__device__ int clip_exact(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, int& nev) {
+// -1 when the new edge finds no free slot (its points then go to pend, the
+// polygon's other edges being final); nev counts crossing events.
+__device__ int clip_exact(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, int& nev,
+                          PendingEdge& pend) {
   const double dfx = yx - px, dfy = yy - py;
   const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
   const double c = dfx * mx + dfy * my;
@@ -377,17 +400,11 @@ __device__ int clip_exact(const Poly& P, int& ne, double px, double py, double y
   }
   const bool ynull = isnan(Yx) && isnan(Yy);
   if (!ynull && !(same_value(Xx, Yx) && same_value(Xy, Yy))) {
-    if (ne >= P.cap_e) return -1;
-    const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
-    if (ax * by - ay * bx > 0.0) {
-      set_v1(P, ne, Yx, Yy, px, py);
-      set_v2(P, ne, Xx, Xy, px, py);
-    } else {
-      set_v1(P, ne, Xx, Xy, px, py);
-      set_v2(P, ne, Yx, Yy, px, py);
+    if (ne >= P.cap_e) {
+      pend = PendingEdge{Xx, Xy, Yx, Yy};
+      return -1;
     }
-    P.lab[P.at(ne)] = label;
-    ++ne;
+    append_edge(P, ne, Xx, Xy, Yx, Yy, px, py, label);
     return 1;
   }
   return 0;
@@ -425,7 +442,8 @@ __device__ __forceinline__ void put_vertex(const Poly& P, int k, bool first, dou
   RY[a] = fy;
 }
 
-__device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm) {
+__device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm,
+                         PendingEdge& pend) {
   const double dfx = yx - px, dfy = yy - py;
   const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
   const double c = dfx * mx + dfy * my;
@@ -539,7 +557,10 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   const double Xx = xl0 ? X0x : X1x, Xy = xl0 ? X0y : X1y;
   const double Yx = yf0 ? X0x : X1x, Yy = yf0 ? X0y : X1y;
   if (same_value(Xx, Yx) && same_value(Xy, Yy)) return 0;
-  if (ne >= P.cap_e) return -1;
+  if (ne >= P.cap_e) {
+    pend = PendingEdge{Xx, Xy, Yx, Yy};
+    return -1;
+  }
   const float rXx = xl0 ? q0x : q1x, rXy = xl0 ? q0y : q1y;
   const float rYx = yf0 ? q0x : q1x, rYy = yf0 ? q0y : q1y;
   const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
@@ -583,14 +604,28 @@ constexpr size_t clip_smem(int cap) {
   return (size_t)cap * CLIP_TPB * (4 * sizeof(double) + sizeof(int) + 4 * sizeof(float));
 }
 
+// A polygon of the first pass whose new edge found no free slot, captured at
+// that point: its other edges (final for this clip), the new edge's points,
+// and where the candidate search stands.  The second pass appends the edge
+// in its larger slots and continues the search, so the polygon is computed
+// exactly as in one pass with LV_MAX_EDGES slots.
+struct ClipResume {
+  int i, ne, label, pn, s, se, chain_ok, pad;
+  double xx, xy, yx, yy;
+  double v1x[ME_SMALL], v1y[ME_SMALL], v2x[ME_SMALL], v2y[ME_SMALL];
+  int lab[ME_SMALL];
+};
+
 // One polygon per thread (i, active): the whole warp takes part, so threads
-// without a polygon pass active = false.  Returns false when the polygon
-// needed more than CAP edge slots and `retry` is set: then nothing of it is
-// written (the caller queues it for the pass with LV_MAX_EDGES slots);
-// without `retry` that case is the reference's edge overflow error.
+// without a polygon pass active = false.  With `save` (the first pass, CAP
+// slots), a polygon whose new edge finds no free slot is captured into
+// save[atomicAdd(save_n, 1)] and not written; with `resume` (the second
+// pass) the polygon continues from such a capture.  Without `save`, running
+// out of slots is the reference's edge overflow error.
 template <int CAP>
-__device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ path, const double2* __restrict__ x,
-                             int i, bool active, const CellsDev& cl, const MeshDev& m, int* status, bool retry) {
+__device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ path, const double2* __restrict__ x,
+                             int i, bool active, const CellsDev& cl, const MeshDev& m, int* status,
+                             ClipResume* save, int* save_n, const ClipResume* resume) {
   extern __shared__ double smem[];
   const int t = threadIdx.x;
   Poly P;
@@ -608,7 +643,25 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
 
   double px = 0.0, py = 0.0;
   int ne = 0;
-  if (active) {
+  int pn = -1, s = 0, se = 0;
+  bool chain_ok = true;
+  if (active && resume) {
+    const double2 xi = x[i];
+    px = xi.x;
+    py = xi.y;
+    // the captured edges, then the new edge that had no slot
+    ne = resume->ne;
+    for (int k = 0; k < ne; ++k) {
+      set_v1(P, k, resume->v1x[k], resume->v1y[k], px, py);
+      set_v2(P, k, resume->v2x[k], resume->v2y[k], px, py);
+      P.lab[P.at(k)] = resume->lab[k];
+    }
+    append_edge(P, ne, resume->xx, resume->xy, resume->yx, resume->yy, px, py, resume->label);
+    pn = resume->pn;
+    s = resume->s;
+    se = resume->se;
+    chain_ok = resume->chain_ok != 0;
+  } else if (active) {
     const double2 xi = x[i];
     px = xi.x;
     py = xi.y;
@@ -637,8 +690,7 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   const float x32 = (float)px, y32 = (float)py;
   const float xp32 = (float)g.xperiod, yp32 = (float)g.yperiod;
   float prr_up = active ? prr_upper(P, ne) : 0.0f;
-  bool chain_ok = true;
-  int pn = -1, s = 0, se = 0;
+  bool saved = false;
   // voronoigrid.jl:53-81, in rounds
   while (true) {
     bool have = false;
@@ -693,22 +745,47 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       get_arrow(g, xq.x, xq.y, px, py, vx, vy);
       const double yx = px + vx, yy = py + vy;
       int r = 2;
-      if (chain_ok) r = clip_fast(P, ne, px, py, yx, yy, cj, g.bigm);
+      PendingEdge pend;
+      if (chain_ok) r = clip_fast(P, ne, px, py, yx, yy, cj, g.bigm, pend);
       if (r == 2) {
         int nev = 0;
-        r = clip_exact(P, ne, px, py, yx, yy, cj, nev);
-        if (nev != 0 && !(r == 1 && nev == 2)) chain_ok = false;
+        r = clip_exact(P, ne, px, py, yx, yy, cj, nev, pend);
+        // (an edge without a slot counts as added)
+        if (nev != 0 && !(r != 0 && nev == 2)) chain_ok = false;
       }
       if (r < 0) {
-        flag = LV_FLAG_EDGE_OVERFLOW;
+        if (save) {
+          ClipResume& c = save[atomicAdd(save_n, 1)];
+          c.i = i;
+          c.ne = ne;
+          c.label = cj;
+          c.pn = pn;
+          c.s = s;
+          c.se = se;
+          c.chain_ok = chain_ok ? 1 : 0;
+          c.xx = pend.xx;
+          c.xy = pend.xy;
+          c.yx = pend.yx;
+          c.yy = pend.yy;
+          for (int k = 0; k < ne; ++k) {
+            const int a = P.at(k);
+            c.v1x[k] = P.v1x[a];
+            c.v1y[k] = P.v1y[a];
+            c.v2x[k] = P.v2x[a];
+            c.v2y[k] = P.v2y[a];
+            c.lab[k] = P.lab[a];
+          }
+          saved = true;
+        } else {
+          flag = LV_FLAG_EDGE_OVERFLOW;
+        }
         done = true;
       }
       prr_up = prr_upper(P, ne);
     }
   }
-  // a polygon that overflowed the first pass's slots is not written (requeued)
-  const bool requeue = active && flag == LV_FLAG_EDGE_OVERFLOW && retry;
-  const bool emit = active && !requeue;
+  // a polygon captured for the second pass is not written here
+  const bool emit = active && !saved;
   if (emit && flag) atomicOr(status, flag);
 
   // sort_edges! (IO.jl:35-48)
@@ -797,7 +874,7 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     }
   }
   __syncwarp();
-  if (!emit) return !requeue;
+  if (!emit) return;
   double A = 0.0, cx = 0.0, cy = 0.0;
   for (int k = 0; k < ne; ++k) {
     const int a = P.at(k);
@@ -809,17 +886,16 @@ __device__ bool clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   m.nfaces[i] = __popc(fmask);
   m.area[i] = A;
   m.centroid[i] = make_double2(cx / A, cy / A);
-  return true;
 }
 
 // first pass: every polygon with CAP slots; the ones that need more are
-// appended to redo[] (redo_n counts them)
+// captured into redo[] (redo_n counts them)
 template <int CAP>
 __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
                                                    const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
-                                                   int* status, int* redo, int* redo_n) {
+                                                   int* status, ClipResume* redo, int* redo_n) {
   const int i = blockIdx.x * CLIP_TPB + threadIdx.x;
-  if (!clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, true)) redo[atomicAdd(redo_n, 1)] = i;
+  clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, redo, redo_n, nullptr);
 }
 
 // second pass: the queued polygons with LV_MAX_EDGES slots.  The queue is
@@ -828,7 +904,7 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
 // and the pass lasts about one polygon's clipping instead of a block's share.
 __global__ void __launch_bounds__(CLIP_TPB) k_clip_redo(GridDev g, const PathNodeDev* __restrict__ path,
                                                         const double2* __restrict__ x, CellsDev cl, MeshDev m,
-                                                        int* status, const int* __restrict__ redo,
+                                                        int* status, const ClipResume* __restrict__ redo,
                                                         const int* __restrict__ redo_n) {
   const int cnt = *redo_n;
   const int per_round = gridDim.x * CLIP_TPB;
@@ -837,7 +913,8 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip_redo(GridDev g, const PathNod
     const int q = base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x;
     const bool on = q < cnt;
     // warps without a polygon skip the call (uniform per warp: q grows with the lane)
-    if (__any_sync(0xffffffffu, on)) clip_polygon<ME>(g, path, x, on ? redo[q] : 0, on, cl, m, status, false);
+    if (__any_sync(0xffffffffu, on))
+      clip_polygon<ME>(g, path, x, on ? redo[q].i : 0, on, cl, m, status, nullptr, nullptr, on ? redo + q : nullptr);
     __syncwarp();
   }
 }
@@ -902,9 +979,15 @@ int lv_mesh_remesh(lv_ctx* c) {
   }
   {
     KernelTimer kt(c, LV_KF_CLIP);
-    // the queue of polygons for the second pass lives in the solver's scratch
-    // (free during a remesh): n ints, then the count
-    int* redo = reinterpret_cast<int*>(c->sv.xs);
+    // the captures for the second pass (one per particle at most), then the count
+    if (!c->clip_resume) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, sizeof(ClipResume) * (size_t)c->cap) != cudaSuccess)
+        return lv_fail(c, LV_ERR_CUDA, "allocation of the clipping captures failed");
+      c->allocs.push_back(p);
+      c->clip_resume = p;
+    }
+    ClipResume* redo = static_cast<ClipResume*>(c->clip_resume);
     int* redo_n = c->sv.iters + LV_IT_REDO;
     cudaMemsetAsync(redo_n, 0, sizeof(int), s);
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
