@@ -237,7 +237,8 @@ constexpr int ME = LV_MAX_EDGES;
 // 12 slots 1.49 / 14.2, 14 slots 1.52 / 16.6, all 20 slots in one pass
 // 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16; with
 // the second pass spread over every SM: 9 slots 1.123 / 9.58, 8 slots (eight
-// blocks per SM) 1.140 / 9.08.
+// blocks per SM) 1.140 / 9.08; with the second pass resuming the captured
+// polygons: 9 slots 1.054 / 9.92, 8 slots 1.122 / 10.29.
 constexpr int ME_SMALL = 9;
 
 struct Poly {
