@@ -1082,6 +1082,7 @@ struct LearnSystem {
 struct LearnState {
   float *params = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
   __nv_bfloat16* wbf = nullptr;
+  bool wbf_valid = false;  // wbf holds the current weights (set by every forward that converts them)
   int adam_t = 0;
   int cap = 0;
   int64_t nnz_cap = 0;
@@ -1192,6 +1193,7 @@ void init_params(LearnState* L, unsigned long long seed, cudaStream_t s) {
   fill(OFF_RO, HID, HID, 0.01f);
   fill(OFF_RO2, HID, HID, 0.01f);
   cudaMemcpyAsync(L->params, p.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s);
+  L->wbf_valid = false;
   cudaMemsetAsync(L->m1, 0, sizeof(float) * NPARAM, s);
   cudaMemsetAsync(L->m2, 0, sizeof(float) * NPARAM, s);
   L->adam_t = 0;
@@ -1226,7 +1228,11 @@ int forward(lv_ctx* c, const LearnSystem& S) {
   // 128-row tiles, all at once while they fit four blocks per SM (the
   // aggregation is latency-bound), else a persistent loop over the tiles
   const int nb = std::max(1, std::min((S.n + TC_ROWS - 1) / TC_ROWS, 4 * c->num_sms));
-  k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
+  if (!L->wbf_valid) {  // BF16 weights once per change of the parameters
+    k_to_bf16<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->params, L->wbf);
+    L->wbf_valid = true;
+    c->launches++;
+  }
   k_layer_fwd<FIN><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0,
                                            0, L->Z0, L->H1, c->status);
   k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1,
@@ -1240,7 +1246,7 @@ int forward(lv_ctx* c, const LearnSystem& S) {
                                                               L->gl2);
     c->launches++;
   }
-  c->launches += 5;
+  c->launches += 4;
   return lv_cuda_check(c, cudaGetLastError(), "learned: forward");
 }
 
@@ -1386,6 +1392,7 @@ int lv_learn_set_params(lv_ctx* c, const float* in) {
   if (!c || !in) return LV_ERR_BAD_ARGUMENT;
   if (int rc = ensure_state(c)) return rc;
   cudaMemcpyAsync(c->learn->params, in, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, c->stream);
+  c->learn->wbf_valid = false;
   c->learn->factor_ready = true;
   return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_learn_set_params");
 }
@@ -1488,6 +1495,7 @@ int lv_learn_train(lv_ctx* c, int32_t steps, float lr, int32_t K, uint64_t seed,
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - powf(b1, (float)L->adam_t), c2 = 1.f - powf(b2, (float)L->adam_t);
     k_adam<<<lv_blocks(NPARAM, TPB), TPB, 0, s>>>(NPARAM, L->params, L->grad, L->m1, L->m2, lr, b1, b2, c1, c2);
+    L->wbf_valid = false;
     c->launches += 2;
     if (dl) cudaMemcpyAsync(dl + st, L->loss, sizeof(double), cudaMemcpyDeviceToDevice, s);
   }
