@@ -344,7 +344,9 @@ __device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, int i, bool o
   __shared__ bool s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nsum = singular ? LV_SG_SUMS : 5;
-  for (int q = 0; q < nsum; ++q) {
+#pragma unroll
+  for (int q = 0; q < LV_SG_SUMS; ++q) {
+    if (q >= nsum) break;  // uniform
     double v = acc[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) sh[q][wid] = v;
@@ -362,17 +364,29 @@ __device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, int i, bool o
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  for (int q = 0; q < nsum; ++q) {
-    double v = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += LV_SG_TPB) v += __ldcg(sv.sgpart + (size_t)q * gridDim.x + b);
+  // every block's partials of every sum, the loads of all sums together
+  double pv[LV_SG_SUMS];
+#pragma unroll
+  for (int q = 0; q < LV_SG_SUMS; ++q) pv[q] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += LV_SG_TPB) {
+#pragma unroll
+    for (int q = 0; q < LV_SG_SUMS; ++q)
+      if (q < nsum) pv[q] += __ldcg(sv.sgpart + (size_t)q * gridDim.x + b);
+  }
+#pragma unroll
+  for (int q = 0; q < LV_SG_SUMS; ++q) {
+    if (q >= nsum) break;
+    double v = pv[q];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) sh[q][wid] = v;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     double t[LV_SG_SUMS] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int q = 0; q < nsum; ++q)
-      for (int k = 0; k < LV_SG_TPB / 32; ++k) t[q] += sh[q][k];
+#pragma unroll
+    for (int q = 0; q < LV_SG_SUMS; ++q)
+      if (q < nsum)
+        for (int k = 0; k < LV_SG_TPB / 32; ++k) t[q] += sh[q][k];
     double r1 = t[0], r2 = t[1];
     if (singular) {
       r1 -= t[5] * t[6] / (double)n;
