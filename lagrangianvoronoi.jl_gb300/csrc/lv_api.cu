@@ -174,6 +174,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   const double r_max = prm->r_max > 0 ? prm->r_max : 10.0 * dr;
   g.dr = dr;
   g.h = h;
+  g.rh = 1.0 / h;
   g.xper = prm->xperiodic ? 1 : 0;
   g.yper = prm->yperiodic ? 1 : 0;
   g.bminx = prm->xmin[0];

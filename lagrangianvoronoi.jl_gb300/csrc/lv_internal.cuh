@@ -47,6 +47,7 @@ struct GridDev {
   double cminx, cminy, cmaxx, cmaxy;  // cropping rectangle
   double ox, oy;                      // cell-list origin = cropping.xmin - (h, h)
   double h, rr_max, xperiod, yperiod, dr;
+  double rh;                          // RN(1/h): the cell-key divisions by h through div_rcp
   double dx_hi, dy_hi;                // offsets from the origin beyond which a key is surely > n1 (> n2)
   int xper, yper;
   int n1, n2;

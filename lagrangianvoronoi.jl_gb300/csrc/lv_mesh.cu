@@ -107,7 +107,7 @@ __global__ void k_scan_add(int* out, int len, const int* sums, int ntiles) {
 __device__ __forceinline__ int cell_of(const GridDev& g, double px, double py, bool quick) {
   double dx = px - g.ox, dy = py - g.oy;
   if (quick && (dx < 0.0 || dy < 0.0 || dx >= g.dx_hi || dy >= g.dy_hi)) return -1;
-  double f1 = floor(dx / g.h), f2 = floor(dy / g.h);
+  double f1 = floor(div_rcp(dx, g.h, g.rh)), f2 = floor(div_rcp(dy, g.h, g.rh));
   if (!(fabs(f1) < 1e15) || !(fabs(f2) < 1e15)) return -2;
   long long i1 = (long long)f1 + 1, i2 = (long long)f2 + 1;
   if (i1 < 1 || i1 > g.n1 || i2 < 1 || i2 > g.n2) return -1;
@@ -679,7 +679,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   bool done = !active;
   long long k1 = 0, k2 = 0;
   if (active) {
-    const double f1 = floor((px - g.ox) / g.h), f2 = floor((py - g.oy) / g.h);
+    const double f1 = floor(div_rcp(px - g.ox, g.h, g.rh)), f2 = floor(div_rcp(py - g.oy, g.h, g.rh));
     if (!(fabs(f1) < 1e15) || !(fabs(f2) < 1e15)) {
       flag = LV_FLAG_NONFINITE;
       done = true;
