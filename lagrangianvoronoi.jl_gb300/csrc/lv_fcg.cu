@@ -1149,8 +1149,15 @@ __global__ void __launch_bounds__(128) k_build_minv_reg(int n, const int* __rest
                                                         const int* __restrict__ col, const float* __restrict__ gd,
                                                         const float* __restrict__ gl, const int* __restrict__ rev,
                                                         const float* __restrict__ dh, float eps, int stride, int* mcnt,
-                                                        int* mcol, float* mval, float* mdiag, int* over) {
+                                                        int* mcol, float* mval, float* mdiag, int* over, int* mok,
+                                                        int* stage_stat) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    // the status words of this build, before any later kernel updates them
+    *mok = 1;
+    stage_stat[0] = 1;
+    stage_stat[1] = stage_stat[2] = stage_stat[3] = 0;
+  }
   if (i >= n) return;
   int cols[MREG];
   float vals[MREG];
@@ -1338,9 +1345,11 @@ int lv_fcg_build_minv(lv_ctx* c) {
   lv_learn_factor_ptrs(c, &gd, &gl, &dh, &rev);
   lv_learn_factor2_ptrs(c, &rowptr2, &col2, &gl2, &rev2);
   if (!gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
-  const int one = 1;
-  cudaMemcpyAsync(c->sv.mok, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
   if (rowptr2) {
+    const int one = 1;
+    cudaMemcpyAsync(c->sv.mok, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
+    const int init[4] = {1, 0, 0, 0};
+    cudaMemcpyAsync(c->sv.stage_stat, init, sizeof(init), cudaMemcpyHostToDevice, c->stream);
     k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, rowptr2, col2,
                                                             gl2, rev2, dh, c->learn_eps, c->sv.mrows, c->sv.mcnt,
                                                             c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok, nullptr);
@@ -1350,7 +1359,8 @@ int lv_fcg_build_minv(lv_ctx* c) {
     int* over = c->sv.remap;  // scratch: the staged image build rewrites it below
     k_build_minv_reg<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, dh,
                                                                 c->learn_eps, c->sv.mrows, c->sv.mcnt, c->sv.mcol,
-                                                                c->sv.mval, c->sv.mdiag, over);
+                                                                c->sv.mval, c->sv.mdiag, over, c->sv.mok,
+                                                                c->sv.stage_stat);
     LV_LAUNCH_CHECK(c, "k_build_minv_reg");
     k_build_minv<<<lv_blocks(n, 128), 128, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, nullptr, nullptr,
                                                             nullptr, nullptr, dh, c->learn_eps, c->sv.mrows,
@@ -1367,8 +1377,7 @@ int lv_fcg_build_minv(lv_ctx* c) {
   int nb, R;
   fcg_shape(c, n, &nb, &R);
   if (c->fcg_halo && stage_fits(c, nb, R) && nb <= std::min(c->num_sms * 2, FCG_MAX_BLOCKS)) {
-    const int init[4] = {1, 0, 0, 0};
-    cudaMemcpyAsync(c->sv.stage_stat, init, sizeof(init), cudaMemcpyHostToDevice, c->stream);
+    // (stage_stat was initialised by the first kernel of the M^-1 build)
     k_stage_build<<<nb, STG_BUILD_TPB, STG_BUILD_SMEM, c->stream>>>(
         n, (n + nb - 1) / nb, c->sv.rowptr, c->sv.col, c->sv.mcnt, c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.dinv,
         c->sv.mrows, static_cast<StageImage*>(c->sv.stage), c->sv.remap, c->sv.stage_stat);
