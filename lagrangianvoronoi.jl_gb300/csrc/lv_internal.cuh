@@ -261,6 +261,7 @@ struct lv_ctx {
   bool fcg_halo = true;    // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   bool fcg_reset = true;   // clear the flag-reduced solver's counter, flags and bases before its next launch
   bool flen_valid = false;  // m.flen belongs to the current mesh
+  bool ccount_clean = false;  // the cell counts are zero (cleared by the last completed order pass)
   void* clip_resume = nullptr;  // captures of the first clipping pass (cap entries, allocated on first use)
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;

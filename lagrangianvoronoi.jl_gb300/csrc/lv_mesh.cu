@@ -149,8 +149,9 @@ done:
 // the grid), so that the scatter needs neither the cell computation nor
 // atomics.
 __global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int cap, int* ccount, int2* key,
-                            int* status) {
+                            int* status, int* redo_n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *redo_n = 0;  // the clipping pass's capture count, for this remesh
   if (i >= n) return;
   double2 p = x[i];
   int nim = image_count(g);
@@ -185,10 +186,12 @@ __global__ void k_bin_scatter(GridDev g, int n, int cap, const int2* __restrict_
 
 // Insertion order of the reference with one thread is the particle index
 // order; atomics scatter arbitrarily, so each cell is sorted back.
+// (also clears the cell counts for the next remesh: the scan has consumed them)
 __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* citem, float2* cpos,
-                            const double2* __restrict__ x, int item_cap) {
+                            const double2* __restrict__ x, int item_cap, int* ccount) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
+  ccount[c] = 0;
   int a = cstart[c], b = min(cstart[c + 1], item_cap);
   for (int s = a + 1; s < b; ++s) {
     int v = citem[s];
@@ -959,16 +962,21 @@ int lv_mesh_remesh(lv_ctx* c) {
   const int nc = c->c.ncells;
   {
   KernelTimer kt(c, LV_KF_BIN);
-  cudaMemsetAsync(c->c.ccount, 0, sizeof(int) * nc, s);
-  k_bin_count<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->cap, c->c.ccount, c->c.bkey, c->status);
+  // the cell counts are clean when the previous remesh completed its order pass
+  if (!c->ccount_clean) cudaMemsetAsync(c->c.ccount, 0, sizeof(int) * nc, s);
+  c->ccount_clean = false;
+  k_bin_count<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, c->s.x, n, c->cap, c->c.ccount, c->c.bkey, c->status,
+                                                  c->sv.iters + LV_IT_REDO);
   LV_LAUNCH_CHECK(c, "k_bin_count");
   int rc = lv_scan_int(c, c->c.ccount, c->c.cstart, nc);
   if (rc) return rc;
   k_bin_scatter<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, n, c->cap, c->c.bkey, c->c.cstart, c->c.citem,
                                                     c->c.item_cap, c->status);
   LV_LAUNCH_CHECK(c, "k_bin_scatter");
-  k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap);
+  k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap,
+                                                  c->c.ccount);
   LV_LAUNCH_CHECK(c, "k_bin_order");
+  c->ccount_clean = true;
   }
   static bool attr_set = false;
   if (!attr_set) {
@@ -989,8 +997,7 @@ int lv_mesh_remesh(lv_ctx* c) {
       c->clip_resume = p;
     }
     ClipResume* redo = static_cast<ClipResume*>(c->clip_resume);
-    int* redo_n = c->sv.iters + LV_IT_REDO;
-    cudaMemsetAsync(redo_n, 0, sizeof(int), s);
+    int* redo_n = c->sv.iters + LV_IT_REDO;  // zeroed by k_bin_count
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
                                                                                    c->m, c->status, redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip");

@@ -29,8 +29,10 @@ constexpr int TPB = 256;
 constexpr int CG_TPB = 256;
 constexpr long long BARRIER_CYCLE_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 
-__global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n) {
+// (also clears the nonsingular flag that k_assemble then sets)
+__global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n, int* nonsingular) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *nonsingular = 0;
   if (i < n) hr[i] = 0.5 / rho[i];
 }
 
@@ -875,10 +877,9 @@ int lv_solver_assemble(lv_ctx* c, double dt) {
   int rc = lv_scan_int(c, c->m.nfaces, c->sv.rowptr, n);
   if (rc) return rc;
   double* hr = c->sv.tmp + 2 * (size_t)c->cap;  // scratch past the scan sums
-  k_half_rho<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s.rho, hr, n);
-  LV_LAUNCH_CHECK(c, "k_half_rho");
   // singular operator <=> every diagonal term is zero (c2 = Inf everywhere)
-  cudaMemsetAsync(c->sv.iters + LV_IT_NONSINGULAR, 0, sizeof(int), s);
+  k_half_rho<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s.rho, hr, n, c->sv.iters + LV_IT_NONSINGULAR);
+  LV_LAUNCH_CHECK(c, "k_half_rho");
   k_assemble<<<lv_blocks(n, TPB), TPB, 0, s>>>(c->s, c->m, c->sv, n, dt, hr, c->sv.iters + LV_IT_NONSINGULAR);
   LV_LAUNCH_CHECK(c, "k_assemble");
   c->op_ready = true;
