@@ -63,7 +63,7 @@ enum lv_field {
 
 /* pressure solver methods */
 enum lv_method {
-  LV_METHOD_JACOBI_PCG = 0,   /* FP64 Jacobi-preconditioned CG (the fallback and the judge) */
+  LV_METHOD_JACOBI_PCG = 0,   /* FP64 Jacobi-preconditioned CG (the fallback, and the plain solver the others are measured against) */
   LV_METHOD_MIXED_IR = 1,     /* FP32 CG inner solves inside FP64 iterative refinement */
   LV_METHOD_LEARNED_PCG = 2   /* mixed IR preconditioned by the learned sparse factor */
 };
