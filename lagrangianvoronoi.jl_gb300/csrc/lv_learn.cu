@@ -230,66 +230,71 @@ __global__ void k_hop2_rev(int n, const int* __restrict__ rowptr2, const int* __
 
 // ---------------------------------------------------------------- forward
 
-// Fills the warp's A tile [16][2KH] (FP32, shared): own rows of Hin and
-// Agg(Hin) = sum_k what_k Hin[col_k].  Lane l handles row l & 15 and half
-// (l >> 4) of the features.
+// Row r's own features and aggregation Agg(Hin)_r = sum_k what_k Hin[col_k]
+// for lane (r, half): half (l >> 4) of the KH features; rows past n give
+// zeros.  Two neighbours per round, their loads issued together; the sum runs
+// over the neighbours in order.
 template <int KH>
-__device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict__ Hin, const int* __restrict__ rowptr,
-                          const int* __restrict__ col, const float* __restrict__ what) {
-  const int lane = threadIdx.x & 31;
-  const int r = lane & 15, half = lane >> 4;
-  const int row = row0 + r;
+__device__ __forceinline__ void aggregate_row(int row, int half, int n, const float* __restrict__ Hin,
+                                              const int* __restrict__ rowptr, const int* __restrict__ col,
+                                              const float* __restrict__ what, float (&own)[KH / 2],
+                                              float (&agg)[KH / 2]) {
   constexpr int FH = KH / 2;
-  float agg[FH];
+  static_assert(FH % 4 == 0, "16-byte feature chunks");
 #pragma unroll
-  for (int f = 0; f < FH; ++f) agg[f] = 0.f;
-  float own[FH];
+  for (int f = 0; f < FH; ++f) agg[f] = own[f] = 0.f;
+  if (row >= n) return;
+  const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
 #pragma unroll
-  for (int f = 0; f < FH; ++f) own[f] = 0.f;
-  if (row < n) {
-    static_assert(FH % 4 == 0, "16-byte feature chunks");
-    const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
+  for (int f = 0; f < FH / 4; ++f) {
+    const float4 v = hr[f];
+    own[4 * f] = v.x;
+    own[4 * f + 1] = v.y;
+    own[4 * f + 2] = v.z;
+    own[4 * f + 3] = v.w;
+  }
+  const int k1 = rowptr[row + 1];
+  for (int k = rowptr[row]; k < k1; k += 2) {
+    const bool two = k + 1 < k1;
+    const int ja = col[k], jb = two ? col[k + 1] : ja;
+    const float wa = what[k], wb = two ? what[k + 1] : 0.f;
+    const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
+    const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
+    float4 va[FH / 4], vb[FH / 4];
 #pragma unroll
     for (int f = 0; f < FH / 4; ++f) {
-      const float4 v = hr[f];
-      own[4 * f] = v.x;
-      own[4 * f + 1] = v.y;
-      own[4 * f + 2] = v.z;
-      own[4 * f + 3] = v.w;
+      va[f] = ha[f];
+      vb[f] = hb[f];
     }
-    // two neighbours per round, their loads issued together; the sum runs
-    // over the neighbours in order
-    const int k1 = rowptr[row + 1];
-    for (int k = rowptr[row]; k < k1; k += 2) {
-      const bool two = k + 1 < k1;
-      const int ja = col[k], jb = two ? col[k + 1] : ja;
-      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
-      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
-      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
-      float4 va[FH / 4], vb[FH / 4];
+#pragma unroll
+    for (int f = 0; f < FH / 4; ++f) {
+      agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
+      agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
+      agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
+      agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
+    }
+    if (two) {
 #pragma unroll
       for (int f = 0; f < FH / 4; ++f) {
-        va[f] = ha[f];
-        vb[f] = hb[f];
-      }
-#pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
-        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
-        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
-        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
-      }
-      if (two) {
-#pragma unroll
-        for (int f = 0; f < FH / 4; ++f) {
-          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
-          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
-          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
-          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
-        }
+        agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
+        agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
+        agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
+        agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
       }
     }
   }
+}
+
+// Fills the warp's A tile [16][2KH] (FP32, shared): own rows of Hin and
+// Agg(Hin); lane l handles row l & 15 and half (l >> 4) of the features.
+template <int KH>
+__device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict__ Hin, const int* __restrict__ rowptr,
+                          const int* __restrict__ col, const float* __restrict__ what) {
+  constexpr int FH = KH / 2;
+  const int lane = threadIdx.x & 31;
+  const int r = lane & 15, half = lane >> 4;
+  float own[FH], agg[FH];
+  aggregate_row<KH>(row0 + r, half, n, Hin, rowptr, col, what, own, agg);
   float* t = tile + r * (2 * KH);
 #pragma unroll
   for (int f = 0; f < FH; ++f) {
@@ -358,53 +363,8 @@ __device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const
   constexpr int K = 2 * KH, FH = KH / 2;
   const int lane = threadIdx.x & 31;
   const int r = lane & 15, half = lane >> 4;
-  const int row = row0 + rl + r;
-  float agg[FH], own[FH];
-#pragma unroll
-  for (int f = 0; f < FH; ++f) agg[f] = own[f] = 0.f;
-  if (row < n) {
-    const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
-#pragma unroll
-    for (int f = 0; f < FH / 4; ++f) {
-      const float4 v = hr[f];
-      own[4 * f] = v.x;
-      own[4 * f + 1] = v.y;
-      own[4 * f + 2] = v.z;
-      own[4 * f + 3] = v.w;
-    }
-    // two neighbours per round, their loads issued together; the sum runs
-    // over the neighbours in order
-    const int k1 = rowptr[row + 1];
-    for (int k = rowptr[row]; k < k1; k += 2) {
-      const bool two = k + 1 < k1;
-      const int ja = col[k], jb = two ? col[k + 1] : ja;
-      const float wa = what[k], wb = two ? what[k + 1] : 0.f;
-      const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
-      const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
-      float4 va[FH / 4], vb[FH / 4];
-#pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        va[f] = ha[f];
-        vb[f] = hb[f];
-      }
-#pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
-        agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
-        agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
-        agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
-      }
-      if (two) {
-#pragma unroll
-        for (int f = 0; f < FH / 4; ++f) {
-          agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
-          agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
-          agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
-          agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
-        }
-      }
-    }
-  }
+  float own[FH], agg[FH];
+  aggregate_row<KH>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
 #pragma unroll
   for (int f = 0; f < FH; f += 2) {
     *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, half * FH + f, K)) = pack_bf16(own[f], own[f + 1]);
