@@ -13,7 +13,9 @@
 //   k_bin_order    per cell: restore insertion (index) order, cache float2 positions
 //   k_clip         one thread per polygon: candidate search along the cell path,
 //                  half-plane clipping in shared memory, edge ordering, area,
-//                  centroid and the interior-face quantities every operator uses.
+//                  centroid and the interior-face quantities every operator uses
+//   k_clip_redo    the polygons that outgrew the first pass's edge slots,
+//                  resumed from their captures with LV_MAX_EDGES slots
 #include <math.h>
 
 #include "lv_internal.cuh"
@@ -234,8 +236,9 @@ constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
 // edge slots of the first clipping pass: shared memory for 9 edges per
 // polygon (52 bytes a slot) lets seven blocks share an SM (three with
-// LV_MAX_EDGES); a polygon that needs more at any point is redone by a second
-// pass with LV_MAX_EDGES slots, spread over every SM.  Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
+// LV_MAX_EDGES); a polygon that needs more at any point is captured and
+// finished by a second pass with LV_MAX_EDGES slots, spread over every SM.
+// Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
 // before the warp-uniform clip: 8 slots 1.84 / 12.9, 10 slots 1.44 / 12.8,
 // 12 slots 1.49 / 14.2, 14 slots 1.52 / 16.6, all 20 slots in one pass
 // 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16; with
@@ -902,10 +905,11 @@ __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev*
   clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, redo, redo_n, nullptr);
 }
 
-// second pass: the queued polygons with LV_MAX_EDGES slots.  The queue is
-// short, so its polygons are dealt round-robin over all resident blocks
-// (queue entry t * gridDim.x + b to thread t of block b): every SM gets some,
-// and the pass lasts about one polygon's clipping instead of a block's share.
+// second pass: the captured polygons, resumed with LV_MAX_EDGES slots.  The
+// captures are few, so they are dealt round-robin over all resident blocks
+// (capture t * gridDim.x + b to thread t of block b): every SM gets some, and
+// the pass lasts about one polygon's remaining clipping instead of a block's
+// share.
 __global__ void __launch_bounds__(CLIP_TPB) k_clip_redo(GridDev g, const PathNodeDev* __restrict__ path,
                                                         const double2* __restrict__ x, CellsDev cl, MeshDev m,
                                                         int* status, const ClipResume* __restrict__ redo,
