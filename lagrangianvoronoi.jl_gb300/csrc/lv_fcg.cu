@@ -67,7 +67,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 }
 
 // Per-block image of the staged learned solve, built once per factor by
-// k_stage_build and copied to shared memory at launch.  The rows whose u the
+// k_stage_build and moved to shared memory at launch (bulk copies of each
+// field's used prefix, below).  The rows whose u the
 // block computes (its own rows and its halo: the rows outside the block that
 // its operator rows reference) take positions ordered by their M^-1 entry
 // count, longest first; thread t applies positions t, t + 512, ...  Positions
