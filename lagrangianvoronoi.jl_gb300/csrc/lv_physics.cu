@@ -31,7 +31,10 @@ __device__ __forceinline__ size_t face_slot(int k, int nf, int cap, int i) {
 
 __device__ __forceinline__ double jmax(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double jmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double dot2(double2 a, double2 b) { return a.x * b.x + a.y * b.y; }
+// a wall velocity pair (x, y of two labels), passed to kernels by value
+struct Wall2 {
+  double x, y, z, w;
+};
 
 // ------------------------------------------------------------------- EOS
 
@@ -149,7 +152,7 @@ __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n
 //   te  = dot(dS, vbc - v_i)/dt                 per boundary edge
 // and k_rhs / k_rhs_gp subtract or add them in the reference's order, so b and
 // GP are bit-identical to evaluating refresh! in full every sweep.
-__global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, double4 vbc_ud, double4 vbc_rl) {
+__global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, Wall2 vbc_ud, Wall2 vbc_rl) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n,
 }
 
 // bdary_friction! (diffusion.jl:64-79) with a constant wall velocity per label.
-__global__ void k_friction(StateDev s, MeshDev m, int n, double dt, double4 w_ud, double4 w_rl) {
+__global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, Wall2 w_rl) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
@@ -841,8 +844,8 @@ int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepar
     if (vbc)
       for (int k = 0; k < 8; ++k) w[k] = vbc[k];
     // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
-    double4 ud = make_double4(w[0], w[1], w[4], w[5]);
-    double4 rl = make_double4(w[2], w[3], w[6], w[7]);
+    const Wall2 ud{w[0], w[1], w[4], w[5]};
+    const Wall2 rl{w[2], w[3], w[6], w[7]};
     LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl);
   }
   static_assert(TPB == LV_SG_TPB, "the sweep-guess sums assume 256 threads per block");
@@ -876,8 +879,8 @@ int lv_phys_friction(lv_ctx* c, const double* vwall, double dt) {
   double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (vwall)
     for (int k = 0; k < 8; ++k) w[k] = vwall[k];
-  double4 ud = make_double4(w[0], w[1], w[4], w[5]);
-  double4 rl = make_double4(w[2], w[3], w[6], w[7]);
+  const Wall2 ud{w[0], w[1], w[4], w[5]};
+  const Wall2 rl{w[2], w[3], w[6], w[7]};
   LAUNCH(k_friction, c->s, c->m, c->n, dt, ud, rl);
   return LV_OK;
 }
