@@ -282,6 +282,11 @@ int lv_solver_halo(lv_ctx* ctx, int32_t* max_rows);
  * off).  lv_solver_forget forgets that history, e.g. after the state was
  * replaced (a restart from a checkpoint): the next call starts like the first. */
 int lv_solver_forget(lv_ctx* ctx);
+/* Polygons of the last remesh that outgrew the first clipping pass's edge
+ * slots and were finished by the second pass (LVGPU_CLIP_SLOTS=5..8 lowers
+ * the first pass's slots, so that tests can drive most polygons through the
+ * second pass); synchronises. */
+int lv_mesh_captures(lv_ctx* ctx, int32_t* count);
 
 /* Per-kernel-family device times in ms accumulated since the last reset:
  * out[0] mesh, [1] operators, [2] pressure solve, [3] other.  Returns the

@@ -211,6 +211,12 @@ class VoronoiGrid:
                                         _lib.ptr(items, C.c_int32)))
         return starts, items[:ni.value]
 
+    def clip_captures(self):
+        """Polygons of the last remesh finished by the second clipping pass."""
+        n = C.c_int32()
+        _check(self, _lib.load().lv_mesh_captures(self._ctx, C.byref(n)))
+        return int(n.value)
+
     def synchronize(self):
         _check(self, _lib.load().lv_synchronize(self._ctx))
 

@@ -91,6 +91,7 @@ SIGNATURES = {
     "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
     "lv_solver_halo": (C.c_int, [_vp, _pi32]),
     "lv_solver_forget": (C.c_int, [_vp]),
+    "lv_mesh_captures": (C.c_int, [_vp, _pi32]),
     "lv_learn_init": (C.c_int, [_vp, C.c_uint64]),
     "lv_learn_num_params": (_i32, []),
     "lv_learn_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),

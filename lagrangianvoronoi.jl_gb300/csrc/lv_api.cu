@@ -842,6 +842,15 @@ int lv_kernel_time(lv_ctx* c, int32_t fam, int64_t* launches, double* ms, int32_
   return LV_OK;
 }
 
+int lv_mesh_captures(lv_ctx* c, int32_t* count) {
+  if (!c || !count) return LV_ERR_BAD_ARGUMENT;
+  if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
+  int v = 0;
+  if (int rc = lv_mesh_captures_count(c, &v)) return rc;
+  *count = v;
+  return LV_OK;
+}
+
 int lv_solver_forget(lv_ctx* c) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   c->sg_valid = 0;

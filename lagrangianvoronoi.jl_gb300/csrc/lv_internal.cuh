@@ -429,6 +429,7 @@ int lv_cuda_check(lv_ctx* c, cudaError_t e, const char* what);
 // ---- mesh (lv_mesh.cu)
 int lv_mesh_remesh(lv_ctx* c);
 int lv_mesh_face_len(lv_ctx* c);  // fills m.flen unless it is current
+int lv_mesh_captures_count(lv_ctx* c, int* count);  // second-pass polygons of the last remesh (synchronises)
 int lv_scan_int(lv_ctx* c, const int* in, int* out, int len);  // exclusive, out[len] = total
 
 // ---- physics (lv_physics.cu)

@@ -17,6 +17,7 @@
 //   k_clip_redo    the polygons that outgrew the first pass's edge slots,
 //                  resumed from their captures with LV_MAX_EDGES slots
 #include <math.h>
+#include <stdlib.h>
 
 #include "lv_internal.cuh"
 
@@ -632,7 +633,7 @@ struct ClipResume {
 template <int CAP>
 __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ path, const double2* __restrict__ x,
                              int i, bool active, const CellsDev& cl, const MeshDev& m, int* status,
-                             ClipResume* save, int* save_n, const ClipResume* resume) {
+                             ClipResume* save, int* save_n, const ClipResume* resume, int slots = CAP) {
   extern __shared__ double smem[];
   const int t = threadIdx.x;
   Poly P;
@@ -646,7 +647,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   P.r2x = P.r1y + CAP * CLIP_TPB;
   P.r2y = P.r2x + CAP * CLIP_TPB;
   P.t = t;
-  P.cap_e = CAP;
+  P.cap_e = slots;  // <= CAP
 
   double px = 0.0, py = 0.0;
   int ne = 0;
@@ -900,9 +901,9 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
 template <int CAP>
 __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
                                                    const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
-                                                   int* status, ClipResume* redo, int* redo_n) {
+                                                   int* status, ClipResume* redo, int* redo_n, int slots) {
   const int i = blockIdx.x * CLIP_TPB + threadIdx.x;
-  clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, redo, redo_n, nullptr);
+  clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, redo, redo_n, nullptr, slots);
 }
 
 // second pass: the captured polygons, resumed with LV_MAX_EDGES slots.  The
@@ -948,6 +949,14 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len) {
 __global__ void k_face_len(MeshDev m, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) lv_face_lengths(m, i);
+}
+
+int lv_mesh_captures_count(lv_ctx* c, int* count) {
+  int v = 0;
+  cudaMemcpyAsync(&v, c->sv.iters + LV_IT_REDO, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (int rc = lv_cuda_check(c, cudaStreamSynchronize(c->stream), "lv_mesh_captures")) return rc;
+  *count = v;
+  return LV_OK;
 }
 
 int lv_mesh_face_len(lv_ctx* c) {
@@ -1002,8 +1011,16 @@ int lv_mesh_remesh(lv_ctx* c) {
     }
     ClipResume* redo = static_cast<ClipResume*>(c->clip_resume);
     int* redo_n = c->sv.iters + LV_IT_REDO;  // zeroed by k_bin_count
+    // the first pass's slots: ME_SMALL, or fewer (5..ME_SMALL-1) through
+    // LVGPU_CLIP_SLOTS so that tests can drive most polygons through the
+    // second pass (the mesh is the same either way)
+    int slots = ME_SMALL;
+    if (const char* env = getenv("LVGPU_CLIP_SLOTS")) {
+      const int v = atoi(env);
+      if (v >= 5 && v < ME_SMALL) slots = v;
+    }
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
-                                                                                   c->m, c->status, redo, redo_n);
+                                                                                   c->m, c->status, redo, redo_n, slots);
     LV_LAUNCH_CHECK(c, "k_clip");
     // three 20-slot blocks fit an SM
     k_clip_redo<<<3 * c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status,
