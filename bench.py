@@ -1,32 +1,39 @@
 #!/usr/bin/env python
 """Benchmark of the Lagrangian Voronoi time step on GB300.
 
-Workload: the Taylor-Green vortex flow, periodic unit square, 256 x 256 =
-65,536 seeds on a jittered lattice (SplitMix64 seed 12345, U(-0.1h, 0.1h)),
-u = sin(2 pi x) cos(2 pi y), v = -cos(2 pi x) sin(2 pi y), Re = 100,
-dt = 5e-4, FP64, stiffened gas (c0 = 50, gamma = 1.4), pressure solved by
-FP64 Jacobi-PCG to ||r|| <= 1e-8 ||b|| in each of the 10 fixed-point sweeps.
-One step is the reference's step! (move!, stiffened_eos!, find_pressure!,
-pressure_step!, find_D!, viscous_step!, find_dv!, relaxation_step!) with
-both remeshes.
+Default workload: the double shear layer, periodic unit square, 2048 x 2048
+= 4,194,304 seeds on a jittered lattice (SplitMix64 seed 12345,
+U(-0.1h, 0.1h)), u = tanh(80(y - 1/4)) for y <= 1/2 else tanh(80(3/4 - y)),
+v = 0.05 sin(2 pi x), Re = 10,000 (mu = 1e-4), ideal gas (gamma = 1.4,
+P0 = 100/gamma), dt = 0.1 dr / 2, FP64 state and geometry.  One step is the
+reference's step! (examples/doubleshear.jl: move!, ideal_eos!,
+find_pressure! with 10 fixed-point sweeps, pressure_step!, find_D!,
+viscous_step!, find_dv!, relaxation_step!) with both remeshes.  The
+pressure sweeps are solved by the learned-preconditioned mixed-precision
+solver (FP32 inner CG inside FP64 iterative refinement) to an FP64 residual
+||b - A x|| <= 1e-8 ||b||; every timed sweep is checked to have converged.
+--config selects another of the five flows (gresho 50^2, taylor_green 256^2,
+rayleigh_taylor 512x1024, cavity 1024^2, double_shear 2048^2), --solver the
+pressure solver.
 
 Metric: particle-steps/s (particles x steps / device time of the steps).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config NAME] [--solver jacobi_pcg|mixed_ir|learned_pcg]
 
 --impl reference times the CPU restatement of the reference's algorithm
-(the oracle, reference solver settings: MINRES atol = rtol = 1e-6,
-itmax = 1000) on all host cores for the same workload.  With --gpus N > 1
-(torchrun) every rank runs an independent replica of the workload.
+(the oracle, with the reference's solver settings: MINRES atol = rtol =
+1e-6, itmax = 1000) on all host cores for the same workload.  With --gpus N
+> 1 (torchrun) every rank runs an independent replica of the workload.
 """
 import argparse
 import ctypes as C
 import json
-import math
 import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 
 import numpy as np
@@ -34,20 +41,48 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-NX = NY = 256
-N = NX * NY
-WORKLOAD = "taylor_green_256x256"
-
-
-def set_size(nx):
-    """The benchmark workload is 256 x 256; other sizes are for profiling."""
-    global NX, NY, N, WORKLOAD
-    NX = NY = int(nx)
-    N = NX * NY
-    WORKLOAD = f"taylor_green_{NX}x{NY}"
 METRIC = "particle-steps/s at 1 GB300; pressure solve ms & CG iters, learned vs plain PCG @1e-8"
 UNIT = "particle-steps/s"
+L2_BYTES = 129 << 20
 L2_FLUSH_BYTES = 512 << 20
+# bytes of device state per particle (x, v, dv, momentum, D, GP, e, P, rho,
+# c2, mass, energy, quality, mu, phase), the mesh and the operator excluded
+STATE_BYTES_PER_PARTICLE = 196
+
+# (default lattice nx, ny) of each flow: the sizes of the five workloads
+CONFIG_SIZES = {"gresho": (50, 50), "taylor_green": (256, 256), "rayleigh_taylor": (512, 1024),
+                "cavity": (1024, 1024), "double_shear": (2048, 2048)}
+
+
+class Workload:
+    def __init__(self, name, nx=None):
+        import workloads as W
+        dnx, dny = CONFIG_SIZES[name]
+        nx = int(nx) if nx else dnx
+        ny = nx * dny // dnx
+        self.name = name
+        self.flow = W.rayleigh_taylor(nx, ny) if name == "rayleigh_taylor" else W.FLOWS[name](nx)
+        if name == "taylor_green":
+            # the 256 x 256 workload has dt = 5e-4; other sizes keep its CFL number
+            self.flow.dt = 5e-4 * 256.0 / nx
+        self.nx, self.ny = nx, ny
+        self.n = nx * ny
+        self.label = f"{name}_{nx}x{ny}"
+
+    def describe(self):
+        f = self.flow
+        d = {"workload": self.label, "particles": self.n, "dt": f.dt, "periodic": bool(f.periodic)}
+        if f.eos == "stiffened":
+            d["eos"] = f"stiffened gamma={f.gamma} P0={f.P0:.6g}"
+        elif f.eos == "ideal":
+            d["eos"] = f"ideal gamma={f.gamma}"
+        else:
+            d["eos"] = "incompressible (c2 = Inf)"
+        d["mu"] = getattr(f, "mu", None) if self.name != "rayleigh_taylor" else f"rho/{f.Re}"
+        d["artificial_viscosity"] = bool(f.artificial_viscosity)
+        if f.walls is not None:
+            d["walls"] = {str(k): v for k, v in f.walls.items()} or "no-slip"
+        return d
 
 
 def load_package():
@@ -82,18 +117,12 @@ def allmax(world, v):
     return float(t.item())
 
 
-def flow():
-    import workloads as W
-    fl = W.taylor_green(NX)
-    # the 256 x 256 workload has dt = 5e-4; profiling sizes keep its CFL number
-    fl.dt = 5e-4 * 256.0 / NX
-    return fl
-
-
 # ------------------------------------------------------------------ clocks
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region.
+    The sampler is started, and its first sample awaited, before the region
+    begins, so that its start-up does not overlap the timed work."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -102,29 +131,43 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.lines = []
+        self.marks = []
+        self._first = threading.Event()
 
-    def __enter__(self):
+    def _reader(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.perf_counter(), line))
+            self._first.set()
+
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return self
+        threading.Thread(target=self._reader, daemon=True).start()
+        self._first.wait(5.0)
         return self
 
-    def __exit__(self, *a):
-        self.out = ""
+    def mark(self):
+        self.marks.append(time.perf_counter())
+
+    def stop(self):
         if self.proc is not None:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                self.out, _ = self.proc.communicate()
 
-    def summary(self):
+    def summary(self, t0=None, t1=None):
         rows = []
-        for line in (self.out or "").splitlines():
+        for ts, line in self.lines:
+            if t0 is not None and not (t0 <= ts <= t1 + 0.25):
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -142,17 +185,18 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ our arm
 
-# the fields that carry a Taylor-Green state from one step to the next (the
-# mesh follows from x by remesh)
+# the fields that carry a state from one step to the next (the mesh follows
+# from x by remesh)
 STATE_FIELDS = ["x", "v", "e", "P", "rho", "c2", "dv", "mass", "momentum", "energy", "phase", "quality", "D", "mu"]
 
 
-def setup_grid(lv, fl):
+def setup_grid(lv, wl):
     import harness as H
     from lvgpu import populate as pop
     import workloads as W
+    fl = wl.flow
     x = H.seeds(pop, fl)
-    g = lv.VoronoiGrid(lv.Rectangle(fl.xlims, fl.ylims), fl.dr, xperiodic=True, yperiodic=True)
+    g = lv.VoronoiGrid(lv.Rectangle(fl.xlims, fl.ylims), fl.dr, xperiodic=fl.periodic, yperiodic=fl.periodic)
     g.push(x)
     lv.remesh(g)
     for k, v in W.initial_fields(fl, g["x"], g["area"]).items():
@@ -161,19 +205,49 @@ def setup_grid(lv, fl):
 
 
 def gpu_step(lv, g, solver, fl, snapshot=False, stats=False):
-    dt = fl.dt
-    lv.move(g, dt)
-    lv.stiffened_eos(g, fl.gamma, fl.P0)
-    st = lv.find_pressure(solver, dt, 10, stats=stats)
-    if snapshot:
-        L = lv._lib.load()
-        assert L.lv_learn_add_system(g._ctx) == 0
-    lv.pressure_step(g, dt)
-    lv.find_D(g)
-    lv.viscous_step(g, dt, fl.artificial_viscosity)
-    lv.find_dv(g, dt)
-    lv.relaxation_step(g, dt)
+    """The reference's step! of the flow (tests/workloads.py:step_sequence),
+    through the package's public API; returns the per-sweep solver stats
+    when stats=True (which synchronises)."""
+    import workloads as W
+    dt, seq = W.step_sequence(fl)
+    st = None
+    for op, kw in seq:
+        if op == "move":
+            lv.move(g, dt)
+        elif op == "gravity_step":
+            lv.gravity_step(g, kw["g"], dt)
+        elif op == "stiffened_eos":
+            lv.stiffened_eos(g, kw["gamma"], kw["P0"])
+        elif op == "ideal_eos":
+            lv.ideal_eos(g, kw["gamma"])
+        elif op == "find_pressure":
+            # the examples call find_pressure!(solver, dt) with zero_vbc
+            st = lv.find_pressure(solver, dt, 10, stats=stats)
+            if snapshot:
+                assert lv._lib.load().lv_learn_add_system(g._ctx) == 0
+        elif op == "pressure_step":
+            lv.pressure_step(g, dt)
+        elif op == "find_D":
+            lv.find_D(g)
+        elif op == "viscous_step":
+            lv.viscous_step(g, dt, kw["artificial_viscosity"])
+        elif op == "bdary_friction":
+            lv.bdary_friction(g, kw["walls"], dt)
+        elif op == "find_dv":
+            lv.find_dv(g, dt)
+        elif op == "multiphase_projection":
+            lv.multiphase_projection(lv.MultiphaseSolver(g))
+        elif op == "relaxation_step":
+            lv.relaxation_step(g, dt)
+        else:
+            raise ValueError(op)
     return st
+
+
+def unconverged(L, g):
+    n = C.c_int64()
+    assert L.lv_solver_unconverged(g._ctx, C.byref(n)) == 0
+    return n.value
 
 
 def solver_comparison(lv, L, g, fl, steps, train_info):
@@ -190,10 +264,13 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
             L.lv_kernel_time(g._ctx, f, None, None, 1)
         s0, i0 = C.c_int64(), C.c_int64()
         L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
+        u0 = unconverged(L, g)
         fallbacks = 0
+        per_sweep = []
         for _ in range(steps):
             st = gpu_step(lv, g, solver, fl, stats=True)
             fallbacks += sum(1 for rec in st if method == "learned_pcg" and rec[3] != 2)
+            per_sweep.append([rec[0] for rec in st])
         s1, i1 = C.c_int64(), C.c_int64()
         L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
         ms = {}
@@ -206,7 +283,9 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
                        "factor_ms_per_step": ms["learn"] / steps,
                        "pcg_kernel_ms_per_step": ms["pcg"] / steps,
                        "cg_iters_per_step": (i1.value - i0.value) / steps,
-                       "us_per_iteration": 1e3 * ms["pcg"] / max(i1.value - i0.value, 1)}
+                       "cg_iters_per_sweep_last_step": per_sweep[-1],
+                       "us_per_iteration": 1e3 * ms["pcg"] / max(i1.value - i0.value, 1),
+                       "unconverged_sweeps": unconverged(L, g) - u0}
         if method == "learned_pcg":
             out[method]["fallbacks_to_jacobi"] = fallbacks
     out["learned_pcg"]["training"] = train_info
@@ -220,23 +299,7 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
     return out
 
 
-def run_ours(args, world, rank, local):
-    import torch
-    torch.cuda.set_device(local)
-    lv = load_package()
-    L = lv._lib.load()
-    fl = flow()
-    g = setup_grid(lv, fl)
-    # warm-up with the Jacobi mixed solver: its iteration count is the
-    # learned solver's fallback reference
-    solver = lv.PressureSolver(g, method="mixed_ir" if args.solver == "learned_pcg" else args.solver, tol=1e-8)
-    stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
-    # warm-up steps also snapshot the pressure operators the learned
-    # preconditioner is trained on (the solver's own systems)
-    for _ in range(args.warmup):
-        gpu_step(lv, g, solver, fl, snapshot=True)
-    g.synchronize()
+def train_learned(L, g, args):
     t_tr = time.perf_counter()
     train_steps = args.train_steps if (args.solver == "learned_pcg" or not args.no_compare) else 0
     losses = np.zeros(max(train_steps, 1), np.float32)
@@ -245,12 +308,34 @@ def run_ours(args, world, rank, local):
     if train_steps:
         assert L.lv_learn_train(g._ctx, train_steps, args.train_lr, args.train_probes, 99,
                                 losses.ctypes.data_as(C.POINTER(C.c_float))) == 0
-    train_info = {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps,
-                  "objective": "fsai-kaporin" if args.train_probes == 0 else f"hutchinson x{args.train_probes}",
-                  "pattern": "lower triangle" if args.learn_hops == 1 else "lower triangle + two-hop",
-                  "lr": args.train_lr,
-                  "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
-                  "loss_last": float(losses[-10:].mean())}
+    return {"systems": int(L.lv_learn_num_systems(g._ctx)), "adam_steps": train_steps,
+            "objective": "fsai-kaporin" if args.train_probes == 0 else f"hutchinson x{args.train_probes}",
+            "pattern": "lower triangle" if args.learn_hops == 1 else "lower triangle + two-hop",
+            "lr": args.train_lr, "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
+            "loss_last": float(losses[-10:].mean())}
+
+
+def run_ours(args, world, rank, local, wl):
+    import torch
+    torch.cuda.set_device(local)
+    lv = load_package()
+    L = lv._lib.load()
+    fl = wl.flow
+    N = wl.n
+    g = setup_grid(lv, wl)
+    # warm-up with the Jacobi mixed solver: its iteration count is the
+    # learned solver's fallback reference
+    solver = lv.PressureSolver(g, method="mixed_ir" if args.solver == "learned_pcg" else args.solver, tol=1e-8)
+    stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
+    # between timed steps an L2 flush when the state fits in L2
+    flush_l2 = N * STATE_BYTES_PER_PARTICLE < 4 * L2_BYTES
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}") if flush_l2 else None
+    # warm-up steps also snapshot the pressure operators the learned
+    # preconditioner is trained on (the solver's own systems)
+    for _ in range(args.warmup):
+        gpu_step(lv, g, solver, fl, snapshot=True)
+    g.synchronize()
+    train_info = train_learned(L, g, args)
 
     solver = lv.PressureSolver(g, method=args.solver, tol=1e-8)
     # the state the passes start from: each pass restores it, forgets the
@@ -265,30 +350,37 @@ def run_ours(args, world, rank, local):
         gpu_step(lv, g, solver, fl)
         g.synchronize()
 
+    def between_steps(ev0):
+        with torch.cuda.stream(stream):
+            if flush is not None:
+                flush.zero_()
+            ev0.record(stream)
+
     restore()
 
-    # ---- timed region: K steps, device time from events on the library's stream,
-    # an L2 flush (512 MiB write) between steps outside the events; no per-family
-    # instrumentation inside it
+    # ---- timed region: K steps, device time from events on the library's stream
+    # (an L2 flush between steps outside the events when the state fits in L2);
+    # no per-family instrumentation inside it
     fam = lv._lib.KERNEL_FAMILIES
     s0, i0 = C.c_int64(), C.c_int64()
     L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
+    u0 = unconverged(L, g)
     launches0 = g.launch_count()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(local).start()
     barrier(world)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                ev[k][0].record(stream)
-            gpu_step(lv, g, solver, fl)
-            with torch.cuda.stream(stream):
-                ev[k][1].record(stream)
-        g.synchronize()
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        between_steps(ev[k][0])
+        gpu_step(lv, g, solver, fl)
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+    g.synchronize()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    wall = t1 - t0
+    clk.stop()
     barrier(world)
     launches = g.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -296,6 +388,9 @@ def run_ours(args, world, rank, local):
     s1, i1 = C.c_int64(), C.c_int64()
     L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
     solves, iters = s1.value - s0.value, i1.value - i0.value
+    n_unconverged = unconverged(L, g) - u0
+    if n_unconverged:
+        raise RuntimeError(f"{n_unconverged} of {solves} timed pressure sweeps did not reach the 1e-8 residual")
     max_ms = allmax(world, dev_ms)
     # ---- the same number of steps again with every kernel family bracketed by
     # CUDA events (lv_kernel_timing): the per-family device times and the
@@ -307,9 +402,7 @@ def run_ours(args, world, rank, local):
     L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
     ev_i = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-            ev_i[k][0].record(stream)
+        between_steps(ev_i[k][0])
         gpu_step(lv, g, solver, fl)
         with torch.cuda.stream(stream):
             ev_i[k][1].record(stream)
@@ -339,6 +432,7 @@ def run_ours(args, world, rank, local):
     h2d = sum(bufs[0][k].nbytes for k in in_names)
     d2h = sum(bufs[0][k].nbytes for k in out_names)
     e2e_steps = max(1, args.steps)
+    u0 = unconverged(L, g)
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -349,6 +443,9 @@ def run_ours(args, world, rank, local):
         g.get_many(out_names, out=[dst[n_] for n_ in out_names])
     g.synchronize()
     e2e_s = allmax(world, time.perf_counter() - t0)
+    e2e_unconverged = unconverged(L, g) - u0
+    if e2e_unconverged:
+        raise RuntimeError(f"{e2e_unconverged} end-to-end pressure sweeps did not reach the 1e-8 residual")
 
     comparison = solver_comparison(lv, L, g, fl, 3, train_info) if not args.no_compare else None
     if rank != 0:
@@ -356,7 +453,7 @@ def run_ours(args, world, rank, local):
     value = world * N * args.steps / (max_ms / 1e3)
     e2e_value = world * N * e2e_steps / e2e_s
     ms_per_step = max_ms / args.steps
-    clocks = clk.summary()
+    clocks = clk.summary(t0=None)
 
     # ---- roofline of the dominant kernel family
     # interior faces (= off-diagonal nonzeros of the pressure operator)
@@ -367,9 +464,6 @@ def run_ours(args, world, rank, local):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # algorithmic bytes per unit (per particle): FP64 PCG iteration
-    # (8+4)*nnz + 4N + 4*8N + 3*8N with nnz = F + N (diagonal included);
-    # clip + geometry 16N + 28F + 28N
     # per CG iteration, the bytes a streaming implementation moves: FP64
     # Jacobi-PCG 12 B per nonzero (value + column) + 60 B per row (vectors);
     # FP32 inner CG 8 B per nonzero + 28 B per row, and the learned M^-1 about
@@ -380,14 +474,14 @@ def run_ours(args, world, rank, local):
     else:
         per_it = 8 * (F + N) + 28 * N + (80 * N if args.solver == "learned_pcg" else 0)
     pcg_bytes = iters * per_it
-    clip_bytes = kt["clip"][0] * (16 * N + 28 * F + 28 * N)
-    fams = {"pcg": iters_i * per_it, "clip": clip_bytes}  # bytes of the instrumented pass
+    clip_unit = 16 * N + 28 * F + 28 * N  # per remesh: read x; write nbr, lrr, mid; area, centroid, nface
+    fams = {"pcg": iters_i * per_it, "clip": kt["clip"][0] * clip_unit}  # bytes of the instrumented pass
     # compulsory bytes of the whole step (per kernel family, the per-unit
     # counts above): re-bin 32N and clip 16N + 28F + 28N per remesh; CSR
     # assembly 28F + 68N + 12 nnz per find_pressure; RHS 28F + 80N per sweep;
     # the CG iterations; ten other face passes of 28F + 40N
     remeshes = kt["clip"][0]
-    step_bytes = (remeshes * (32 * N + 16 * N + 28 * F + 28 * N)
+    step_bytes = (remeshes * (32 * N + clip_unit)
                   + args.steps * (28 * F + 68 * N + 12 * (F + N))
                   + solves * (28 * F + 80 * N)
                   + pcg_bytes
@@ -401,46 +495,61 @@ def run_ours(args, world, rank, local):
         if args.solver == "jacobi_pcg":
             kname = "k_pcg_reg<2>" if N <= 2 * 128 * 2 * 152 else "k_pcg"
         else:
-            # the learned solve runs the staged instantiation when the per-block
-            # images fit shared memory (they do for these workloads)
             staged = 1 if args.solver == "learned_pcg" else 0
             kname = (f"k_fcg<1,{staged}>" if N <= 152 * 512 else
                      (f"k_fcg<2,{staged}>" if N <= 152 * 1024 else "k_lpcg_str"))
     else:
         kname = "k_clip"
-    traffic = read_traffic(WORKLOAD, dom, kname)
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": read_traffic(wl.label, dom, kname),
+                "peak_source": peak_src, "units_per_launch": N if dom == "clip" else None,
+                "algorithmic_bytes_per_launch": fams[dom] / dom_launches,
+                "launch_ms": dom_ms / dom_launches, "note": ROOFLINE_NOTE.get(kname, "")}
+    if dom == "clip":
+        # the bound that applies: FP64 operations per polygon over the measured
+        # FP64 rate of this part (a microbenchmark: 0.60 T FP64 thread
+        # operations per second)
+        roofline["fp64"] = {"ops_per_polygon": CLIP_FP64_OPS, "peak_ops_per_s": FP64_OPS_PEAK,
+                            "frac": CLIP_FP64_OPS * N / (dom_ms / dom_launches / 1e3) / FP64_OPS_PEAK}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
-        "config": {"workload": WORKLOAD, "particles": N,
-                   "solver": SOLVER_DESC[args.solver] + ", tol 1e-8 (FP64 residual), 10 sweeps/step",
-                   "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": f"replicas x{world}",
-                   "l2": "512 MiB buffer written between timed steps (the 256x256 state, ~15 MB, fits in L2)"},
+        "vs_baseline": None, "dtype": "f64 (fp32 inner CG)" if args.solver != "jacobi_pcg" else "f64",
+        "data": "synthetic (seeded jittered lattice, analytic initial field)",
+        "config": dict(wl.describe(), **{
+            "solver": SOLVER_DESC[args.solver] + ", tol 1e-8 (FP64 residual), 10 sweeps/step",
+            "parallelism": f"replicas x{world}",
+            "l2": ("512 MiB buffer written between timed steps (the state fits in L2)" if flush_l2 else
+                   f"no flush: the state ({N * STATE_BYTES_PER_PARTICLE / 1e9:.2f} GB) is larger than L2")}),
         "pressure": {"solve_ms_per_step": (kt["pcg"][1] + kt["rhs"][1] + kt["learn"][1]) / args.steps,
                      "pcg_ms_per_step": kt["pcg"][1] / args.steps, "cg_iters_per_step": iters / args.steps,
-                     "solves": solves, "solvers": comparison},
+                     "solves": solves, "unconverged_sweeps": n_unconverged,
+                     "e2e_unconverged_sweeps": e2e_unconverged, "solvers": comparison},
         "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kt.items()},
         "instrumented_pass": {"ms_per_step": instr_ms / args.steps, "cg_iters_per_step": iters_i / args.steps},
         "full_step_roofline": {"bytes_per_step": step_bytes / args.steps, "achieved": step_gbs, "peak": hbm_peak,
                                "unit": "GB/s", "frac": step_gbs / hbm_peak},
-        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "peak_source": peak_src, "note": ROOFLINE_NOTE.get(kname, "")},
+        "roofline": roofline,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "wall_s_timed": wall,
+        "host_gap_ms_per_step": (wall * 1e3 - dev_ms) / args.steps,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, sample_steps=2)
+        line["cpu_baseline"] = cpu_baseline(args, wl)
     return line
 
 
+# FP64 thread operations per polygon of k_clip (ncu: dadd + dmul + dfma thread
+# instructions per polygon on a Taylor-Green mesh) and this part's FP64 rate
+CLIP_FP64_OPS = 1109
+FP64_OPS_PEAK = 0.60e12
+
 # what bounds each dominant kernel instead of HBM (from the ncu summaries in profiles/)
 ROOFLINE_NOTE = {
-    "k_clip": "FP64-pipe and FP64-latency bound: sm__pipe_fp64_cycles_active 62% at ~12 warps/SM, 13 of 32 lanes"
-              " active per instruction (profiles/k_clip_taylor_green_1024.md); its compulsory traffic is 212 B per polygon",
+    "k_clip": "FP64-pipe and FP64-latency bound (profiles/k_clip_*.md); its compulsory traffic is 212 B per"
+              " polygon, so its HBM fraction is small by construction: see roofline.fp64",
     "k_fcg<1,1>": "synchronisation-latency bound: a grid-wide reduction and a neighbour exchange per CG iteration"
                   " (profiles/k_fcg_taylor_green_256.md)",
     "k_fcg<1,0>": "synchronisation-latency bound (profiles/k_fcg_taylor_green_256.md)",
@@ -469,19 +578,21 @@ def read_traffic(workload, family, kernel):
 
 # ------------------------------------------------------------ reference arm
 
-def oracle_grid(fl):
+def oracle_grid(wl):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import lvref
     import harness as H
     import workloads as W
     from importlib import util
+    fl = wl.flow
     spec = util.spec_from_file_location("pop_b", os.path.join(ROOT, "lagrangianvoronoi.jl_gb300", "populate.py"))
     pop = util.module_from_spec(spec)
     spec.loader.exec_module(pop)
     lvref.build()
     threads = lvref.set_threads(os.cpu_count() or 1)
     x = H.seeds(pop, fl)
-    og = lvref.OracleGrid(fl.xlims, fl.ylims, fl.dr, len(x), xperiodic=True, yperiodic=True, max_edges=20)
+    og = lvref.OracleGrid(fl.xlims, fl.ylims, fl.dr, len(x), xperiodic=fl.periodic, yperiodic=fl.periodic,
+                          max_edges=20)
     og.set("x", x)
     assert og.remesh() == 0
     for k, v in W.initial_fields(fl, x, og.edges()["area"]).items():
@@ -489,54 +600,71 @@ def oracle_grid(fl):
     return og, threads
 
 
-def oracle_step(og, fl):
-    dt = fl.dt
-    assert og.move(dt) == 0
-    og.stiffened_eos(fl.gamma, fl.P0)
-    og.find_pressure(dt, 10, None, method="minres", tol=1e-6, itmax=1000)
-    og.pressure_step(dt)
-    og.find_D()
-    og.viscous_step(dt, fl.artificial_viscosity)
-    og.find_dv(dt)
-    assert og.relaxation_step(dt) == 0
+def oracle_step(og, wl):
+    """The same step! on the oracle, with the reference's solver settings."""
+    import harness as H
+    import workloads as W
+    fl = wl.flow
+    dt, seq = W.step_sequence(fl)
+    for op, kw in seq:
+        if op == "find_pressure":
+            og.find_pressure(dt, 10, None, method="minres", tol=1e-6, itmax=1000)
+        else:
+            H.apply(None, fl, og, op, kw, False)
 
 
-def cpu_baseline(args, sample_steps=2):
-    fl = flow()
-    og, threads = oracle_grid(fl)
-    oracle_step(og, fl)  # warm-up
+def cpu_baseline(args, wl):
+    """The oracle on the host cores: one warm-up step and one timed step for
+    workloads above 1M particles, else two timed steps."""
+    og, threads = oracle_grid(wl)
+    big = wl.n > 1_000_000
+    if not big:
+        oracle_step(og, wl)  # warm-up
+    sample_steps = 1 if big else 2
     t0 = time.perf_counter()
     for _ in range(sample_steps):
-        oracle_step(og, fl)
+        oracle_step(og, wl)
     dt = time.perf_counter() - t0
-    return {"value": N * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{sample_steps} full steps of {WORKLOAD} after 1 warm-up step, oracle restatement "
-                      f"with the reference's solver (MINRES atol=rtol=1e-6, itmax=1000), OpenMP {threads} threads"}
+    return {"value": wl.n * sample_steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample_steps} full step(s) of {wl.label}" + ("" if big else " after 1 warm-up step") +
+                      f", oracle restatement with the reference's solver (MINRES atol=rtol=1e-6, itmax=1000), "
+                      f"OpenMP {threads} threads"}
 
 
-def run_reference(args, world, rank):
+REF_BUDGET_S = 150.0
+
+
+def run_reference(args, world, rank, wl):
     if rank != 0:
         return None
-    fl = flow()
-    og, threads = oracle_grid(fl)
-    for _ in range(args.warmup):
-        oracle_step(og, fl)
+    og, threads = oracle_grid(wl)
+    # warm-up, then as many of the K steps as fit the time budget (at least one)
+    warm = max(0, min(args.warmup, 1))
+    t_w = None
+    for _ in range(warm):
+        t0 = time.perf_counter()
+        oracle_step(og, wl)
+        t_w = time.perf_counter() - t0
+    steps = args.steps
+    if t_w is not None:
+        steps = max(1, min(args.steps, int(REF_BUDGET_S / max(t_w, 1e-9))))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        oracle_step(og, fl)
+    for _ in range(steps):
+        oracle_step(og, wl)
     dt = time.perf_counter() - t0
-    value = N * args.steps / dt
+    value = wl.n * steps / dt
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered lattice, analytic initial field)",
-        "config": {"workload": WORKLOAD, "particles": N,
-                   "solver": "minres fp64 atol=rtol=1e-6 itmax=1000, 10 sweeps/step (reference settings)",
-                   "eos": "stiffened c0=50", "dt": fl.dt, "parallelism": "host threads"},
+        "config": dict(wl.describe(), **{
+            "solver": "minres fp64 atol=rtol=1e-6 itmax=1000, 10 sweeps/step (reference settings)",
+            "parallelism": "host threads"}),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps; the reference is "
-                                   "Julia and no Julia runtime exists on this machine, so its algorithm runs as "
-                                   "the C++ restatement (oracle/)"},
+                         "sample": f"{steps} of the {args.steps} requested full steps after {warm} warm-up "
+                                   f"step(s) (as many as fit {REF_BUDGET_S:.0f} s); the reference is Julia and no "
+                                   "Julia runtime exists on this machine, so its algorithm runs as the C++ "
+                                   "restatement (oracle/)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -547,9 +675,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="double_shear", choices=sorted(CONFIG_SIZES),
+                    help="flow of the workload (default: the double shear layer, 2048 x 2048)")
+    ap.add_argument("--nx", type=int, default=0, help="lattice columns (0: the workload's size; others for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
-    ap.add_argument("--nx", type=int, default=256, help="lattice side (the workload is 256; others for profiling)")
     ap.add_argument("--solver", default="learned_pcg", choices=["jacobi_pcg", "mixed_ir", "learned_pcg"],
                     help="pressure solver of the timed steps")
     ap.add_argument("--train-steps", type=int, default=400, help="Adam steps of the learned preconditioner")
@@ -558,13 +688,13 @@ def main():
     ap.add_argument("--learn-hops", type=int, default=1, choices=[1, 2],
                     help="pattern of the learned factor: 1 the operator's lower triangle, 2 with two-hop neighbours")
     args = ap.parse_args()
-    set_size(args.nx)
+    wl = Workload(args.config, args.nx or None)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
     if args.impl == "reference":
-        line = run_reference(args, world, rank)
+        line = run_reference(args, world, rank, wl)
     else:
-        line = run_ours(args, world, rank, local)
+        line = run_ours(args, world, rank, local, wl)
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if world > 1:

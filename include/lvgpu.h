@@ -270,6 +270,14 @@ int lv_kernel_time(lv_ctx* ctx, int32_t family, int64_t* launches, double* ms, i
 /* Cumulative pressure-solver counters since creation: linear solves and CG
  * iterations (inner iterations for the mixed-precision solver); synchronises. */
 int lv_solver_counters(lv_ctx* ctx, int64_t* solves, int64_t* iterations);
+/* Cumulative count of linear solves (pressure sweeps, lv_solve) that ended
+ * with a recursive or true residual above tol ||b|| (itmax reached, or a
+ * non-finite residual); synchronises.  lv_find_pressure without stats queues
+ * its sweeps and returns at once, so a caller that does not ask for stats
+ * reads this count (e.g. once after a run of steps) to learn that every
+ * sweep converged.  No counterpart in the reference, whose find_pressure!
+ * leaves Krylov's statistics unread (pressure.jl:219-220). */
+int lv_solver_unconverged(lv_ctx* ctx, int64_t* solves);
 /* Diagnostic of the learned solve for systems that fit one block per SM:
  * the largest halo (rows outside a block that the block's rows reference)
  * over the blocks of the last built factor, or 0 when that solve moves

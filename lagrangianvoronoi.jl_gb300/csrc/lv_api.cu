@@ -866,6 +866,16 @@ int lv_solver_halo(lv_ctx* c, int32_t* max_rows) {
   return LV_OK;
 }
 
+int lv_solver_unconverged(lv_ctx* c, int64_t* solves) {
+  if (!c || !solves) return LV_ERR_BAD_ARGUMENT;
+  long long h[3] = {0, 0, 0};
+  cudaMemcpyAsync(h, c->sv.counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return lv_cuda_check(c, e, "lv_solver_unconverged");
+  *solves = h[2];
+  return LV_OK;
+}
+
 int lv_solver_counters(lv_ctx* c, int64_t* solves, int64_t* iterations) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   long long h[2] = {0, 0};

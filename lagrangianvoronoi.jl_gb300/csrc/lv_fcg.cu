@@ -861,8 +861,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
     a.out_d[0] = rtrue2;
     a.out_d[1] = bnorm2;
     a.out_d[2] = rtrue2;
-    a.counters[0] += 1;
-    a.counters[1] += it;
+    count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
   }
 }
 

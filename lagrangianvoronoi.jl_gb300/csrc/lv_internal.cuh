@@ -104,6 +104,16 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   return a / b;
 }
 
+// Epilogue of every pressure solve (one thread): the cumulative counters
+// [0] solves, [1] iterations and [2] solves whose recursive (rr) or true (tr)
+// residual is not within tol of ||b|| (NaN counts as not converged).
+__device__ __forceinline__ void count_solve(long long* counters, int it, double rr, double bb, double tr,
+                                            double tol2) {
+  counters[0] += 1;
+  counters[1] += it;
+  if (!(rr <= tol2 * bb && tr <= tol2 * bb)) counters[2] += 1;
+}
+
 // The sweep's start P + c0 (P - pprev) + c1 D, rounded operation by
 // operation (no contraction) so that every kernel that forms it agrees.
 __device__ __forceinline__ double sweep_shift(double p, double pv, double d, double c0, double c1) {
@@ -193,7 +203,7 @@ struct SolverDev {
   int dinc_slots;
   float *dinv32, *r32, *z32, *p32, *q32, *d32, *e32, *f32a, *f32b;
   unsigned long long* rtag;  // staged solve: r of every row tagged with its exchange's epoch
-  long long* counters; // [0] solves, [1] CG iterations (device-side, cumulative)
+  long long* counters; // [0] solves, [1] CG iterations, [2] solves that ended above the tolerance (cumulative)
   double* part;       // reduction partials [4][maxblocks]
   unsigned* bar;      // grid barrier {count, generation}
   int* iters;         // device-side stats

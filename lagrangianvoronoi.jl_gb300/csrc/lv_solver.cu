@@ -285,8 +285,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     const double tr = grid_total(a.part, 0, sh);
     if (threadIdx.x == 0) {
       *a.out_iters = it;
-      a.counters[0] += 1;
-      a.counters[1] += it;
+      count_solve(a.counters, it, rr, bb, tr, a.tol2);
       a.out_d[0] = rr;
       a.out_d[1] = bb;
       a.out_d[2] = tr;
@@ -519,8 +518,7 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
     a.out_d[0] = rtrue2;
     a.out_d[1] = bnorm2;
     a.out_d[2] = rtrue2;
-    a.counters[0] += 1;
-    a.counters[1] += it;
+    count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
   }
 }
 
@@ -857,8 +855,7 @@ __global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, St
     a.out_d[0] = rtrue2;
     a.out_d[1] = bnorm2;
     a.out_d[2] = rtrue2;
-    a.counters[0] += 1;
-    a.counters[1] += it;
+    count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
   }
 }
 
@@ -1171,9 +1168,9 @@ extern "C" int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t
   int* nonsingular = reinterpret_cast<int*>(misc + 2);
   int* iters = reinterpret_cast<int*>(misc + 3);
   double* outd = misc + 4;                                     // rr, bb, true rr
-  long long* counters = reinterpret_cast<long long*>(misc + 8);
+  long long* counters = reinterpret_cast<long long*>(misc + 8);  // 3 words
   // what must start at zero: barrier, status, flag, counters
-  if (cudaMemsetAsync(misc, 0, sizeof(double) * 10, s) != cudaSuccess) return LV_ERR_CUDA;
+  if (cudaMemsetAsync(misc, 0, sizeof(double) * 11, s) != cudaSuccess) return LV_ERR_CUDA;
   k_noalloc_diag<<<lv_blocks(n, TPB), TPB, 0, s>>>(n, diag, rowptr, w, adiag, dinv, nonsingular);
   if (cudaGetLastError() != cudaSuccess) return LV_ERR_CUDA;
   int sms = 0, per_sm = 0;

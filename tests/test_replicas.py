@@ -30,7 +30,7 @@ def _worker(rank, world, port, q):
     # the reference arm does its work on rank 0 only
     class A:
         steps, warmup = 1, 0
-    out = bench.run_reference(A, w, r) if r != 0 else "skipped"
+    out = bench.run_reference(A, w, r, bench.Workload("gresho", 16)) if r != 0 else "skipped"
     import torch.distributed as dist
     dist.destroy_process_group()
     q.put((rank, m, out))
