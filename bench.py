@@ -497,7 +497,7 @@ def run_ours(args, world, rank, local, wl):
         else:
             staged = 1 if args.solver == "learned_pcg" else 0
             kname = (f"k_fcg<1,{staged}>" if N <= 152 * 512 else
-                     (f"k_fcg<2,{staged}>" if N <= 152 * 1024 else "k_lpcg_str"))
+                     (f"k_fcg<2,{staged}>" if N <= 152 * 1024 else f"k_big<{'true' if staged else 'false'}>"))
     else:
         kname = "k_clip"
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

@@ -98,7 +98,7 @@ int sync_status(lv_ctx* c) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return lv_cuda_check(c, e, "stream synchronize");
   int flags = *c->status_host;
-  if (flags & LV_FLAG_BARRIER_TIMEOUT) c->fcg_reset = true;  // a solver launch stopped part-way
+  if (flags & LV_FLAG_BARRIER_TIMEOUT) c->fcg_reset = c->big_reset = true;  // a solver launch stopped part-way
   if (flags) {
     cudaMemsetAsync(c->status, 0, sizeof(int), c->stream);
     int code = decode_status(flags);

@@ -17,6 +17,7 @@
 // exchanges (nexchange: per-block flags, each block waits only for the blocks
 // whose rows it reads).  A Jacobi iteration costs one exchange and one phase,
 // a learned one two exchanges and one phase.
+#include <algorithm>
 #include <cstddef>
 #include <cstdlib>
 
@@ -25,7 +26,6 @@
 namespace {
 
 constexpr int FCG_TPB = 512;
-constexpr int FCG_NW = FCG_TPB / 32;
 constexpr int FKR = 8;    // operator entries per row held in registers
 constexpr int FKM = 12;   // preconditioner off-diagonal entries per row held in registers
 constexpr int MMAX = 96;  // preconditioner off-diagonal entries per row (storage slots)
@@ -176,7 +176,8 @@ __device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
 __shared__ unsigned s_base[2];
 
 // thread 0: arrive and wait for phase ph; returns 0 on timeout
-__device__ __forceinline__ int arrive_wait(const FcgArgs& a, unsigned ph) {
+template <class Args>
+__device__ __forceinline__ int arrive_wait(const Args& a, unsigned ph) {
   red_release_add(a.counter, 1u);
   const unsigned target = s_base[0] + ph * (unsigned)a.nb;
   const long long t0 = clock64();
@@ -217,8 +218,8 @@ struct Words<double> {
   }
 };
 
-template <int NV, typename T>
-__device__ bool fphase(const FcgArgs& a, unsigned ph, const T (&v)[NV], T (&tot)[NV]) {
+template <int NV, typename T, class Args>
+__device__ bool fphase(const Args& a, unsigned ph, const T (&v)[NV], T (&tot)[NV]) {
   constexpr int NWD = NV * Words<T>::N;
   static_assert(NWD <= RG_WORDS, "at most four words per block");
   __shared__ T shw[NV * 32];
@@ -236,7 +237,8 @@ __device__ bool fphase(const FcgArgs& a, unsigned ph, const T (&v)[NV], T (&tot)
   if (wid == 0) {
     unsigned wd[NWD];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) Words<T>::put(allsum(lane < FCG_NW ? shw[k * 32 + lane] : T(0)), wd + k * Words<T>::N);
+    for (int k = 0; k < NV; ++k)
+      Words<T>::put(allsum(lane < (int)(blockDim.x >> 5) ? shw[k * 32 + lane] : T(0)), wd + k * Words<T>::N);
     if (lane == 0) {
 #pragma unroll
       for (int q = 0; q < NWD; ++q) __stcg(words + (size_t)q * a.nb + blockIdx.x, wd[q]);
@@ -292,7 +294,8 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
 // Point to point: each block raises its own flag and waits only for its
 // neighbours' flags.  Consecutive exchanges are always separated by a
 // grid-wide phase, so one buffer per exchanged vector suffices.
-__device__ bool nexchange(const FcgArgs& a, unsigned e, const unsigned* mask) {
+template <class Args>
+__device__ bool nexchange(const Args& a, unsigned e, const unsigned* mask) {
   __syncthreads();
   const unsigned ee = s_base[1] + e;
   if (threadIdx.x == 0) st_release_u32(a.flags + (size_t)blockIdx.x * FLAG_STRIDE, ee);
@@ -1218,6 +1221,379 @@ __global__ void __launch_bounds__(128) k_build_minv_reg(int n, const int* __rest
   mdiag[i] = di * (dsum + eps) * di;
 }
 
+// ---------------------------------------------------------------------------
+// Streaming mixed-precision solve for systems beyond the register-resident
+// solver (k_big): the refinement and the single-reduction CG of k_fcg, with
+// the operator read in the mesh's slot-major face layout (column = the face's
+// neighbour m.fnbr[k*cap + i], FP32 and FP64 weights per slot, written by the
+// assembly) and every vector in global memory.  One 1024-thread block per SM;
+// block b owns the contiguous rows [b*rpb, (b+1)*rpb), thread t the rows
+// rb0 + t + k*1024, so every vector pass is coalesced.  Neighbour values move
+// through point-to-point exchanges (a block waits only for the blocks whose
+// rows its rows reference, from a mask built once per operator), dot products
+// through grid-wide phases.  A Jacobi iteration makes two passes over the
+// rows (w = A u with the dots; the vector updates with u = D^-1 r), one
+// exchange and one phase; a learned one a third pass (u = M^-1 r from the
+// explicit slot-major M^-1) and a second exchange.  The FP64 correction
+// x += sigma d of a refinement step is never exchanged: the next residual
+// pass reads x_j + sigma d_j of every neighbour, and the owners fold the
+// correction into x after the phase that ends that pass.
+// ---------------------------------------------------------------------------
+constexpr int BIG_TPB = 1024;
+constexpr int BIG_TPB_L = 640;
+constexpr int BIG_SB = 8;    // slots loaded together (FP32 passes)
+constexpr int BIG_SB64 = 4;  // (FP64 residual)
+constexpr int BIG_MASK_WORDS = FCG_MAX_BLOCKS / 32;
+
+struct BigArgs {
+  int n, nb, rpb, cap;        // cap: slot stride of the face arrays
+  const int* nf;              // faces per row
+  const int* fcol;            // slot-major neighbour index
+  const float* w32e;          // slot-major weights, FP32 and FP64
+  const double* w64e;
+  const float* dg32;          // the reference's diagonal term (FP32)
+  const float* dinv32;        // 1 / (diag + sum_j w_ij) (FP32)
+  const double* diag;
+  const double* b;
+  double* x;
+  double* r64;
+  float *r, *u, *w, *p, *s, *d;
+  const int* mcnt;            // learned M^-1: off-diagonal count, slot-major entries, diagonal
+  const int* mcol;
+  const float* mval;
+  const float* mdiag;
+  int mstride;
+  const int* minv_ok;
+  int learned;
+  const unsigned* masks;      // [nb][BIG_MASK_WORDS] blocks whose rows a block references
+  unsigned long long* slots;  // partial words [2 parities][RG_WORDS][nb]
+  unsigned* counter;
+  unsigned* sync_base;
+  unsigned* flags;
+  int* status;
+  double tol2;
+  int itmax;
+  const int* nonsingular;
+  int sg_mode;                // as FcgArgs
+  double* pprev;
+  double* bprev;
+  const float* sgD;
+  float* sgstore;
+  const double* sgcoef;
+  int* jref;
+  int* out_iters;
+  int* out_outer;
+  int* out_method;
+  double* out_d;
+  long long* counters;
+};
+
+// Blocks whose rows the operator's (and with M^-1 also M^-1's) rows of each
+// block reference: one block per solve block, bit j of mask[b] for block j.
+__global__ void __launch_bounds__(BIG_TPB) k_big_masks(int n, int rpb, int cap, const int* __restrict__ nf,
+                                                       const int* __restrict__ fcol, const int* __restrict__ mcnt,
+                                                       const int* __restrict__ mcol, int mstride,
+                                                       unsigned* masks) {
+  __shared__ unsigned sm[BIG_MASK_WORDS];
+  for (int t = threadIdx.x; t < BIG_MASK_WORDS; t += blockDim.x) sm[t] = 0u;
+  __syncthreads();
+  const int me = blockIdx.x;
+  const int rb0 = me * rpb, rb1 = min(n, rb0 + rpb);
+  auto mark = [&](int j) {
+    const int bj = j / rpb;
+    if (bj != me) atomicOr(&sm[bj >> 5], 1u << (bj & 31));
+  };
+  for (int i = rb0 + (int)threadIdx.x; i < rb1; i += blockDim.x) {
+    const int m = nf[i];
+    for (int k = 0; k < m; ++k) mark(fcol[(size_t)k * cap + i]);
+    if (mcnt) {
+      const int q = mcnt[i];
+      for (int k = 0; k < q; ++k) mark(mcol[(size_t)k * mstride + i]);
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < BIG_MASK_WORDS; t += blockDim.x) masks[(size_t)me * BIG_MASK_WORDS + t] = sm[t];
+}
+
+// Row i's FP32 difference-form product dg_i v_i + sum_k w_k (v_i - v_j).
+// The face count and the first BIG_SB slots (columns and weights) are loaded
+// together: slots below LV_MAX_EDGES lie inside the arrays whatever the row's
+// count, and a slot past it (a stale value) only selects the row itself and
+// is not added.  Then the gathers of the neighbours' values.
+__device__ __forceinline__ float big_row32(const BigArgs& a, int i, float vi, const float* __restrict__ v) {
+  const int nfi = ld_nc(a.nf + i);
+  int jj[BIG_SB];
+  float wv[BIG_SB], xv[BIG_SB];
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q) {
+    jj[q] = ld_nc(a.fcol + (size_t)q * a.cap + i);
+    wv[q] = ld_nc(a.w32e + (size_t)q * a.cap + i);
+  }
+  float acc = ld_nc(a.dg32 + i) * vi;
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q) xv[q] = __ldcg(v + (q < nfi ? jj[q] : i));
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q)
+    if (q < nfi) acc = fmaf(wv[q], vi - xv[q], acc);
+  for (int k = BIG_SB; k < nfi; ++k) {
+    const size_t e = (size_t)k * a.cap + i;
+    acc = fmaf(ld_nc(a.w32e + e), vi - __ldcg(v + ld_nc(a.fcol + e)), acc);
+  }
+  return acc;
+}
+
+// Row i's FP64 residual b_i - (diag_i x_i + sum_k w_k (x_i - x_j)), the slots
+// in the same order (the columns of the first BIG_SB slots loaded with the
+// face count, the weights and gathers BIG_SB64 at a time).
+__device__ __forceinline__ double big_res64(const BigArgs& a, int i, double bi) {
+  const int nfi = ld_nc(a.nf + i);
+  int jj[BIG_SB];
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q) jj[q] = ld_nc(a.fcol + (size_t)q * a.cap + i);
+  const double xi = __ldcg(a.x + i);
+  double acc = ld_nc(a.diag + i) * xi;
+#pragma unroll
+  for (int h = 0; h < BIG_SB; h += BIG_SB64) {
+    if (h >= nfi) break;
+    double wv[BIG_SB64], xv[BIG_SB64];
+#pragma unroll
+    for (int q = 0; q < BIG_SB64; ++q) {
+      wv[q] = ld_nc(a.w64e + (size_t)(h + q) * a.cap + i);
+      xv[q] = __ldcg(a.x + (h + q < nfi ? jj[h + q] : i));
+    }
+#pragma unroll
+    for (int q = 0; q < BIG_SB64; ++q)
+      if (h + q < nfi) acc += wv[q] * (xi - xv[q]);
+  }
+  for (int k = BIG_SB; k < nfi; ++k) {
+    const size_t e = (size_t)k * a.cap + i;
+    acc += ld_nc(a.w64e + e) * (xi - __ldcg(a.x + ld_nc(a.fcol + e)));
+  }
+  return bi - acc;
+}
+
+// Row i of u = M^-1 r: md_i r_i + the row's slots in order (the count and
+// two chunks of BIG_SB slots loaded ahead: M^-1 has MMAX slots per row).
+__device__ __forceinline__ float big_mrow(const BigArgs& a, int i, const float* __restrict__ r) {
+  const int mc = ld_nc(a.mcnt + i);
+  int j0[BIG_SB], j1[BIG_SB];
+  float v0[BIG_SB], v1[BIG_SB], r0[BIG_SB], r1[BIG_SB];
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q) {
+    j0[q] = ld_nc(a.mcol + (size_t)q * a.mstride + i);
+    v0[q] = ld_nc(a.mval + (size_t)q * a.mstride + i);
+  }
+  float acc = ld_nc(a.mdiag + i) * __ldcg(r + i);
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q) r0[q] = __ldcg(r + (q < mc ? j0[q] : i));
+  if (mc > BIG_SB) {
+#pragma unroll
+    for (int q = 0; q < BIG_SB; ++q) {
+      j1[q] = ld_nc(a.mcol + (size_t)(BIG_SB + q) * a.mstride + i);
+      v1[q] = ld_nc(a.mval + (size_t)(BIG_SB + q) * a.mstride + i);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < BIG_SB; ++q)
+    if (q < mc) acc = fmaf(v0[q], r0[q], acc);
+  if (mc > BIG_SB) {
+#pragma unroll
+    for (int q = 0; q < BIG_SB; ++q) r1[q] = __ldcg(r + (BIG_SB + q < mc ? j1[q] : i));
+#pragma unroll
+    for (int q = 0; q < BIG_SB; ++q)
+      if (BIG_SB + q < mc) acc = fmaf(v1[q], r1[q], acc);
+    for (int k = 2 * BIG_SB; k < mc; ++k) {
+      const size_t e = (size_t)k * a.mstride + i;
+      acc = fmaf(ld_nc(a.mval + e), __ldcg(r + ld_nc(a.mcol + e)), acc);
+    }
+  }
+  return acc;
+}
+
+// (the learned instantiation runs 640 threads a block: its M^-1 rows keep two
+// chunks of slots in flight, which needs more than 64 registers a thread)
+template <bool LEARNED>
+__global__ void __launch_bounds__(LEARNED ? BIG_TPB_L : BIG_TPB, 1) k_big(BigArgs a) {
+  constexpr int TPB = LEARNED ? BIG_TPB_L : BIG_TPB;
+  const int n = a.n;
+  const int rb0 = blockIdx.x * a.rpb;
+  const int rb1 = min(n, rb0 + a.rpb);
+  const int t = threadIdx.x;
+  float* __restrict__ vr = a.r;
+  float* __restrict__ vu = a.u;
+  float* __restrict__ vw = a.w;
+  float* __restrict__ vp = a.p;
+  float* __restrict__ vs = a.s;
+  float* __restrict__ vd = a.d;
+  __shared__ unsigned s_mask[BIG_MASK_WORDS];
+  if (t == 0) {
+    s_base[0] = __ldcg(a.sync_base);
+    s_base[1] = __ldcg(a.sync_base + 1);
+  }
+  for (int q = t; q < BIG_MASK_WORDS; q += TPB) s_mask[q] = __ldcg(a.masks + (size_t)blockIdx.x * BIG_MASK_WORDS + q);
+  __syncthreads();
+  const bool learned0 = LEARNED && a.learned != 0 && *a.minv_ok != 0;
+  unsigned ep = 0, xe = 0;
+  bool ok = true;
+  double bmean = 0.0;
+  if (*a.nonsingular == 0) {
+    // singular operator: b projected to zero mean
+    double v[1] = {0.0}, tt[1];
+    for (int i = rb0 + t; i < rb1; i += TPB) v[0] += a.b[i];
+    ok = fphase<1, double>(a, ++ep, v, tt);
+    __shared__ double s_mean;
+    if (t == 0) s_mean = tt[0] / (double)n;
+    __syncthreads();
+    bmean = s_mean;
+  }
+  // the sweep's start (own rows): P and b kept for the next sweep, the last
+  // sweep's change stored, and with a shift P moved to the Galerkin start;
+  // the neighbours see the shifted P after the exchange
+  if (ok && a.sg_mode) {
+    const double c0 = a.sg_mode == 2 ? a.sgcoef[0] : 0.0, c1 = a.sg_mode == 2 ? a.sgcoef[1] : 0.0;
+    for (int i = rb0 + t; i < rb1; i += TPB) {
+      const double p0 = a.x[i], pv = a.pprev[i];
+      if (a.sgstore) a.sgstore[i] = (float)(p0 - pv);
+      a.pprev[i] = p0;
+      a.bprev[i] = a.b[i];
+      if (a.sg_mode == 2) a.x[i] = sweep_shift(p0, pv, a.sgD ? (double)a.sgD[i] : 0.0, c0, c1);
+    }
+    if (a.sg_mode == 2) ok = nexchange(a, ++xe, s_mask);
+  }
+  const int jref = *a.jref;
+  const int capit = jref > 0 ? jref : a.itmax;
+  bool learned = learned0;
+  int it = 0, updates = 0;
+  double bnorm2 = 0.0, rtrue2 = 0.0;
+  float gam_old = 1.f, alpha = 1.f;
+  bool fall = false;
+  // u = M^-1 r from the exchanged r
+  auto mpass = [&]() {
+    for (int i = rb0 + t; i < rb1; i += TPB) vu[i] = big_mrow(a, i, vr);
+  };
+  while (ok) {
+    // ---- FP64 residual b - A x (difference form)
+    double v2[2] = {0.0, 0.0}, t2[2];
+    for (int i = rb0 + t; i < rb1; i += TPB) {
+      const double bi = a.b[i] - bmean;
+      const double ri = big_res64(a, i, bi);
+      a.r64[i] = ri;
+      v2[0] += ri * ri;
+      v2[1] += bi * bi;
+    }
+    if (!(ok = fphase<2, double>(a, ++ep, v2, t2))) break;
+    rtrue2 = t2[0];
+    bnorm2 = t2[1];
+    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax || updates >= FCG_MAX_UPDATES) break;
+    __shared__ double s_sig[2];
+    __shared__ float s_rho_upd;
+    if (t == 0) {
+      const double sg = sqrt(rtrue2);
+      s_sig[0] = sg;
+      s_sig[1] = 1.0 / sg;
+      s_rho_upd = fmaxf(FCG_UPDATE_DROP * FCG_UPDATE_DROP, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
+    }
+    __syncthreads();
+    const double sigma = s_sig[0], inv_sigma = s_sig[1];
+    const float rho_upd = s_rho_upd;
+    ++updates;
+    if (fall) {
+      learned = false;
+      fall = false;
+    }
+    // restart: r = r64 / sigma, u = M^-1 r
+    for (int i = rb0 + t; i < rb1; i += TPB) {
+      const float ri = (float)(a.r64[i] * inv_sigma);
+      vr[i] = ri;
+      if (!learned) vu[i] = a.dinv32[i] * ri;
+    }
+    if (learned) {
+      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+      mpass();
+    }
+    bool first = true;  // p, s, d start from zero (never read)
+    while (true) {
+      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+      // w = A u (FP32 difference form) with the dots (r,u), (w,u), (r,r)
+      float v3[3] = {0.f, 0.f, 0.f}, t3[3];
+      for (int i = rb0 + t; i < rb1; i += TPB) {
+        const float ui = __ldcg(vu + i), ri = __ldcg(vr + i);
+        const float acc = big_row32(a, i, ui, vu);
+        vw[i] = acc;
+        v3[0] = fmaf(ri, ui, v3[0]);
+        v3[1] = fmaf(acc, ui, v3[1]);
+        v3[2] = fmaf(ri, ri, v3[2]);
+      }
+      if (!(ok = fphase<3, float>(a, ++ep, v3, t3))) break;
+      const float gam = t3[0], delta = t3[1], rho = t3[2];
+      if (rho <= rho_upd || it >= a.itmax || !(delta > 0.f)) break;
+      if (learned && it >= capit) {
+        fall = true;
+        break;
+      }
+      const float beta = first ? 0.f : gam / gam_old;
+      alpha = first ? gam / delta : gam / (delta - beta * gam / alpha);
+      // two rows per round, every load issued before the stores
+      for (int i = rb0 + t; i < rb1; i += 2 * TPB) {
+        const int i2 = i + TPB;
+        const bool on2 = i2 < rb1;
+        const int k2 = on2 ? i2 : i;
+        float ui[2], wi[2], pi[2], si[2], di[2], ri[2], dv[2];
+        ui[0] = __ldcg(vu + i), ui[1] = __ldcg(vu + k2);
+        wi[0] = __ldcg(vw + i), wi[1] = __ldcg(vw + k2);
+        ri[0] = __ldcg(vr + i), ri[1] = __ldcg(vr + k2);
+        if (!first) {
+          pi[0] = __ldcg(vp + i), pi[1] = __ldcg(vp + k2);
+          si[0] = __ldcg(vs + i), si[1] = __ldcg(vs + k2);
+          di[0] = __ldcg(vd + i), di[1] = __ldcg(vd + k2);
+        }
+        if (!learned) dv[0] = a.dinv32[i], dv[1] = a.dinv32[k2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          pi[h] = first ? ui[h] : fmaf(beta, pi[h], ui[h]);
+          si[h] = first ? wi[h] : fmaf(beta, si[h], wi[h]);
+          di[h] = first ? alpha * pi[h] : fmaf(alpha, pi[h], di[h]);
+          ri[h] = fmaf(-alpha, si[h], ri[h]);
+        }
+        vp[i] = pi[0], vs[i] = si[0], vd[i] = di[0], vr[i] = ri[0];
+        if (!learned) vu[i] = dv[0] * ri[0];
+        if (on2) {
+          vp[i2] = pi[1], vs[i2] = si[1], vd[i2] = di[1], vr[i2] = ri[1];
+          if (!learned) vu[i2] = dv[1] * ri[1];
+        }
+      }
+      gam_old = gam;
+      first = false;
+      ++it;
+      if (learned) {
+        if (!(ok = nexchange(a, ++xe, s_mask))) break;
+        mpass();
+      }
+    }
+    if (!ok) break;
+    // the correction: x += sigma d on the own rows, then the neighbours' x
+    // for the next residual
+    if (!first) {
+      for (int i = rb0 + t; i < rb1; i += TPB) a.x[i] += sigma * (double)__ldcg(vd + i);
+      if (!(ok = nexchange(a, ++xe, s_mask))) break;
+    }
+  }
+  if (ok && blockIdx.x == 0 && t == 0) {
+    a.sync_base[0] = s_base[0] + ep * (unsigned)a.nb;
+    a.sync_base[1] = s_base[1] + xe;
+    *a.out_iters = it;
+    *a.out_outer = updates;
+    *a.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
+    if (!a.learned) *a.jref = it;
+    a.out_d[0] = rtrue2;
+    a.out_d[1] = bnorm2;
+    a.out_d[2] = rtrue2;
+    count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
+  }
+}
+
+int g_big_blocks_per_sm[2] = {-1, -1};
+
 int g_fcg_blocks_per_sm[2] = {-1, -1};
 int g_fcg_halo_blocks_per_sm[2] = {-1, -1};
 
@@ -1272,7 +1648,7 @@ int lv_fcg_capacity(lv_ctx* c) {
 
 static int ensure_minv(lv_ctx* c) {
   SolverDev& sv = c->sv;
-  const int rows = std::min(c->cap, lv_fcg_capacity(c));
+  const int rows = c->cap;
   if (sv.mrows >= rows && sv.mcnt) return LV_OK;
   cudaFree(sv.mcnt);
   cudaFree(sv.mcol);
@@ -1338,8 +1714,8 @@ int lv_fcg_halo_info(lv_ctx* c, int* max_rows) {
 // lv_learn_factor_current).
 int lv_fcg_build_minv(lv_ctx* c) {
   const int n = c->n;
-  if (n > lv_fcg_capacity(c)) return LV_OK;  // the streaming solver applies the factor itself
   if (int rc = ensure_minv(c)) return rc;
+  c->big_masks_valid = false;  // the streaming solver's masks cover M^-1's pattern
   const float *gd, *gl, *dh, *gl2;
   const int *rev, *rowptr2, *col2, *rev2;
   lv_learn_factor_ptrs(c, &gd, &gl, &dh, &rev);
@@ -1376,7 +1752,8 @@ int lv_fcg_build_minv(lv_ctx* c) {
   c->sv.stage_ready = false;
   int nb, R;
   fcg_shape(c, n, &nb, &R);
-  if (c->fcg_halo && stage_fits(c, nb, R) && nb <= std::min(c->num_sms * 2, FCG_MAX_BLOCKS)) {
+  if (n <= lv_fcg_capacity(c) && c->fcg_halo && stage_fits(c, nb, R) &&
+      nb <= std::min(c->num_sms * 2, FCG_MAX_BLOCKS)) {
     // (stage_stat was initialised by the first kernel of the M^-1 build)
     k_stage_build<<<nb, STG_BUILD_TPB, STG_BUILD_SMEM, c->stream>>>(
         n, (n + nb - 1) / nb, c->sv.rowptr, c->sv.col, c->sv.mcnt, c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.dinv,
@@ -1473,6 +1850,147 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   if (e != cudaSuccess) {
     c->fcg_reset = true;
     return lv_cuda_check(c, e, "k_fcg cooperative launch");
+  }
+  return LV_OK;
+}
+
+// ------------------------------------------------------- streaming solver
+
+namespace {
+constexpr int BIG_SLOT_OFF = 64;                                  // u32 words: counter, bases, then partials
+constexpr int BIG_FLAG_OFF = BIG_SLOT_OFF + 2 * RG_WORDS * FCG_MAX_BLOCKS;
+constexpr int BIG_SYNC_WORDS = BIG_FLAG_OFF + FLAG_STRIDE * FCG_MAX_BLOCKS;
+
+template <class T>
+T* big_alloc(lv_ctx* c, size_t count, bool* ok) {
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)) != cudaSuccess) {
+    *ok = false;
+    return nullptr;
+  }
+  c->allocs.push_back(p);  // freed with the context
+  return static_cast<T*>(p);
+}
+
+int big_blocks(lv_ctx* c, bool learned) {
+  int& b = g_big_blocks_per_sm[learned ? 1 : 0];
+  if (b < 0) {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, learned ? (const void*)k_big<true> : (const void*)k_big<false>,
+                                                  learned ? BIG_TPB_L : BIG_TPB, 0);
+    b = v;
+  }
+  return b >= 1 ? std::min(c->num_sms, FCG_MAX_BLOCKS) : 0;
+}
+}  // namespace
+
+int lv_big_prepare(lv_ctx* c) {
+  SolverDev& sv = c->sv;
+  if (sv.ew32) return LV_OK;
+  const size_t cap = (size_t)c->cap;
+  bool ok = true;
+  sv.ew32 = big_alloc<float>(c, (size_t)LV_MAX_EDGES * cap, &ok);
+  sv.ew64 = big_alloc<double>(c, (size_t)LV_MAX_EDGES * cap, &ok);
+  sv.bvec = big_alloc<float>(c, 6 * cap, &ok);
+  sv.br64 = big_alloc<double>(c, cap, &ok);
+  sv.bmasks = big_alloc<unsigned>(c, (size_t)FCG_MAX_BLOCKS * BIG_MASK_WORDS, &ok);
+  sv.bsync = big_alloc<unsigned>(c, BIG_SYNC_WORDS, &ok);
+  if (!ok) {
+    sv.ew32 = nullptr;
+    sv.ew64 = nullptr;
+    return lv_fail(c, LV_ERR_CUDA, "allocation of the streaming solver's buffers failed");
+  }
+  c->big_reset = true;
+  c->big_masks_valid = false;
+  return LV_OK;
+}
+
+// Launches the streaming mixed-precision solve into x (device), stats into
+// the given slot.
+int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
+  const int n = c->n;
+  SolverDev& sv = c->sv;
+  if (!sv.ew32) return lv_fail(c, LV_ERR_NOT_MESHED, "streaming solve of an operator assembled without its buffers");
+  if (learned && !sv.mcnt) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a preconditioner");
+  const int nb = big_blocks(c, learned);
+  if (nb < 1) return lv_fail(c, LV_ERR_CUDA, "the streaming solver does not fit an SM");
+  const int rpb = (n + nb - 1) / nb;
+  if (!c->big_masks_valid || (learned && !c->big_masks_m)) {
+    // the neighbour blocks of every block: the operator's pattern, and M^-1's
+    // for a learned solve (a superset serves a Jacobi solve too)
+    k_big_masks<<<nb, BIG_TPB, 0, c->stream>>>(n, rpb, c->m.cap, c->m.nfaces, c->m.fnbr, learned ? sv.mcnt : nullptr,
+                                               sv.mcol, sv.mrows, sv.bmasks);
+    LV_LAUNCH_CHECK(c, "k_big_masks");
+    c->big_masks_valid = true;
+    c->big_masks_m = learned;
+  }
+  BigArgs a;
+  a.n = n;
+  a.nb = nb;
+  a.rpb = rpb;
+  a.cap = c->m.cap;
+  a.nf = c->m.nfaces;
+  a.fcol = c->m.fnbr;
+  a.w32e = sv.ew32;
+  a.w64e = sv.ew64;
+  a.dg32 = sv.d32;
+  a.dinv32 = sv.dinv32;
+  a.diag = sv.diag;
+  a.b = sv.b;
+  a.x = x;
+  a.r64 = sv.br64;
+  const size_t cap = (size_t)c->cap;
+  a.r = sv.bvec;
+  a.u = sv.bvec + cap;
+  a.w = sv.bvec + 2 * cap;
+  a.p = sv.bvec + 3 * cap;
+  a.s = sv.bvec + 4 * cap;
+  a.d = sv.bvec + 5 * cap;
+  a.mcnt = sv.mcnt;
+  a.mcol = sv.mcol;
+  a.mval = sv.mval;
+  a.mdiag = sv.mdiag;
+  a.mstride = sv.mrows;
+  a.minv_ok = learned ? sv.mok : sv.iters + LV_IT_NONSINGULAR;  // read only in learned mode
+  a.learned = learned ? 1 : 0;
+  a.masks = sv.bmasks;
+  a.counter = sv.bsync;
+  a.sync_base = sv.bsync + 1;
+  a.slots = reinterpret_cast<unsigned long long*>(sv.bsync + BIG_SLOT_OFF);
+  a.flags = sv.bsync + BIG_FLAG_OFF;
+  a.status = c->status;
+  a.tol2 = c->tol * c->tol;
+  a.itmax = c->itmax;
+  a.nonsingular = sv.iters + LV_IT_NONSINGULAR;
+  a.sg_mode = 0;
+  a.pprev = sv.pprev;
+  a.bprev = sv.bprev;
+  a.sgD = nullptr;
+  a.sgstore = nullptr;
+  a.sgcoef = sv.sgomega;
+  if (c->sg_pending && c->sg_P == x) {
+    a.sg_mode = c->sg_shift ? 2 : 1;
+    a.sgD = c->sg_D;
+    a.sgstore = c->sg_store;
+    c->sg_pending = false;
+  }
+  a.jref = sv.iters + LV_IT_JREF + slot;
+  a.out_iters = sv.iters + slot;
+  a.out_outer = sv.iters + LV_IT_OUTER + slot;
+  a.out_method = sv.iters + LV_IT_METHOD + slot;
+  a.out_d = sv.dstats + 3 * slot;
+  a.counters = sv.counters;
+  if (c->big_reset) {
+    cudaMemsetAsync(sv.bsync, 0, sizeof(unsigned) * BIG_SYNC_WORDS, c->stream);
+    c->big_reset = false;
+  }
+  void* args[] = {&a};
+  const void* fn = learned ? (const void*)k_big<true> : (const void*)k_big<false>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(learned ? BIG_TPB_L : BIG_TPB), args, 0, c->stream);
+  c->launches++;
+  if (e != cudaSuccess) {
+    c->big_reset = true;
+    return lv_cuda_check(c, e, "k_big cooperative launch");
   }
   return LV_OK;
 }

@@ -230,6 +230,16 @@ struct SolverDev {
   int *remap = nullptr, *stage_stat = nullptr;
   bool stage_ready = false;
   int stage_max[3] = {0, 0, 0};
+  // streaming solver of large systems (lv_fcg.cu k_big, allocated on first
+  // use): the operator's weights in the slot-major face layout (written by
+  // the assembly while allocated), the FP32 vectors r u w p s d, the FP64
+  // residual, the per-block neighbour masks and the synchronisation words
+  float* ew32 = nullptr;
+  double* ew64 = nullptr;
+  float* bvec = nullptr;
+  double* br64 = nullptr;
+  unsigned* bmasks = nullptr;
+  unsigned* bsync = nullptr;
 };
 
 struct LearnState;  // learned preconditioner (lv_learn.cu)
@@ -270,6 +280,9 @@ struct lv_ctx {
   int sg_n = 0;             // the particle count they belong to
   bool fcg_halo = true;    // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   bool fcg_reset = true;   // clear the flag-reduced solver's counter, flags and bases before its next launch
+  bool big_reset = true;   // the same for the streaming solver's
+  bool big_masks_valid = false;  // its neighbour masks match the operator
+  bool big_masks_m = false;      // and cover M^-1's pattern
   bool flen_valid = false;  // m.flen belongs to the current mesh
   bool ccount_clean = false;  // the cell counts are zero (cleared by the last completed order pass)
   void* clip_resume = nullptr;  // captures of the first clipping pass (cap entries, allocated on first use)
@@ -485,6 +498,9 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned);
 int lv_solver_flush_shift(lv_ctx* c);  // applies a queued sweep start (k_sweep_apply)
 int lv_fcg_halo_info(lv_ctx* c, int* max_rows);
 void lv_fcg_free(lv_ctx* c);
+// streaming solver of systems above lv_fcg_capacity (same methods)
+int lv_big_prepare(lv_ctx* c);  // allocations; called before the assembly of such a system
+int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned);
 
 #define LV_LAUNCH_CHECK(c, what)                                   \
   do {                                                             \

@@ -56,6 +56,10 @@ __global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt
     sv.col[base + k] = j;
     sv.w[base + k] = w;
     sv.w32[base + k] = (float)w;
+    if (sv.ew64) {  // the streaming solver's slot-major copies
+      sv.ew64[f] = w;
+      sv.ew32[f] = (float)w;
+    }
     ad += w;
   }
   const double dinv = 1.0 / ad;
@@ -522,347 +526,8 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
   }
 }
 
-// ---------------------------------------------------------------------------
-// Mixed-precision iterative refinement, register-resident (LV_METHOD_MIXED_IR
-// and LV_METHOD_LEARNED_PCG).
-//
-// Outer loop in FP64: r = b - A x in the reference's difference form (exact
-// on constants), ||r|| checked against tol ||b||.  Inner solve of
-// A d = r / ||r|| by preconditioned CG whose matrix-vector products,
-// preconditioner and vector updates are FP32; its dot products are
-// accumulated in double-float (an unevaluated sum of two floats, ~48-bit
-// significand) from exact float products, and the scalar recurrences are
-// evaluated from those sums; then x += ||r|| d in FP64.  The inner solve
-// stops at a relative reduction MIR_INNER_TOL of its own residual (or once
-// the FP64 target is in reach); the outer loop repeats until the FP64
-// residual meets the tolerance.  (A pipelined single-barrier variant of the
-// FP32 inner CG drifted on the singular operators of incompressible flows,
-// so the inner CG uses the standard recurrences.)
-// ---------------------------------------------------------------------------
-constexpr float MIR_INNER_TOL = 1e-5f;
-constexpr int MIR_MAX_OUTER = 30;
-
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  const float s = a.x + b.x;
-  const float v = s - a.x;
-  float e = (a.x - (s - v)) + (b.x - v);
-  e += a.y + b.y;
-  const float h = s + e;
-  return make_float2(h, e - (h - s));
-}
-
-__device__ __forceinline__ float2 df_prod(float a, float b) {
-  const float p = a * b;
-  return make_float2(p, fmaf(a, b, -p));
-}
-
-__device__ __forceinline__ float2 df_warp_sum(float2 v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    float2 t;
-    t.x = __shfl_down_sync(0xffffffffu, v.x, o);
-    t.y = __shfl_down_sync(0xffffffffu, v.y, o);
-    v = df_add(v, t);
-  }
-  return v;
-}
-
-// Block sums of NV double-float values; result in thread 0.
-template <int NV>
-__device__ void df_block_sums(float2 (&v)[NV], float2* sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    const float2 t = df_warp_sum(v[k]);
-    if (lane == 0) sh[k * 32 + wid] = t;
-  }
-  __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      const float2 t = (lane < (int)(blockDim.x >> 5)) ? sh[k * 32 + lane] : make_float2(0.f, 0.f);
-      v[k] = df_warp_sum(t);
-    }
-  }
-  __syncthreads();
-}
-
-template <int NV>
-__device__ void df_grid_totals(const float2* part, int slot0, float (&tot)[NV]) {
-  __shared__ float s_tot[NV];
-  if (threadIdx.x < 32) {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      float2 t = make_float2(0.f, 0.f);
-      for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) t = df_add(t, part[(slot0 + v) * gridDim.x + b]);
-      t = df_warp_sum(t);
-      if (threadIdx.x == 0) s_tot[v] = t.x + t.y;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int v = 0; v < NV; ++v) tot[v] = s_tot[v];
-  __syncthreads();
-}
-
-// The streaming solver's preconditioner is either Jacobi, z = D^-1 r, or the
-// learned factor,
-//     z = D^-1/2 (Gt^T (Gt r^) + eps r^),   r^ = D^-1/2 r
-// (Gt lower-triangular on the operator's pattern), which needs two neighbour
-// exchanges.  A learned solve whose inner iterations exceed those of the last
-// Jacobi mixed solve (*jref, kept on the device) continues with Jacobi and
-// reports the fallback.
-struct LearnArgs {
-  const float* gd;
-  const float* gl;
-  const float* dh;
-  const int* rev;
-  const int* rowptr2;  // two-hop part of the factor (NULL with the one-hop pattern)
-  const int* col2;
-  const float* gl2;
-  const int* rev2;
-  float eps;
-  float* rhat;  // exchange buffers
-  float* tbuf;
-  float* zbuf;
-  int* jref;      // iterations of the last Jacobi mixed solve
-  int* out_outer;
-  int* out_method;
-  int learned;    // 0: Jacobi preconditioner throughout (LV_METHOD_MIXED_IR)
-};
-
-// ---------------------------------------------------------------------------
-// Streaming variant of the mixed-precision solve for systems too large for
-// the register-resident kernel: the same algorithm (FP64 refinement, FP32
-// inner CG with double-float dots, Jacobi or learned preconditioner), with
-// every vector in global memory and grid-stride loops over the rows.
-// ---------------------------------------------------------------------------
-struct StreamArgs {
-  const float* w32;   // FP32 copy of the off-diagonal weights
-  const float* dg32;  // FP32 diagonal term
-  const float* dinv32;
-  double* r64;        // FP64 residual scratch
-  float *r, *z, *p, *q, *d, *rh, *t;
-};
-
-__device__ __forceinline__ float apply32_row(int i, const int* __restrict__ rowptr, const int* __restrict__ col,
-                                             const float* __restrict__ w32, float dg, const float* __restrict__ v) {
-  const float vi = v[i];
-  float acc = dg * vi;
-  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) acc = fmaf(w32[k], vi - __ldcg(v + col[k]), acc);
-  return acc;
-}
-
-__global__ void __launch_bounds__(CG_TPB) k_lpcg_str(PCGArgs a, LearnArgs la, StreamArgs sa) {
-  __shared__ double sh[4 * 32];
-  __shared__ float2 shf[4 * 32];
-  __shared__ int s_flag[2];
-  const int n = a.n;
-  const int nb = gridDim.x;
-  const int stride = gridDim.x * blockDim.x;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
-  float2* part32 = reinterpret_cast<float2*>(a.part);
-  double bmean = 0.0;
-  if (*a.nonsingular == 0) {
-    double v[1] = {0.0};
-    for (int i = t0; i < n; i += stride) v[0] += a.b[i];
-    block_sums<1>(v, sh);
-    if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
-    if (!grid_barrier(a.bar, a.status)) return;
-    double t[1];
-    grid_totals<1>(a.part, 0, t);
-    bmean = t[0] / (double)n;
-    if (!grid_barrier(a.bar, a.status)) return;
-  }
-  const int jref = *la.jref;
-  const int cap = jref > 0 ? jref : a.itmax;
-  bool learned = la.learned != 0;
-  int it = 0, outer = 0;
-  double bnorm2 = 0.0, rtrue2 = 0.0;
-  // z = M^-1 r (learned mode: two neighbour exchanges)
-  auto precond = [&]() -> bool {
-    if (!learned) {
-      for (int i = t0; i < n; i += stride) sa.z[i] = sa.dinv32[i] * sa.r[i];
-      return true;
-    }
-    for (int i = t0; i < n; i += stride) sa.rh[i] = la.dh[i] * sa.r[i];
-    if (!grid_barrier(a.bar, a.status)) return false;
-    for (int i = t0; i < n; i += stride) {
-      float t = la.gd[i] * sa.rh[i];
-      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
-        const int j = a.col[k];
-        if (j < i) t = fmaf(la.gl[k], __ldcg(sa.rh + j), t);
-      }
-      if (la.rowptr2)
-        for (int e = la.rowptr2[i]; e < la.rowptr2[i + 1]; ++e) {
-          const int j = la.col2[e];
-          if (j < i) t = fmaf(la.gl2[e], __ldcg(sa.rh + j), t);
-        }
-      sa.t[i] = t;
-    }
-    if (!grid_barrier(a.bar, a.status)) return false;
-    for (int i = t0; i < n; i += stride) {
-      float u = la.gd[i] * sa.t[i];
-      for (int k = a.rowptr[i]; k < a.rowptr[i + 1]; ++k) {
-        const int j = a.col[k];
-        if (j > i && la.rev[k] >= 0) u = fmaf(la.gl[la.rev[k]], __ldcg(sa.t + j), u);
-      }
-      if (la.rowptr2)
-        for (int e = la.rowptr2[i]; e < la.rowptr2[i + 1]; ++e) {
-          const int j = la.col2[e];
-          if (j > i && la.rev2[e] >= 0) u = fmaf(la.gl2[la.rev2[e]], __ldcg(sa.t + j), u);
-        }
-      sa.z[i] = la.dh[i] * fmaf(la.eps, sa.rh[i], u);
-    }
-    return true;
-  };
-  for (; outer < MIR_MAX_OUTER; ++outer) {
-    double v[2] = {0.0, 0.0};
-    for (int i = t0; i < n; i += stride) {
-      const double xi = a.x[i];
-      double acc = a.diag[i] * xi;
-      for (int e = a.rowptr[i]; e < a.rowptr[i + 1]; ++e) acc += a.w[e] * (xi - __ldcg(a.x + a.col[e]));
-      const double bi = a.b[i] - bmean;
-      const double ri = bi - acc;
-      sa.r64[i] = ri;
-      v[0] += ri * ri;
-      v[1] += bi * bi;
-    }
-    block_sums<2>(v, sh);
-    if (threadIdx.x == 0) {
-      a.part[0 * nb + blockIdx.x] = v[0];
-      a.part[1 * nb + blockIdx.x] = v[1];
-    }
-    if (!grid_barrier(a.bar, a.status)) return;
-    {
-      double t2[2];
-      grid_totals<2>(a.part, 0, t2);
-      rtrue2 = t2[0];
-      bnorm2 = t2[1];
-    }
-    if (rtrue2 <= a.tol2 * bnorm2 || it >= a.itmax) break;
-    const double sigma = sqrt(rtrue2);
-    const double inv_sigma = 1.0 / sigma;
-    for (int i = t0; i < n; i += stride) {
-      sa.r[i] = (float)(sa.r64[i] * inv_sigma);
-      sa.d[i] = 0.f;
-      sa.p[i] = 0.f;
-      sa.q[i] = 0.f;
-    }
-    const float rho_stop = fmaxf(MIR_INNER_TOL * MIR_INNER_TOL, (float)(0.25 * a.tol2 * bnorm2 / rtrue2));
-    if (!precond()) return;
-    float rz;
-    {
-      float2 v1[1] = {make_float2(0.f, 0.f)};
-      for (int i = t0; i < n; i += stride) v1[0] = df_add(v1[0], df_prod(sa.r[i], sa.z[i]));
-      df_block_sums<1>(v1, shf);
-      if (threadIdx.x == 0) part32[2 * nb + blockIdx.x] = v1[0];
-      if (!grid_barrier(a.bar, a.status)) return;
-      float t1[1];
-      df_grid_totals<1>(part32, 2, t1);
-      rz = t1[0];
-    }
-    float beta = 0.f;
-    while (true) {
-      float2 v1[1] = {make_float2(0.f, 0.f)};
-      for (int i = t0; i < n; i += stride) {
-        const float az = apply32_row(i, a.rowptr, a.col, sa.w32, sa.dg32[i], sa.z);
-        const float pi = fmaf(beta, sa.p[i], sa.z[i]);
-        const float qi = fmaf(beta, sa.q[i], az);
-        sa.p[i] = pi;
-        sa.q[i] = qi;
-        v1[0] = df_add(v1[0], df_prod(pi, qi));
-      }
-      df_block_sums<1>(v1, shf);
-      if (threadIdx.x == 0) part32[3 * nb + blockIdx.x] = v1[0];
-      if (!grid_barrier(a.bar, a.status)) return;
-      float pq[1];
-      df_grid_totals<1>(part32, 3, pq);
-      const float alpha = rz / pq[0];
-      ++it;
-      float rr2, rzn;
-      if (!learned) {
-        float2 v2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        for (int i = t0; i < n; i += stride) {
-          sa.d[i] = fmaf(alpha, sa.p[i], sa.d[i]);
-          const float ri = fmaf(-alpha, sa.q[i], sa.r[i]);
-          const float zi = sa.dinv32[i] * ri;
-          sa.r[i] = ri;
-          sa.z[i] = zi;
-          v2[0] = df_add(v2[0], df_prod(ri, ri));
-          v2[1] = df_add(v2[1], df_prod(ri, zi));
-        }
-        df_block_sums<2>(v2, shf);
-        if (threadIdx.x == 0) {
-          part32[4 * nb + blockIdx.x] = v2[0];
-          part32[5 * nb + blockIdx.x] = v2[1];
-        }
-        if (!grid_barrier(a.bar, a.status)) return;
-        float t2[2];
-        df_grid_totals<2>(part32, 4, t2);
-        rr2 = t2[0];
-        rzn = t2[1];
-      } else {
-        float2 v2[1] = {make_float2(0.f, 0.f)};
-        for (int i = t0; i < n; i += stride) {
-          sa.d[i] = fmaf(alpha, sa.p[i], sa.d[i]);
-          const float ri = fmaf(-alpha, sa.q[i], sa.r[i]);
-          sa.r[i] = ri;
-          v2[0] = df_add(v2[0], df_prod(ri, ri));
-        }
-        df_block_sums<1>(v2, shf);
-        if (threadIdx.x == 0) part32[4 * nb + blockIdx.x] = v2[0];
-        if (!precond()) return;  // its first barrier also publishes the ||r|| partials
-        float t1[1];
-        df_grid_totals<1>(part32, 4, t1);
-        rr2 = t1[0];
-        rzn = 0.f;
-      }
-      if (threadIdx.x == 0) {
-        const int stop = (rr2 <= rho_stop || it >= a.itmax || !(pq[0] > 0.f)) ? 1 : 0;
-        s_flag[0] = stop;
-        s_flag[1] = (learned && it >= cap && !stop) ? 1 : 0;
-      }
-      __syncthreads();
-      const int stop = s_flag[0], fall = s_flag[1];
-      __syncthreads();
-      if (stop) break;
-      if (fall) {
-        learned = false;
-        break;
-      }
-      if (learned) {
-        float2 v3[1] = {make_float2(0.f, 0.f)};
-        for (int i = t0; i < n; i += stride) v3[0] = df_add(v3[0], df_prod(sa.r[i], sa.z[i]));
-        df_block_sums<1>(v3, shf);
-        if (threadIdx.x == 0) part32[5 * nb + blockIdx.x] = v3[0];
-        if (!grid_barrier(a.bar, a.status)) return;
-        float t1[1];
-        df_grid_totals<1>(part32, 5, t1);
-        rzn = t1[0];
-      }
-      beta = rzn / rz;
-      rz = rzn;
-    }
-    for (int i = t0; i < n; i += stride) a.x[i] += sigma * (double)sa.d[i];
-    if (!grid_barrier(a.bar, a.status)) return;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *a.out_iters = it;
-    *la.out_outer = outer;
-    *la.out_method = learned ? LV_METHOD_LEARNED_PCG : LV_METHOD_MIXED_IR;
-    if (!la.learned) *la.jref = it;
-    a.out_d[0] = rtrue2;
-    a.out_d[1] = bnorm2;
-    a.out_d[2] = rtrue2;
-    count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
-  }
-}
-
-
 int g_pcg_blocks_per_sm = -1;
 int g_reg_blocks_per_sm[2] = {-1, -1};
-int g_str_blocks_per_sm = -1;
 
 }  // namespace
 
@@ -870,6 +535,9 @@ int lv_solver_assemble(lv_ctx* c, double dt) {
   if (!c->meshed) return lv_fail(c, LV_ERR_NOT_MESHED, "the grid has not been meshed");
   const int n = c->n;
   cudaStream_t s = c->stream;
+  if (n > lv_fcg_capacity(c))
+    if (int rc = lv_big_prepare(c)) return rc;
+  c->big_masks_valid = false;
   KernelTimer kt(c, LV_KF_RHS);
   int rc = lv_scan_int(c, c->m.nfaces, c->sv.rowptr, n);
   if (rc) return rc;
@@ -992,8 +660,8 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     if (int rc = lv_fcg_build_minv(c)) return rc;
     c->factor_valid = true;
   }
-  // a queued sweep start of x: the flag-reduced solver applies it itself
-  const bool fcg_path = c->method != LV_METHOD_JACOBI_PCG && n <= lv_fcg_capacity(c);
+  // a queued sweep start of x: the mixed-precision solvers apply it themselves
+  const bool fcg_path = c->method != LV_METHOD_JACOBI_PCG;
   if (c->sg_pending && (!fcg_path || c->sg_P != x)) {
     KernelTimer ks(c, LV_KF_RHS);
     if (int rc = lv_solver_flush_shift(c)) return rc;
@@ -1003,50 +671,8 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     const bool learned = c->method == LV_METHOD_LEARNED_PCG;
     // systems that fit one or two blocks per SM: flag-reduced solver
     if (n <= lv_fcg_capacity(c)) return lv_fcg_solve(c, x, slot, learned);  // applies a queued start of x itself
-    // the grid barriers of the cooperative solvers below start from zero
-    cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
     // larger systems: the streaming variant
-    {
-      LearnArgs la;
-      if (learned) {
-        lv_learn_factor_ptrs(c, &la.gd, &la.gl, &la.dh, &la.rev);
-        lv_learn_factor2_ptrs(c, &la.rowptr2, &la.col2, &la.gl2, &la.rev2);
-        if (!la.gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
-      } else {
-        la.gd = la.gl = la.dh = la.gl2 = nullptr;
-        la.rev = la.rowptr2 = la.col2 = la.rev2 = nullptr;
-      }
-      la.eps = c->learn_eps;
-      la.rhat = la.tbuf = la.zbuf = nullptr;
-      la.jref = c->sv.iters + LV_IT_JREF + slot;
-      la.out_outer = c->sv.iters + LV_IT_OUTER + slot;
-      la.out_method = c->sv.iters + LV_IT_METHOD + slot;
-      la.learned = learned ? 1 : 0;
-      StreamArgs sa;  // the FP32 copies were made when the operator was assembled
-      sa.w32 = c->sv.w32;
-      sa.dg32 = c->sv.d32;
-      sa.dinv32 = c->sv.dinv32;
-      sa.r64 = c->sv.r;
-      sa.r = c->sv.r32;
-      sa.z = c->sv.z32;
-      sa.p = c->sv.p32;
-      sa.q = c->sv.q32;
-      sa.d = c->sv.e32;
-      sa.rh = c->sv.f32a;
-      sa.t = c->sv.f32b;
-      if (g_str_blocks_per_sm < 0) {
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_lpcg_str, CG_TPB, 0);
-        g_str_blocks_per_sm = b > 0 ? b : 1;
-      }
-      const int nbs = std::max(1, std::min(c->num_sms * std::min(g_str_blocks_per_sm, 4), lv_blocks(n, CG_TPB)));
-      void* sargs[] = {&a, &la, &sa};
-      cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_lpcg_str, dim3(nbs), dim3(CG_TPB), sargs, 0,
-                                                  c->stream);
-      c->launches++;
-      if (e != cudaSuccess) return lv_cuda_check(c, e, "k_lpcg_str cooperative launch");
-      return LV_OK;
-    }
+    return lv_big_solve(c, x, slot, learned);
   }
   cudaMemsetAsync(c->sv.bar, 0, 2 * sizeof(unsigned), c->stream);
   // small systems: register-resident pipelined CG, one barrier per iteration
