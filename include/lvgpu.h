@@ -163,7 +163,9 @@ int lv_pressure_rhs(lv_ctx* ctx, double dt, int32_t gp_step, const double* vbc);
  * arrays only *nnz is returned. */
 int lv_export_system(lv_ctx* ctx, int64_t* nnz, double* diag, int64_t* rowptr, int32_t* col, double* w, double* b);
 /* Solve A x = b on the current operator with the current method; b and x are
- * host arrays of n doubles, x holds the initial guess on entry. */
+ * host arrays of n doubles, x holds the initial guess on entry.  Returns
+ * LV_ERR_CG_MAXITER when the solve stopped above the tolerance (x then holds
+ * the last iterate). */
 int lv_solve(lv_ctx* ctx, const double* b, double* x, lv_solve_stats* stats);
 /* y = A x on the current operator (host arrays). */
 int lv_operator_apply(lv_ctx* ctx, const double* x, double* y);
@@ -270,6 +272,14 @@ int lv_kernel_time(lv_ctx* ctx, int32_t family, int64_t* launches, double* ms, i
 /* Cumulative pressure-solver counters since creation: linear solves and CG
  * iterations (inner iterations for the mixed-precision solver); synchronises. */
 int lv_solver_counters(lv_ctx* ctx, int64_t* solves, int64_t* iterations);
+/* The persistent solvers wait on one another's blocks (grid phases,
+ * neighbour exchanges); every such wait gives up after `cycles` GPU clock
+ * cycles (<= 0 restores the default, about 2 s), and the call then reports
+ * LV_ERR_BARRIER_TIMEOUT, leaving the context usable: the next solve clears
+ * the solvers' synchronisation words, and the sweep guess forgets its
+ * history.  No counterpart in the reference (its threads never wait on a
+ * GPU); a test lowers the limit to make a wait run out. */
+int lv_set_wait_limit(lv_ctx* ctx, int64_t cycles);
 /* Cumulative count of linear solves (pressure sweeps, lv_solve) that ended
  * with a recursive or true residual above tol ||b|| (itmax reached, or a
  * non-finite residual); synchronises.  lv_find_pressure without stats queues

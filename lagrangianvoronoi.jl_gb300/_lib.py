@@ -90,6 +90,7 @@ SIGNATURES = {
     "lv_kernel_time": (C.c_int, [_vp, _i32, _pi64, _pd, _i32]),
     "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
     "lv_solver_unconverged": (C.c_int, [_vp, _pi64]),
+    "lv_set_wait_limit": (C.c_int, [_vp, _i64]),
     "lv_solver_halo": (C.c_int, [_vp, _pi32]),
     "lv_solver_forget": (C.c_int, [_vp]),
     "lv_mesh_captures": (C.c_int, [_vp, _pi32]),

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -68,14 +69,35 @@ std::vector<PathNodeDev> build_path(const GridDev& g) {
   return out;
 }
 
+}  // namespace
+
+// Function attributes (dynamic shared memory beyond 48 KB, carveouts) belong
+// to a device: they are set once per device, by the first context created on
+// it, whichever host thread that is.
+int lv_device_setup(int dev) {
+  static std::once_flag once[LV_MAX_DEVICES];
+  static int rc[LV_MAX_DEVICES];
+  if (dev < 0 || dev >= LV_MAX_DEVICES) return LV_ERR_BAD_ARGUMENT;
+  std::call_once(once[dev], [dev]() {
+    int r = lv_mesh_device_setup();
+    if (r == LV_OK) r = lv_fcg_device_setup();
+    rc[dev] = r;
+  });
+  return rc[dev];
+}
+
+namespace {
+
 int nimages(const GridDev& g) { return 1 + (g.xper ? 2 : 0) + (g.yper ? 2 : 0) + ((g.xper && g.yper) ? 4 : 0); }
 
 int decode_status(int flags) {
+  // root causes first: a cell list that overflowed leaves candidates out of
+  // the clip, which can also destroy the mesh or overflow a polygon
   if (flags & LV_FLAG_NAN_VELOCITY) return LV_ERR_NAN_VELOCITY;
   if (flags & LV_FLAG_NONFINITE) return LV_ERR_NONFINITE_POSITION;
+  if (flags & LV_FLAG_CELL_OVERFLOW) return LV_ERR_CELL_OVERFLOW;
   if (flags & LV_FLAG_MESH_DESTROYED) return LV_ERR_MESH_DESTROYED;
   if (flags & LV_FLAG_EDGE_OVERFLOW) return LV_ERR_EDGE_OVERFLOW;
-  if (flags & LV_FLAG_CELL_OVERFLOW) return LV_ERR_CELL_OVERFLOW;
   if (flags & LV_FLAG_BARRIER_TIMEOUT) return LV_ERR_BARRIER_TIMEOUT;
   return LV_OK;
 }
@@ -98,7 +120,12 @@ int sync_status(lv_ctx* c) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return lv_cuda_check(c, e, "stream synchronize");
   int flags = *c->status_host;
-  if (flags & LV_FLAG_BARRIER_TIMEOUT) c->fcg_reset = c->big_reset = true;  // a solver launch stopped part-way
+  if (flags & LV_FLAG_BARRIER_TIMEOUT) {
+    // a solver launch stopped part-way: its synchronisation words start
+    // afresh, and the sweeps' history (partly written) is dropped
+    c->fcg_reset = c->big_reset = true;
+    c->sg_valid = 0;
+  }
   if (flags) {
     cudaMemsetAsync(c->status, 0, sizeof(int), c->stream);
     int code = decode_status(flags);
@@ -216,6 +243,21 @@ lv_ctx* lv_create(const lv_params* prm) {
   cudaEventCreate(&c->ev1);
   const char* tenv = getenv("LVGPU_TIMING");
   c->timing = tenv && tenv[0] == '1';
+  // test knobs, read once here: the first clipping pass's edge slots, the
+  // sweep guess, a lowered cell-list capacity
+  if (const char* env = getenv("LVGPU_CLIP_SLOTS")) c->clip_slots = atoi(env);
+  const char* sgenv = getenv("LVGPU_SWEEP_GUESS");
+  c->sweep_guess = !(sgenv && sgenv[0] == '0');
+  long long cell_items = 0;
+  if (const char* env = getenv("LVGPU_CELL_ITEMS")) cell_items = atoll(env);
+  // function attributes are per device: set them once for this one
+  if (c->dev < 0 || c->dev >= LV_MAX_DEVICES || lv_device_setup(c->dev) != LV_OK) {
+    cudaStreamDestroy(c->stream);
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    delete c;
+    return nullptr;
+  }
 
   const int cap = (prm->capacity + 31) / 32 * 32;
   c->cap = cap;
@@ -258,9 +300,14 @@ lv_ctx* lv_create(const lv_params* prm) {
   cl.ncells = g.n1 * g.n2;
   cl.cstart = dalloc<int>(c, (size_t)cl.ncells + 1, &ok);
   cl.ccount = dalloc<int>(c, cl.ncells, &ok);
-  cl.item_cap = cap * nimages(g);
+  // every copy of every seed has a cell-list slot, so the list cannot
+  // overflow; LVGPU_CELL_ITEMS (tests) lowers its capacity to inject that
+  // error (the per-copy keys keep one entry per copy)
+  const int copies = cap * nimages(g);
+  cl.item_cap = copies;
+  if (cell_items > 0 && cell_items < cl.item_cap) cl.item_cap = (int)cell_items;
   cl.citem = dalloc<int>(c, cl.item_cap, &ok);
-  cl.bkey = dalloc<int2>(c, cl.item_cap, &ok);
+  cl.bkey = dalloc<int2>(c, copies, &ok);
   cl.cpos = dalloc<float2>(c, cl.item_cap, &ok);
 
   SolverDev& sv = c->sv;
@@ -701,8 +748,6 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
   c->sg_pending = false;  // a start queued by a call that failed is void
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;
-  const char* env = getenv("LVGPU_SWEEP_GUESS");
-  c->sweep_guess = !(env && env[0] == '0');
   SolverDev& sv = c->sv;
   if (c->sweep_guess && niter > sv.dinc_slots) {
     // one FP32 vector per sweep for the sweeps' changes (kept for the next call)
@@ -774,11 +819,13 @@ int lv_solve(lv_ctx* c, const double* b, double* x, lv_solve_stats* stats) {
   int rc = lv_solver_solve(c, xd, nullptr, 0);
   if (rc) return rc;
   cudaMemcpyAsync(x, xd, 8 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (stats) {
-    rc = lv_solver_fetch_stats(c, stats, 1);
-    if (rc) return rc;
-  }
-  return sync_status(c);
+  lv_solve_stats st;
+  rc = lv_solver_fetch_stats(c, &st, 1);
+  if (rc) return rc;
+  if (stats) *stats = st;
+  rc = sync_status(c);
+  if (rc) return rc;
+  return st.converged ? LV_OK : lv_fail(c, LV_ERR_CG_MAXITER, "the solve stopped at itmax above the tolerance");
 }
 
 int lv_operator_apply(lv_ctx* c, const double* x, double* y) {
@@ -863,6 +910,12 @@ int lv_solver_halo(lv_ctx* c, int32_t* max_rows) {
   int m = 0;
   if (int rc = lv_fcg_halo_info(c, &m)) return rc;
   *max_rows = m;
+  return LV_OK;
+}
+
+int lv_set_wait_limit(lv_ctx* c, int64_t cycles) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  c->spin_limit = cycles > 0 ? (long long)cycles : LV_WAIT_LIMIT_DEFAULT;
   return LV_OK;
 }
 

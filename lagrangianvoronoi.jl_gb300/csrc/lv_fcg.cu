@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdlib>
+#include <mutex>
 
 #include "lv_internal.cuh"
 
@@ -29,7 +30,7 @@ constexpr int FCG_TPB = 512;
 constexpr int FKR = 8;    // operator entries per row held in registers
 constexpr int FKM = 12;   // preconditioner off-diagonal entries per row held in registers
 constexpr int MMAX = 96;  // preconditioner off-diagonal entries per row (storage slots)
-constexpr long long FCG_SPIN_LIMIT = 4000000000LL;  // cycles (about 2 s)
+constexpr long long FCG_SPIN_LIMIT = LV_WAIT_LIMIT_DEFAULT;  // cycles: the bulk copies' waits
 constexpr float FCG_UPDATE_DROP = 1e-5f;  // FP32 residual reduction per refinement step
 constexpr int FCG_MAX_UPDATES = 200;
 
@@ -129,6 +130,7 @@ struct FcgArgs {
   int* status;
   double tol2;
   int itmax;
+  long long spin;   // cycles a wait on another block lasts before it gives up
   const int* nonsingular;
   int learned;
   const int* mcnt;  // learned M^-1: off-diagonal count, slot-major entries, diagonal
@@ -182,7 +184,7 @@ __device__ __forceinline__ int arrive_wait(const Args& a, unsigned ph) {
   const unsigned target = s_base[0] + ph * (unsigned)a.nb;
   const long long t0 = clock64();
   while ((int)(ld_acquire_u32(a.counter) - target) < 0) {
-    if (clock64() - t0 > FCG_SPIN_LIMIT) {
+    if (clock64() - t0 > a.spin) {
       atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
       return 0;
     }
@@ -304,7 +306,7 @@ __device__ bool nexchange(const Args& a, unsigned e, const unsigned* mask) {
   if (t < a.nb && ((mask[t >> 5] >> (t & 31)) & 1u)) {
     const long long t0 = clock64();
     while ((int)(ld_acquire_u32(a.flags + (size_t)t * FLAG_STRIDE) - ee) < 0) {
-      if (clock64() - t0 > FCG_SPIN_LIMIT) {
+      if (clock64() - t0 > a.spin) {
         to = 1;
         atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
         break;
@@ -614,7 +616,7 @@ __global__ void __launch_bounds__(FCG_TPB, 1) k_fcg(FcgArgs a) {
           const long long t0 = clock64();
           do {
             wv[q] = ld_relaxed_u64(a.rtag + ss.img.ext[e]);
-            if (clock64() - t0 > FCG_SPIN_LIMIT) {
+            if (clock64() - t0 > a.spin) {
               late = 1;
               atomicOr(a.status, LV_FLAG_BARRIER_TIMEOUT);
               break;
@@ -1240,7 +1242,6 @@ __global__ void __launch_bounds__(128) k_build_minv_reg(int n, const int* __rest
 // correction into x after the phase that ends that pass.
 // ---------------------------------------------------------------------------
 constexpr int BIG_TPB = 1024;
-constexpr int BIG_TPB_L = 640;
 constexpr int BIG_SB = 8;    // slots loaded together (FP32 passes)
 constexpr int BIG_SB64 = 4;  // (FP64 residual)
 constexpr int BIG_MASK_WORDS = FCG_MAX_BLOCKS / 32;
@@ -1273,6 +1274,7 @@ struct BigArgs {
   int* status;
   double tol2;
   int itmax;
+  long long spin;
   const int* nonsingular;
   int sg_mode;                // as FcgArgs
   double* pprev;
@@ -1372,49 +1374,32 @@ __device__ __forceinline__ double big_res64(const BigArgs& a, int i, double bi) 
   return bi - acc;
 }
 
-// Row i of u = M^-1 r: md_i r_i + the row's slots in order (the count and
-// two chunks of BIG_SB slots loaded ahead: M^-1 has MMAX slots per row).
+// Row i of u = M^-1 r: md_i r_i + the row's slots in order, BIG_SB at a time
+// (the count and the first chunk loaded together: M^-1 has MMAX slots per
+// row, so the chunk lies inside its arrays whatever the count).
 __device__ __forceinline__ float big_mrow(const BigArgs& a, int i, const float* __restrict__ r) {
   const int mc = ld_nc(a.mcnt + i);
-  int j0[BIG_SB], j1[BIG_SB];
-  float v0[BIG_SB], v1[BIG_SB], r0[BIG_SB], r1[BIG_SB];
-#pragma unroll
-  for (int q = 0; q < BIG_SB; ++q) {
-    j0[q] = ld_nc(a.mcol + (size_t)q * a.mstride + i);
-    v0[q] = ld_nc(a.mval + (size_t)q * a.mstride + i);
-  }
   float acc = ld_nc(a.mdiag + i) * __ldcg(r + i);
-#pragma unroll
-  for (int q = 0; q < BIG_SB; ++q) r0[q] = __ldcg(r + (q < mc ? j0[q] : i));
-  if (mc > BIG_SB) {
+  for (int k0 = 0; k0 == 0 || k0 < mc; k0 += BIG_SB) {
+    int jj[BIG_SB];
+    float mv[BIG_SB], rv[BIG_SB];
 #pragma unroll
     for (int q = 0; q < BIG_SB; ++q) {
-      j1[q] = ld_nc(a.mcol + (size_t)(BIG_SB + q) * a.mstride + i);
-      v1[q] = ld_nc(a.mval + (size_t)(BIG_SB + q) * a.mstride + i);
+      jj[q] = ld_nc(a.mcol + (size_t)(k0 + q) * a.mstride + i);
+      mv[q] = ld_nc(a.mval + (size_t)(k0 + q) * a.mstride + i);
     }
-  }
 #pragma unroll
-  for (int q = 0; q < BIG_SB; ++q)
-    if (q < mc) acc = fmaf(v0[q], r0[q], acc);
-  if (mc > BIG_SB) {
-#pragma unroll
-    for (int q = 0; q < BIG_SB; ++q) r1[q] = __ldcg(r + (BIG_SB + q < mc ? j1[q] : i));
+    for (int q = 0; q < BIG_SB; ++q) rv[q] = __ldcg(r + (k0 + q < mc ? jj[q] : i));
 #pragma unroll
     for (int q = 0; q < BIG_SB; ++q)
-      if (BIG_SB + q < mc) acc = fmaf(v1[q], r1[q], acc);
-    for (int k = 2 * BIG_SB; k < mc; ++k) {
-      const size_t e = (size_t)k * a.mstride + i;
-      acc = fmaf(ld_nc(a.mval + e), __ldcg(r + ld_nc(a.mcol + e)), acc);
-    }
+      if (k0 + q < mc) acc = fmaf(mv[q], rv[q], acc);
   }
   return acc;
 }
 
-// (the learned instantiation runs 640 threads a block: its M^-1 rows keep two
-// chunks of slots in flight, which needs more than 64 registers a thread)
 template <bool LEARNED>
-__global__ void __launch_bounds__(LEARNED ? BIG_TPB_L : BIG_TPB, 1) k_big(BigArgs a) {
-  constexpr int TPB = LEARNED ? BIG_TPB_L : BIG_TPB;
+__global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
+  constexpr int TPB = BIG_TPB;
   const int n = a.n;
   const int rb0 = blockIdx.x * a.rpb;
   const int rb1 = min(n, rb0 + a.rpb);
@@ -1607,29 +1592,36 @@ void fcg_shape(const lv_ctx* c, int n, int* nb, int* R) {
   if (n > *nb * FCG_TPB * 2) *nb = std::min(c->num_sms * 2, FCG_MAX_BLOCKS);
 }
 
-// whether the staged mode's shared memory leaves nb blocks co-resident
+// whether the staged mode's shared memory leaves nb blocks co-resident (the
+// shared-memory attributes were set per device by lv_fcg_device_setup; the
+// occupancy is the same on every device of this kind)
 bool stage_fits(const lv_ctx* c, int nb, int R) {
-  if (g_fcg_halo_blocks_per_sm[0] < 0) {
+  static std::once_flag once;
+  std::call_once(once, []() {
     int b1 = 0, b2 = 0;
     const int bytes = (int)sizeof(StageSmem);
-    if (cudaFuncSetAttribute(k_fcg<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_fcg<1, true>, FCG_TPB, bytes);
-    if (cudaFuncSetAttribute(k_fcg<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_fcg<2, true>, FCG_TPB, bytes);
-    cudaGetLastError();
-    if (cudaFuncSetAttribute(k_stage_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STG_BUILD_SMEM) !=
-        cudaSuccess)
-      b1 = b2 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_fcg<1, true>, FCG_TPB, bytes) != cudaSuccess) b1 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_fcg<2, true>, FCG_TPB, bytes) != cudaSuccess) b2 = 0;
     cudaGetLastError();
     g_fcg_halo_blocks_per_sm[0] = b1;
     g_fcg_halo_blocks_per_sm[1] = b2;
-  }
+  });
   return g_fcg_halo_blocks_per_sm[R - 1] * c->num_sms >= nb;
 }
 
 
 
 }  // namespace
+
+// The staged solve's and its image builder's shared memory on the current device.
+int lv_fcg_device_setup() {
+  const int bytes = (int)sizeof(StageSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_fcg<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fcg<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_stage_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STG_BUILD_SMEM);
+  return e == cudaSuccess ? LV_OK : LV_ERR_CUDA;
+}
 
 // Rows the flag-reduced solver holds (one or two blocks per SM, two rows per
 // thread at most); larger systems use the streaming solver.
@@ -1815,6 +1807,7 @@ int lv_fcg_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.status = c->status;
   a.tol2 = c->tol * c->tol;
   a.itmax = c->itmax;
+  a.spin = c->spin_limit;
   a.nonsingular = c->sv.iters + LV_IT_NONSINGULAR;
   a.learned = learned ? 1 : 0;
   a.mcnt = c->sv.mcnt;
@@ -1877,7 +1870,7 @@ int big_blocks(lv_ctx* c, bool learned) {
   if (b < 0) {
     int v = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, learned ? (const void*)k_big<true> : (const void*)k_big<false>,
-                                                  learned ? BIG_TPB_L : BIG_TPB, 0);
+                                                  BIG_TPB, 0);
     b = v;
   }
   return b >= 1 ? std::min(c->num_sms, FCG_MAX_BLOCKS) : 0;
@@ -1961,6 +1954,7 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.status = c->status;
   a.tol2 = c->tol * c->tol;
   a.itmax = c->itmax;
+  a.spin = c->spin_limit;
   a.nonsingular = sv.iters + LV_IT_NONSINGULAR;
   a.sg_mode = 0;
   a.pprev = sv.pprev;
@@ -1986,7 +1980,7 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
   }
   void* args[] = {&a};
   const void* fn = learned ? (const void*)k_big<true> : (const void*)k_big<false>;
-  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(learned ? BIG_TPB_L : BIG_TPB), args, 0, c->stream);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(nb), dim3(BIG_TPB), args, 0, c->stream);
   c->launches++;
   if (e != cudaSuccess) {
     c->big_reset = true;

@@ -33,6 +33,10 @@
 #define LV_IT_FCG_BASE 100     // [2] arrivals and exchange epochs of the flag-reduced solver so far
 #define LV_IT_SIZE 160
 
+// Clock cycles a persistent solver waits on other blocks before it gives up
+// and reports LV_ERR_BARRIER_TIMEOUT (about 2 s at 2 GHz; lv_set_wait_limit).
+#define LV_WAIT_LIMIT_DEFAULT 4000000000LL
+
 // Status bits set on the device with atomicOr; decoded on the host.
 #define LV_FLAG_NAN_VELOCITY 0x1
 #define LV_FLAG_MESH_DESTROYED 0x2
@@ -280,6 +284,8 @@ struct lv_ctx {
   int sg_n = 0;             // the particle count they belong to
   bool fcg_halo = true;    // staged mode of the learned one-block-per-SM solve (LVGPU_FCG_HALO=0 turns it off)
   bool fcg_reset = true;   // clear the flag-reduced solver's counter, flags and bases before its next launch
+  long long spin_limit = LV_WAIT_LIMIT_DEFAULT;  // cycles a solver waits on other blocks (lv_set_wait_limit)
+  int clip_slots = 0;      // first clipping pass's edge slots (0: the default; LVGPU_CLIP_SLOTS)
   bool big_reset = true;   // the same for the streaming solver's
   bool big_masks_valid = false;  // its neighbour masks match the operator
   bool big_masks_m = false;      // and cover M^-1's pattern
@@ -454,6 +460,12 @@ int lv_mesh_remesh(lv_ctx* c);
 int lv_mesh_face_len(lv_ctx* c);  // fills m.flen unless it is current
 int lv_mesh_captures_count(lv_ctx* c, int* count);  // second-pass polygons of the last remesh (synchronises)
 int lv_scan_int(lv_ctx* c, const int* in, int* out, int len);  // exclusive, out[len] = total
+
+// ---- per-device set-up (function attributes), once per device and process
+#define LV_MAX_DEVICES 64
+int lv_device_setup(int dev);  // lv_api.cu; call with dev current
+int lv_mesh_device_setup();    // lv_mesh.cu
+int lv_fcg_device_setup();     // lv_fcg.cu
 
 // ---- physics (lv_physics.cu)
 int lv_phys_move(lv_ctx* c, double dt);

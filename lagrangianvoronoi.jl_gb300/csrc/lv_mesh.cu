@@ -727,8 +727,9 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
           continue;
         }
         const int cell = (int)((c1 - 1) + (long long)g.n1 * (c2 - 1));
-        s = cl.cstart[cell];
-        se = cl.cstart[cell + 1];
+        // (clamped: a cell list that overflowed is reported by the binning)
+        se = min(cl.cstart[cell + 1], cl.item_cap);
+        s = min(cl.cstart[cell], se);
         continue;
       }
       const int j = cl.citem[s];
@@ -967,6 +968,17 @@ int lv_mesh_face_len(lv_ctx* c) {
   return LV_OK;
 }
 
+// The clipping kernels' shared memory and carveout on the current device.
+int lv_mesh_device_setup() {
+  cudaError_t e = cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)clip_smem(ME_SMALL));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME));
+  return e == cudaSuccess ? LV_OK : LV_ERR_CUDA;
+}
+
 int lv_mesh_remesh(lv_ctx* c) {
   const int n = c->n;
   if (n <= 0) return lv_fail(c, LV_ERR_NOT_MESHED, "remesh: no particles");
@@ -991,14 +1003,6 @@ int lv_mesh_remesh(lv_ctx* c) {
   LV_LAUNCH_CHECK(c, "k_bin_order");
   c->ccount_clean = true;
   }
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME_SMALL));
-    cudaFuncSetAttribute(k_clip<ME_SMALL>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    cudaFuncSetAttribute(k_clip_redo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)clip_smem(ME));
-    attr_set = true;
-  }
   {
     KernelTimer kt(c, LV_KF_CLIP);
     // the captures for the second pass (one per particle at most), then the count
@@ -1015,10 +1019,7 @@ int lv_mesh_remesh(lv_ctx* c) {
     // LVGPU_CLIP_SLOTS so that tests can drive most polygons through the
     // second pass (the mesh is the same either way)
     int slots = ME_SMALL;
-    if (const char* env = getenv("LVGPU_CLIP_SLOTS")) {
-      const int v = atoi(env);
-      if (v >= 5 && v < ME_SMALL) slots = v;
-    }
+    if (c->clip_slots >= 5 && c->clip_slots < ME_SMALL) slots = c->clip_slots;
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
                                                                                    c->m, c->status, redo, redo_n, slots);
     LV_LAUNCH_CHECK(c, "k_clip");

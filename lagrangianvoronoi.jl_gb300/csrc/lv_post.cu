@@ -39,7 +39,7 @@ __device__ int nearest(const GridDev& g, const PathNodeDev* __restrict__ path, i
     const long long c1 = k1 + path[pn].di1, c2 = k2 + path[pn].di2;
     if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) continue;
     const int cell = (int)((c1 - 1) + (long long)g.n1 * (c2 - 1));
-    for (int s = cl.cstart[cell]; s < cl.cstart[cell + 1]; ++s) {
+    for (int s = cl.cstart[cell], se = min(cl.cstart[cell + 1], cl.item_cap); s < se; ++s) {
       const int i = cl.citem[s];
       const double2 p = x[i];
       const double dx = p.x - qx, dy = p.y - qy;
@@ -125,7 +125,7 @@ __device__ void movingls(const GridDev& g, const PathNodeDev* __restrict__ path,
       const long long c1 = k1 + path[pn].di1, c2 = k2 + path[pn].di2;
       if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) continue;
       const int cell = (int)((c1 - 1) + (long long)g.n1 * (c2 - 1));
-      for (int s = cl.cstart[cell]; s < cl.cstart[cell + 1]; ++s) {
+      for (int s = cl.cstart[cell], se = min(cl.cstart[cell + 1], cl.item_cap); s < se; ++s) {
         const int j = cl.citem[s];
         const double2 q = x[j];
         double vx, vy;

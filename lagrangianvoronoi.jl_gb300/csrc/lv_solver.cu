@@ -20,6 +20,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "lv_internal.cuh"
 
@@ -27,7 +28,6 @@ namespace {
 
 constexpr int TPB = 256;
 constexpr int CG_TPB = 256;
-constexpr long long BARRIER_CYCLE_LIMIT = 4000000000LL;  // ~2 s at 2 GHz
 
 // (also clears the nonsingular flag that k_assemble then sets)
 __global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n, int* nonsingular) {
@@ -90,9 +90,10 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 // bar[0] is an arrival word, zeroed by the host before the launch: block 0
 // adds 2^31 - (nblocks - 1), every other block adds 1, so the word's top bit
 // flips exactly when the last block arrives and its low bits return to zero
-// for the next barrier.  Every wait is bounded: after ~2 s the block records
-// LV_FLAG_BARRIER_TIMEOUT and the caller leaves the kernel.
-__device__ bool grid_barrier(unsigned* bar, int* status) {
+// for the next barrier.  Every wait is bounded: after `limit` clock cycles
+// (about 2 s by default) the block records LV_FLAG_BARRIER_TIMEOUT and the
+// caller leaves the kernel.
+__device__ bool grid_barrier(unsigned* bar, int* status, long long limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -102,7 +103,7 @@ __device__ bool grid_barrier(unsigned* bar, int* status) {
     const unsigned old = atomicAdd(bar, inc);
     const long long t0 = clock64();
     while (((old ^ ld_acquire_u32(bar)) & 0x80000000u) == 0u) {
-      if (clock64() - t0 > BARRIER_CYCLE_LIMIT) {
+      if (clock64() - t0 > limit) {
         atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
         ok = 0;
         break;
@@ -173,6 +174,7 @@ struct PCGArgs {
   int* status;
   double tol2;
   int itmax;
+  long long spin;          // cycles a grid barrier waits before it gives up
   const int* nonsingular;  // set by k_assemble when some diagonal term is nonzero
   const double* diag;      // the reference's diagonal term (mixed solver only)
   int* out_iters;
@@ -195,9 +197,9 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     for (int i = t0; i < n; i += stride) v[0] += a.b[i];
     block_sums<1>(v, sh);
     if (threadIdx.x == 0) a.part[3 * nb + blockIdx.x] = v[0];
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
     bmean = grid_total(a.part, 3, sh) / (double)n;
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
   }
   // r = b - A x, z = M^-1 r, p = q = 0
   {
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
       a.part[3 * nb + blockIdx.x] = v[2];
     }
   }
-  if (!grid_barrier(a.bar, a.status)) return;
+  if (!grid_barrier(a.bar, a.status, a.spin)) return;
   double rz = grid_total(a.part, 1, sh);
   double rr = grid_total(a.part, 2, sh);
   const double bb = grid_total(a.part, 3, sh);
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
       block_sums<1>(v, sh);
       if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
     }
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
     const double alpha = rz / grid_total(a.part, 0, sh);
     {
       double v[2] = {0.0, 0.0};
@@ -265,7 +267,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
         a.part[2 * nb + blockIdx.x] = v[1];
       }
     }
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
     const double rz_new = grid_total(a.part, 1, sh);
     rr = grid_total(a.part, 2, sh);
     beta = rz_new / rz;
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(CG_TPB) k_pcg(PCGArgs a) {
     block_sums<1>(v, sh);
     if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
   }
-  if (!grid_barrier(a.bar, a.status)) return;
+  if (!grid_barrier(a.bar, a.status, a.spin)) return;
   if (blockIdx.x == 0) {
     const double tr = grid_total(a.part, 0, sh);
     if (threadIdx.x == 0) {
@@ -391,14 +393,14 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
     for (int k = 0; k < R; ++k) v[0] += rr.bb[k];
     block_sums<1>(v, sh);
     if (threadIdx.x == 0) a.part[0 * nb + blockIdx.x] = v[0];
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
     double t[1];
     grid_totals<1>(a.part, 0, t);
     const double mean = t[0] / (double)n;
 #pragma unroll
     for (int k = 0; k < R; ++k)
       if (rr.i[k] < n) rr.bb[k] -= mean;
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
   }
   int it = 0;
   double bnorm2 = 0.0, rtrue2 = 0.0, rho = 0.0;
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
       a.part[0 * nb + blockIdx.x] = v[0];
       a.part[1 * nb + blockIdx.x] = v[1];
     }
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
     double t2[2];
     grid_totals<2>(a.part, 0, t2);
     rtrue2 = t2[0];
@@ -451,7 +453,7 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
         a.part[(slot + 1) * nb + blockIdx.x] = v3[1];
         a.part[(slot + 2) * nb + blockIdx.x] = v3[2];
       }
-      if (!grid_barrier(a.bar, a.status)) return;
+      if (!grid_barrier(a.bar, a.status, a.spin)) return;
       // the scalar recurrences run once per block (thread 0) and are
       // broadcast: FP64 work is paid per warp instruction, so redundant
       // per-thread scalar math would cost as much as the vector updates.
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(SP_TPB) k_pcg_reg(PCGArgs a, double* ubuf, dou
 #pragma unroll
     for (int k = 0; k < R; ++k)
       if (rr.i[k] < n) a.x[rr.i[k]] = x[k];
-    if (!grid_barrier(a.bar, a.status)) return;
+    if (!grid_barrier(a.bar, a.status, a.spin)) return;
   }
 #pragma unroll
   for (int k = 0; k < R; ++k)
@@ -648,6 +650,7 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
   a.status = c->status;
   a.tol2 = c->tol * c->tol;
   a.itmax = c->itmax;
+  a.spin = c->spin_limit;
   a.nonsingular = c->sv.iters + LV_IT_NONSINGULAR;
   a.diag = c->sv.diag;
   a.out_iters = c->sv.iters + slot;
@@ -761,9 +764,10 @@ __global__ void k_noalloc_diag(int n, const double* __restrict__ diag, const int
   if (d != 0.0) atomicOr(nonsingular, 1);
 }
 
-// Device address of the scratch array, looked up once per device.
-double* g_noalloc_dev[64] = {nullptr};
-bool g_noalloc_ready[64] = {false};
+// Device address of the scratch array, looked up once per device (by the
+// first call on that device, whichever host thread makes it).
+double* g_noalloc_dev[LV_MAX_DEVICES] = {nullptr};
+std::once_flag g_noalloc_once[LV_MAX_DEVICES];
 
 }  // namespace
 
@@ -773,17 +777,16 @@ extern "C" int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t
   if (n <= 0 || n > LV_NOALLOC_MAX_ROWS) return LV_ERR_BAD_ARGUMENT;
   if (!diag || !rowptr || !col || !w || !b || !x || !(tol > 0) || itmax <= 0) return LV_ERR_BAD_ARGUMENT;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return LV_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= LV_MAX_DEVICES) return LV_ERR_CUDA;
   // First call on this device: resolve the array's device address with the
   // device current.  The host-side name g_noalloc_scratch is only a stand-in
   // and must never be passed to a kernel.
-  if (!g_noalloc_ready[dev]) {
+  std::call_once(g_noalloc_once[dev], [dev]() {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return LV_ERR_CUDA;
-    g_noalloc_dev[dev] = static_cast<double*>(p);
-    g_noalloc_ready[dev] = true;
-  }
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) == cudaSuccess) g_noalloc_dev[dev] = static_cast<double*>(p);
+  });
   double* base = g_noalloc_dev[dev];
+  if (!base) return LV_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t M = LV_NOALLOC_MAX_ROWS;
   double* adiag = base;
@@ -822,6 +825,7 @@ extern "C" int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t
   a.status = status;
   a.tol2 = tol * tol;
   a.itmax = itmax;
+  a.spin = LV_WAIT_LIMIT_DEFAULT;
   a.nonsingular = nonsingular;
   a.diag = diag;
   a.out_iters = iters;
@@ -841,5 +845,7 @@ extern "C" int lv_pcg_solve_noalloc(int32_t n, const double* diag, const int32_t
   if (st & LV_FLAG_BARRIER_TIMEOUT) return LV_ERR_BARRIER_TIMEOUT;
   if (iterations) *iterations = it;
   if (rel_residual) *rel_residual = d3[1] > 0 ? sqrt(d3[2] / d3[1]) : sqrt(d3[2]);
-  return (d3[0] <= tol * tol * d3[1]) ? LV_OK : LV_ERR_CG_MAXITER;
+  // both the recursive residual (the loop's test) and the true one recomputed
+  // at the end must meet the tolerance
+  return (d3[0] <= tol * tol * d3[1] && d3[2] <= tol * tol * d3[1]) ? LV_OK : LV_ERR_CG_MAXITER;
 }
