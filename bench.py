@@ -255,8 +255,9 @@ def solver_comparison(lv, L, g, fl, steps, train_info):
     solve kernels (+ operator/RHS/factor kernels) and CG iterations per step."""
     fam = lv._lib.KERNEL_FAMILIES
     out = {}
-    for method in ("jacobi_pcg", "mixed_ir", "learned_pcg"):
-        solver = lv.PressureSolver(g, method=method, tol=1e-8)
+    for method in ("jacobi_pcg", "mixed_ir", "learned_pcg", "minres"):
+        # minres: the reference's own solve (tol 1e-6 absolute + relative, itmax 1000)
+        solver = lv.PressureSolver(g, method=method, tol=None if method == "minres" else 1e-8)
         gpu_step(lv, g, solver, fl)  # settle
         g.synchronize()
         L.lv_kernel_timing(g._ctx, 1)
@@ -325,7 +326,8 @@ def run_ours(args, world, rank, local, wl):
     g = setup_grid(lv, wl)
     # warm-up with the Jacobi mixed solver: its iteration count is the
     # learned solver's fallback reference
-    solver = lv.PressureSolver(g, method="mixed_ir" if args.solver == "learned_pcg" else args.solver, tol=1e-8)
+    solver = lv.PressureSolver(g, method="mixed_ir" if args.solver == "learned_pcg" else args.solver,
+                               tol=None if args.solver == "minres" else 1e-8)
     stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
     # between timed steps an L2 flush when the state fits in L2
     flush_l2 = N * STATE_BYTES_PER_PARTICLE < 4 * L2_BYTES
@@ -337,7 +339,7 @@ def run_ours(args, world, rank, local, wl):
     g.synchronize()
     train_info = train_learned(L, g, args)
 
-    solver = lv.PressureSolver(g, method=args.solver, tol=1e-8)
+    solver = lv.PressureSolver(g, method=args.solver, tol=None if args.solver == "minres" else 1e-8)
     # the state the passes start from: each pass restores it, forgets the
     # sweep-guess history and runs one untimed step with the timed solver, so
     # the timed, the instrumented and the end-to-end passes run the same steps
@@ -492,7 +494,9 @@ def run_ours(args, world, rank, local, wl):
     dom_launches = max(kt[dom][0], 1)
     achieved = (fams[dom] / dom_launches) / ((dom_ms / dom_launches) / 1e3) / 1e9 if dom_ms > 0 else 0.0
     if dom == "pcg":
-        if args.solver == "jacobi_pcg":
+        if args.solver == "minres":
+            kname = "k_minres"
+        elif args.solver == "jacobi_pcg":
             kname = "k_pcg_reg<2>" if N <= 2 * 128 * 2 * 152 else "k_pcg"
         else:
             staged = 1 if args.solver == "learned_pcg" else 0
@@ -517,7 +521,8 @@ def run_ours(args, world, rank, local, wl):
         "vs_baseline": None, "dtype": "f64 (fp32 inner CG)" if args.solver != "jacobi_pcg" else "f64",
         "data": "synthetic (seeded jittered lattice, analytic initial field)",
         "config": dict(wl.describe(), **{
-            "solver": SOLVER_DESC[args.solver] + ", tol 1e-8 (FP64 residual), 10 sweeps/step",
+            "solver": SOLVER_DESC[args.solver] + ("" if args.solver == "minres" else
+                                                  ", tol 1e-8 (FP64 residual)") + ", 10 sweeps/step",
             "parallelism": f"replicas x{world}",
             "l2": ("512 MiB buffer written between timed steps (the state fits in L2)" if flush_l2 else
                    f"no flush: the state ({N * STATE_BYTES_PER_PARTICLE / 1e9:.2f} GB) is larger than L2")}),
@@ -559,6 +564,7 @@ SOLVER_DESC = {
     "jacobi_pcg": "jacobi_pcg fp64",
     "mixed_ir": "mixed_ir: fp32 jacobi CG inside fp64 refinement",
     "learned_pcg": "learned_pcg: fp32 CG preconditioned by the trained factor inside fp64 refinement",
+    "minres": "minres fp64 (the reference's solve: atol = rtol = 1e-6, itmax 1000)",
 }
 
 
@@ -680,7 +686,7 @@ def main():
     ap.add_argument("--nx", type=int, default=0, help="lattice columns (0: the workload's size; others for profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the per-solver comparison")
-    ap.add_argument("--solver", default="learned_pcg", choices=["jacobi_pcg", "mixed_ir", "learned_pcg"],
+    ap.add_argument("--solver", default="learned_pcg", choices=["jacobi_pcg", "mixed_ir", "learned_pcg", "minres"],
                     help="pressure solver of the timed steps")
     ap.add_argument("--train-steps", type=int, default=400, help="Adam steps of the learned preconditioner")
     ap.add_argument("--train-probes", type=int, default=0, help="0: FSAI/Kaporin objective; K: Hutchinson, K probes")

@@ -65,7 +65,10 @@ enum lv_field {
 enum lv_method {
   LV_METHOD_JACOBI_PCG = 0,   /* FP64 Jacobi-preconditioned CG (the fallback, and the plain solver the others are measured against) */
   LV_METHOD_MIXED_IR = 1,     /* FP32 CG inner solves inside FP64 iterative refinement */
-  LV_METHOD_LEARNED_PCG = 2   /* mixed IR preconditioned by the learned sparse factor */
+  LV_METHOD_LEARNED_PCG = 2,  /* mixed IR preconditioned by the learned sparse factor */
+  LV_METHOD_MINRES = 3        /* the reference's solve: FP64 MINRES without a preconditioner, stopping at
+                                 ||r|| <= tol + tol ||r0|| (Krylov.jl minres!, atol = rtol = tol,
+                                 pressure.jl:219), warm-started from P in every sweep */
 };
 
 typedef struct lv_params {
@@ -147,13 +150,30 @@ int lv_bdary_friction(lv_ctx* ctx, const double* vwall, double dt);
 int lv_find_dv(lv_ctx* ctx, double dt, double alpha);                 /* find_dv! (relaxation.jl:10-25) */
 int lv_relaxation_step(lv_ctx* ctx, double dt, int32_t rusanov);      /* relaxation_step! (relaxation.jl:36-73), remeshes */
 
-/* PressureSolver(grid) options (pressure.jl:142-159): method, relative
- * residual tolerance and iteration cap. */
+/* PressureSolver(grid) options (pressure.jl:142-159): method, tolerance and
+ * iteration cap.  The CG methods stop at ||b - A x|| <= tol ||b||; MINRES
+ * at the reference's test.  The reference's PressureSolver is
+ * LV_METHOD_MINRES, tol 1e-6, itmax 1000, which a new context starts with. */
 int lv_set_solver(lv_ctx* ctx, int32_t method, double tol, int32_t itmax);
 /* find_pressure!(solver, dt, niter; boundary_velocity) (pressure.jl:215-224).
  * vbc[4][2] (constant boundary velocity per label) may be NULL (zero_vbc).
  * niter <= 31.  stats[niter] may be NULL; when given, the call synchronises. */
 int lv_find_pressure(lv_ctx* ctx, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats);
+/* Boundary edges of the last remesh, as boundaries(p) yields them
+ * (iterators.jl:46-57) over the polygons in index order: *nb, their
+ * midpoints mid[nb][2] = midpoint(e) (geometry.jl:145-147) and labels[nb]
+ * (-1..-4); with mid and labels NULL only *nb.  Synchronises. */
+int lv_get_boundary_edges(lv_ctx* ctx, int64_t* nb, double* mid, int32_t* labels);
+/* find_pressure!(solver, dt, niter; boundary_velocity) with the velocity
+ * given per boundary edge: vb[nb][2] = boundary_velocity(midpoint(e),
+ * e.label) in the order of lv_get_boundary_edges (pressure.jl:182), nb its
+ * count.  The host evaluates the reference's closure at those midpoints. */
+int lv_find_pressure_edges(lv_ctx* ctx, double dt, int32_t niter, int64_t nb, const double* vb,
+                           lv_solve_stats* stats);
+/* bdary_friction!(grid, vDirichlet, dt; charfun) per boundary edge
+ * (diffusion.jl:64-79): vb[nb][2] = vDirichlet(m) and active[nb] =
+ * charfun(m) (NULL: every edge) at the midpoints of lv_get_boundary_edges. */
+int lv_bdary_friction_edges(lv_ctx* ctx, int64_t nb, const double* vb, const uint8_t* active, double dt);
 /* Pieces of find_pressure! for inspection: PressureOperator refresh!
  * (pressure.jl:104-117) into the device CSR; solver refresh! (pressure.jl:162-203). */
 int lv_pressure_operator(lv_ctx* ctx, double dt);

@@ -33,6 +33,7 @@ __all__ = [
     "export_grid", "export_points", "LinearExpansion", "QuadraticExpansion", "CubicExpansion", "gaussian_kernel",
     "power_vector", "poly_eval", "nearest_polygon", "movingls", "point_value", "integral",
     "LvError", "BDARY_UP", "BDARY_RIGHT", "BDARY_DOWN", "BDARY_LEFT", "LV_MAX_EDGES", "wall_velocity_table",
+    "zero_vbc",
 ]
 
 
@@ -201,6 +202,19 @@ class VoronoiGrid:
         a, b = F["rowptr"][i], F["rowptr"][i + 1]
         return [(int(F["nbr"][k]), F["mid"][k], F["y"][k]) for k in range(a, b)]
 
+    def boundary_edges(self):
+        """boundaries(p) (src/iterators.jl:46-57) over all polygons: the
+        midpoints [nb][2] and labels [nb] of the boundary edges, in the order
+        the per-edge entry points take their values."""
+        L = _lib.load()
+        nb = C.c_int64()
+        _check(self, L.lv_get_boundary_edges(self._ctx, C.byref(nb), None, None))
+        mid = np.zeros((nb.value, 2))
+        lab = np.zeros(nb.value, np.int32)
+        if nb.value:
+            _check(self, L.lv_get_boundary_edges(self._ctx, None, _lib.ptr(mid), _lib.ptr(lab, C.c_int32)))
+        return mid, lab
+
     def cell_list(self):
         L = _lib.load()
         nc, ni = C.c_int64(), C.c_int64()
@@ -222,6 +236,22 @@ class VoronoiGrid:
 
     def launch_count(self):
         return int(_lib.load().lv_launch_count(self._ctx)) if self._ctx is not None else 0
+
+
+def zero_vbc(x, label):
+    """The default boundary velocity of find_pressure! (src/pressure.jl:205-207)."""
+    return (0.0, 0.0)
+
+
+def _per_edge(f):
+    """Whether a boundary closure is the reference's per-point form: f(x,
+    label) for find_pressure!, f(x) for bdary_friction! (a one-argument
+    closure of find_pressure! takes the label only, the label-table form)."""
+    import inspect
+    try:
+        return len(inspect.signature(f).parameters)
+    except (TypeError, ValueError):
+        return 2
 
 
 def wall_velocity_table(boundary_velocity):
@@ -282,13 +312,32 @@ def viscous_step(grid, dt, artificial_viscosity=True):
     _check(grid, _lib.load().lv_viscous_step(grid._ctx, float(dt), int(bool(artificial_viscosity))))
 
 
-def bdary_friction(grid, vDirichlet, dt):
-    """bdary_friction!(grid, vDirichlet, dt) (src/diffusion.jl:64-79);
-    vDirichlet as in wall_velocity_table."""
+def bdary_friction(grid, vDirichlet, dt, charfun=None):
+    """bdary_friction!(grid, vDirichlet, dt; charfun) (src/diffusion.jl:64-79).
+    vDirichlet is the reference's closure of the boundary point, vDirichlet(x)
+    -> (vx, vy), evaluated here at every boundary edge's midpoint, with
+    charfun(x) -> bool selecting the edges; or a constant wall velocity per
+    label (a dict {label: (vx, vy)}, None for zero)."""
+    L = _lib.load()
+    if callable(vDirichlet) or charfun is not None:
+        mid, lab = grid.boundary_edges()
+        if callable(vDirichlet):
+            vb = np.array([vDirichlet(m) for m in mid], dtype=np.float64).reshape(-1, 2)
+        else:
+            t = wall_velocity_table(vDirichlet)
+            t = np.zeros(8) if t is None else t
+            vb = t.reshape(4, 2)[-lab - 1] if len(lab) else np.zeros((0, 2))
+        vb = np.ascontiguousarray(vb)
+        act = None
+        if charfun is not None:
+            act = np.ascontiguousarray(np.array([bool(charfun(m)) for m in mid], dtype=np.uint8))
+        _check(grid, L.lv_bdary_friction_edges(grid._ctx, len(mid), _lib.ptr(vb),
+                                               None if act is None else _lib.ptr(act, C.c_uint8), float(dt)))
+        return
     t = wall_velocity_table(vDirichlet)
     if t is None:
         t = np.zeros(8)
-    _check(grid, _lib.load().lv_bdary_friction(grid._ctx, _lib.ptr(t), float(dt)))
+    _check(grid, L.lv_bdary_friction(grid._ctx, _lib.ptr(t), float(dt)))
 
 
 def find_dv(grid, dt, alpha=1.0):
@@ -301,15 +350,19 @@ def relaxation_step(grid, dt, rusanov=True):
 
 
 class PressureSolver:
-    """PressureSolver(grid) (src/pressure.jl:142-159) with the solver choice:
-    method 'jacobi_pcg' (FP64, the default), 'mixed_ir' or 'learned_pcg';
-    tol is the relative residual ||b - A x|| / ||b||."""
+    """PressureSolver(grid) (src/pressure.jl:142-159) with the solver choice.
+    The default is the reference's own solve: method 'minres' (FP64 MINRES
+    without a preconditioner, stopping at ||r|| <= tol + tol ||r0||, warm
+    started from P), tol 1e-6, itmax 1000 (pressure.jl:219).  The CG methods
+    'jacobi_pcg' (FP64), 'mixed_ir' and 'learned_pcg' (FP32 inner CG in FP64
+    refinement) stop at the relative residual ||b - A x|| / ||b|| <= tol."""
 
-    def __init__(self, grid, method="jacobi_pcg", tol=1e-8, itmax=10000, verbose=False):
+    def __init__(self, grid, method="minres", tol=None, itmax=None, verbose=False):
         self.grid = grid
         self.method = method
-        self.tol = float(tol)
-        self.itmax = int(itmax)
+        ref = method == "minres"
+        self.tol = float(tol if tol is not None else (1e-6 if ref else 1e-8))
+        self.itmax = int(itmax if itmax is not None else (1000 if ref else 10000))
         self.verbose = verbose
         self.last_stats = []
 
@@ -320,20 +373,32 @@ class PressureSolver:
 
 def find_pressure(solver, dt, niter=10, boundary_velocity=None, stats=True):
     """find_pressure!(solver, dt, niter; boundary_velocity) (src/pressure.jl:215-224).
+    boundary_velocity is the reference's closure boundary_velocity(x, label)
+    -> (vx, vy), evaluated here at every boundary edge's midpoint
+    (pressure.jl:182); or a constant velocity per label (a dict {label:
+    (vx, vy)} or a closure of the label alone); None or zero_vbc for zero.
     Returns per-sweep (iterations, converged, rel_residual, method used,
     refinement steps) when stats=True (which synchronises); stats=False
     queues the work and returns None."""
     g = solver.grid
     solver.configure()
-    vbc = wall_velocity_table(boundary_velocity)
+    L = _lib.load()
+    st = (LvSolveStats * niter)() if stats else None
+    if boundary_velocity is zero_vbc:
+        boundary_velocity = None
+    if callable(boundary_velocity) and _per_edge(boundary_velocity) >= 2:
+        mid, lab = g.boundary_edges()
+        vb = np.ascontiguousarray(np.array([boundary_velocity(m, int(l)) for m, l in zip(mid, lab)],
+                                           dtype=np.float64).reshape(-1, 2))
+        _check(g, L.lv_find_pressure_edges(g._ctx, float(dt), int(niter), len(mid), _lib.ptr(vb), st))
+    else:
+        vbc = wall_velocity_table(boundary_velocity)
+        _check(g, L.lv_find_pressure(g._ctx, float(dt), int(niter), _lib.ptr(vbc), st))
     if stats:
-        st = (LvSolveStats * niter)()
-        _check(g, _lib.load().lv_find_pressure(g._ctx, float(dt), int(niter), _lib.ptr(vbc), st))
         solver.last_stats = [(s.iterations, bool(s.converged), s.rel_residual, s.method, s.outer) for s in st]
         if solver.verbose:
             print(solver.last_stats)
         return solver.last_stats
-    _check(g, _lib.load().lv_find_pressure(g._ctx, float(dt), int(niter), _lib.ptr(vbc), None))
     return None
 
 

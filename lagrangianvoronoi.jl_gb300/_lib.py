@@ -21,7 +21,7 @@ FIELDS = {"x": (0, 2), "v": (1, 2), "e": (2, 1), "P": (3, 1), "rho": (4, 1), "c2
           "mass": (7, 1), "momentum": (8, 2), "energy": (9, 1), "phase": (10, 1), "quality": (11, 1),
           "D": (12, 4), "mu": (13, 1), "area": (20, 1), "centroid": (21, 2)}
 
-METHODS = {"jacobi_pcg": 0, "mixed_ir": 1, "learned_pcg": 2}
+METHODS = {"jacobi_pcg": 0, "mixed_ir": 1, "learned_pcg": 2, "minres": 3}
 
 
 class LvParams(C.Structure):
@@ -91,6 +91,9 @@ SIGNATURES = {
     "lv_solver_counters": (C.c_int, [_vp, _pi64, _pi64]),
     "lv_solver_unconverged": (C.c_int, [_vp, _pi64]),
     "lv_set_wait_limit": (C.c_int, [_vp, _i64]),
+    "lv_get_boundary_edges": (C.c_int, [_vp, _pi64, _pd, _pi32]),
+    "lv_find_pressure_edges": (C.c_int, [_vp, _d, _i32, _i64, _pd, _pst]),
+    "lv_bdary_friction_edges": (C.c_int, [_vp, _i64, _pd, C.POINTER(C.c_uint8), _d]),
     "lv_solver_halo": (C.c_int, [_vp, _pi32]),
     "lv_solver_forget": (C.c_int, [_vp]),
     "lv_mesh_captures": (C.c_int, [_vp, _pi32]),

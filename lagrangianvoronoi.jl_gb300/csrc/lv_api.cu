@@ -123,7 +123,7 @@ int sync_status(lv_ctx* c) {
   if (flags & LV_FLAG_BARRIER_TIMEOUT) {
     // a solver launch stopped part-way: its synchronisation words start
     // afresh, and the sweeps' history (partly written) is dropped
-    c->fcg_reset = c->big_reset = true;
+    c->fcg_reset = c->big_reset = c->mr_reset = true;
     c->sg_valid = 0;
   }
   if (flags) {
@@ -722,7 +722,7 @@ int lv_relaxation_step(lv_ctx* c, double dt, int32_t rusanov) {
 
 int lv_set_solver(lv_ctx* c, int32_t method, double tol, int32_t itmax) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
-  if (method < LV_METHOD_JACOBI_PCG || method > LV_METHOD_LEARNED_PCG || !(tol > 0) || itmax <= 0)
+  if (method < LV_METHOD_JACOBI_PCG || method > LV_METHOD_MINRES || !(tol > 0) || itmax <= 0)
     return lv_fail(c, LV_ERR_BAD_ARGUMENT, "lv_set_solver: bad method, tol or itmax");
   c->method = method;
   c->tol = tol;
@@ -742,14 +742,48 @@ int lv_pressure_rhs(lv_ctx* c, double dt, int32_t gp_step, const double* vbc) {
   return lv_phys_rhs(c, dt, gp_step, vbc, 1);
 }
 
+static int find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats);
+
 int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
   if (!c || niter < 0 || niter > 31) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 31]");
+  c->rhs_bvel = nullptr;
+  return find_pressure(c, dt, niter, vbc, stats);
+}
+
+int lv_find_pressure_edges(lv_ctx* c, double dt, int32_t niter, int64_t nb, const double* vb, lv_solve_stats* stats) {
+  if (!c || niter < 0 || niter > 31) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "niter must be in [0, 31]");
+  if (int rc = lv_bnd_upload(c, nb, vb, nullptr)) return rc;
+  c->rhs_bvel = c->bnd_vel;  // read by the first sweep's right-hand side preparation
+  const int rc = find_pressure(c, dt, niter, nullptr, stats);
+  c->rhs_bvel = nullptr;
+  return rc;
+}
+
+int lv_get_boundary_edges(lv_ctx* c, int64_t* nb, double* mid, int32_t* label) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  if (int rc = lv_bnd_prepare(c)) return rc;
+  if (nb) *nb = c->bnd_count;
+  if (!mid && !label) return LV_OK;
+  return lv_bnd_list(c, mid, label);
+}
+
+int lv_bdary_friction_edges(lv_ctx* c, int64_t nb, const double* vb, const uint8_t* active, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  if (int rc = lv_bnd_upload(c, nb, vb, active)) return rc;
+  return lv_phys_friction(c, nullptr, dt, c->bnd_vel, active ? c->bnd_act : nullptr);
+}
+
+static int find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_solve_stats* stats) {
   Timer t(c, 2);
   c->sg_pending = false;  // a start queued by a call that failed is void
   int rc = lv_solver_assemble(c, dt);
   if (rc) return rc;
   SolverDev& sv = c->sv;
-  if (c->sweep_guess && niter > sv.dinc_slots) {
+  // MINRES is the reference's solve, warm-started from P as the reference
+  // does (pressure.jl:219); the Galerkin start serves the CG methods
+  const bool guess = c->sweep_guess && c->method != LV_METHOD_MINRES;
+  if (guess && niter > sv.dinc_slots) {
     // one FP32 vector per sweep for the sweeps' changes (kept for the next call)
     cudaFree(sv.dinc);
     sv.dinc = nullptr;
@@ -759,14 +793,14 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
       return lv_fail(c, LV_ERR_CUDA, "allocation of the sweep-guess history failed");
     sv.dinc_slots = niter;
   }
-  if (c->sg_n != c->n) c->sg_valid = 0;
+  if (c->sg_n != c->n || !guess) c->sg_valid = 0;
   const size_t cap = (size_t)c->cap;
   for (int it = 1; it <= niter; ++it) {
     // the previous call's change of this sweep, while it is still there
-    const float* D = (c->sweep_guess && it <= c->sg_valid) ? sv.dinc + (size_t)(it - 1) * cap : nullptr;
-    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1, c->sweep_guess ? 1 : 0, D);
+    const float* D = (guess && it <= c->sg_valid) ? sv.dinc + (size_t)(it - 1) * cap : nullptr;
+    rc = lv_phys_rhs(c, dt, it > 1, vbc, it == 1, guess ? 1 : 0, D);
     if (rc) return rc;
-    if (c->sweep_guess) {
+    if (guess) {
       KernelTimer kt(c, LV_KF_RHS);  // prepares the sweep's system, like the right-hand side
       // this call's change of the previous sweep replaces the old one
       float* store = it >= 2 ? sv.dinc + (size_t)(it - 2) * cap : nullptr;
@@ -776,7 +810,7 @@ int lv_find_pressure(lv_ctx* c, double dt, int32_t niter, const double* vbc, lv_
     rc = lv_solver_solve(c, c->s.P, nullptr, it - 1);
     if (rc) return rc;
   }
-  if (c->sweep_guess && niter >= 1) {
+  if (guess && niter >= 1) {
     KernelTimer kt(c, LV_KF_RHS);
     rc = lv_solver_sweep_store(c, c->s.P, sv.dinc + (size_t)(niter - 1) * cap);
     if (rc) return rc;

@@ -1374,22 +1374,25 @@ __device__ __forceinline__ double big_res64(const BigArgs& a, int i, double bi) 
   return bi - acc;
 }
 
-// Row i of u = M^-1 r: md_i r_i + the row's slots in order, BIG_SB at a time
-// (the count and the first chunk loaded together: M^-1 has MMAX slots per
-// row, so the chunk lies inside its arrays whatever the count).
+// Row i of u = M^-1 r: md_i r_i + the row's slots in order, BIG_SB at a time.
+// The slot loads wait for the row's count and stop at its last slot (a
+// speculative chunk past the count cost more DRAM traffic than the round
+// trip it saves: M^-1 rows have about 18 entries, so whole unused slot lines
+// were fetched).
 __device__ __forceinline__ float big_mrow(const BigArgs& a, int i, const float* __restrict__ r) {
-  const int mc = ld_nc(a.mcnt + i);
-  float acc = ld_nc(a.mdiag + i) * __ldcg(r + i);
-  for (int k0 = 0; k0 == 0 || k0 < mc; k0 += BIG_SB) {
+  const int mc = a.mcnt[i];
+  float acc = a.mdiag[i] * __ldcg(r + i);
+  for (int k0 = 0; k0 < mc; k0 += BIG_SB) {
     int jj[BIG_SB];
     float mv[BIG_SB], rv[BIG_SB];
 #pragma unroll
     for (int q = 0; q < BIG_SB; ++q) {
-      jj[q] = ld_nc(a.mcol + (size_t)(k0 + q) * a.mstride + i);
-      mv[q] = ld_nc(a.mval + (size_t)(k0 + q) * a.mstride + i);
+      const size_t e = (size_t)min(k0 + q, mc - 1) * a.mstride + i;
+      jj[q] = ld_nc(a.mcol + e);
+      mv[q] = ld_nc(a.mval + e);
     }
 #pragma unroll
-    for (int q = 0; q < BIG_SB; ++q) rv[q] = __ldcg(r + (k0 + q < mc ? jj[q] : i));
+    for (int q = 0; q < BIG_SB; ++q) rv[q] = __ldcg(r + jj[q]);
 #pragma unroll
     for (int q = 0; q < BIG_SB; ++q)
       if (k0 + q < mc) acc = fmaf(mv[q], rv[q], acc);
@@ -1574,6 +1577,215 @@ __global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
     a.out_d[1] = bnorm2;
     a.out_d[2] = rtrue2;
     count_solve(a.counters, it, rtrue2, bnorm2, rtrue2, a.tol2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// MINRES (Paige & Saunders, SIAM J. Numer. Anal. 12, 1975) in FP64 without a
+// preconditioner: the reference's default pressure solve, Krylov.jl's
+// minres! with atol = rtol = tol (pressure.jl:219-220).  The recurrences and
+// stopping tests are the oracle's restatement's: phibar = ||r|| <= atol +
+// rtol ||r0||, or ||A r|| / (||A|| ||r||) <= rtol (an inconsistent singular
+// system), or a Lanczos breakdown (beta = 0).  A persistent kernel over the
+// operator's CSR; each iteration makes two passes, each ending in a
+// grid-wide phase (alpha = (v, y), then beta^2 = (y, y)), and one pass over
+// the own rows for the direction and the iterate.  The Lanczos vector v =
+// y / beta of a neighbour is formed from its y where it is gathered, so no
+// neighbour exchange is needed; the scalar recurrences run once per block.
+// ---------------------------------------------------------------------------
+constexpr int MR_TPB = 1024;
+constexpr int MR_EB = 4;  // entries loaded together
+
+struct MinresArgs {
+  int n, nb, rpb;
+  const int* rowptr;
+  const int* col;
+  const double* w;
+  const double* diag;
+  const double* b;
+  double* x;
+  double* lz[2];  // the Lanczos vectors r1, r2 (roles swap every iteration)
+  double* dw[3];  // the directions w, w1, w2 (roles rotate every iteration)
+  unsigned long long* slots;
+  unsigned* counter;
+  unsigned* sync_base;
+  int* status;
+  long long spin;
+  double atol, rtol, tol2;
+  int itmax;
+  int* out_iters;
+  int* out_solved;
+  int* out_method;
+  double* out_d;
+  long long* counters;
+};
+
+// (diag_i v_i + sum_e w_e (v_i - v_j)) with v = sc * src, the entries in
+// order, MR_EB loads at a time
+__device__ __forceinline__ double mr_apply(const MinresArgs& a, int i, const double* src, double sc, double vi) {
+  const int e0 = a.rowptr[i], e1 = a.rowptr[i + 1];
+  double acc = a.diag[i] * vi;
+  for (int b0 = e0; b0 < e1; b0 += MR_EB) {
+    int j[MR_EB];
+    double wv[MR_EB], xv[MR_EB];
+#pragma unroll
+    for (int q = 0; q < MR_EB; ++q) {
+      const int e = min(b0 + q, e1 - 1);
+      j[q] = ld_nc(a.col + e);
+      wv[q] = ld_nc(a.w + e);
+    }
+#pragma unroll
+    for (int q = 0; q < MR_EB; ++q) xv[q] = sc * __ldcg(src + j[q]);
+#pragma unroll
+    for (int q = 0; q < MR_EB; ++q)
+      if (b0 + q < e1) acc += wv[q] * (vi - xv[q]);
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(MR_TPB, 1) k_minres(MinresArgs a) {
+  const int n = a.n, t = threadIdx.x;
+  const int rb0 = blockIdx.x * a.rpb, rb1 = min(n, rb0 + a.rpb);
+  if (t == 0) {
+    s_base[0] = __ldcg(a.sync_base);
+    s_base[1] = __ldcg(a.sync_base + 1);
+  }
+  __syncthreads();
+  unsigned ep = 0;
+  // the scalar recurrences, formed by thread 0 of every block from the
+  // phases' totals (bit-identical in all blocks, so all take the same exits)
+  __shared__ double sc[16];
+  enum { BETA, OLDB, DBAR, EPSLN, PHIBAR, CS, SN, TNORM2, S, ALFA, PHI, DENOM, OLDEPS, DELTA, TOL, BB };
+  __shared__ int s_stop;
+  // r1 = b - A x (x as given), r2 = r1, w = w2 = 0; beta1 = ||r1||
+  double* R1 = a.lz[0];
+  double* R2 = a.lz[1];
+  double v2[2] = {0.0, 0.0}, t2[2];
+  for (int i = rb0 + t; i < rb1; i += MR_TPB) {
+    const double xi = __ldcg(a.x + i);
+    const double bi = a.b[i];
+    const double r = bi - mr_apply(a, i, a.x, 1.0, xi);
+    R1[i] = r;
+    R2[i] = r;
+    a.dw[0][i] = 0.0;
+    a.dw[2][i] = 0.0;
+    v2[0] += r * r;
+    v2[1] += bi * bi;
+  }
+  bool ok = fphase<2, double>(a, ++ep, v2, t2);
+  if (t == 0) {
+    const double beta1 = sqrt(t2[0]);
+    sc[BETA] = beta1;
+    sc[OLDB] = 0.0;
+    sc[DBAR] = 0.0;
+    sc[EPSLN] = 0.0;
+    sc[PHIBAR] = beta1;
+    sc[CS] = -1.0;
+    sc[SN] = 0.0;
+    sc[TNORM2] = 0.0;
+    sc[TOL] = a.atol + a.rtol * beta1;
+    sc[BB] = t2[1];
+    s_stop = beta1 == 0.0 ? 2 : 0;  // 2: solved
+  }
+  __syncthreads();
+  int itn = 0;
+  int wi = 0;  // w = dw[wi], w1 = dw[(wi + 1) % 3], w2 = dw[(wi + 2) % 3] before the rotation
+  while (ok && s_stop == 0 && itn < a.itmax) {
+    ++itn;
+    const double beta = sc[BETA], oldb = sc[OLDB];
+    if (t == 0) sc[S] = 1.0 / beta;
+    __syncthreads();
+    const double s = sc[S];
+    // y = A v - (beta / oldb) r1 with v = s r2 (the neighbours' v from their r2)
+    const double c1 = itn >= 2 ? beta / oldb : 0.0;
+    double va[1] = {0.0}, ta[1];
+    for (int i = rb0 + t; i < rb1; i += MR_TPB) {
+      const double vi = s * __ldcg(R2 + i);
+      double y = mr_apply(a, i, R2, s, vi);
+      if (itn >= 2) y -= c1 * R1[i];
+      R1[i] = y;
+      va[0] += vi * y;
+    }
+    if (!(ok = fphase<1, double>(a, ++ep, va, ta))) break;
+    // y -= (alfa / beta) r2; then r1 <- r2, r2 <- y; beta^2 = (y, y)
+    const double c2 = ta[0] / beta;
+    double vb[1] = {0.0}, tb[1];
+    for (int i = rb0 + t; i < rb1; i += MR_TPB) {
+      const double y = R1[i] - c2 * R2[i];
+      R1[i] = y;
+      vb[0] += y * y;
+    }
+    if (!(ok = fphase<1, double>(a, ++ep, vb, tb))) break;
+    if (t == 0) {
+      const double eps = 2.220446049250313e-16;
+      const double alfa = ta[0];
+      const double ob = beta;
+      const double nb = sqrt(tb[0]);
+      sc[OLDB] = ob;
+      sc[BETA] = nb;
+      sc[TNORM2] += alfa * alfa + ob * ob + nb * nb;
+      const double oldeps = sc[EPSLN];
+      const double delta = sc[CS] * sc[DBAR] + sc[SN] * alfa;
+      const double gbar = sc[SN] * sc[DBAR] - sc[CS] * alfa;
+      sc[EPSLN] = sc[SN] * nb;
+      sc[DBAR] = -sc[CS] * nb;
+      const double root = sqrt(gbar * gbar + sc[DBAR] * sc[DBAR]);
+      const double gamma = fmax(sqrt(gbar * gbar + nb * nb), eps);
+      sc[CS] = gbar / gamma;
+      sc[SN] = nb / gamma;
+      sc[PHI] = sc[CS] * sc[PHIBAR];
+      sc[PHIBAR] = sc[SN] * sc[PHIBAR];
+      sc[DENOM] = 1.0 / gamma;
+      sc[OLDEPS] = oldeps;
+      sc[DELTA] = delta;
+      const double rnorm = sc[PHIBAR], anorm = sqrt(sc[TNORM2]), arnorm = sc[PHIBAR] * root;
+      int st = 0;
+      if (rnorm <= sc[TOL]) st = 2;
+      else if (anorm > 0 && rnorm > 0 && arnorm / (anorm * rnorm) <= a.rtol) st = 2;
+      else if (nb == 0.0) st = 2;
+      s_stop = st;
+    }
+    __syncthreads();
+    // w1 <- w2, w2 <- w, w = (v - oldeps w1 - delta w2) denom; x += phi w,
+    // with v = s r2 (r2 before its swap below)
+    wi = (wi + 1) % 3;
+    double* Wn = a.dw[wi];             // the new w (the old w1's buffer)
+    double* Wm1 = a.dw[(wi + 1) % 3];  // w1: the old w2
+    double* Wm2 = a.dw[(wi + 2) % 3];  // w2: the old w
+    const double phi = sc[PHI], denom = sc[DENOM], oldeps = sc[OLDEPS], delta = sc[DELTA];
+    for (int i = rb0 + t; i < rb1; i += MR_TPB) {
+      const double vi = s * R2[i];
+      const double wv = (vi - oldeps * Wm1[i] - delta * Wm2[i]) * denom;
+      Wn[i] = wv;
+      a.x[i] += phi * wv;
+    }
+    // r1 <- r2, r2 <- y
+    double* tmp = R1;
+    R1 = R2;
+    R2 = tmp;
+  }
+  // the true residual of the final iterate
+  double vr[1] = {0.0}, tr[1] = {0.0};
+  if (ok) {
+    for (int i = rb0 + t; i < rb1; i += MR_TPB) {
+      const double xi = a.x[i];
+      const double r = a.b[i] - mr_apply(a, i, a.x, 1.0, xi);
+      vr[0] += r * r;
+    }
+    ok = fphase<1, double>(a, ++ep, vr, tr);
+  }
+  if (ok && blockIdx.x == 0 && t == 0) {
+    a.sync_base[0] = s_base[0] + ep * (unsigned)a.nb;
+    const int solved = s_stop == 2 ? 1 : 0;
+    *a.out_iters = itn;
+    *a.out_solved = solved;
+    *a.out_method = LV_METHOD_MINRES;
+    a.out_d[0] = tr[0];
+    a.out_d[1] = sc[BB];
+    a.out_d[2] = tr[0];
+    a.counters[0] += 1;
+    a.counters[1] += itn;
+    if (!solved) a.counters[2] += 1;
   }
 }
 
@@ -1985,6 +2197,72 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
   if (e != cudaSuccess) {
     c->big_reset = true;
     return lv_cuda_check(c, e, "k_big cooperative launch");
+  }
+  return LV_OK;
+}
+
+// ------------------------------------------------------------------ MINRES
+
+int lv_minres_solve(lv_ctx* c, double* x, int slot) {
+  SolverDev& sv = c->sv;
+  const int n = c->n;
+  static std::once_flag once;
+  static int per_sm = 0;
+  std::call_once(once, []() {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_minres, MR_TPB, 0) != cudaSuccess) per_sm = 0;
+  });
+  if (per_sm < 1) return lv_fail(c, LV_ERR_CUDA, "the MINRES kernel does not fit an SM");
+  if (!sv.mrvec) {
+    bool ok = true;
+    sv.mrvec = big_alloc<double>(c, 5 * (size_t)c->cap, &ok);
+    sv.mrsync = big_alloc<unsigned>(c, BIG_SLOT_OFF + 2 * RG_WORDS * FCG_MAX_BLOCKS, &ok);
+    if (!ok) {
+      sv.mrvec = nullptr;
+      return lv_fail(c, LV_ERR_CUDA, "allocation of the MINRES vectors failed");
+    }
+    c->mr_reset = true;
+  }
+  const int nb = std::max(1, std::min(std::min(c->num_sms, FCG_MAX_BLOCKS), lv_blocks(n, 64)));
+  MinresArgs a;
+  a.n = n;
+  a.nb = nb;
+  a.rpb = (n + nb - 1) / nb;
+  a.rowptr = sv.rowptr;
+  a.col = sv.col;
+  a.w = sv.w;
+  a.diag = sv.diag;
+  a.b = sv.b;
+  a.x = x;
+  const size_t cap = (size_t)c->cap;
+  a.lz[0] = sv.mrvec;
+  a.lz[1] = sv.mrvec + cap;
+  a.dw[0] = sv.mrvec + 2 * cap;
+  a.dw[1] = sv.mrvec + 3 * cap;
+  a.dw[2] = sv.mrvec + 4 * cap;
+  a.counter = sv.mrsync;
+  a.sync_base = sv.mrsync + 1;
+  a.slots = reinterpret_cast<unsigned long long*>(sv.mrsync + BIG_SLOT_OFF);
+  a.status = c->status;
+  a.spin = c->spin_limit;
+  a.atol = c->tol;
+  a.rtol = c->tol;
+  a.tol2 = c->tol * c->tol;
+  a.itmax = c->itmax;
+  a.out_iters = sv.iters + slot;
+  a.out_solved = sv.iters + LV_IT_OUTER + slot;
+  a.out_method = sv.iters + LV_IT_METHOD + slot;
+  a.out_d = sv.dstats + 3 * slot;
+  a.counters = sv.counters;
+  if (c->mr_reset) {
+    cudaMemsetAsync(sv.mrsync, 0, sizeof(unsigned) * (BIG_SLOT_OFF + 2 * RG_WORDS * FCG_MAX_BLOCKS), c->stream);
+    c->mr_reset = false;
+  }
+  void* args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_minres, dim3(nb), dim3(MR_TPB), args, 0, c->stream);
+  c->launches++;
+  if (e != cudaSuccess) {
+    c->mr_reset = true;
+    return lv_cuda_check(c, e, "k_minres cooperative launch");
   }
   return LV_OK;
 }

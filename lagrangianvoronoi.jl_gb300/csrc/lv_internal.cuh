@@ -244,6 +244,10 @@ struct SolverDev {
   double* br64 = nullptr;
   unsigned* bmasks = nullptr;
   unsigned* bsync = nullptr;
+  // MINRES (lv_fcg.cu k_minres, allocated on first use): r1, r2, w, w1, w2
+  // and its synchronisation words
+  double* mrvec = nullptr;
+  unsigned* mrsync = nullptr;
 };
 
 struct LearnState;  // learned preconditioner (lv_learn.cu)
@@ -265,9 +269,9 @@ struct lv_ctx {
   SolverDev sv{};
   int* status = nullptr;      // device status word
   int* status_host = nullptr; // pinned
-  int method = LV_METHOD_JACOBI_PCG;
-  double tol = 1e-8;
-  int itmax = 10000;
+  int method = LV_METHOD_MINRES;  // the reference's PressureSolver (pressure.jl:142-159, 219)
+  double tol = 1e-6;
+  int itmax = 1000;
   bool op_ready = false;
   double* mp_buf = nullptr;  // multiphase projection vectors (allocated on first use)
   LearnState* learn = nullptr;
@@ -287,11 +291,23 @@ struct lv_ctx {
   long long spin_limit = LV_WAIT_LIMIT_DEFAULT;  // cycles a solver waits on other blocks (lv_set_wait_limit)
   int clip_slots = 0;      // first clipping pass's edge slots (0: the default; LVGPU_CLIP_SLOTS)
   bool big_reset = true;   // the same for the streaming solver's
+  bool mr_reset = true;    // the same for MINRES's
   bool big_masks_valid = false;  // its neighbour masks match the operator
   bool big_masks_m = false;      // and cover M^-1's pattern
   bool flen_valid = false;  // m.flen belongs to the current mesh
   bool ccount_clean = false;  // the cell counts are zero (cleared by the last completed order pass)
   void* clip_resume = nullptr;  // captures of the first clipping pass (cap entries, allocated on first use)
+  // boundary edges of the current mesh: per-polygon counts and offsets, the
+  // count, room for per-edge values (velocity, charfun flag, label)
+  int* bnd_cnt = nullptr;
+  int* bnd_off = nullptr;
+  int bnd_count = 0;
+  int bnd_room = 0;
+  bool bnd_valid = false;
+  double2* bnd_vel = nullptr;
+  unsigned char* bnd_act = nullptr;
+  int* bnd_lab = nullptr;
+  const double2* rhs_bvel = nullptr;  // per-edge boundary velocities of the running lv_find_pressure_edges
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
@@ -474,7 +490,15 @@ int lv_phys_gravity(lv_ctx* c, double gx, double gy, double dt);
 int lv_phys_pressure_step(lv_ctx* c, double dt);
 int lv_phys_find_D(lv_ctx* c);
 int lv_phys_viscous(lv_ctx* c, double dt, int av);
-int lv_phys_friction(lv_ctx* c, const double* vwall, double dt);
+// vwall: the label table (bvel null) or ignored; bvel/act: per boundary edge
+// (lv_bnd_upload), act may be null
+int lv_phys_friction(lv_ctx* c, const double* vwall, double dt, const double2* bvel = nullptr,
+                     const unsigned char* act = nullptr);
+// boundary edges of the current mesh (lv_physics.cu): offsets (once per mesh,
+// synchronises), the list of midpoints and labels, per-edge values
+int lv_bnd_prepare(lv_ctx* c);
+int lv_bnd_list(lv_ctx* c, double* mid, int* lab);
+int lv_bnd_upload(lv_ctx* c, int64_t nb, const double* vb, const unsigned char* act);
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
 // prepare = 1 evaluates the sweep-invariant terms (first sweep of find_pressure!)
@@ -513,6 +537,8 @@ void lv_fcg_free(lv_ctx* c);
 // streaming solver of systems above lv_fcg_capacity (same methods)
 int lv_big_prepare(lv_ctx* c);  // allocations; called before the assembly of such a system
 int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned);
+// MINRES without a preconditioner (LV_METHOD_MINRES), any size
+int lv_minres_solve(lv_ctx* c, double* x, int slot);
 
 #define LV_LAUNCH_CHECK(c, what)                                   \
   do {                                                             \

@@ -983,6 +983,7 @@ int lv_mesh_remesh(lv_ctx* c) {
   const int n = c->n;
   if (n <= 0) return lv_fail(c, LV_ERR_NOT_MESHED, "remesh: no particles");
   c->flen_valid = false;
+  c->bnd_valid = false;
   cudaStream_t s = c->stream;
   const int nc = c->c.ncells;
   {

@@ -152,7 +152,11 @@ __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n
 //   te  = dot(dS, vbc - v_i)/dt                 per boundary edge
 // and k_rhs / k_rhs_gp subtract or add them in the reference's order, so b and
 // GP are bit-identical to evaluating refresh! in full every sweep.
-__global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, Wall2 vbc_ud, Wall2 vbc_rl) {
+// Boundary velocities come from the label table, or per boundary edge (bvel,
+// the edges of polygon i from boff[i] on, in its edge order) when bvel is set.
+__global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, Wall2 vbc_ud,
+                                                     Wall2 vbc_rl, const double2* __restrict__ bvel,
+                                                     const int* __restrict__ boff) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
@@ -190,6 +194,7 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
     }
   }
   if (nf < ne) {
+    int jb = bvel ? boff[i] : 0;
     for (int k = 0; k < ne; ++k) {
       const size_t f = (size_t)k * cap + i;
       const int lab = m.elab[f];
@@ -197,11 +202,17 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
       const double2 a = m.ev1[f], b = m.ev2[f];
       const double dSx = a.y - b.y, dSy = b.x - a.x;
       double wx, wy;
-      switch (lab) {
-        case LV_BDARY_UP: wx = vbc_ud.x; wy = vbc_ud.y; break;
-        case LV_BDARY_RIGHT: wx = vbc_rl.x; wy = vbc_rl.y; break;
-        case LV_BDARY_DOWN: wx = vbc_ud.z; wy = vbc_ud.w; break;
-        default: wx = vbc_rl.z; wy = vbc_rl.w; break;
+      if (bvel) {
+        const double2 wv = bvel[jb++];
+        wx = wv.x;
+        wy = wv.y;
+      } else {
+        switch (lab) {
+          case LV_BDARY_UP: wx = vbc_ud.x; wy = vbc_ud.y; break;
+          case LV_BDARY_RIGHT: wx = vbc_rl.x; wy = vbc_rl.y; break;
+          case LV_BDARY_DOWN: wx = vbc_ud.z; wy = vbc_ud.w; break;
+          default: wx = vbc_rl.z; wy = vbc_rl.w; break;
+        }
       }
       sv.rhs_te[f] = (dSx * (wx - vi.x) + dSy * (wy - vi.y)) / dt;
     }
@@ -469,8 +480,12 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n,
   s.e[i] = ei;
 }
 
-// bdary_friction! (diffusion.jl:64-79) with a constant wall velocity per label.
-__global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, Wall2 w_rl) {
+// bdary_friction! (diffusion.jl:64-79): the wall velocity from the label
+// table, or per boundary edge (bvel from boff[i], as in k_rhs_prep) with the
+// edges whose act is 0 skipped (charfun; act may be null).
+__global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, Wall2 w_rl,
+                           const double2* __restrict__ bvel, const int* __restrict__ boff,
+                           const unsigned char* __restrict__ act) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
@@ -483,10 +498,13 @@ __global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, 
   double tmp = 1.0;
   double2 vi = s.v[i];
   double ei = s.e[i];
+  int jb = bvel ? boff[i] : 0;
   for (int k = 0; k < ne; ++k) {
     const size_t f = (size_t)k * cap + i;
     const int lab = m.elab[f];
     if (lab >= 0) continue;
+    const int q = jb++;
+    if (bvel && act && !act[q]) continue;  // if !charfun(m) continue end
     const double2 a = m.ev1[f], b = m.ev2[f];
     const double mx = 0.5 * (a.x + b.x), my = 0.5 * (a.y + b.y);
     const double nx0 = a.y - b.y, ny0 = b.x - a.x;
@@ -496,11 +514,16 @@ __global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, 
     const double len = sqrt(lx * lx + ly * ly);
     const double lrr = len / fabs((mx - xi.x) * nx + (my - xi.y) * ny);
     double wx, wy;
-    switch (lab) {
-      case LV_BDARY_UP: wx = w_ud.x; wy = w_ud.y; break;
-      case LV_BDARY_RIGHT: wx = w_rl.x; wy = w_rl.y; break;
-      case LV_BDARY_DOWN: wx = w_ud.z; wy = w_ud.w; break;
-      default: wx = w_rl.z; wy = w_rl.w; break;
+    if (bvel) {
+      wx = bvel[q].x;
+      wy = bvel[q].y;
+    } else {
+      switch (lab) {
+        case LV_BDARY_UP: wx = w_ud.x; wy = w_ud.y; break;
+        case LV_BDARY_RIGHT: wx = w_rl.x; wy = w_rl.y; break;
+        case LV_BDARY_DOWN: wx = w_ud.z; wy = w_ud.w; break;
+        default: wx = w_rl.z; wy = w_rl.w; break;
+      }
     }
     const double fx = mu * lrr * wx / mi, fy = mu * lrr * wy / mi;
     tmp += dt * mu * lrr / mi;
@@ -846,7 +869,8 @@ int lv_phys_rhs(lv_ctx* c, double dt, int gp_step, const double* vbc, int prepar
     // vbc[4][2] indexed by -label-1: UP, RIGHT, DOWN, LEFT
     const Wall2 ud{w[0], w[1], w[4], w[5]};
     const Wall2 rl{w[2], w[3], w[6], w[7]};
-    LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl);
+    LAUNCH_F(LV_KF_RHS, k_rhs_prep, c->s, c->m, c->sv, c->n, dt, ud, rl, c->rhs_bvel,
+             c->rhs_bvel ? c->bnd_off : nullptr);
   }
   static_assert(TPB == LV_SG_TPB, "the sweep-guess sums assume 256 threads per block");
   // the guess sums ride on the second pass (sweeps >= 2), on the first pass
@@ -874,15 +898,102 @@ int lv_phys_viscous(lv_ctx* c, double dt, int av) {
   return LV_OK;
 }
 
-int lv_phys_friction(lv_ctx* c, const double* vwall, double dt) {
+int lv_phys_friction(lv_ctx* c, const double* vwall, double dt, const double2* bvel, const unsigned char* act) {
   if (int rc = need_mesh(c)) return rc;
   double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (vwall)
     for (int k = 0; k < 8; ++k) w[k] = vwall[k];
   const Wall2 ud{w[0], w[1], w[4], w[5]};
   const Wall2 rl{w[2], w[3], w[6], w[7]};
-  LAUNCH(k_friction, c->s, c->m, c->n, dt, ud, rl);
+  LAUNCH(k_friction, c->s, c->m, c->n, dt, ud, rl, bvel, bvel ? c->bnd_off : nullptr, act);
   return LV_OK;
+}
+
+// ------------------------------------------------------ boundary edges
+//
+// The boundary edges of the current mesh in the order of boundaries(p)
+// (iterators.jl:46-57) over the polygons: polygon i's edges start at
+// bnd_off[i] (a scan of the per-polygon counts, built once per mesh).
+
+__global__ void k_bnd_count(MeshDev m, int n, int* cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cnt[i] = m.nedges[i] - m.nfaces[i];
+}
+
+__global__ void k_bnd_list(MeshDev m, int n, const int* __restrict__ off, double2* mid, int* lab) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, ne = m.nedges[i];
+  int q = off[i];
+  for (int k = 0; k < ne; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int l = m.elab[f];
+    if (l >= 0) continue;
+    const double2 a = m.ev1[f], b = m.ev2[f];
+    mid[q] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));  // midpoint(e), geometry.jl:145-147
+    lab[q] = l;
+    ++q;
+  }
+}
+
+// Offsets and count of the current mesh's boundary edges (synchronises once
+// per mesh) and room for per-edge values.
+int lv_bnd_prepare(lv_ctx* c) {
+  if (int rc = need_mesh(c)) return rc;
+  if (c->bnd_valid) return LV_OK;
+  const int n = c->n;
+  if (!c->bnd_off) {
+    if (cudaMalloc(&c->bnd_off, sizeof(int) * ((size_t)c->cap + 1)) != cudaSuccess ||
+        cudaMalloc(&c->bnd_cnt, sizeof(int) * (size_t)c->cap) != cudaSuccess)
+      return lv_fail(c, LV_ERR_CUDA, "allocation of the boundary-edge offsets failed");
+    c->allocs.push_back(c->bnd_off);
+    c->allocs.push_back(c->bnd_cnt);
+  }
+  k_bnd_count<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(c->m, n, c->bnd_cnt);
+  LV_LAUNCH_CHECK(c, "k_bnd_count");
+  if (int rc = lv_scan_int(c, c->bnd_cnt, c->bnd_off, n)) return rc;
+  int total = 0;
+  cudaMemcpyAsync(&total, c->bnd_off + n, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (int rc = lv_cuda_check(c, cudaStreamSynchronize(c->stream), "boundary edges")) return rc;
+  if (total > c->bnd_room) {
+    cudaFree(c->bnd_vel);
+    cudaFree(c->bnd_act);
+    cudaFree(c->bnd_lab);
+    c->bnd_vel = nullptr;
+    c->bnd_act = nullptr;
+    c->bnd_lab = nullptr;
+    c->bnd_room = 0;
+    const size_t room = (size_t)total + 1024;
+    if (cudaMalloc(&c->bnd_vel, sizeof(double2) * room) != cudaSuccess ||
+        cudaMalloc(&c->bnd_act, room) != cudaSuccess || cudaMalloc(&c->bnd_lab, sizeof(int) * room) != cudaSuccess)
+      return lv_fail(c, LV_ERR_CUDA, "allocation of the boundary-edge values failed");
+    c->bnd_room = (int)room;
+  }
+  c->bnd_count = total;
+  c->bnd_valid = true;
+  return LV_OK;
+}
+
+int lv_bnd_list(lv_ctx* c, double* mid, int* lab) {
+  if (int rc = lv_bnd_prepare(c)) return rc;
+  const int nb = c->bnd_count;
+  if (nb == 0) return LV_OK;
+  k_bnd_list<<<lv_blocks(c->n, TPB), TPB, 0, c->stream>>>(c->m, c->n, c->bnd_off, c->bnd_vel, c->bnd_lab);
+  LV_LAUNCH_CHECK(c, "k_bnd_list");
+  if (mid) cudaMemcpyAsync(mid, c->bnd_vel, sizeof(double2) * nb, cudaMemcpyDeviceToHost, c->stream);
+  if (lab) cudaMemcpyAsync(lab, c->bnd_lab, sizeof(int) * nb, cudaMemcpyDeviceToHost, c->stream);
+  return lv_cuda_check(c, cudaStreamSynchronize(c->stream), "boundary edges");
+}
+
+// Uploads per-edge values (nb must be the current count); act may be null.
+int lv_bnd_upload(lv_ctx* c, int64_t nb, const double* vb, const unsigned char* act) {
+  if (int rc = lv_bnd_prepare(c)) return rc;
+  if (nb != c->bnd_count || (nb > 0 && !vb))
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "per-edge boundary values: nb is not the mesh's boundary-edge count");
+  if (nb == 0) return LV_OK;
+  cudaMemcpyAsync(c->bnd_vel, vb, sizeof(double2) * (size_t)nb, cudaMemcpyHostToDevice, c->stream);
+  if (act) cudaMemcpyAsync(c->bnd_act, act, (size_t)nb, cudaMemcpyHostToDevice, c->stream);
+  return lv_cuda_check(c, cudaGetLastError(), "boundary values upload");
 }
 
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha) {

@@ -664,12 +664,13 @@ int lv_solver_solve(lv_ctx* c, double* x, lv_solve_stats*, int slot) {
     c->factor_valid = true;
   }
   // a queued sweep start of x: the mixed-precision solvers apply it themselves
-  const bool fcg_path = c->method != LV_METHOD_JACOBI_PCG;
+  const bool fcg_path = c->method == LV_METHOD_MIXED_IR || c->method == LV_METHOD_LEARNED_PCG;
   if (c->sg_pending && (!fcg_path || c->sg_P != x)) {
     KernelTimer ks(c, LV_KF_RHS);
     if (int rc = lv_solver_flush_shift(c)) return rc;
   }
   KernelTimer kt(c, LV_KF_PCG);
+  if (c->method == LV_METHOD_MINRES) return lv_minres_solve(c, x, slot);
   if (c->method != LV_METHOD_JACOBI_PCG) {
     const bool learned = c->method == LV_METHOD_LEARNED_PCG;
     // systems that fit one or two blocks per SM: flag-reduced solver
@@ -721,9 +722,16 @@ int lv_solver_fetch_stats(lv_ctx* c, lv_solve_stats* out, int count) {
   for (int k = 0; k < count; ++k) {
     const double rr = d[3 * k], bb = d[3 * k + 1], tr = d[3 * k + 2];
     out[k].iterations = it[k];
-    out[k].converged = (rr <= c->tol * c->tol * bb) ? 1 : 0;
-    out[k].outer = c->method == LV_METHOD_JACOBI_PCG ? 0 : outer[k];
-    out[k].method = c->method == LV_METHOD_JACOBI_PCG ? c->method : meth[k];
+    if (c->method == LV_METHOD_MINRES) {
+      // MINRES's own stopping tests (absolute + relative, least squares)
+      out[k].converged = outer[k] != 0 ? 1 : 0;
+      out[k].outer = 0;
+      out[k].method = LV_METHOD_MINRES;
+    } else {
+      out[k].converged = (rr <= c->tol * c->tol * bb) ? 1 : 0;
+      out[k].outer = c->method == LV_METHOD_JACOBI_PCG ? 0 : outer[k];
+      out[k].method = c->method == LV_METHOD_JACOBI_PCG ? c->method : meth[k];
+    }
     out[k].rel_residual = bb > 0 ? sqrt(tr / bb) : sqrt(tr);
   }
   return LV_OK;

@@ -110,7 +110,24 @@ struct Grid {
   int sweep_n = 0;
   std::vector<V2> GP;
   int status = ST_OK;
+  // boundary closures evaluated per boundary edge by the caller (the order of
+  // boundaries(p) over the polygons, iterators.jl:46-57): velocity and
+  // charfun flag; used instead of the label table while edge_mode is set
+  bool edge_mode = false;
+  std::vector<V2> edge_vel;
+  std::vector<uint8_t> edge_act;
 };
+
+// first boundary edge of every polygon in the per-edge order
+std::vector<int64_t> boundary_offsets(const Grid& g) {
+  std::vector<int64_t> off(g.n + 1, 0);
+  for (int i = 0; i < g.n; ++i) {
+    int64_t c = 0;
+    for (const auto& e : g.edges[i]) c += e.label < 0 ? 1 : 0;
+    off[i + 1] = off[i] + c;
+  }
+  return off;
+}
 
 // ---------------------------------------------------------------- cell list
 
@@ -460,6 +477,7 @@ double bdot(const double* a, const double* b, int n) {
 // pressure.jl:162-203 — right-hand side, warm start and pressure gradient.
 // vbc[4][2] holds a constant wall velocity per boundary label (-1..-4).
 void refresh_rhs(Grid& g, double dt, bool gp_step, const double* vbc) {
+  const std::vector<int64_t> boff = g.edge_mode ? boundary_offsets(g) : std::vector<int64_t>();
   g.b.assign(g.n, 0.0);
   g.Psol.assign(g.n, 0.0);
   g.GP.assign(g.n, V2{0.0, 0.0});
@@ -476,11 +494,13 @@ void refresh_rhs(Grid& g, double dt, bool gp_step, const double* vbc) {
       bi -= (lrr / dt) * dot(g.v[i] - g.v[j], m - y);
       gp = gp - (lrr * (g.P[i] - g.P[j])) * (m - xi);
     });
+    int64_t q = g.edge_mode ? boff[i] : 0;
     for (const auto& e : g.edges[i]) {
       if (e.label >= 0) continue;
       V2 dS{e.v1.y - e.v2.y, e.v2.x - e.v1.x};
       int slot = (int)(-e.label - 1);
-      V2 wall = vbc ? V2{vbc[2 * slot], vbc[2 * slot + 1]} : V2{0.0, 0.0};
+      // vbc = boundary_velocity(midpoint(e), e.label) (pressure.jl:182)
+      V2 wall = g.edge_mode ? g.edge_vel[q++] : (vbc ? V2{vbc[2 * slot], vbc[2 * slot + 1]} : V2{0.0, 0.0});
       bi -= dot(dS, wall - g.v[i]) / dt;
     }
     g.b[i] = bi;
@@ -716,18 +736,23 @@ void find_D(Grid& g) {  // diffusion.jl:8-19
 
 // diffusion.jl:64-79 with a constant wall velocity per boundary label.
 void bdary_friction(Grid& g, const double* vwall, double dt) {
+  const std::vector<int64_t> boff = g.edge_mode ? boundary_offsets(g) : std::vector<int64_t>();
 #pragma omp parallel for
   for (int i = 0; i < g.n; ++i) {
     double tmp = 1.0;
     V2 vi = g.v[i];
     double ei = g.e[i];
+    int64_t q = g.edge_mode ? boff[i] : 0;
     for (const auto& e : g.edges[i]) {
       if (e.label >= 0) continue;
       V2 m = 0.5 * (e.v1 + e.v2);
+      const int64_t qe = q++;
+      if (g.edge_mode && !g.edge_act.empty() && !g.edge_act[qe]) continue;  // if !charfun(m) continue end
       V2 nv = normal_vector(e);
       double lrr = len(e) / std::fabs(dot(m - g.x[i], nv));
       int slot = (int)(-e.label - 1);
-      V2 wall{vwall[2 * slot], vwall[2 * slot + 1]};
+      // vDirichlet(m): per edge, or the label table
+      V2 wall = g.edge_mode ? g.edge_vel[qe] : V2{vwall[2 * slot], vwall[2 * slot + 1]};
       V2 f{g.mu[i] * lrr * wall.x / g.mass[i], g.mu[i] * lrr * wall.y / g.mass[i]};
       tmp += dt * g.mu[i] * lrr / g.mass[i];
       ei += dt * dot(f, vi);
@@ -1126,6 +1151,38 @@ int lvref_pressure_step(void* h, double dt) { pressure_step(*static_cast<Grid*>(
 int lvref_find_D(void* h) { find_D(*static_cast<Grid*>(h)); return 0; }
 int lvref_viscous_step(void* h, double dt, int av) { viscous_step(*static_cast<Grid*>(h), dt, av != 0); return 0; }
 int lvref_bdary_friction(void* h, const double* vwall, double dt) { bdary_friction(*static_cast<Grid*>(h), vwall, dt); return 0; }
+
+// The boundary edges in the per-edge order: midpoints mid[nb][2] =
+// midpoint(e) and labels; returns nb (arrays filled when cap >= nb).
+int64_t lvref_boundary_edges(void* h, double* mid, int32_t* lab, int64_t cap) {
+  Grid* g = static_cast<Grid*>(h);
+  int64_t q = 0;
+  for (int i = 0; i < g->n; ++i)
+    for (const auto& e : g->edges[i]) {
+      if (e.label >= 0) continue;
+      if (q < cap) {
+        const V2 m = 0.5 * (e.v1 + e.v2);
+        if (mid) {
+          mid[2 * q] = m.x;
+          mid[2 * q + 1] = m.y;
+        }
+        if (lab) lab[q] = (int32_t)e.label;
+      }
+      ++q;
+    }
+  return q;
+}
+
+// Per-edge boundary values for refresh_rhs and bdary_friction (vb NULL: back
+// to the label table); act may be NULL (every edge).
+int lvref_set_edge_values(void* h, int64_t nb, const double* vb, const uint8_t* act) {
+  Grid* g = static_cast<Grid*>(h);
+  g->edge_mode = vb != nullptr;
+  g->edge_vel.assign(vb ? nb : 0, V2{0.0, 0.0});
+  for (int64_t q = 0; vb && q < nb; ++q) g->edge_vel[q] = V2{vb[2 * q], vb[2 * q + 1]};
+  g->edge_act.assign(act ? act : nullptr, act ? act + nb : nullptr);
+  return 0;
+}
 int lvref_find_dv(void* h, double dt, double alpha) { find_dv(*static_cast<Grid*>(h), dt, alpha); return 0; }
 
 int lvref_relaxation_step(void* h, double dt, int rusanov) {

@@ -47,6 +47,8 @@ def lib():
         vp, d, i32, i64 = C.c_void_p, C.c_double, C.c_int32, C.c_int64
         pd, pi32, pi64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
         sig = {
+            "lvref_boundary_edges": (i64, [vp, pd, pi32, i64]),
+            "lvref_set_edge_values": (C.c_int, [vp, i64, pd, C.POINTER(C.c_uint8)]),
             "lvref_create": (vp, [C.POINTER(GridParams), C.c_int]),
             "lvref_destroy": (None, [vp]),
             "lvref_num_threads": (C.c_int, [C.c_int]),
@@ -205,6 +207,25 @@ class OracleGrid:
     def bdary_friction(self, vwall, dt):
         w = np.ascontiguousarray(np.asarray(vwall, np.float64).reshape(8))
         return lib().lvref_bdary_friction(self.h, _p(w), dt)
+
+    def boundary_edges(self):
+        """Midpoints [nb][2] and labels [nb] of the boundary edges, in the
+        order of boundaries(p) over the polygons."""
+        nb = lib().lvref_boundary_edges(self.h, None, None, 0)
+        mid = np.zeros((nb, 2))
+        lab = np.zeros(nb, np.int32)
+        lib().lvref_boundary_edges(self.h, _p(mid), _p(lab, C.c_int32), nb)
+        return mid, lab
+
+    def set_edge_values(self, vb=None, act=None):
+        """Per-edge boundary velocities (and charfun flags) for the next
+        right-hand sides and frictions; vb None returns to the label table."""
+        if vb is None:
+            lib().lvref_set_edge_values(self.h, 0, None, None)
+            return
+        vb = np.ascontiguousarray(np.asarray(vb, np.float64).reshape(-1, 2))
+        a = None if act is None else np.ascontiguousarray(np.asarray(act, np.uint8))
+        lib().lvref_set_edge_values(self.h, len(vb), _p(vb), None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint8)))
 
     def find_dv(self, dt, alpha=1.0):
         return lib().lvref_find_dv(self.h, dt, alpha)

@@ -110,7 +110,7 @@ def test_pcg_solution(lv, oracle, mk):
     singular = not np.any(og.pressure_operator(dt)["diag"] != 0)
     bp = b - b.mean() if singular else b
     x0 = og.get("P").copy()
-    solver = lv.PressureSolver(g, tol=1e-8)
+    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
     solver.configure()
     xg = x0.copy()
     st = lv.LvSolveStats()
@@ -138,7 +138,7 @@ def test_find_pressure_sweeps(lv, oracle, mk, guess, monkeypatch):
     monkeypatch.setenv("LVGPU_SWEEP_GUESS", guess)
     flow = mk()
     g, og = _setup(lv, oracle, flow)
-    solver = lv.PressureSolver(g, tol=1e-8)
+    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
     st = lv.find_pressure(solver, flow.dt, 10, boundary_velocity=flow.walls or None)
     ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8, guess=guess == "1")
     assert all(s[1] for s in st), st
@@ -164,7 +164,7 @@ def test_find_pressure_sweep_guess(lv, oracle, mk, monkeypatch):
     for guess in ("0", "1"):
         monkeypatch.setenv("LVGPU_SWEEP_GUESS", guess)
         g, og = _setup(lv, oracle, flow)
-        solver = lv.PressureSolver(g, tol=1e-8)
+        solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
         runs[guess] = (g, og, lv.find_pressure(solver, flow.dt, 10, boundary_velocity=flow.walls or None))
     g, og, st = runs["1"]
     ref = og.find_pressure(flow.dt, 10, H.wall_table(flow), method="pcg", tol=1e-8)

@@ -27,7 +27,7 @@ def test_steps_match_oracle(lv, oracle, name, mk, nsteps):
     g = H.make_gpu(lv, flow, x)
     og = H.make_oracle(oracle, flow, x)
     H.init_both(flow, g, og)
-    solver = lv.PressureSolver(g, tol=1e-8)
+    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
     dt, seq = W.step_sequence(flow)
     for s in range(nsteps):
         for op, kw in seq:

@@ -49,7 +49,7 @@ def test_noalloc_solve_matches_regular_solve(lv, oracle, mk):
     L = lv._lib.load()
     p = lv._lib.ptr
     # the regular entry point on the same system
-    solver = lv.PressureSolver(g, tol=1e-8)
+    solver = lv.PressureSolver(g, method="jacobi_pcg", tol=1e-8)
     solver.configure()
     x_reg = S["x0"].copy()
     st = lv.LvSolveStats()
