@@ -330,7 +330,7 @@ def run_ours(args, world, rank, local, wl):
                                tol=None if args.solver == "minres" else 1e-8)
     stream = torch.cuda.ExternalStream(L.lv_stream(g._ctx), device=local)
     # between timed steps an L2 flush when the state fits in L2
-    flush_l2 = N * STATE_BYTES_PER_PARTICLE < 4 * L2_BYTES
+    flush_l2 = N * STATE_BYTES_PER_PARTICLE < L2_BYTES
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}") if flush_l2 else None
     # warm-up steps also snapshot the pressure operators the learned
     # preconditioner is trained on (the solver's own systems)
@@ -505,7 +505,9 @@ def run_ours(args, world, rank, local, wl):
     else:
         kname = "k_clip"
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": read_traffic(wl.label, dom, kname),
+                "frac": achieved / hbm_peak,
+                "traffic": read_traffic(wl.label, dom, kname,
+                                        {"per_polygon": N, "per_iteration": iters_i / max(kt["pcg"][0], 1)}),
                 "peak_source": peak_src, "units_per_launch": N if dom == "clip" else None,
                 "algorithmic_bytes_per_launch": fams[dom] / dom_launches,
                 "launch_ms": dom_ms / dom_launches, "note": ROOFLINE_NOTE.get(kname, "")}
@@ -568,16 +570,21 @@ SOLVER_DESC = {
 }
 
 
-def read_traffic(workload, family, kernel):
+def read_traffic(workload, family, kernel, units):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
     of the kernel on this workload, from the committed ncu summary table
-    profiles/traffic.txt (columns: family workload bytes_per_launch kernel ...)."""
+    profiles/traffic.txt (columns: family workload bytes kernel note...),
+    whose bytes are per launch or, when the note starts with per_polygon or
+    per_iteration, per unit: units[that unit] scales them to a launch."""
     path = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(path):
         return None
     for ln in open(path):
         f = ln.split()
         if len(f) >= 4 and not ln.startswith("#") and f[0] == family and f[1] == workload and f[3] == kernel:
+            unit = f[4].rstrip(";") if len(f) > 4 else ""
+            if unit in units:
+                return float(f[2]) * units[unit]
             return float(f[2])
     return None
 
