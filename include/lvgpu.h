@@ -57,6 +57,8 @@ enum lv_field {
   LV_FIELD_X = 0, LV_FIELD_V = 1, LV_FIELD_E = 2, LV_FIELD_P = 3, LV_FIELD_RHO = 4, LV_FIELD_C2 = 5,
   LV_FIELD_DV = 6, LV_FIELD_MASS = 7, LV_FIELD_MOMENTUM = 8, LV_FIELD_ENERGY = 9, LV_FIELD_PHASE = 10,
   LV_FIELD_QUALITY = 11, LV_FIELD_D = 12, LV_FIELD_MU = 13,
+  /* PolygonNSF (celldefs.jl:49-56): temperature, heat conductivity k, specific heat cV */
+  LV_FIELD_T = 14, LV_FIELD_K = 15, LV_FIELD_CV = 16,
   /* read-only geometry derived by lv_remesh */
   LV_FIELD_AREA = 20, LV_FIELD_CENTROID = 21
 };
@@ -148,6 +150,21 @@ int lv_viscous_step(lv_ctx* ctx, double dt, int32_t artificial_viscosity); /* vi
  * wall velocity per boundary label: vwall[4][2] indexed by -label-1. */
 int lv_bdary_friction(lv_ctx* ctx, const double* vwall, double dt);
 int lv_find_dv(lv_ctx* ctx, double dt, double alpha);                 /* find_dv! (relaxation.jl:10-25) */
+/* viscous_step!(solver::ViscousSolver, dt) (viscous_solver.jl:43-129): the
+ * implicit viscous step, (m/dt) v_new - sum_j 0.5 lrr (mu_i + mu_j)(v_j - v_i)
+ * = (m/dt) v, both components together solved by MINRES with atol = rtol =
+ * 1e-6, itmax = 2000; stats may be NULL (when given, the call synchronises). */
+int lv_viscous_solve(lv_ctx* ctx, double dt, lv_solve_stats* stats);
+/* Navier-Stokes-Fourier (fourier.jl), on LV_FIELD_T, LV_FIELD_K, LV_FIELD_CV:
+ * ideal_temperature!(grid): T = (e - v.v/2) / cV; fourier_step!(grid, dt):
+ * e -= dt k_ij / m lrr (T_i - T_j); heat_from_bdary!(grid, dt, T_bc, gamma)
+ * with T_bc(midpoint(e), e.label) evaluated per boundary edge by the caller
+ * (the order of lv_get_boundary_edges; NaN for an adiabatic edge).  A
+ * boundary polygon with cV <= 0 (the reference asserts cV > 0) is reported
+ * as LV_ERR_BAD_ARGUMENT by the next synchronising call. */
+int lv_ideal_temperature(lv_ctx* ctx);
+int lv_fourier_step(lv_ctx* ctx, double dt);
+int lv_heat_from_bdary_edges(lv_ctx* ctx, int64_t nb, const double* T_bc, double gamma, double dt);
 int lv_relaxation_step(lv_ctx* ctx, double dt, int32_t rusanov);      /* relaxation_step! (relaxation.jl:36-73), remeshes */
 
 /* PressureSolver(grid) options (pressure.jl:142-159): method, tolerance and

@@ -33,7 +33,7 @@ __all__ = [
     "export_grid", "export_points", "LinearExpansion", "QuadraticExpansion", "CubicExpansion", "gaussian_kernel",
     "power_vector", "poly_eval", "nearest_polygon", "movingls", "point_value", "integral",
     "LvError", "BDARY_UP", "BDARY_RIGHT", "BDARY_DOWN", "BDARY_LEFT", "LV_MAX_EDGES", "wall_velocity_table",
-    "zero_vbc",
+    "zero_vbc", "ViscousSolver", "ideal_temperature", "fourier_step", "heat_from_bdary",
 ]
 
 
@@ -308,8 +308,48 @@ def find_D(grid):
     _check(grid, _lib.load().lv_find_D(grid._ctx))
 
 
-def viscous_step(grid, dt, artificial_viscosity=True):
-    _check(grid, _lib.load().lv_viscous_step(grid._ctx, float(dt), int(bool(artificial_viscosity))))
+class ViscousSolver:
+    """ViscousSolver(grid) (src/viscous_solver.jl:43-66): the implicit viscous
+    step, solved by MINRES (atol = rtol = 1e-6, itmax = 2000)."""
+
+    def __init__(self, grid, verbose=0):
+        self.grid = grid
+        self.verbose = verbose
+        self.last_stats = None
+
+
+def viscous_step(target, dt, artificial_viscosity=True):
+    """viscous_step!(grid, dt; artificial_viscosity) (src/diffusion.jl:39-53),
+    explicit; or viscous_step!(solver::ViscousSolver, dt)
+    (src/viscous_solver.jl:109-129), implicit: returns (iterations,
+    converged)."""
+    if isinstance(target, ViscousSolver):
+        g = target.grid
+        st = LvSolveStats()
+        _check(g, _lib.load().lv_viscous_solve(g._ctx, float(dt), C.byref(st)))
+        target.last_stats = (st.iterations, bool(st.converged), st.rel_residual)
+        return st.iterations, bool(st.converged)
+    _check(target, _lib.load().lv_viscous_step(target._ctx, float(dt), int(bool(artificial_viscosity))))
+
+
+def ideal_temperature(grid):
+    """ideal_temperature!(grid) (src/fourier.jl:1-12): T = (e - |v|^2/2) / cV."""
+    _check(grid, _lib.load().lv_ideal_temperature(grid._ctx))
+
+
+def fourier_step(grid, dt):
+    """fourier_step!(grid, dt) (src/fourier.jl:14-28): heat conduction with the
+    fields T and k."""
+    _check(grid, _lib.load().lv_fourier_step(grid._ctx, float(dt)))
+
+
+def heat_from_bdary(grid, dt, T_bc, gamma=1.4):
+    """heat_from_bdary!(grid, dt, T_bc, gamma) (src/fourier.jl:30-62):
+    T_bc(x, label) -> wall temperature (NaN: adiabatic), evaluated here at
+    every boundary edge's midpoint."""
+    mid, lab = grid.boundary_edges()
+    Tb = np.ascontiguousarray(np.array([T_bc(m, int(l)) for m, l in zip(mid, lab)], dtype=np.float64))
+    _check(grid, _lib.load().lv_heat_from_bdary_edges(grid._ctx, len(mid), _lib.ptr(Tb), float(gamma), float(dt)))
 
 
 def bdary_friction(grid, vDirichlet, dt, charfun=None):

@@ -19,7 +19,8 @@ LV_MAX_EDGES = 20
 
 FIELDS = {"x": (0, 2), "v": (1, 2), "e": (2, 1), "P": (3, 1), "rho": (4, 1), "c2": (5, 1), "dv": (6, 2),
           "mass": (7, 1), "momentum": (8, 2), "energy": (9, 1), "phase": (10, 1), "quality": (11, 1),
-          "D": (12, 4), "mu": (13, 1), "area": (20, 1), "centroid": (21, 2)}
+          "D": (12, 4), "mu": (13, 1), "T": (14, 1), "k": (15, 1), "cV": (16, 1), "area": (20, 1),
+          "centroid": (21, 2)}
 
 METHODS = {"jacobi_pcg": 0, "mixed_ir": 1, "learned_pcg": 2, "minres": 3}
 
@@ -94,6 +95,10 @@ SIGNATURES = {
     "lv_get_boundary_edges": (C.c_int, [_vp, _pi64, _pd, _pi32]),
     "lv_find_pressure_edges": (C.c_int, [_vp, _d, _i32, _i64, _pd, _pst]),
     "lv_bdary_friction_edges": (C.c_int, [_vp, _i64, _pd, C.POINTER(C.c_uint8), _d]),
+    "lv_viscous_solve": (C.c_int, [_vp, _d, _pst]),
+    "lv_ideal_temperature": (C.c_int, [_vp]),
+    "lv_fourier_step": (C.c_int, [_vp, _d]),
+    "lv_heat_from_bdary_edges": (C.c_int, [_vp, _i64, _pd, _d, _d]),
     "lv_solver_halo": (C.c_int, [_vp, _pi32]),
     "lv_solver_forget": (C.c_int, [_vp]),
     "lv_mesh_captures": (C.c_int, [_vp, _pi32]),

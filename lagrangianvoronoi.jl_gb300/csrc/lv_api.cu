@@ -99,6 +99,7 @@ int decode_status(int flags) {
   if (flags & LV_FLAG_MESH_DESTROYED) return LV_ERR_MESH_DESTROYED;
   if (flags & LV_FLAG_EDGE_OVERFLOW) return LV_ERR_EDGE_OVERFLOW;
   if (flags & LV_FLAG_BARRIER_TIMEOUT) return LV_ERR_BARRIER_TIMEOUT;
+  if (flags & LV_FLAG_BAD_INPUT) return LV_ERR_BAD_ARGUMENT;
   return LV_OK;
 }
 
@@ -110,6 +111,7 @@ const char* status_message(int code) {
     case LV_ERR_CELL_OVERFLOW: return "cell list capacity exceeded";
     case LV_ERR_NONFINITE_POSITION: return "non-finite particle position";
     case LV_ERR_BARRIER_TIMEOUT: return "grid barrier timed out in a persistent kernel";
+    case LV_ERR_BAD_ARGUMENT: return "heat_from_bdary!: every boundary polygon needs cV > 0";
     default: return "";
   }
 }
@@ -278,6 +280,9 @@ lv_ctx* lv_create(const lv_params* prm) {
   s.energy = dalloc<double>(c, cap, &ok);
   s.quality = dalloc<double>(c, cap, &ok);
   s.mu = dalloc<double>(c, cap, &ok);
+  s.T = dalloc<double>(c, cap, &ok);
+  s.kc = dalloc<double>(c, cap, &ok);
+  s.cV = dalloc<double>(c, cap, &ok);
   s.phase = dalloc<int>(c, cap, &ok);
 
   MeshDev& m = c->m;
@@ -404,7 +409,8 @@ int lv_set_positions(lv_ctx* c, int32_t n, const double* x) {
   StateDev& st = c->s;
   const size_t cap = c->cap;
   for (double2* p : {st.x, st.v, st.dv, st.mom, st.Da, st.Db, st.GP}) cudaMemsetAsync(p, 0, 16 * cap, s);
-  for (double* p : {st.e, st.P, st.rho, st.c2, st.mass, st.energy, st.quality, st.mu}) cudaMemsetAsync(p, 0, 8 * cap, s);
+  for (double* p : {st.e, st.P, st.rho, st.c2, st.mass, st.energy, st.quality, st.mu, st.T, st.kc, st.cV})
+    cudaMemsetAsync(p, 0, 8 * cap, s);
   cudaMemsetAsync(st.phase, 0, 4 * cap, s);
   cudaError_t e = cudaMemcpyAsync(st.x, x, 16 * (size_t)n, cudaMemcpyHostToDevice, s);
   c->meshed = false;
@@ -426,6 +432,9 @@ static double* dptr1(lv_ctx* c, int f) {
     case LV_FIELD_ENERGY: return s.energy;
     case LV_FIELD_QUALITY: return s.quality;
     case LV_FIELD_MU: return s.mu;
+    case LV_FIELD_T: return s.T;
+    case LV_FIELD_K: return s.kc;
+    case LV_FIELD_CV: return s.cV;
     case LV_FIELD_AREA: return c->m.area;
     default: return nullptr;
   }
@@ -706,6 +715,40 @@ int lv_bdary_friction(lv_ctx* c, const double* vwall, double dt) {
   if (!c) return LV_ERR_BAD_ARGUMENT;
   Timer t(c, 1);
   return lv_phys_friction(c, vwall, dt);
+}
+int lv_ideal_temperature(lv_ctx* c) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_ideal_temperature(c);
+}
+int lv_fourier_step(lv_ctx* c, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  return lv_phys_fourier(c, dt);
+}
+int lv_heat_from_bdary_edges(lv_ctx* c, int64_t nb, const double* T_bc, double gamma, double dt) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  (void)gamma;  // the reference's signature carries it; its body uses cV
+  Timer t(c, 1);
+  return lv_phys_heat_bdary(c, nb, T_bc, dt);
+}
+int lv_viscous_solve(lv_ctx* c, double dt, lv_solve_stats* stats) {
+  if (!c) return LV_ERR_BAD_ARGUMENT;
+  Timer t(c, 1);
+  if (int rc = lv_phys_viscous_implicit(c, dt)) return rc;
+  if (!stats) return LV_OK;
+  int it = 0, solved = 0;
+  double d[3] = {0, 0, 0};
+  cudaMemcpyAsync(&it, c->sv.iters + LV_IT_ITERS + LV_VISC_SLOT, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(&solved, c->sv.iters + LV_IT_OUTER + LV_VISC_SLOT, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(d, c->sv.dstats + 3 * LV_VISC_SLOT, sizeof(d), cudaMemcpyDeviceToHost, c->stream);
+  if (int rc = sync_status(c)) return rc;
+  stats->iterations = it;
+  stats->converged = solved;
+  stats->outer = 0;
+  stats->method = LV_METHOD_MINRES;
+  stats->rel_residual = d[1] > 0 ? sqrt(d[0] / d[1]) : sqrt(d[0]);
+  return LV_OK;
 }
 int lv_find_dv(lv_ctx* c, double dt, double alpha) {
   if (!c) return LV_ERR_BAD_ARGUMENT;

@@ -1597,7 +1597,10 @@ constexpr int MR_TPB = 1024;
 constexpr int MR_EB = 4;  // entries loaded together
 
 struct MinresArgs {
-  int n, nb, rpb;
+  int n, nb, rpb;   // n: unknowns (ncomp per particle, interleaved); rpb: unknowns per block
+  int ncomp;        // 1: the pressure; 2: the two velocity components of the viscous system
+  int eform;        // 0: y_i = diag_i v_i + sum_e w_e (v_i - v_j) (PressureOperator, pressure.jl:119-130);
+                    // 1: y_i = sum_e w_e v_j, then + diag_i v_i (ThreadedMat mul!, viscous_solver.jl:12-22)
   const int* rowptr;
   const int* col;
   const double* w;
@@ -1620,11 +1623,12 @@ struct MinresArgs {
   long long* counters;
 };
 
-// (diag_i v_i + sum_e w_e (v_i - v_j)) with v = sc * src, the entries in
-// order, MR_EB loads at a time
-__device__ __forceinline__ double mr_apply(const MinresArgs& a, int i, const double* src, double sc, double vi) {
+// Row r of A v with v = sc * src (unknown r is component c of particle i),
+// in the operator's form (eform), the entries in order, MR_EB loads at a time
+__device__ __forceinline__ double mr_apply(const MinresArgs& a, int r, const double* src, double sc, double vi) {
+  const int i = a.ncomp == 1 ? r : r >> 1, c = r - i * a.ncomp;
   const int e0 = a.rowptr[i], e1 = a.rowptr[i + 1];
-  double acc = a.diag[i] * vi;
+  double acc = a.eform ? 0.0 : a.diag[i] * vi;
   for (int b0 = e0; b0 < e1; b0 += MR_EB) {
     int j[MR_EB];
     double wv[MR_EB], xv[MR_EB];
@@ -1635,11 +1639,12 @@ __device__ __forceinline__ double mr_apply(const MinresArgs& a, int i, const dou
       wv[q] = ld_nc(a.w + e);
     }
 #pragma unroll
-    for (int q = 0; q < MR_EB; ++q) xv[q] = sc * __ldcg(src + j[q]);
+    for (int q = 0; q < MR_EB; ++q) xv[q] = sc * __ldcg(src + (size_t)a.ncomp * j[q] + c);
 #pragma unroll
     for (int q = 0; q < MR_EB; ++q)
-      if (b0 + q < e1) acc += wv[q] * (vi - xv[q]);
+      if (b0 + q < e1) acc += a.eform ? wv[q] * xv[q] : wv[q] * (vi - xv[q]);
   }
+  if (a.eform) acc += a.diag[i] * vi;
   return acc;
 }
 
@@ -2203,9 +2208,20 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
 
 // ------------------------------------------------------------------ MINRES
 
+// MINRES on the operator (rowptr, col, w, diag) of ncomp unknowns per
+// particle in the given form, right-hand side b, iterate x, tolerances as the
+// reference's minres! (atol = rtol = tol); statistics into `slot`.
+static int minres_launch(lv_ctx* c, const int* rowptr, const int* col, const double* w, const double* diag,
+                         const double* b, double* x, int ncomp, int eform, double tol, int itmax, int slot);
+
 int lv_minres_solve(lv_ctx* c, double* x, int slot) {
+  return minres_launch(c, c->sv.rowptr, c->sv.col, c->sv.w, c->sv.diag, c->sv.b, x, 1, 0, c->tol, c->itmax, slot);
+}
+
+static int minres_launch(lv_ctx* c, const int* rowptr, const int* col, const double* w, const double* diag,
+                         const double* b, double* x, int ncomp, int eform, double tol, int itmax, int slot) {
   SolverDev& sv = c->sv;
-  const int n = c->n;
+  const int n = c->n * ncomp;
   static std::once_flag once;
   static int per_sm = 0;
   std::call_once(once, []() {
@@ -2214,7 +2230,7 @@ int lv_minres_solve(lv_ctx* c, double* x, int slot) {
   if (per_sm < 1) return lv_fail(c, LV_ERR_CUDA, "the MINRES kernel does not fit an SM");
   if (!sv.mrvec) {
     bool ok = true;
-    sv.mrvec = big_alloc<double>(c, 5 * (size_t)c->cap, &ok);
+    sv.mrvec = big_alloc<double>(c, 10 * (size_t)c->cap, &ok);  // five vectors of up to 2 cap unknowns
     sv.mrsync = big_alloc<unsigned>(c, BIG_SLOT_OFF + 2 * RG_WORDS * FCG_MAX_BLOCKS, &ok);
     if (!ok) {
       sv.mrvec = nullptr;
@@ -2227,13 +2243,15 @@ int lv_minres_solve(lv_ctx* c, double* x, int slot) {
   a.n = n;
   a.nb = nb;
   a.rpb = (n + nb - 1) / nb;
-  a.rowptr = sv.rowptr;
-  a.col = sv.col;
-  a.w = sv.w;
-  a.diag = sv.diag;
-  a.b = sv.b;
+  a.ncomp = ncomp;
+  a.eform = eform;
+  a.rowptr = rowptr;
+  a.col = col;
+  a.w = w;
+  a.diag = diag;
+  a.b = b;
   a.x = x;
-  const size_t cap = (size_t)c->cap;
+  const size_t cap = 2 * (size_t)c->cap;
   a.lz[0] = sv.mrvec;
   a.lz[1] = sv.mrvec + cap;
   a.dw[0] = sv.mrvec + 2 * cap;
@@ -2244,10 +2262,10 @@ int lv_minres_solve(lv_ctx* c, double* x, int slot) {
   a.slots = reinterpret_cast<unsigned long long*>(sv.mrsync + BIG_SLOT_OFF);
   a.status = c->status;
   a.spin = c->spin_limit;
-  a.atol = c->tol;
-  a.rtol = c->tol;
-  a.tol2 = c->tol * c->tol;
-  a.itmax = c->itmax;
+  a.atol = tol;
+  a.rtol = tol;
+  a.tol2 = tol * tol;
+  a.itmax = itmax;
   a.out_iters = sv.iters + slot;
   a.out_solved = sv.iters + LV_IT_OUTER + slot;
   a.out_method = sv.iters + LV_IT_METHOD + slot;
@@ -2265,4 +2283,9 @@ int lv_minres_solve(lv_ctx* c, double* x, int slot) {
     return lv_cuda_check(c, e, "k_minres cooperative launch");
   }
   return LV_OK;
+}
+
+int lv_minres_general(lv_ctx* c, const int* rowptr, const int* col, const double* w, const double* diag,
+                      const double* b, double* x, int ncomp, int eform, double tol, int itmax, int slot) {
+  return minres_launch(c, rowptr, col, w, diag, b, x, ncomp, eform, tol, itmax, slot);
 }

@@ -44,6 +44,7 @@
 #define LV_FLAG_CELL_OVERFLOW 0x8
 #define LV_FLAG_NONFINITE 0x10
 #define LV_FLAG_BARRIER_TIMEOUT 0x20
+#define LV_FLAG_BAD_INPUT 0x40  // a field value the reference asserts against (heat_from_bdary!: cV > 0)
 
 // Domain and cell-list constants passed to kernels by value.
 struct GridDev {
@@ -72,6 +73,7 @@ struct PathNodeDev {
 struct StateDev {
   double2 *x, *v, *dv, *mom, *Da, *Db, *GP;
   double *e, *P, *rho, *c2, *mass, *energy, *quality, *mu;
+  double *T, *kc, *cV;  // temperature, heat conductivity, specific heat (PolygonNSF, celldefs.jl:49-56)
   int* phase;
 };
 
@@ -308,6 +310,14 @@ struct lv_ctx {
   unsigned char* bnd_act = nullptr;
   int* bnd_lab = nullptr;
   const double2* rhs_bvel = nullptr;  // per-edge boundary velocities of the running lv_find_pressure_edges
+  // implicit viscous system (ViscousSolver): CSR of the face pattern, entries,
+  // diagonal, right-hand side and iterate (2 cap interleaved unknowns)
+  int* vs_rowptr = nullptr;
+  int* vs_col = nullptr;
+  double* vs_w = nullptr;
+  double* vs_diag = nullptr;
+  double* vs_b = nullptr;
+  double* vs_u = nullptr;
   float learn_eps = 1e-4f;  // eps of M^-1 = D^-1/2 (Gt^T Gt + eps I) D^-1/2
   std::string err;
   int64_t launches = 0;
@@ -499,6 +509,12 @@ int lv_phys_friction(lv_ctx* c, const double* vwall, double dt, const double2* b
 int lv_bnd_prepare(lv_ctx* c);
 int lv_bnd_list(lv_ctx* c, double* mid, int* lab);
 int lv_bnd_upload(lv_ctx* c, int64_t nb, const double* vb, const unsigned char* act);
+// Fourier heat conduction (fourier.jl) and the implicit viscous step (viscous_solver.jl)
+int lv_phys_ideal_temperature(lv_ctx* c);
+int lv_phys_fourier(lv_ctx* c, double dt);
+int lv_phys_heat_bdary(lv_ctx* c, int64_t nb, const double* Tb, double dt);
+int lv_phys_viscous_implicit(lv_ctx* c, double dt);
+#define LV_VISC_SLOT 31  // stats slot of the implicit viscous solve
 int lv_phys_find_dv(lv_ctx* c, double dt, double alpha);
 int lv_phys_relax(lv_ctx* c, double dt, int rusanov);
 // prepare = 1 evaluates the sweep-invariant terms (first sweep of find_pressure!)
@@ -539,6 +555,10 @@ int lv_big_prepare(lv_ctx* c);  // allocations; called before the assembly of su
 int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned);
 // MINRES without a preconditioner (LV_METHOD_MINRES), any size
 int lv_minres_solve(lv_ctx* c, double* x, int slot);
+// the same kernel on another operator: ncomp unknowns per particle
+// (interleaved), eform 1 the ThreadedMat row form (entries, then the diagonal)
+int lv_minres_general(lv_ctx* c, const int* rowptr, const int* col, const double* w, const double* diag,
+                      const double* b, double* x, int ncomp, int eform, double tol, int itmax, int slot);
 
 #define LV_LAUNCH_CHECK(c, what)                                   \
   do {                                                             \

@@ -909,6 +909,187 @@ int lv_phys_friction(lv_ctx* c, const double* vwall, double dt, const double2* b
   return LV_OK;
 }
 
+// ------------------------------------------------------ Fourier heat (fourier.jl)
+
+// ideal_temperature! (fourier.jl:1-12): T = eint(p) / cV, eint = e - v.v / 2 (pressure.jl:32-34)
+__global__ void k_ideal_temperature(StateDev s, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = s.v[i];
+  s.T[i] = (s.e[i] - 0.5 * (v.x * v.x + v.y * v.y)) / s.cV[i];
+}
+
+// fourier_step! (fourier.jl:14-28): e -= dt k / m lrr (T_i - T_j), k = (k_i + k_j)/2, faces in order
+__global__ void k_fourier(StateDev s, MeshDev m, int n, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double Ti = s.T[i], ki = s.kc[i], mi = s.mass[i];
+  double e = s.e[i];
+  for (int k0 = 0; k0 < nf; k0 += FB) {
+    int j[FB];
+    double lrr[FB], Tj[FB], kj[FB];
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      const size_t f = face_slot(k0 + u, nf, cap, i);
+      j[u] = ld_nc(m.fnbr + f);
+      lrr[u] = ld_nc(m.flrr + f);
+    }
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      Tj[u] = ld_nc(s.T + j[u]);
+      kj[u] = ld_nc(s.kc + j[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < FB; ++u) {
+      if (k0 + u >= nf) break;
+      const double k = 0.5 * (ki + kj[u]);
+      e = e - dt * k / mi * lrr[u] * (Ti - Tj[u]);
+    }
+  }
+  s.e[i] = e;
+}
+
+// heat_from_bdary! (fourier.jl:30-62): an implicit boundary heat flux from
+// the wall temperatures Tb (per boundary edge, from boff[i] in edge order;
+// NaN: adiabatic).  The reference asserts cV > 0: a boundary polygon without
+// it raises LV_FLAG_BAD_INPUT and is left unchanged.
+__global__ void k_heat_bdary(GridDev g, StateDev s, MeshDev m, int n, double dt, const double* __restrict__ Tb,
+                             const int* __restrict__ boff, int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
+  if (nf == ne) return;  // !isboundary(p)
+  const double cV = s.cV[i];
+  if (!(cV > 0.0)) {
+    atomicOr(status, LV_FLAG_BAD_INPUT);
+    return;
+  }
+  const double2 xi = s.x[i], v = s.v[i];
+  double implicit_factor = 1.0;
+  const double thermal_D = s.kc[i] / (s.rho[i] * cV);
+  const double e_kinetic = 0.5 * (v.x * v.x + v.y * v.y);
+  double T = (s.e[i] - e_kinetic) / cV;
+  const double A = m.area[i];
+  int q = boff[i];
+  for (int k = 0; k < ne; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    if (m.elab[f] >= 0) continue;
+    const double Tw = Tb[q++];
+    const double2 a = m.ev1[f], b = m.ev2[f];
+    const double mx = 0.5 * (a.x + b.x), my = 0.5 * (a.y + b.y);
+    const double nx0 = a.y - b.y, ny0 = b.x - a.x;
+    const double nn = sqrt(nx0 * nx0 + ny0 * ny0);
+    const double nx = nx0 / nn, ny = ny0 / nn;
+    const double lx = a.x - b.x, ly = a.y - b.y;
+    const double len = sqrt(lx * lx + ly * ly);
+    const double lrr = len / fabs((mx - xi.x) * nx + (my - xi.y) * ny) + 0.01 * g.dr;
+    if (!isnan(Tw)) {
+      const double tmp = dt * thermal_D * lrr / A;
+      T = T + tmp * Tw;
+      implicit_factor = implicit_factor + tmp;
+    }
+  }
+  T = T / implicit_factor;
+  s.T[i] = T;
+  s.e[i] = e_kinetic + cV * T;
+}
+
+// ------------------------------------------------------ implicit viscosity (viscous_solver.jl)
+
+// ViscousSolver assemble! (viscous_solver.jl:79-107): per particle the
+// neighbours' entries -0.5 lrr (mu_i + mu_j) in face order and the self entry
+// vv = m/dt minus them (the rows of both velocity components hold the same
+// entries); b = (m/dt) v and the first guess v, interleaved (v_index).
+__global__ void k_visc_sys(StateDev s, MeshDev m, int n, double dt, const int* __restrict__ rowptr, int* col,
+                           double* w, double* diag, double* b, double* u0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int cap = m.cap, nf = m.nfaces[i];
+  const double mi = s.mass[i], mui = s.mu[i];
+  const double2 v = s.v[i];
+  const int base = rowptr[i];
+  b[2 * (size_t)i] = mi / dt * v.x;
+  b[2 * (size_t)i + 1] = mi / dt * v.y;
+  u0[2 * (size_t)i] = v.x;
+  u0[2 * (size_t)i + 1] = v.y;
+  double vv = mi / dt;
+  for (int k = 0; k < nf; ++k) {
+    const size_t f = (size_t)k * cap + i;
+    const int j = m.fnbr[f];
+    const double wv = -0.5 * m.flrr[f] * (mui + s.mu[j]);
+    col[base + k] = j;
+    w[base + k] = wv;
+    vv = vv - wv;
+  }
+  diag[i] = vv;
+}
+
+__global__ void k_visc_store(StateDev s, int n, const double* __restrict__ u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) s.v[i] = make_double2(u[2 * (size_t)i], u[2 * (size_t)i + 1]);
+}
+
+int lv_phys_ideal_temperature(lv_ctx* c) {
+  LAUNCH(k_ideal_temperature, c->s, c->n);
+  return LV_OK;
+}
+
+int lv_phys_fourier(lv_ctx* c, double dt) {
+  if (int rc = need_mesh(c)) return rc;
+  LAUNCH(k_fourier, c->s, c->m, c->n, dt);
+  return LV_OK;
+}
+
+int lv_phys_heat_bdary(lv_ctx* c, int64_t nb, const double* Tb, double dt) {
+  if (int rc = lv_bnd_prepare(c)) return rc;
+  if (nb != c->bnd_count || (nb > 0 && !Tb))
+    return lv_fail(c, LV_ERR_BAD_ARGUMENT, "heat_from_bdary!: nb is not the mesh's boundary-edge count");
+  double* dTb = reinterpret_cast<double*>(c->bnd_vel);  // room for 2 nb doubles
+  if (nb > 0) cudaMemcpyAsync(dTb, Tb, sizeof(double) * (size_t)nb, cudaMemcpyHostToDevice, c->stream);
+  LAUNCH(k_heat_bdary, c->g, c->s, c->m, c->n, dt, dTb, c->bnd_off, c->status);
+  return LV_OK;
+}
+
+// viscous_step!(solver::ViscousSolver, dt) (viscous_solver.jl:109-129): the
+// implicit system solved by MINRES with atol = rtol = 1e-6, itmax = 2000
+// (the device MINRES on the 2n interleaved unknowns, the ThreadedMat row
+// form), then v = the solution.  Statistics into stats slot 31.
+int lv_phys_viscous_implicit(lv_ctx* c, double dt) {
+  if (int rc = need_mesh(c)) return rc;
+  const int n = c->n;
+  if (!c->vs_col) {
+    bool ok = cudaMalloc(&c->vs_rowptr, sizeof(int) * ((size_t)c->cap + 1)) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->vs_col, sizeof(int) * (size_t)c->sv.nnz_cap) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->vs_w, sizeof(double) * (size_t)c->sv.nnz_cap) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->vs_diag, sizeof(double) * (size_t)c->cap) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->vs_b, sizeof(double) * 2 * (size_t)c->cap) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->vs_u, sizeof(double) * 2 * (size_t)c->cap) == cudaSuccess;
+    for (void* p : {(void*)c->vs_rowptr, (void*)c->vs_col, (void*)c->vs_w, (void*)c->vs_diag, (void*)c->vs_b,
+                    (void*)c->vs_u})
+      if (p) c->allocs.push_back(p);
+    if (!ok) {
+      c->vs_col = nullptr;
+      return lv_fail(c, LV_ERR_CUDA, "allocation of the viscous system failed");
+    }
+  }
+  {
+    KernelTimer kt(c, LV_KF_OPS);
+    if (int rc = lv_scan_int(c, c->m.nfaces, c->vs_rowptr, n)) return rc;
+    k_visc_sys<<<lv_blocks(n, TPB), TPB, 0, c->stream>>>(c->s, c->m, n, dt, c->vs_rowptr, c->vs_col, c->vs_w,
+                                                          c->vs_diag, c->vs_b, c->vs_u);
+    LV_LAUNCH_CHECK(c, "k_visc_sys");
+  }
+  {
+    KernelTimer kt(c, LV_KF_PCG);
+    if (int rc = lv_minres_general(c, c->vs_rowptr, c->vs_col, c->vs_w, c->vs_diag, c->vs_b, c->vs_u, 2, 1, 1e-6,
+                                   2000, LV_VISC_SLOT))
+      return rc;
+  }
+  LAUNCH(k_visc_store, c->s, n, c->vs_u);
+  return LV_OK;
+}
+
 // ------------------------------------------------------ boundary edges
 //
 // The boundary edges of the current mesh in the order of boundaries(p)

@@ -95,6 +95,7 @@ struct Grid {
   int n = 0;
   std::vector<V2> x, v, dv, momentum;
   std::vector<double> rho, e, P, c2, mass, energy, quality, mu;
+  std::vector<double> T, kc, cV;  // PolygonNSF (celldefs.jl:49-56): temperature, conductivity, specific heat
   std::vector<int32_t> phase;
   std::vector<M2> D;
   std::vector<std::vector<Edge>> edges;
@@ -531,11 +532,21 @@ struct SolveStats {
 // MINRES (Paige & Saunders 1975) with warm start; stops when
 // ||r|| <= atol + rtol*||r0|| or when the least-squares test
 // ||A r|| <= rtol*||A||*||r|| holds (inconsistent singular systems).
+template <class Op>
+int minres_op(int n, Op op_apply, const std::vector<double>& bvec, std::vector<double>& x, double atol, double rtol,
+              int itmax, SolveStats* st);
+
 int minres_solve(const Grid& g, const std::vector<double>& bvec, std::vector<double>& x, double atol, double rtol,
                  int itmax, SolveStats* st) {
-  const int n = g.n;
+  return minres_op(g.n, [&](const double* in, double* out) { op_mul(g, in, out); }, bvec, x, atol, rtol, itmax, st);
+}
+
+// The same MINRES with the operator y = A x given by op_apply(x, y) on n unknowns.
+template <class Op>
+int minres_op(int n, Op op_apply, const std::vector<double>& bvec, std::vector<double>& x, double atol, double rtol,
+              int itmax, SolveStats* st) {
   std::vector<double> r1(n), r2(n), y(n), v(n), w(n, 0.0), w1(n), w2(n, 0.0), Ax(n);
-  op_mul(g, x.data(), Ax.data());
+  op_apply(x.data(), Ax.data());
   for (int i = 0; i < n; ++i) r1[i] = bvec[i] - Ax[i];
   y = r1;
   double beta1 = std::sqrt(bdot(r1.data(), y.data(), n));
@@ -551,7 +562,7 @@ int minres_solve(const Grid& g, const std::vector<double>& bvec, std::vector<dou
       ++itn;
       double s = 1.0 / beta;
       for (int i = 0; i < n; ++i) v[i] = s * y[i];
-      op_mul(g, v.data(), y.data());
+      op_apply(v.data(), y.data());
       if (itn >= 2)
         for (int i = 0; i < n; ++i) y[i] -= (beta / oldb) * r1[i];
       double alfa = bdot(v.data(), y.data(), n);
@@ -597,7 +608,7 @@ int minres_solve(const Grid& g, const std::vector<double>& bvec, std::vector<dou
     }
   }
   if (st) {
-    op_mul(g, x.data(), Ax.data());
+    op_apply(x.data(), Ax.data());
     std::vector<double> r(n);
     for (int i = 0; i < n; ++i) r[i] = bvec[i] - Ax[i];
     double bn = std::sqrt(bdot(bvec.data(), bvec.data(), n));
@@ -761,6 +772,109 @@ void bdary_friction(Grid& g, const double* vwall, double dt) {
     g.v[i] = V2{vi.x / tmp, vi.y / tmp};
     g.e[i] = ei;
   }
+}
+
+// ideal_temperature! (fourier.jl:1-12): T = eint(p)/cV, eint = e - norm_squared(v)/2 (pressure.jl:32-34)
+void ideal_temperature(Grid& g) {
+#pragma omp parallel for
+  for (int i = 0; i < g.n; ++i) g.T[i] = (g.e[i] - 0.5 * dot(g.v[i], g.v[i])) / g.cV[i];
+}
+
+// fourier_step! (fourier.jl:14-28)
+void fourier_step(Grid& g, double dt) {
+#pragma omp parallel for
+  for (int i = 0; i < g.n; ++i) {
+    const V2 xi = g.x[i];
+    double ei = g.e[i];
+    for_faces(g, i, [&](int j, const Edge& e, V2 y) {
+      double lrr = lr_ratio(xi - y, e);
+      double k = 0.5 * (g.kc[i] + g.kc[j]);
+      ei = ei - dt * k / g.mass[i] * lrr * (g.T[i] - g.T[j]);
+    });
+    g.e[i] = ei;
+  }
+}
+
+// heat_from_bdary! (fourier.jl:30-62) with the wall temperatures T_bc(m,
+// label) given per boundary edge in the per-edge order (NaN: adiabatic).
+// Returns ST_BAD_ARGUMENT where the reference's @assert(p.cV > 0) fails.
+int heat_from_bdary(Grid& g, double dt, const double* Tb) {
+  const std::vector<int64_t> boff = boundary_offsets(g);
+  int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+  for (int i = 0; i < g.n; ++i) {
+    bool bd = false;
+    for (const auto& e : g.edges[i]) bd = bd || e.label < 0;
+    if (!bd) continue;
+    if (!(g.cV[i] > 0.0)) {
+      bad = 1;
+      continue;
+    }
+    double implicit_factor = 1.0;
+    const double thermal_D = g.kc[i] / (g.rho[i] * g.cV[i]);
+    const double e_kinetic = 0.5 * dot(g.v[i], g.v[i]);
+    double T = (g.e[i] - e_kinetic) / g.cV[i];
+    const double A = poly_area(g.edges[i], g.x[i]);
+    int64_t q = boff[i];
+    for (const auto& e : g.edges[i]) {
+      if (e.label >= 0) continue;
+      const double Tw = Tb[q++];
+      V2 m = 0.5 * (e.v1 + e.v2);
+      V2 nv = normal_vector(e);
+      double lrr = len(e) / std::fabs(dot(m - g.x[i], nv)) + 0.01 * g.dr;
+      if (!std::isnan(Tw)) {
+        double tmp = dt * thermal_D * lrr / A;
+        T += tmp * Tw;
+        implicit_factor += tmp;
+      }
+    }
+    T /= implicit_factor;
+    g.T[i] = T;
+    g.e[i] = e_kinetic + g.cV[i] * T;
+  }
+  return bad ? ST_BAD_ARGUMENT : ST_OK;
+}
+
+// ViscousSolver + viscous_step!(solver, dt) (viscous_solver.jl:43-129): rows
+// 2i, 2i+1 (v_index) hold the neighbours' entries -0.5 lrr (mu_i + mu_j) in
+// face order, then the self entry vv = m/dt minus them; the ThreadedMat
+// product accumulates a row from 0.0 in that order.  MINRES (atol = rtol =
+// 1e-6, itmax = 2000) from the first guess v; then v = the solution.
+int viscous_solve(Grid& g, double dt, double tol, int itmax, SolveStats* st) {
+  const int n = g.n;
+  std::vector<std::vector<int32_t>> rows(n);
+  std::vector<std::vector<double>> vals(n);
+  std::vector<double> b(2 * n), u(2 * n);
+#pragma omp parallel for
+  for (int i = 0; i < n; ++i) {
+    const V2 xi = g.x[i];
+    b[2 * i] = g.mass[i] / dt * g.v[i].x;
+    b[2 * i + 1] = g.mass[i] / dt * g.v[i].y;
+    u[2 * i] = g.v[i].x;
+    u[2 * i + 1] = g.v[i].y;
+    double vv = g.mass[i] / dt;
+    for_faces(g, i, [&](int j, const Edge& e, V2 y) {
+      double lrr = lr_ratio(xi - y, e);
+      double wv = -0.5 * lrr * (g.mu[i] + g.mu[j]);
+      rows[i].push_back(j);
+      vals[i].push_back(wv);
+      vv -= wv;
+    });
+    rows[i].push_back(i);
+    vals[i].push_back(vv);
+  }
+  auto apply = [&](const double* in, double* out) {
+#pragma omp parallel for
+    for (int r = 0; r < 2 * n; ++r) {
+      const int i = r / 2, c = r % 2;
+      double yr = 0.0;
+      for (size_t k = 0; k < rows[i].size(); ++k) yr += vals[i][k] * in[2 * rows[i][k] + c];
+      out[r] = yr;
+    }
+  };
+  minres_op(2 * n, apply, b, u, tol, tol, itmax, st);
+  for (int i = 0; i < n; ++i) g.v[i] = V2{u[2 * i], u[2 * i + 1]};
+  return ST_OK;
 }
 
 void find_dv(Grid& g, double dt, double alpha) {  // relaxation.jl:10-25
@@ -933,7 +1047,7 @@ struct lvref_grid_params {
 
 enum {
   F_X = 0, F_V = 1, F_E = 2, F_P = 3, F_RHO = 4, F_C2 = 5, F_DV = 6, F_MASS = 7, F_MOMENTUM = 8,
-  F_ENERGY = 9, F_PHASE = 10, F_QUALITY = 11, F_D = 12, F_MU = 13
+  F_ENERGY = 9, F_PHASE = 10, F_QUALITY = 11, F_D = 12, F_MU = 13, F_T = 14, F_K = 15, F_CV = 16
 };
 
 void* lvref_create(const lvref_grid_params* p, int n) {
@@ -962,7 +1076,8 @@ void* lvref_create(const lvref_grid_params* p, int n) {
   g->v.assign(n, V2{0, 0});
   g->dv.assign(n, V2{0, 0});
   g->momentum.assign(n, V2{0, 0});
-  for (auto* f : {&g->rho, &g->e, &g->P, &g->c2, &g->mass, &g->energy, &g->quality, &g->mu}) f->assign(n, 0.0);
+  for (auto* f : {&g->rho, &g->e, &g->P, &g->c2, &g->mass, &g->energy, &g->quality, &g->mu, &g->T, &g->kc, &g->cV})
+    f->assign(n, 0.0);
   g->phase.assign(n, 0);
   g->D.assign(n, M2{0, 0, 0, 0});
   g->edges.assign(n, {});
@@ -1018,6 +1133,9 @@ int lvref_set_field(void* h, int f, const double* src) {
     case F_ENERGY: std::memcpy(g->energy.data(), src, 8 * n); break;
     case F_QUALITY: std::memcpy(g->quality.data(), src, 8 * n); break;
     case F_MU: std::memcpy(g->mu.data(), src, 8 * n); break;
+    case F_T: std::memcpy(g->T.data(), src, 8 * n); break;
+    case F_K: std::memcpy(g->kc.data(), src, 8 * n); break;
+    case F_CV: std::memcpy(g->cV.data(), src, 8 * n); break;
     default: return ST_BAD_ARGUMENT;
   }
   return 0;
@@ -1041,6 +1159,9 @@ int lvref_get_field(void* h, int f, double* dst) {
     case F_ENERGY: std::memcpy(dst, g->energy.data(), 8 * n); break;
     case F_QUALITY: std::memcpy(dst, g->quality.data(), 8 * n); break;
     case F_MU: std::memcpy(dst, g->mu.data(), 8 * n); break;
+    case F_T: std::memcpy(dst, g->T.data(), 8 * n); break;
+    case F_K: std::memcpy(dst, g->kc.data(), 8 * n); break;
+    case F_CV: std::memcpy(dst, g->cV.data(), 8 * n); break;
     default: return ST_BAD_ARGUMENT;
   }
   return 0;
@@ -1151,6 +1272,13 @@ int lvref_pressure_step(void* h, double dt) { pressure_step(*static_cast<Grid*>(
 int lvref_find_D(void* h) { find_D(*static_cast<Grid*>(h)); return 0; }
 int lvref_viscous_step(void* h, double dt, int av) { viscous_step(*static_cast<Grid*>(h), dt, av != 0); return 0; }
 int lvref_bdary_friction(void* h, const double* vwall, double dt) { bdary_friction(*static_cast<Grid*>(h), vwall, dt); return 0; }
+
+int lvref_ideal_temperature(void* h) { ideal_temperature(*static_cast<Grid*>(h)); return 0; }
+int lvref_fourier_step(void* h, double dt) { fourier_step(*static_cast<Grid*>(h), dt); return 0; }
+int lvref_heat_from_bdary(void* h, double dt, const double* Tb) { return heat_from_bdary(*static_cast<Grid*>(h), dt, Tb); }
+int lvref_viscous_solve(void* h, double dt, double tol, int itmax, SolveStats* st) {
+  return viscous_solve(*static_cast<Grid*>(h), dt, tol, itmax, st);
+}
 
 // The boundary edges in the per-edge order: midpoints mid[nb][2] =
 // midpoint(e) and labels; returns nb (arrays filled when cap >= nb).

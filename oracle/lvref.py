@@ -14,11 +14,11 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
-F_X, F_V, F_E, F_P, F_RHO, F_C2, F_DV, F_MASS, F_MOMENTUM, F_ENERGY, F_PHASE, F_QUALITY, F_D, F_MU = range(14)
+F_X, F_V, F_E, F_P, F_RHO, F_C2, F_DV, F_MASS, F_MOMENTUM, F_ENERGY, F_PHASE, F_QUALITY, F_D, F_MU, F_T, F_K, F_CV = range(17)
 NCOMP = {F_X: 2, F_V: 2, F_DV: 2, F_MOMENTUM: 2, F_D: 4}
 FIELD_NAMES = {"x": F_X, "v": F_V, "e": F_E, "P": F_P, "rho": F_RHO, "c2": F_C2, "dv": F_DV, "mass": F_MASS,
                "momentum": F_MOMENTUM, "energy": F_ENERGY, "phase": F_PHASE, "quality": F_QUALITY, "D": F_D,
-               "mu": F_MU}
+               "mu": F_MU, "T": F_T, "k": F_K, "cV": F_CV}
 
 
 class GridParams(C.Structure):
@@ -47,6 +47,10 @@ def lib():
         vp, d, i32, i64 = C.c_void_p, C.c_double, C.c_int32, C.c_int64
         pd, pi32, pi64 = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
         sig = {
+            "lvref_ideal_temperature": (C.c_int, [vp]),
+            "lvref_fourier_step": (C.c_int, [vp, d]),
+            "lvref_heat_from_bdary": (C.c_int, [vp, d, pd]),
+            "lvref_viscous_solve": (C.c_int, [vp, d, d, C.c_int, C.POINTER(SolveStats)]),
             "lvref_boundary_edges": (i64, [vp, pd, pi32, i64]),
             "lvref_set_edge_values": (C.c_int, [vp, i64, pd, C.POINTER(C.c_uint8)]),
             "lvref_create": (vp, [C.POINTER(GridParams), C.c_int]),
@@ -207,6 +211,23 @@ class OracleGrid:
     def bdary_friction(self, vwall, dt):
         w = np.ascontiguousarray(np.asarray(vwall, np.float64).reshape(8))
         return lib().lvref_bdary_friction(self.h, _p(w), dt)
+
+    def ideal_temperature(self):
+        lib().lvref_ideal_temperature(self.h)
+
+    def fourier_step(self, dt):
+        lib().lvref_fourier_step(self.h, dt)
+
+    def heat_from_bdary(self, dt, Tb):
+        """Tb: the wall temperature of every boundary edge (NaN: adiabatic)."""
+        t = np.ascontiguousarray(np.asarray(Tb, np.float64))
+        return lib().lvref_heat_from_bdary(self.h, dt, _p(t))
+
+    def viscous_solve(self, dt, tol=1e-6, itmax=2000):
+        """ViscousSolver + viscous_step!(solver, dt): returns (iterations, converged, rel_residual)."""
+        st = SolveStats()
+        lib().lvref_viscous_solve(self.h, dt, tol, itmax, C.byref(st))
+        return st.iterations, st.converged, st.rel_residual
 
     def boundary_edges(self):
         """Midpoints [nb][2] and labels [nb] of the boundary edges, in the
