@@ -352,10 +352,17 @@ def run_ours(args, world, rank, local, wl):
         gpu_step(lv, g, solver, fl)
         g.synchronize()
 
-    def between_steps(ev0):
+    # events around the L2 flush (outside the step events), to report its time
+    ev_f = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+
+    def between_steps(ev0, k=None):
         with torch.cuda.stream(stream):
             if flush is not None:
+                if k is not None:
+                    ev_f[k][0].record(stream)
                 flush.zero_()
+                if k is not None:
+                    ev_f[k][1].record(stream)
             ev0.record(stream)
 
     restore()
@@ -374,7 +381,7 @@ def run_ours(args, world, rank, local, wl):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        between_steps(ev[k][0])
+        between_steps(ev[k][0], k)
         gpu_step(lv, g, solver, fl)
         with torch.cuda.stream(stream):
             ev[k][1].record(stream)
@@ -386,6 +393,7 @@ def run_ours(args, world, rank, local, wl):
     barrier(world)
     launches = g.launch_count() - launches0
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    flush_ms = float(sum(a.elapsed_time(b) for a, b in ev_f)) / args.steps if flush is not None else 0.0
     dev_ms = float(sum(step_ms))
     s1, i1 = C.c_int64(), C.c_int64()
     L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
@@ -542,6 +550,7 @@ def run_ours(args, world, rank, local, wl):
         "gpu_launches": launches,
         "wall_s_timed": wall,
         "host_gap_ms_per_step": (wall * 1e3 - dev_ms) / args.steps,
+        "l2_flush_ms_per_step": flush_ms,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, wl)
