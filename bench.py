@@ -332,6 +332,11 @@ def run_ours(args, world, rank, local, wl):
     # between timed steps an L2 flush when the state fits in L2
     flush_l2 = N * STATE_BYTES_PER_PARTICLE < L2_BYTES
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}") if flush_l2 else None
+    if flush is not None:
+        # the first fill loads torch's kernel (~0.25 s of host time): once here, outside the timed steps
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
     # warm-up steps also snapshot the pressure operators the learned
     # preconditioner is trained on (the solver's own systems)
     for _ in range(args.warmup):
