@@ -229,9 +229,21 @@ lv_ctx* lv_create(const lv_params* prm) {
   g.dy_hi = (double)g.n2 * h * (1.0 + 1e-12);
   const double bigm = std::max(std::max(fabs(g.cminx), fabs(g.cmaxx)), std::max(fabs(g.cminy), fabs(g.cmaxy)));
   g.bigm = (float)(bigm * (1.0 + 1e-6));
-  g.delta32 = (float)(ldexp(1.0, -22) * (bigm + std::max(g.xperiod, g.yperiod)));
   c->path_host = build_path(g);
   g.npath = (int)c->path_host.size();
+  // The clipping's float candidate offset from the seed is
+  //   ((cpos - float(x - O_seedcell)) + float(di) * float(h)),
+  // each offset in [0, h] rounded once to FP64 and once to float.  Its error
+  // per component is at most 2^-24 h (4 + 3 |di|) (two offsets, their
+  // difference, the product and the sum, each a float rounding) plus the FP64
+  // rounding of the cell corners and of the reference's arrow (a few ulps of
+  // the largest coordinate); |di| <= dmax over the nodes the search visits.
+  int dmax = 0;
+  for (const PathNodeDev& nd : c->path_host)
+    if (!nd.beyond) dmax = std::max(dmax, std::max(abs(nd.di1), abs(nd.di2)));
+  g.h32 = (float)h;
+  g.delta32 = (float)((ldexp(1.0, -24) * h * (6.0 + 4.0 * dmax) +
+                       2e-15 * (bigm + std::max(g.xperiod, g.yperiod) + 2.0 * h)) * (1.0 + 1e-6));
 
   cudaDeviceProp p;
   cudaGetDeviceProperties(&p, c->dev);

@@ -8,7 +8,8 @@
 //           ("ELL") layout: slot k of particle i lives at [k*cap + i], so a
 //           warp reading slot k of 32 consecutive particles is coalesced.
 //   cells   cell list as CSR over the n1*n2 cells: cstart[ncells+1],
-//           citem[] (particle index), cpos32[] (float2 copy of its position).
+//           citem[] (particle index), cpos[] (float2 offset of the copy from its
+//           cell's lower corner; NaN for a periodic image).
 //   solver  CSR of the pressure operator: rowptr[n+1], col[nnz], w[nnz]
 //           (off-diagonal weights), adiag = diag + sum_j w_ij, dinv = 1/adiag.
 #pragma once
@@ -57,8 +58,10 @@ struct GridDev {
   int xper, yper;
   int n1, n2;
   int npath;
-  float delta32;  // bound on |float(a) - float(b) - (a - b)| for positions inside the cropping box
+  float delta32;  // bound on the error of a candidate's float offset from the seed, per component
+                  // (formed from the cell-relative offsets cpos and the path node's cell offset)
   float bigm;     // max |coordinate| inside the cropping box
+  float h32;      // (float)h
 };
 
 // One node of the candidate path (neighborlist.jl:29-41): cell offset and
@@ -189,7 +192,7 @@ struct CellsDev {
   int* cstart;   // [ncells + 1]
   int* ccount;   // [ncells] counts
   int* citem;    // [item_cap]
-  float2* cpos;  // [item_cap]
+  float2* cpos;  // [item_cap] offset from the cell's lower corner (NaN: a periodic image)
   int2* bkey;    // [images][cap]: cell and rank in the cell of every copy (re-binning)
   int item_cap;
 };

@@ -188,10 +188,15 @@ __global__ void k_bin_scatter(GridDev g, int n, int cap, const int2* __restrict_
 }
 
 // Insertion order of the reference with one thread is the particle index
-// order; atomics scatter arbitrarily, so each cell is sorted back.
+// order; atomics scatter arbitrarily, so each cell is sorted back.  Each item
+// then gets the float offset of its particle from the cell's lower corner
+// (the clipping's float tests; an offset below h carries an error of 2^-24 h
+// instead of 2^-24 of the coordinate), or NaN when the item is a periodic
+// image (its copy 0, the particle itself, lies in another cell), which the
+// clipping decides in FP64.
 // (also clears the cell counts for the next remesh: the scan has consumed them)
-__global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* citem, float2* cpos,
-                            const double2* __restrict__ x, int item_cap, int* ccount) {
+__global__ void k_bin_order(GridDev g, const int2* __restrict__ key, int ncells, const int* __restrict__ cstart,
+                            int* citem, float2* cpos, const double2* __restrict__ x, int item_cap, int* ccount) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   ccount[c] = 0;
@@ -205,9 +210,16 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
     }
     citem[t + 1] = v;
   }
+  const double ox = g.ox + (double)(c % g.n1) * g.h, oy = g.oy + (double)(c / g.n1) * g.h;
+  const float qnan = __int_as_float(0x7fc00000);
   for (int s = a; s < b; ++s) {
-    double2 p = x[citem[s]];
-    cpos[s] = make_float2((float)p.x, (float)p.y);
+    const int i = citem[s];
+    if (key[i].x == c) {
+      const double2 p = x[i];
+      cpos[s] = make_float2((float)(p.x - ox), (float)(p.y - oy));
+    } else {
+      cpos[s] = make_float2(qnan, qnan);
+    }
   }
 }
 
@@ -224,6 +236,9 @@ __global__ void k_bin_order(int ncells, const int* __restrict__ cstart, int* cit
 //    the bisector come from float; only vertices within the margin and the
 //    two crossing edges (whose intersection must be exact) are evaluated in
 //    FP64 with the reference's expressions;
+//  * a candidate's offset from the seed is formed in float from offsets to
+//    the cell corners (stored by the binning) and the path node's cell
+//    offset, so its error scales with the cell size, not with the coordinates;
 //  * the influence radius is an upper bound, which can only admit extra
 //    candidates that cannot cut (no-ops), and is replaced by the exact FP64
 //    value where the reference's "mesh destroyed" test needs it;
@@ -582,8 +597,8 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
 
 // Conservative float test: true only when the FP64 clip by this candidate
 // provably changes nothing (every vertex strictly inside the half-plane by
-// more than the rounding margin).  d32 = float(q) - float(x) carries an
-// absolute error <= g.delta32 per component.
+// more than the rounding margin).  The candidate's float offset (dx, dy) from
+// the seed carries an absolute error <= g.delta32 per component.
 __device__ __forceinline__ bool prefilter_no_cut(const Poly& P, int ne, float dx, float dy, float prr_up,
                                                  const GridDev& g) {
   const float d2 = dx * dx + dy * dy;
@@ -695,8 +710,18 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       k2 = (long long)f2 + 1;
     }
   }
-  const float x32 = (float)px, y32 = (float)py;
-  const float xp32 = (float)g.xperiod, yp32 = (float)g.yperiod;
+  // the seed's float offset from its cell's lower corner, and the current
+  // path node's cell offset (di1 h, di2 h) in float
+  float xo = 0.0f, yo = 0.0f, dhx = 0.0f, dhy = 0.0f;
+  if (active && !done) {
+    xo = (float)(px - (g.ox + (double)(k1 - 1) * g.h));
+    yo = (float)(py - (g.oy + (double)(k2 - 1) * g.h));
+    if (pn >= 0 && pn < g.npath) {  // a resumed search: the node it stands in
+      const PathNodeDev nd = path[pn];
+      dhx = (float)nd.di1 * g.h32;
+      dhy = (float)nd.di2 * g.h32;
+    }
+  }
   float prr_up = active ? prr_upper(P, ne) : 0.0f;
   bool saved = false;
   // voronoigrid.jl:53-81, in rounds
@@ -721,6 +746,8 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
           done = true;
           break;
         }
+        dhx = (float)nd.di1 * g.h32;
+        dhy = (float)nd.di2 * g.h32;
         const long long c1 = k1 + nd.di1, c2 = k2 + nd.di2;
         if (c1 < 1 || c1 > g.n1 || c2 < 1 || c2 > g.n2) {
           s = se = 0;
@@ -736,9 +763,9 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       const float2 q32 = cl.cpos[s];
       ++s;
       if (j == i) continue;  // y == x exactly: get_arrow(x, x) = 0
-      const float ddx = q32.x - x32, ddy = q32.y - y32;
-      const bool far_image = (g.xper && fabsf(ddx) > 0.45f * xp32) || (g.yper && fabsf(ddy) > 0.45f * yp32);
-      if (!far_image) {
+      // a periodic image (NaN offset) goes to the FP64 clip
+      if (!isnan(q32.x)) {
+        const float ddx = (q32.x - xo) + dhx, ddy = (q32.y - yo) + dhy;
         const float d2 = ddx * ddx + ddy * ddy;
         const float lo = d2 * (1.0f - 1e-6f) - 4.0f * g.delta32 * sqrtf(d2) - 4.0f * g.delta32 * g.delta32;
         if (lo > prr_up * (1.0f + 1e-6f)) continue;  // farther than the influence radius: cannot cut
@@ -999,8 +1026,8 @@ int lv_mesh_remesh(lv_ctx* c) {
   k_bin_scatter<<<lv_blocks(n, 256), 256, 0, s>>>(c->g, n, c->cap, c->c.bkey, c->c.cstart, c->c.citem,
                                                     c->c.item_cap, c->status);
   LV_LAUNCH_CHECK(c, "k_bin_scatter");
-  k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x, c->c.item_cap,
-                                                  c->c.ccount);
+  k_bin_order<<<lv_blocks(nc, 256), 256, 0, s>>>(c->g, c->c.bkey, nc, c->c.cstart, c->c.citem, c->c.cpos, c->s.x,
+                                                  c->c.item_cap, c->c.ccount);
   LV_LAUNCH_CHECK(c, "k_bin_order");
   c->ccount_clean = true;
   }
