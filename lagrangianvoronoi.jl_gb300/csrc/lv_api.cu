@@ -242,6 +242,11 @@ lv_ctx* lv_create(const lv_params* prm) {
   for (const PathNodeDev& nd : c->path_host)
     if (!nd.beyond) dmax = std::max(dmax, std::max(abs(nd.di1), abs(nd.di2)));
   g.h32 = (float)h;
+  {
+    const double hxp = 0.5 * g.xperiod, hyp = 0.5 * g.yperiod;
+    memcpy(&g.hxbits, &hxp, sizeof(double));
+    memcpy(&g.hybits, &hyp, sizeof(double));
+  }
   g.delta32 = (float)((ldexp(1.0, -24) * h * (6.0 + 4.0 * dmax) +
                        2e-15 * (bigm + std::max(g.xperiod, g.yperiod) + 2.0 * h)) * (1.0 + 1e-6));
 

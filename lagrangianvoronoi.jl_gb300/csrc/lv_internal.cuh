@@ -62,6 +62,7 @@ struct GridDev {
                   // (formed from the cell-relative offsets cpos and the path node's cell offset)
   float bigm;     // max |coordinate| inside the cropping box
   float h32;      // (float)h
+  long long hxbits, hybits;  // bit patterns of 0.5 * xperiod, 0.5 * yperiod (get_arrow's wrap test)
 };
 
 // One node of the candidate path (neighborlist.jl:29-41): cell offset and
@@ -111,6 +112,26 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
     return fma(r, y, q);
   }
   return a / b;
+}
+
+// 0.5 * v exactly, on the integer pipe: for a normal v whose exponent field
+// is at least 2 the product is v with the exponent lowered by one (no
+// rounding); zeros, subnormals, the smallest normals, infinities and NaN take
+// the multiplication.  FP64 instructions are priced per warp on this GPU, and
+// a halving is a frequent term of the reference's midpoints.
+__device__ __forceinline__ double half_exact(double v) {
+  const int hi = __double2hiint(v);
+  const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
+  if (e - 2u < 0x7fdu) return __hiloint2double(hi - (1 << 20), __double2loint(v));
+  return 0.5 * v;
+}
+
+// |v| > t for a double v and a positive finite t given by its bit pattern,
+// on the integer pipe (the order of non-negative doubles is the order of
+// their bit patterns; a NaN v compares greater, which the callers map to NaN
+// either way).
+__device__ __forceinline__ bool abs_greater(double v, long long tbits) {
+  return (__double_as_longlong(v) & 0x7fffffffffffffffLL) > tbits;
 }
 
 // Epilogue of every pressure solve (one thread): the cumulative counters

@@ -342,12 +342,6 @@ __device__ __forceinline__ void copy_slot(const Poly& P, int dst, int src) {
   P.r2y[a] = P.r2y[l];
 }
 
-__device__ __forceinline__ float prr_upper(const Poly& P, int ne) {
-  float m = 0.0f;
-  for (int k = 0; k < ne; ++k) m = fmaxf(m, d2_up(P.r1x[P.at(k)], P.r1y[P.at(k)]));
-  return m;
-}
-
 // polygon.jl:101-107, exact
 __device__ double influence_rr_exact(const Poly& P, int ne, double px, double py) {
   double rr = 0.0;
@@ -468,7 +462,7 @@ __device__ __forceinline__ void put_vertex(const Poly& P, int k, bool first, dou
 __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm,
                          PendingEdge& pend) {
   const double dfx = yx - px, dfy = yy - py;
-  const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
+  const double mx = half_exact(yx + px), my = half_exact(yy + py);
   const double c = dfx * mx + dfy * my;
   const float dx = (float)dfx, dy = (float)dfy;
   const float dd2 = dx * dx + dy * dy;
@@ -586,8 +580,20 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   }
   const float rXx = xl0 ? q0x : q1x, rXy = xl0 ? q0y : q1y;
   const float rYx = yf0 ? q0x : q1x, rYy = yf0 ? q0y : q1y;
-  const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
-  const bool inv = ax * by - ay * bx > 0.0;  // reorient counter-clockwise: Y -> X
+  // reorient counter-clockwise (Y -> X) when the reference's FP64
+  // (Y - X) x (p - X) > 0.  That product equals (X - p) x (Y - p), which the
+  // float offsets give to within 1e-6 of |rXx rYy| + |rXy rYx| (their 2^-24
+  // roundings and the float arithmetic) plus the FP64 rounding of the
+  // reference's expression (a few 1e-16 of the squared offsets); outside
+  // that margin its sign decides, otherwise the reference's expression does.
+  const float cf = rXx * rYy - rXy * rYx;
+  const float mo = 1e-6f * (fabsf(rXx * rYy) + fabsf(rXy * rYx)) +
+                   1e-14f * ((rXx * rXx + rXy * rXy) + (rYx * rYx + rYy * rYy)) + 1e-30f;
+  bool inv = cf > 0.0f;
+  if (!(fabsf(cf) > mo)) {
+    const double ax = Yx - Xx, ay = Yy - Xy, bx = px - Xx, by = py - Xy;
+    inv = ax * by - ay * bx > 0.0;
+  }
   put_vertex(P, ne, true, inv ? Yx : Xx, inv ? Yy : Xy, inv ? rYx : rXx, inv ? rYy : rXy);
   put_vertex(P, ne, false, inv ? Xx : Yx, inv ? Xy : Yy, inv ? rXx : rYx, inv ? rXy : rYy);
   P.lab[P.at(ne)] = label;
@@ -595,31 +601,14 @@ __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx
   return 1;
 }
 
-// Conservative float test: true only when the FP64 clip by this candidate
-// provably changes nothing (every vertex strictly inside the half-plane by
-// more than the rounding margin).  The candidate's float offset (dx, dy) from
-// the seed carries an absolute error <= g.delta32 per component.
-__device__ __forceinline__ bool prefilter_no_cut(const Poly& P, int ne, float dx, float dy, float prr_up,
-                                                 const GridDev& g) {
-  const float d2 = dx * dx + dy * dy;
-  const float D = sqrtf(d2) + 2.0f * g.delta32;
-  const float R = 0.5f * sqrtf(prr_up) * 1.0001f;
-  const float margin = 2.0f * g.delta32 * (R + 2.0f * D) + 4e-6f * (D * R + D * D) + 4e-15f * D * g.bigm + 1e-14f;
-  const float half = 0.5f * d2;
-  for (int k = 0; k < ne; ++k) {
-    const float f = dx * P.r1x[P.at(k)] + dy * P.r1y[P.at(k)] - half;
-    if (!(f < -margin)) return false;
-  }
-  return true;
-}
-
 // voronoigrid.jl:116-125
 __device__ __forceinline__ void get_arrow(const GridDev& g, double ax, double ay, double bx, double by, double& vx,
                                           double& vy) {
   vx = ax - bx;
   vy = ay - by;
-  if (g.xper && fabs(vx) > 0.5 * g.xperiod) vx -= (vx > 0 ? 1.0 : -1.0) * g.xperiod;
-  if (g.yper && fabs(vy) > 0.5 * g.yperiod) vy -= (vy > 0 ? 1.0 : -1.0) * g.yperiod;
+  // fabs(v) > 0.5 * period, compared on the integer pipe (the wrap is rare)
+  if (g.xper && abs_greater(vx, g.hxbits)) vx -= (vx > 0 ? 1.0 : -1.0) * g.xperiod;
+  if (g.yper && abs_greater(vy, g.hybits)) vy -= (vy > 0 ? 1.0 : -1.0) * g.yperiod;
 }
 
 // Shared-memory bytes of a block whose polygons have `cap` edge slots.
@@ -722,9 +711,55 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       dhy = (float)nd.di2 * g.h32;
     }
   }
-  float prr_up = active ? prr_upper(P, ne) : 0.0f;
+  // The float offsets of the polygon's vertices (v1 of each edge) in
+  // registers for the candidate tests, refreshed after each clip; slots past
+  // ne hold the seed (0, 0), which lies inside every half-plane (and adds 0
+  // to the influence bound).
+  float vrx[CAP], vry[CAP];
+  auto cache_poly = [&]() {
+#pragma unroll
+    for (int k = 0; k < CAP; ++k) {
+      const bool in = k < ne;
+      vrx[k] = in ? P.r1x[P.at(k)] : 0.0f;
+      vry[k] = in ? P.r1y[P.at(k)] : 0.0f;
+    }
+  };
+  // float upper bound of the influence radius prr = max 4 |v1 - x|^2
+  auto prr_cached = [&]() -> float {
+    float m = 0.0f;
+#pragma unroll
+    for (int k = 0; k < CAP; ++k) m = fmaxf(m, d2_up(vrx[k], vry[k]));
+    return m;
+  };
+  if (active) cache_poly();
+  float prr_up = active ? prr_cached() : 0.0f;
   bool saved = false;
-  // voronoigrid.jl:53-81, in rounds
+  // whether candidate j (float offset q from its cell's corner) may cut the
+  // current polygon; false only when provably not: farther than the
+  // influence radius, or every vertex strictly inside the half-plane by more
+  // than the rounding margin (the candidate's float offset from the seed
+  // carries an absolute error <= g.delta32 per component)
+  auto may_cut = [&](int j, float2 q) -> bool {
+    if (j == i) return false;  // y == x exactly: get_arrow(x, x) = 0
+    if (isnan(q.x)) return true;  // a periodic image: the FP64 clip decides
+    const float dx = (q.x - xo) + dhx, dy = (q.y - yo) + dhy;
+    const float d2 = dx * dx + dy * dy;
+    const float dd = sqrtf(d2);
+    const float lo = d2 * (1.0f - 1e-6f) - 4.0f * g.delta32 * dd - 4.0f * g.delta32 * g.delta32;
+    if (lo > prr_up * (1.0f + 1e-6f)) return false;  // farther than the influence radius
+    if (!chain_ok) return true;
+    const float D = dd + 2.0f * g.delta32;
+    const float R = 0.5f * sqrtf(prr_up) * 1.0001f;
+    const float margin = 2.0f * g.delta32 * (R + 2.0f * D) + 4e-6f * (D * R + D * D) + 4e-15f * D * g.bigm + 1e-14f;
+    float fm = 0.0f;  // the seed's value; every vertex's below
+#pragma unroll
+    for (int k = 0; k < CAP; ++k) fm = fmaxf(fm, __fmaf_rn(dx, vrx[k], dy * vry[k]));
+    return !(fm - 0.5f * d2 < -margin);
+  };
+  // voronoigrid.jl:53-81, in rounds.  Between two clips a lane scans its
+  // candidates in groups of up to CLIP_GROUP items of one cell, whose loads
+  // are issued together (the scan is bound by the latency of these loads).
+  constexpr int CLIP_GROUP = 4;
   while (true) {
     bool have = false;
     int cj = 0;
@@ -757,22 +792,26 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
         // (clamped: a cell list that overflowed is reported by the binning)
         se = min(cl.cstart[cell + 1], cl.item_cap);
         s = min(cl.cstart[cell], se);
-        continue;
+        if (s >= se) continue;
       }
-      const int j = cl.citem[s];
-      const float2 q32 = cl.cpos[s];
-      ++s;
-      if (j == i) continue;  // y == x exactly: get_arrow(x, x) = 0
-      // a periodic image (NaN offset) goes to the FP64 clip
-      if (!isnan(q32.x)) {
-        const float ddx = (q32.x - xo) + dhx, ddy = (q32.y - yo) + dhy;
-        const float d2 = ddx * ddx + ddy * ddy;
-        const float lo = d2 * (1.0f - 1e-6f) - 4.0f * g.delta32 * sqrtf(d2) - 4.0f * g.delta32 * g.delta32;
-        if (lo > prr_up * (1.0f + 1e-6f)) continue;  // farther than the influence radius: cannot cut
-        if (chain_ok && prefilter_no_cut(P, ne, ddx, ddy, prr_up, g)) continue;
+      const int cnt = min(CLIP_GROUP, se - s);
+      int jj[CLIP_GROUP];
+      float2 qq[CLIP_GROUP];
+#pragma unroll
+      for (int u = 0; u < CLIP_GROUP; ++u) {
+        const int idx = s + min(u, cnt - 1);
+        jj[u] = cl.citem[idx];
+        qq[u] = cl.cpos[idx];
       }
-      have = true;
-      cj = j;
+      int adv = cnt;
+#pragma unroll
+      for (int u = 0; u < CLIP_GROUP; ++u)
+        if (!have && u < cnt && may_cut(jj[u], qq[u])) {
+          have = true;
+          cj = jj[u];
+          adv = u + 1;
+        }
+      s += adv;
     }
     if (!__any_sync(0xffffffffu, have)) break;
     if (have) {
@@ -817,7 +856,8 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
         }
         done = true;
       }
-      prr_up = prr_upper(P, ne);
+      cache_poly();
+      prr_up = prr_cached();
     }
   }
   // a polygon captured for the second pass is not written here
@@ -884,7 +924,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       const double v1x = P.v1x[a], v1y = P.v1y[a], v2x = P.v2x[a], v2y = P.v2y[a];
       const int lab = P.lab[a];
       const double ax = v1x - tpx, ay = v1y - tpy, bx = v2x - tpx, by = v2y - tpy;
-      const double dA = 0.5 * fabs(ax * by - ay * bx);
+      const double dA = half_exact(fabs(ax * by - ay * bx));
       const double sx = (tpx + v1x) + v2x, sy = (tpy + v1y) + v2y;
       P.v1x[a] = dA;
       P.v1y[a] = div3(dA * sx);
@@ -904,7 +944,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
         const size_t f = (size_t)__popc(tfm & ((1u << k) - 1u)) * cap + ti;
         m.fnbr[f] = lab;
         m.flrr[f] = sqrt(l2 / r2);
-        m.fm[f] = make_double2(0.5 * (v1x + v2x), 0.5 * (v1y + v2y));
+        m.fm[f] = make_double2(half_exact(v1x + v2x), half_exact(v1y + v2y));
         m.fy[f] = make_double2(yx, yy);
       }
     }
