@@ -316,6 +316,7 @@ lv_ctx* lv_create(const lv_params* prm) {
   m.fm = dalloc<double2>(c, ell, &ok);
   m.fy = dalloc<double2>(c, ell, &ok);
   m.area = dalloc<double>(c, cap, &ok);
+  m.rperm = dalloc<int>(c, cap, &ok);
   m.centroid = dalloc<double2>(c, cap, &ok);
 
   CellsDev& cl = c->c;

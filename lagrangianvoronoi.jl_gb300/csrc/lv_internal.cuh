@@ -92,7 +92,17 @@ struct MeshDev {
   double2 *fm, *fy;
   double* area;
   double2* centroid;
+  // The face kernels' thread -> row map: within each window of
+  // LV_RPERM_WINDOW consecutive rows, the rows ordered by face count (stable),
+  // so that the rows of a warp have nearly the same number of faces.  FP64
+  // instructions are priced per warp on this GPU, and a warp runs its face
+  // loop as often as its largest row needs.  Rebuilt by every remesh.
+  int* rperm;
 };
+constexpr int LV_RPERM_WINDOW = 256;
+
+// The row of face-kernel thread t (t < n).
+__device__ __forceinline__ int face_row(const MeshDev& m, int t) { return __ldg(m.rperm + t); }
 
 // RN(a / b) from y = RN(1/b) without a division (Markstein, IBM J. Res. Dev.
 // 34(1), 1990): q0 = RN(a y) lies within 1.5 ulp of a/b, one correction

@@ -1014,6 +1014,37 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len) {
   return LV_OK;
 }
 
+// The face kernels' row order (MeshDev::rperm): one block per window of
+// LV_RPERM_WINDOW rows, a stable counting sort by face count.  Lanes of a
+// warp with the same count rank themselves by __match_any_sync; the counts of
+// each warp and bucket give every bucket's and warp's offset.
+constexpr int RP_BUCKETS = LV_MAX_EDGES + 2;  // face counts 0..LV_MAX_EDGES, then rows past n
+__global__ void __launch_bounds__(LV_RPERM_WINDOW) k_rperm(MeshDev m, int n) {
+  constexpr int NW = LV_RPERM_WINDOW / 32;
+  __shared__ int wc[NW][RP_BUCKETS], wo[NW][RP_BUCKETS];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int i = blockIdx.x * LV_RPERM_WINDOW + t;
+  for (int k = t; k < NW * RP_BUCKETS; k += LV_RPERM_WINDOW) wc[k / RP_BUCKETS][k % RP_BUCKETS] = 0;
+  __syncthreads();
+  const int b = i < n ? min(max(m.nfaces[i], 0), LV_MAX_EDGES) : LV_MAX_EDGES + 1;
+  const unsigned same = __match_any_sync(0xffffffffu, b);
+  const int rank = __popc(same & ((1u << lane) - 1u));
+  if (lane == __ffs(same) - 1) wc[w][b] = __popc(same);
+  __syncthreads();
+  if (t < RP_BUCKETS) {
+    // bucket t: its start over the window, then each warp's offset in it
+    int acc = 0;
+    for (int q = 0; q < t; ++q)
+      for (int v = 0; v < NW; ++v) acc += wc[v][q];
+    for (int v = 0; v < NW; ++v) {
+      wo[v][t] = acc;
+      acc += wc[v][t];
+    }
+  }
+  __syncthreads();
+  if (i < n) m.rperm[blockIdx.x * LV_RPERM_WINDOW + wo[w][b] + rank] = i;
+}
+
 __global__ void k_face_len(MeshDev m, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) lv_face_lengths(m, i);
@@ -1095,6 +1126,8 @@ int lv_mesh_remesh(lv_ctx* c) {
     k_clip_redo<<<3 * c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status,
                                                                redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip_redo");
+    k_rperm<<<(n + LV_RPERM_WINDOW - 1) / LV_RPERM_WINDOW, LV_RPERM_WINDOW, 0, s>>>(c->m, n);
+    LV_LAUNCH_CHECK(c, "k_rperm");
   }
   c->meshed = true;
   c->op_ready = false;

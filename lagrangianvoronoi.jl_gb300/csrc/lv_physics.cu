@@ -69,8 +69,9 @@ __global__ void k_gravity(StateDev s, int n, double gx, double gy, double dt) {
 
 // pressure_step! (pressure.jl:10-25), velocity pass.
 __global__ void k_pstep_v(StateDev s, MeshDev m, int n, double dt) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double Pi = s.P[i], mi = s.mass[i];
@@ -101,8 +102,9 @@ __global__ void k_pstep_v(StateDev s, MeshDev m, int n, double dt) {
 
 // pressure_step! energy pass (uses the updated velocities).
 __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n, double dt) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double Pi = s.P[i], mi = s.mass[i];
@@ -157,8 +159,9 @@ __global__ void __launch_bounds__(TPB, 2) k_pstep_e(StateDev s, MeshDev m, int n
 __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, SolverDev sv, int n, double dt, Wall2 vbc_ud,
                                                      Wall2 vbc_rl, const double2* __restrict__ bvel,
                                                      const int* __restrict__ boff) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   const double2 xi = s.x[i];
   const double2 vi = s.v[i];
@@ -225,8 +228,9 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
 // previous call's change D (lv_sweep_sums; all threads of the block take
 // part, so rows past n do not return early).
 __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess, const float* D) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool on = i < n;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n;
+  const int i = on ? face_row(m, t) : t;
   double bi = 0.0, Pi = 0.0;
   if (on) {
     const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
@@ -303,8 +307,9 @@ __global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int
 // d1 and D (nullptr: none) and the residual b_k - b_{k-1} (lv_sweep_sums;
 // all threads of the block take part, so rows past n do not return early).
 __global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess, const float* D) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool on = i < n;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = t < n;
+  const int i = on ? face_row(m, t) : t;
   double bi = 0.0;
   if (on) {
     const int cap = m.cap, nf = m.nfaces[i];
@@ -342,8 +347,9 @@ __global__ void k_rhs_gp(StateDev s, MeshDev m, SolverDev sv, int n, int guess, 
 
 // find_D! (diffusion.jl:8-19)
 __global__ void k_find_D(StateDev s, MeshDev m, int n) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 vi = s.v[i];
   double d11 = 0.0, d21 = 0.0, d12 = 0.0, d22 = 0.0;
@@ -397,8 +403,9 @@ __global__ void k_stress(StateDev s, int n, double avdr, double2* Sa, double2* S
 // viscous_step! velocity pass (diffusion.jl:41-46)
 __global__ void __launch_bounds__(TPB, 2) k_visc_v(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
                          const double2* __restrict__ Sb) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double mi = s.mass[i];
@@ -439,8 +446,9 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_v(StateDev s, MeshDev m, int n,
 // viscous_step! energy pass (diffusion.jl:47-52)
 __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n, double dt, const double2* __restrict__ Sa,
                          const double2* __restrict__ Sb) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double mi = s.mass[i];
@@ -486,8 +494,9 @@ __global__ void __launch_bounds__(TPB, 2) k_visc_e(StateDev s, MeshDev m, int n,
 __global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, Wall2 w_rl,
                            const double2* __restrict__ bvel, const int* __restrict__ boff,
                            const unsigned char* __restrict__ act) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   if (nf == ne) {
     // no boundary edge: v = v/1.0 leaves v unchanged
@@ -539,8 +548,9 @@ __global__ void k_friction(StateDev s, MeshDev m, int n, double dt, Wall2 w_ud, 
 
 // find_dv! (relaxation.jl:10-25)
 __global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double2 c = m.centroid[i];
@@ -577,8 +587,9 @@ __global__ void k_find_dv(StateDev s, MeshDev m, int n, double dt, double alpha)
 // reads it (the same expression, so the same value); lens: also the face
 // lengths of the mesh (lv_face_lengths)
 __global__ void k_norm_dv(StateDev s, MeshDev m, int n, double* ndv, int lens) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const double2 d = s.dv[i];
   ndv[i] = sqrt(d.x * d.x + d.y * d.y);
   if (lens) lv_face_lengths(m, i);
@@ -586,8 +597,9 @@ __global__ void k_norm_dv(StateDev s, MeshDev m, int n, double* ndv, int lens) {
 
 // ndv: |dv| of every particle (k_norm_dv), read when rusanov is set
 __global__ void __launch_bounds__(TPB, 2) k_relax_flux(StateDev s, MeshDev m, int n, double dt, int rusanov, const double* __restrict__ ndv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const double rp = s.rho[i], ep = s.e[i];
@@ -734,8 +746,9 @@ __global__ void k_move(GridDev g, StateDev s, MeshDev m, int n, double dt, int* 
 // relaxation.jl:157-169: b_i = -sum_{cross-phase faces} lrr (dot(dv_i - dv_j, m - z)
 //                                   - 0.5 dot(dv_i + dv_j, x_i - y))
 __global__ void k_mp_rhs(StateDev s, MeshDev m, int n, double* b) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i], dvi = s.dv[i];
   const int ph = s.phase[i];
@@ -757,8 +770,9 @@ __global__ void k_mp_rhs(StateDev s, MeshDev m, int n, double* b) {
 
 // relaxation.jl:92-106: tmp_i = -(1/area) sum lrr (x_i - x_j)(m - x_i)
 __global__ void k_mp_apply1(StateDev s, MeshDev m, int n, const double* __restrict__ xin, double2* tmp) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const int ph = s.phase[i];
@@ -780,8 +794,9 @@ __global__ void k_mp_apply1(StateDev s, MeshDev m, int n, const double* __restri
 
 // relaxation.jl:107-121
 __global__ void k_mp_apply2(StateDev s, MeshDev m, int n, const double2* __restrict__ tmp, double* res) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double2 xi = s.x[i];
   const int ph = s.phase[i];
@@ -921,8 +936,9 @@ __global__ void k_ideal_temperature(StateDev s, int n) {
 
 // fourier_step! (fourier.jl:14-28): e -= dt k / m lrr (T_i - T_j), k = (k_i + k_j)/2, faces in order
 __global__ void k_fourier(StateDev s, MeshDev m, int n, double dt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double Ti = s.T[i], ki = s.kc[i], mi = s.mass[i];
   double e = s.e[i];
@@ -956,8 +972,9 @@ __global__ void k_fourier(StateDev s, MeshDev m, int n, double dt) {
 // it raises LV_FLAG_BAD_INPUT and is left unchanged.
 __global__ void k_heat_bdary(GridDev g, StateDev s, MeshDev m, int n, double dt, const double* __restrict__ Tb,
                              const int* __restrict__ boff, int* status) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i], ne = m.nedges[i];
   if (nf == ne) return;  // !isboundary(p)
   const double cV = s.cV[i];
@@ -1003,8 +1020,9 @@ __global__ void k_heat_bdary(GridDev g, StateDev s, MeshDev m, int n, double dt,
 // entries); b = (m/dt) v and the first guess v, interleaved (v_index).
 __global__ void k_visc_sys(StateDev s, MeshDev m, int n, double dt, const int* __restrict__ rowptr, int* col,
                            double* w, double* diag, double* b, double* u0) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double mi = s.mass[i], mui = s.mu[i];
   const double2 v = s.v[i];

@@ -41,8 +41,9 @@ __global__ void k_half_rho(const double* __restrict__ rho, double* hr, int n, in
 // guess) and the flag of a nonsingular operator (some diagonal term != 0).
 __global__ void k_assemble(StateDev s, MeshDev m, SolverDev sv, int n, double dt, const double* __restrict__ hr,
                            int* nonsingular) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = face_row(m, t);
   const int cap = m.cap, nf = m.nfaces[i];
   const double rho = s.rho[i];
   const double diag = s.mass[i] / (rho * rho * s.c2[i] * (dt * dt));
