@@ -124,18 +124,6 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   return a / b;
 }
 
-// 0.5 * v exactly, on the integer pipe: for a normal v whose exponent field
-// is at least 2 the product is v with the exponent lowered by one (no
-// rounding); zeros, subnormals, the smallest normals, infinities and NaN take
-// the multiplication.  FP64 instructions are priced per warp on this GPU, and
-// a halving is a frequent term of the reference's midpoints.
-__device__ __forceinline__ double half_exact(double v) {
-  const int hi = __double2hiint(v);
-  const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
-  if (e - 2u < 0x7fdu) return __hiloint2double(hi - (1 << 20), __double2loint(v));
-  return 0.5 * v;
-}
-
 // |v| > t for a double v and a positive finite t given by its bit pattern,
 // on the integer pipe (the order of non-negative doubles is the order of
 // their bit patterns; a NaN v compares greater, which the callers map to NaN
@@ -431,23 +419,27 @@ __device__ __forceinline__ void lv_sweep_sums(const SolverDev& sv, int i, bool o
     acc[6] = d1;
     acc[7] = (double)f2;
   }
-  __shared__ double sh[LV_SG_SUMS][LV_SG_TPB / 32];
+  // The block's sums: warp q adds sum q over the block's threads (eight
+  // values per lane, then five shuffle levels).  FP64 additions are priced
+  // per warp instruction on this GPU, so one warp per sum instead of a
+  // shuffle tree in every warp.
+  __shared__ double sh[LV_SG_SUMS][LV_SG_TPB];
   __shared__ bool s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nsum = singular ? LV_SG_SUMS : 5;
 #pragma unroll
-  for (int q = 0; q < LV_SG_SUMS; ++q) {
-    if (q >= nsum) break;  // uniform
-    double v = acc[q];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[q][wid] = v;
-  }
+  for (int q = 0; q < LV_SG_SUMS; ++q)
+    if (q < nsum) sh[q][threadIdx.x] = acc[q];
   __syncthreads();
-  if ((int)threadIdx.x < nsum) {
+  if (wid < nsum) {
     double v = 0.0;
-    for (int k = 0; k < LV_SG_TPB / 32; ++k) v += sh[threadIdx.x][k];
-    sv.sgpart[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
-    __threadfence();
+#pragma unroll
+    for (int k = 0; k < LV_SG_TPB / 32; ++k) v += sh[wid][lane + 32 * k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      sv.sgpart[(size_t)wid * gridDim.x + blockIdx.x] = v;
+      __threadfence();
+    }
   }
   __syncthreads();
   unsigned* counter = sv.bar + 3;

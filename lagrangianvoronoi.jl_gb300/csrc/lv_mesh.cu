@@ -462,7 +462,7 @@ __device__ __forceinline__ void put_vertex(const Poly& P, int k, bool first, dou
 __device__ int clip_fast(const Poly& P, int& ne, double px, double py, double yx, double yy, int label, float bigm,
                          PendingEdge& pend) {
   const double dfx = yx - px, dfy = yy - py;
-  const double mx = half_exact(yx + px), my = half_exact(yy + py);
+  const double mx = 0.5 * (yx + px), my = 0.5 * (yy + py);
   const double c = dfx * mx + dfy * my;
   const float dx = (float)dfx, dy = (float)dfy;
   const float dd2 = dx * dx + dy * dy;
@@ -924,7 +924,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       const double v1x = P.v1x[a], v1y = P.v1y[a], v2x = P.v2x[a], v2y = P.v2y[a];
       const int lab = P.lab[a];
       const double ax = v1x - tpx, ay = v1y - tpy, bx = v2x - tpx, by = v2y - tpy;
-      const double dA = half_exact(fabs(ax * by - ay * bx));
+      const double dA = 0.5 * fabs(ax * by - ay * bx);
       const double sx = (tpx + v1x) + v2x, sy = (tpy + v1y) + v2y;
       P.v1x[a] = dA;
       P.v1y[a] = div3(dA * sx);
@@ -944,7 +944,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
         const size_t f = (size_t)__popc(tfm & ((1u << k) - 1u)) * cap + ti;
         m.fnbr[f] = lab;
         m.flrr[f] = sqrt(l2 / r2);
-        m.fm[f] = make_double2(half_exact(v1x + v2x), half_exact(v1y + v2y));
+        m.fm[f] = make_double2(0.5 * (v1x + v2x), 0.5 * (v1y + v2y));
         m.fy[f] = make_double2(yx, yy);
       }
     }
