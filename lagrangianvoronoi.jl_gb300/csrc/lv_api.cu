@@ -242,6 +242,12 @@ lv_ctx* lv_create(const lv_params* prm) {
   for (const PathNodeDev& nd : c->path_host)
     if (!nd.beyond) dmax = std::max(dmax, std::max(abs(nd.di1), abs(nd.di2)));
   g.h32 = (float)h;
+  // four cell sizes of margin: the grid ends 2h past the cropping box, and
+  // the float rounding of a position is far below h
+  g.ixlo = (float)(g.bminx + r_max + 4.0 * h);
+  g.ixhi = (float)(g.bmaxx - r_max - 4.0 * h);
+  g.iylo = (float)(g.bminy + r_max + 4.0 * h);
+  g.iyhi = (float)(g.bmaxy - r_max - 4.0 * h);
   {
     const double hxp = 0.5 * g.xperiod, hyp = 0.5 * g.yperiod;
     memcpy(&g.hxbits, &hxp, sizeof(double));

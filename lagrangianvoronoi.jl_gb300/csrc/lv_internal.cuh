@@ -63,6 +63,10 @@ struct GridDev {
   float bigm;     // max |coordinate| inside the cropping box
   float h32;      // (float)h
   long long hxbits, hybits;  // bit patterns of 0.5 * xperiod, 0.5 * yperiod (get_arrow's wrap test)
+  // a position whose float x lies strictly inside (ixlo, ixhi) has no
+  // x-shifted periodic image in the cell grid (likewise y): the images only
+  // reach the grid from within r_max + 2h of a periodic boundary
+  float ixlo, ixhi, iylo, iyhi;
 };
 
 // One node of the candidate path (neighborlist.jl:29-41): cell offset and

@@ -122,23 +122,33 @@ __device__ __forceinline__ int cell_of(const GridDev& g, double px, double py, b
 __device__ __forceinline__ int image_count(const GridDev& g) {
   return 1 + (g.xper ? 2 : 0) + (g.yper ? 2 : 0) + ((g.xper && g.yper) ? 4 : 0);
 }
-__device__ __forceinline__ void image_pos(const GridDev& g, int k, double px, double py, double& qx, double& qy) {
-  // order: x; x+X, x-X (xper); x+Y, x-Y (yper); x+X+Y, x+X-Y, x-X+Y, x-X-Y (both)
-  int sx = 0, sy = 0;
-  if (k > 0) {
-    int kk = k - 1;
-    if (g.xper) {
-      if (kk < 2) { sx = kk == 0 ? 1 : -1; goto done; }
-      kk -= 2;
+// the period shifts (sx, sy) of copy k, in the order
+// x; x+X, x-X (xper); x+Y, x-Y (yper); x+X+Y, x+X-Y, x-X+Y, x-X-Y (both)
+__device__ __forceinline__ void image_shift(const GridDev& g, int k, int& sx, int& sy) {
+  sx = 0;
+  sy = 0;
+  if (k == 0) return;
+  int kk = k - 1;
+  if (g.xper) {
+    if (kk < 2) {
+      sx = kk == 0 ? 1 : -1;
+      return;
     }
-    if (g.yper) {
-      if (kk < 2) { sy = kk == 0 ? 1 : -1; goto done; }
-      kk -= 2;
-    }
-    sx = (kk < 2) ? 1 : -1;
-    sy = (kk % 2 == 0) ? 1 : -1;
+    kk -= 2;
   }
-done:
+  if (g.yper) {
+    if (kk < 2) {
+      sy = kk == 0 ? 1 : -1;
+      return;
+    }
+    kk -= 2;
+  }
+  sx = (kk < 2) ? 1 : -1;
+  sy = (kk % 2 == 0) ? 1 : -1;
+}
+__device__ __forceinline__ void image_pos(const GridDev& g, int k, double px, double py, double& qx, double& qy) {
+  int sx, sy;
+  image_shift(g, k, sx, sy);
   qx = px;
   qy = py;
   if (sx > 0) qx = qx + g.xperiod;
@@ -158,7 +168,19 @@ __global__ void k_bin_count(GridDev g, const double2* __restrict__ x, int n, int
   if (i >= n) return;
   double2 p = x[i];
   int nim = image_count(g);
+  // x- (y-) shifted images of a position well inside the domain lie outside
+  // the grid (decided in float, skipping their FP64 position and cell tests)
+  const float fx = (float)p.x, fy = (float)p.y;
+  const bool farx = fx > g.ixlo && fx < g.ixhi, fary = fy > g.iylo && fy < g.iyhi;
   for (int k = 0; k < nim; ++k) {
+    if (k > 0 && (farx || fary)) {
+      int sx, sy;
+      image_shift(g, k, sx, sy);
+      if ((sx != 0 && farx) || (sy != 0 && fary)) {
+        key[(size_t)k * cap + i] = make_int2(-1, 0);
+        continue;
+      }
+    }
     double qx, qy;
     image_pos(g, k, p.x, p.y, qx, qy);
     int c = cell_of(g, qx, qy, k > 0);

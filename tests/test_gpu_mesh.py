@@ -34,8 +34,10 @@ def test_cell_list_bit_exact(lv, oracle, name):
 
 
 @pytest.mark.parametrize("name", list(SMALL))
-@pytest.mark.parametrize("jitter", [0.1, 0.3])
+@pytest.mark.parametrize("jitter", [0.0, 0.1, 0.3])
 def test_polygons_bit_exact(lv, oracle, name, jitter):
+    """jitter 0: the unperturbed lattice, where four seeds share every
+    vertex and the clipping meets vertices on the bisector (signum 0)."""
     flow = SMALL[name]()
     x, g, og = _pair(lv, oracle, flow, seed=7, jitter=jitter)
     counts, verts, labels = g.geometry()
@@ -67,6 +69,29 @@ def test_faces_bit_exact(lv, oracle, name):
     rp, nb = F["rowptr"], F["nbr"]
     pairs = {(i, int(nb[k])) for i in range(len(x)) for k in range(rp[i], rp[i + 1])}
     assert all((j, i) in pairs for (i, j) in pairs)
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_hex_lattice_bit_exact(lv, oracle, periodic):
+    """populate_hex! seeds (src/populate.jl:155-179): three cells meet at every
+    vertex and the rows are offset by half a spacing."""
+    from lvgpu import populate as pop
+    flow = W.taylor_green(40) if periodic else W.cavity(40)
+    x = pop.hex_seeds(flow.xlims, flow.ylims, flow.dr)
+    g = H.make_gpu(lv, flow, x)
+    og = H.make_oracle(oracle, flow, x)
+    counts, verts, labels = g.geometry()
+    E = og.edges(maxe=20)
+    assert E["status"] == 0
+    assert np.array_equal(counts, E["counts"])
+    for i in range(len(x)):
+        k = counts[i]
+        assert np.array_equal(labels[i, :k], E["labels"][i, :k]), i
+        assert np.array_equal(verts[i, :k], E["verts"][i, :k]), i
+    assert np.array_equal(g["area"], E["area"])
+    F, R = g.faces(), og.faces()
+    for key in ("rowptr", "nbr", "lrr", "mid", "y", "len"):
+        assert np.array_equal(F[key], R[key]), key
 
 
 def test_remesh_after_motion(lv, oracle):
