@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __r
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int row = row0 + quarter * 32 + lane;
     if (row < n) {
-      float4* zr = reinterpret_cast<float4*>(Z + (size_t)row * HID + cb);
+      float4* zr = Z ? reinterpret_cast<float4*>(Z + (size_t)row * HID + cb) : nullptr;
       float4* hr = reinterpret_cast<float4*>(Hout + (size_t)row * HID + cb);
       const float4* hin = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + cb);
 #pragma unroll
@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __r
         h[1] = h0.y + fmaxf(z[1], 0.f);
         h[2] = h0.z + fmaxf(z[2], 0.f);
         h[3] = h0.w + fmaxf(z[3], 0.f);
-        zr[c4] = make_float4(z[0], z[1], z[2], z[3]);
+        if (zr) zr[c4] = make_float4(z[0], z[1], z[2], z[3]);
         hr[c4] = make_float4(h[0], h[1], h[2], h[3]);
       }
     }
@@ -1182,7 +1182,9 @@ int prepare(lv_ctx* c, const LearnSystem& S) {
   return lv_cuda_check(c, cudaGetLastError(), "learned: prepare");
 }
 
-int forward(lv_ctx* c, const LearnSystem& S) {
+// infer: the per-step factor, which needs no pre-activations (Z is kept for
+// the backward pass of training only)
+int forward(lv_ctx* c, const LearnSystem& S, bool infer = false) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
   // 128-row tiles, all at once while they fit four blocks per SM (the
@@ -1194,11 +1196,11 @@ int forward(lv_ctx* c, const LearnSystem& S) {
     c->launches++;
   }
   k_layer_fwd<FIN><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0,
-                                           0, L->Z0, L->H1, c->status);
+                                           0, infer ? nullptr : L->Z0, L->H1, c->status);
   k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1,
-                                           1, L->Z1, L->H2, c->status);
+                                           1, infer ? nullptr : L->Z1, L->H2, c->status);
   k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2,
-                                           1, L->Z2, L->H3, c->status);
+                                           1, infer ? nullptr : L->Z2, L->H3, c->status);
   k_readout<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd,
                                                            L->gl);
   if (L->hops == 2) {
@@ -1293,7 +1295,7 @@ int lv_learn_factor_current(lv_ctx* c) {
   // an untrained network (all parameters zero) gives Gt = I, i.e. Jacobi
   LearnSystem S = current_system(c);
   if (int rc = prepare(c, S)) return rc;
-  return forward(c, S);
+  return forward(c, S, true);
 }
 
 void lv_learn_free(lv_ctx* c) {
