@@ -230,57 +230,93 @@ __global__ void k_hop2_rev(int n, const int* __restrict__ rowptr2, const int* __
 
 // ---------------------------------------------------------------- forward
 
+// Feature rows stored as FP32 (training, whose backward pass reads them) or
+// as BF16 (the per-step factor: the layer products take BF16 operands
+// anyway, and half the bytes move).  A 16-byte chunk holds PER features.
+template <typename T>
+struct FeatIO;
+template <>
+struct FeatIO<float> {
+  static constexpr int PER = 4;
+  using Chunk = float4;
+  __device__ static float get(const float4& c, int e) { return e == 0 ? c.x : (e == 1 ? c.y : (e == 2 ? c.z : c.w)); }
+  // NB neighbours per round: their loads in flight together
+  static constexpr int NB = 2;
+};
+template <>
+struct FeatIO<__nv_bfloat16> {
+  static constexpr int PER = 8;
+  using Chunk = uint4;
+  __device__ static float get(const uint4& c, int e) {
+    const unsigned u = e < 2 ? c.x : (e < 4 ? c.y : (e < 6 ? c.z : c.w));
+    return __uint_as_float((e & 1) ? (u & 0xffff0000u) : (u << 16));
+  }
+  static constexpr int NB = 4;
+};
+
+// 16 features of a row from registers
+__device__ __forceinline__ void store_feat(float* p, const float (&h)[16]) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) q[c] = make_float4(h[4 * c], h[4 * c + 1], h[4 * c + 2], h[4 * c + 3]);
+}
+__device__ __forceinline__ void store_feat(__nv_bfloat16* p, const float (&h)[16]) {
+  uint4* q = reinterpret_cast<uint4*>(p);
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+    q[c] = make_uint4(pack_bf16(h[8 * c], h[8 * c + 1]), pack_bf16(h[8 * c + 2], h[8 * c + 3]),
+                      pack_bf16(h[8 * c + 4], h[8 * c + 5]), pack_bf16(h[8 * c + 6], h[8 * c + 7]));
+}
+
 // Row r's own features and aggregation Agg(Hin)_r = sum_k what_k Hin[col_k]
 // for lane (r, half): half (l >> 4) of the KH features; rows past n give
-// zeros.  Two neighbours per round, their loads issued together; the sum runs
-// over the neighbours in order.
-template <int KH>
-__device__ __forceinline__ void aggregate_row(int row, int half, int n, const float* __restrict__ Hin,
+// zeros.  FeatIO<T>::NB neighbours per round, their loads issued together;
+// the sum runs over the neighbours in order.
+template <int KH, typename T>
+__device__ __forceinline__ void aggregate_row(int row, int half, int n, const T* __restrict__ Hin,
                                               const int* __restrict__ rowptr, const int* __restrict__ col,
                                               const float* __restrict__ what, float (&own)[KH / 2],
                                               float (&agg)[KH / 2]) {
-  constexpr int FH = KH / 2;
-  static_assert(FH % 4 == 0, "16-byte feature chunks");
+  using IO = FeatIO<T>;
+  using Chunk = typename IO::Chunk;
+  constexpr int FH = KH / 2, PER = IO::PER, NC = FH / PER, NB = IO::NB;
+  static_assert(FH % PER == 0, "16-byte feature chunks");
 #pragma unroll
   for (int f = 0; f < FH; ++f) agg[f] = own[f] = 0.f;
   if (row >= n) return;
-  const float4* hr = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
+  {
+    const Chunk* hr = reinterpret_cast<const Chunk*>(Hin + (size_t)row * KH + half * FH);
 #pragma unroll
-  for (int f = 0; f < FH / 4; ++f) {
-    const float4 v = hr[f];
-    own[4 * f] = v.x;
-    own[4 * f + 1] = v.y;
-    own[4 * f + 2] = v.z;
-    own[4 * f + 3] = v.w;
+    for (int c = 0; c < NC; ++c) {
+      const Chunk v = hr[c];
+#pragma unroll
+      for (int e = 0; e < PER; ++e) own[c * PER + e] = IO::get(v, e);
+    }
   }
   const int k1 = rowptr[row + 1];
-  for (int k = rowptr[row]; k < k1; k += 2) {
-    const bool two = k + 1 < k1;
-    const int ja = col[k], jb = two ? col[k + 1] : ja;
-    const float wa = what[k], wb = two ? what[k + 1] : 0.f;
-    const float4* ha = reinterpret_cast<const float4*>(Hin + (size_t)ja * KH + half * FH);
-    const float4* hb = reinterpret_cast<const float4*>(Hin + (size_t)jb * KH + half * FH);
-    float4 va[FH / 4], vb[FH / 4];
+  for (int k = rowptr[row]; k < k1; k += NB) {
+    int jj[NB];
+    float ww[NB];
 #pragma unroll
-    for (int f = 0; f < FH / 4; ++f) {
-      va[f] = ha[f];
-      vb[f] = hb[f];
+    for (int u = 0; u < NB; ++u) {
+      const int kk = min(k + u, k1 - 1);
+      jj[u] = col[kk];
+      ww[u] = what[kk];
+    }
+    Chunk ch[NB][NC];
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const Chunk* hj = reinterpret_cast<const Chunk*>(Hin + (size_t)jj[u] * KH + half * FH);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) ch[u][c] = hj[c];
     }
 #pragma unroll
-    for (int f = 0; f < FH / 4; ++f) {
-      agg[4 * f] = fmaf(wa, va[f].x, agg[4 * f]);
-      agg[4 * f + 1] = fmaf(wa, va[f].y, agg[4 * f + 1]);
-      agg[4 * f + 2] = fmaf(wa, va[f].z, agg[4 * f + 2]);
-      agg[4 * f + 3] = fmaf(wa, va[f].w, agg[4 * f + 3]);
-    }
-    if (two) {
+    for (int u = 0; u < NB; ++u) {
+      if (k + u >= k1) break;
 #pragma unroll
-      for (int f = 0; f < FH / 4; ++f) {
-        agg[4 * f] = fmaf(wb, vb[f].x, agg[4 * f]);
-        agg[4 * f + 1] = fmaf(wb, vb[f].y, agg[4 * f + 1]);
-        agg[4 * f + 2] = fmaf(wb, vb[f].z, agg[4 * f + 2]);
-        agg[4 * f + 3] = fmaf(wb, vb[f].w, agg[4 * f + 3]);
-      }
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int e = 0; e < PER; ++e) agg[c * PER + e] = fmaf(ww[u], IO::get(ch[u][c], e), agg[c * PER + e]);
     }
   }
 }
@@ -294,7 +330,7 @@ __device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict_
   const int lane = threadIdx.x & 31;
   const int r = lane & 15, half = lane >> 4;
   float own[FH], agg[FH];
-  aggregate_row<KH>(row0 + r, half, n, Hin, rowptr, col, what, own, agg);
+  aggregate_row<KH, float>(row0 + r, half, n, Hin, rowptr, col, what, own, agg);
   float* t = tile + r * (2 * KH);
 #pragma unroll
   for (int f = 0; f < FH; ++f) {
@@ -356,15 +392,15 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned bar, unsigned parity) {
 
 // fill_xcat into the A operand: the warp's 16 rows [Hin, Agg Hin] as BF16
 // pairs at their K-major core-matrix positions (rows past n are zeros)
-template <int KH>
-__device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const float* __restrict__ Hin,
+template <int KH, typename TIN>
+__device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const TIN* __restrict__ Hin,
                                const int* __restrict__ rowptr, const int* __restrict__ col,
                                const float* __restrict__ what) {
   constexpr int K = 2 * KH, FH = KH / 2;
   const int lane = threadIdx.x & 31;
   const int r = lane & 15, half = lane >> 4;
   float own[FH], agg[FH];
-  aggregate_row<KH>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
+  aggregate_row<KH, TIN>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
 #pragma unroll
   for (int f = 0; f < FH; f += 2) {
     *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, half * FH + f, K)) = pack_bf16(own[f], own[f + 1]);
@@ -372,12 +408,12 @@ __device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const
   }
 }
 
-template <int KH>
-__global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __restrict__ Hin,
+template <int KH, typename TIN, typename TOUT>
+__global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const TIN* __restrict__ Hin,
                                                       const int* __restrict__ rowptr, const int* __restrict__ col,
                                                       const float* __restrict__ what,
                                                       const __nv_bfloat16* __restrict__ W,
-                                                      const float* __restrict__ bias, int res, float* Z, float* Hout,
+                                                      const float* __restrict__ bias, int res, float* Z, TOUT* Hout,
                                                       int* status) {
   constexpr int K = 2 * KH;
   static_assert(K % 16 == 0, "K in steps of 16");
@@ -413,7 +449,7 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __r
   for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
     const int row0 = tl * TC_ROWS;
     // A: each warp its 16 rows
-    fill_xcat_umma<KH>(sA, warp * 16, row0, n, Hin, rowptr, col, what);
+    fill_xcat_umma<KH, TIN>(sA, warp * 16, row0, n, Hin, rowptr, col, what);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A, for the tensor cores
     tc_fence_before();
     __syncthreads();
@@ -459,23 +495,28 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __r
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int row = row0 + quarter * 32 + lane;
     if (row < n) {
-      float4* zr = Z ? reinterpret_cast<float4*>(Z + (size_t)row * HID + cb) : nullptr;
-      float4* hr = reinterpret_cast<float4*>(Hout + (size_t)row * HID + cb);
-      const float4* hin = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + cb);
+      float z[DC], h[DC];
 #pragma unroll
-      for (int c4 = 0; c4 < DC / 4; ++c4) {
-        float z[4], h[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) z[e] = __uint_as_float(d[4 * c4 + e]) + bias[cb + 4 * c4 + e];
-        float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (res) h0 = hin[c4];  // res: KH == HID
-        h[0] = h0.x + fmaxf(z[0], 0.f);
-        h[1] = h0.y + fmaxf(z[1], 0.f);
-        h[2] = h0.z + fmaxf(z[2], 0.f);
-        h[3] = h0.w + fmaxf(z[3], 0.f);
-        if (zr) zr[c4] = make_float4(z[0], z[1], z[2], z[3]);
-        hr[c4] = make_float4(h[0], h[1], h[2], h[3]);
+      for (int e = 0; e < DC; ++e) {
+        z[e] = __uint_as_float(d[e]) + bias[cb + e];
+        h[e] = fmaxf(z[e], 0.f);
       }
+      if (res) {  // res: KH == HID
+        using IO = FeatIO<TIN>;
+        const typename IO::Chunk* hin = reinterpret_cast<const typename IO::Chunk*>(Hin + (size_t)row * KH + cb);
+#pragma unroll
+        for (int c = 0; c < DC / IO::PER; ++c) {
+          const typename IO::Chunk v = hin[c];
+#pragma unroll
+          for (int e = 0; e < IO::PER; ++e) h[c * IO::PER + e] = IO::get(v, e) + h[c * IO::PER + e];
+        }
+      }
+      if (Z) {
+        float4* zr = reinterpret_cast<float4*>(Z + (size_t)row * HID + cb);
+#pragma unroll
+        for (int c4 = 0; c4 < DC / 4; ++c4) zr[c4] = make_float4(z[4 * c4], z[4 * c4 + 1], z[4 * c4 + 2], z[4 * c4 + 3]);
+      }
+      store_feat(Hout + (size_t)row * HID + cb, h);
     }
     // every warp has read D and the tensor cores are done with A before the
     // next tile writes them
@@ -492,8 +533,22 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const float* __r
 // coalesced and the dot products finish with two shuffles.
 constexpr int RO_LANES = 4;
 constexpr int RO_F = HID / RO_LANES;
+// the RO_F features of lane q's quarter of row i
+template <typename T>
+__device__ __forceinline__ void load_quarter(const T* __restrict__ H, int i, int q, float (&v)[RO_F]) {
+  using IO = FeatIO<T>;
+  const typename IO::Chunk* p = reinterpret_cast<const typename IO::Chunk*>(H + (size_t)i * HID + q * RO_F);
+#pragma unroll
+  for (int c = 0; c < RO_F / IO::PER; ++c) {
+    const typename IO::Chunk ch = p[c];
+#pragma unroll
+    for (int e = 0; e < IO::PER; ++e) v[c * IO::PER + e] = IO::get(ch, e);
+  }
+}
+
+template <typename T>
 __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                          const float* __restrict__ what, const float* __restrict__ H, const float* __restrict__ params,
+                          const float* __restrict__ what, const T* __restrict__ H, const float* __restrict__ params,
                           float* gd, float* gl) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gt / RO_LANES, q = gt % RO_LANES;
@@ -503,7 +558,8 @@ __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __re
   float hro[RO_F];
   float d = 0.f;
   if (on) {
-    const float* hi = H + (size_t)i * HID + q * RO_F;
+    float hi[RO_F];
+    load_quarter(H, i, q, hi);
 #pragma unroll
     for (int c = 0; c < RO_F; ++c) {
       const float h = hi[c];
@@ -521,7 +577,8 @@ __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __re
     const int j = col[k];
     float v = 0.f;
     if (j < i) {
-      const float* hj = H + (size_t)j * HID + q * RO_F;
+      float hj[RO_F];
+      load_quarter(H, j, q, hj);
 #pragma unroll
       for (int c = 0; c < RO_F; ++c) v = fmaf(hro[c], hj[c], v);
     }
@@ -532,8 +589,9 @@ __global__ void k_readout(int n, const int* __restrict__ rowptr, const int* __re
 }
 
 // two-hop readout: gl2_e = pw_e sum_c ro2_c H_ic H_jc (j = col2_e < i), four lanes per row
+template <typename T>
 __global__ void k_readout2(int n, const int* __restrict__ rowptr2, const int* __restrict__ col2,
-                           const float* __restrict__ pw, const float* __restrict__ H,
+                           const float* __restrict__ pw, const T* __restrict__ H,
                            const float* __restrict__ params, float* gl2) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gt / RO_LANES, q = gt % RO_LANES;
@@ -543,7 +601,8 @@ __global__ void k_readout2(int n, const int* __restrict__ rowptr2, const int* __
 #pragma unroll
   for (int c = 0; c < RO_F; ++c) hro[c] = 0.f;
   if (on) {
-    const float* hi = H + (size_t)i * HID + q * RO_F;
+    float hi[RO_F];
+    load_quarter(H, i, q, hi);
 #pragma unroll
     for (int c = 0; c < RO_F; ++c) hro[c] = hi[c] * ro2[c];
   }
@@ -553,7 +612,8 @@ __global__ void k_readout2(int n, const int* __restrict__ rowptr2, const int* __
     const int j = col2[e];
     float v = 0.f;
     if (j < i) {
-      const float* hj = H + (size_t)j * HID + q * RO_F;
+      float hj[RO_F];
+      load_quarter(H, j, q, hj);
 #pragma unroll
       for (int c = 0; c < RO_F; ++c) v = fmaf(hro[c], hj[c], v);
     }
@@ -1195,18 +1255,34 @@ int forward(lv_ctx* c, const LearnSystem& S, bool infer = false) {
     L->wbf_valid = true;
     c->launches++;
   }
-  k_layer_fwd<FIN><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->params + OFF_B0,
-                                           0, infer ? nullptr : L->Z0, L->H1, c->status);
-  k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->params + OFF_B1,
-                                           1, infer ? nullptr : L->Z1, L->H2, c->status);
-  k_layer_fwd<HID><<<nb, TC_TPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->params + OFF_B2,
-                                           1, infer ? nullptr : L->Z2, L->H3, c->status);
-  k_readout<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd,
-                                                           L->gl);
-  if (L->hops == 2) {
-    k_readout2<<<lv_blocks(S.n * RO_LANES, TPB), TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, L->H3, L->params,
-                                                              L->gl2);
-    c->launches++;
+  const int gb = lv_blocks(S.n * RO_LANES, TPB);
+  if (infer) {
+    // the hidden features in BF16 (the buffers of the FP32 ones), no Z
+    typedef __nv_bfloat16 B16;
+    B16 *h1 = reinterpret_cast<B16*>(L->H1), *h2 = reinterpret_cast<B16*>(L->H2), *h3 = reinterpret_cast<B16*>(L->H3);
+    k_layer_fwd<FIN, float, B16><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0,
+                                                         L->params + OFF_B0, 0, nullptr, h1, c->status);
+    k_layer_fwd<HID, B16, B16><<<nb, TC_TPB, 0, s>>>(S.n, h1, S.rowptr, S.col, L->what, L->wbf + WBF_W1,
+                                                       L->params + OFF_B1, 1, nullptr, h2, c->status);
+    k_layer_fwd<HID, B16, B16><<<nb, TC_TPB, 0, s>>>(S.n, h2, S.rowptr, S.col, L->what, L->wbf + WBF_W2,
+                                                       L->params + OFF_B2, 1, nullptr, h3, c->status);
+    k_readout<B16><<<gb, TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, h3, L->params, L->gd, L->gl);
+    if (L->hops == 2) {
+      k_readout2<B16><<<gb, TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, h3, L->params, L->gl2);
+      c->launches++;
+    }
+  } else {
+    k_layer_fwd<FIN, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0,
+                                                           L->params + OFF_B0, 0, L->Z0, L->H1, c->status);
+    k_layer_fwd<HID, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1,
+                                                           L->params + OFF_B1, 1, L->Z1, L->H2, c->status);
+    k_layer_fwd<HID, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2,
+                                                           L->params + OFF_B2, 1, L->Z2, L->H3, c->status);
+    k_readout<float><<<gb, TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd, L->gl);
+    if (L->hops == 2) {
+      k_readout2<float><<<gb, TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, L->H3, L->params, L->gl2);
+      c->launches++;
+    }
   }
   c->launches += 4;
   return lv_cuda_check(c, cudaGetLastError(), "learned: forward");

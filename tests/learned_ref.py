@@ -139,11 +139,14 @@ def layer(G, H, W, b, res):
     return (H if res else 0.0) + torch.relu(Z)
 
 
-def factor(G, params):
+def factor(G, params, store_bf16=False):
+    """store_bf16: the hidden features rounded to bfloat16 after each layer,
+    as the per-step factor (inference) stores them."""
     P = unpack(params)
-    H1 = layer(G, G["X"], P["W0"], P["b0"], False)
-    H2 = layer(G, H1, P["W1"], P["b1"], True)
-    H3 = layer(G, H2, P["W2"], P["b2"], True)
+    keep = bf16 if store_bf16 else (lambda t: t)
+    H1 = keep(layer(G, G["X"], P["W0"], P["b0"], False))
+    H2 = keep(layer(G, H1, P["W1"], P["b1"], True))
+    H3 = keep(layer(G, H2, P["W2"], P["b2"], True))
     gd = 1.0 + H3 @ P["rd"]
     lower = G["col"] < G["ri"]
     gl = G["what"] * ((H3[G["ri"]] * H3[G["col"]]) @ P["ro"])
@@ -205,10 +208,12 @@ def loss_and_grad(rowptr, col, w, diag, adiag, params, probes, hops=1):
     return float(L.detach()), p.grad.numpy().copy()
 
 
-def forward_values(rowptr, col, w, diag, adiag, params, hops=1):
+def forward_values(rowptr, col, w, diag, adiag, params, hops=1, store_bf16=True):
+    """The factor as lv_learn_factor computes it (the per-step inference,
+    hidden features stored in bfloat16)."""
     G = prepare(rowptr, col, w, diag, adiag, hops)
     with torch.no_grad():
-        gd, gl = factor(G, torch.tensor(np.asarray(params, np.float64)))
+        gd, gl = factor(G, torch.tensor(np.asarray(params, np.float64)), store_bf16)
     if hops == 2:
         return gd.numpy(), gl.numpy(), G["X"].numpy(), (G["rp2"], G["col2"].numpy(), G["gl2"].numpy())
     return gd.numpy(), gl.numpy(), G["X"].numpy()
