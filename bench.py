@@ -54,6 +54,10 @@ CONFIG_SIZES = {"gresho": (50, 50), "taylor_green": (256, 256), "rayleigh_taylor
                 "cavity": (1024, 1024), "double_shear": (2048, 2048)}
 
 
+# the step counts the five workloads are specified with
+CONFIG_STEPS = {"gresho": 100, "taylor_green": 200, "rayleigh_taylor": 300, "cavity": 500, "double_shear": 500}
+
+
 class Workload:
     def __init__(self, name, nx=None):
         import workloads as W
@@ -314,6 +318,75 @@ def train_learned(L, g, args):
             "pattern": "lower triangle" if args.learn_hops == 1 else "lower triangle + two-hop",
             "lr": args.train_lr, "seconds": time.perf_counter() - t_tr, "loss_first": float(losses[0]),
             "loss_last": float(losses[-10:].mean())}
+
+
+def full_run(args, wl):
+    """The whole run of a workload (its specified step count, or --full-steps)
+    through the public API: warm-up steps with the Jacobi mixed solver, which
+    also give the learned preconditioner its training systems, then the
+    remaining steps with --solver.  Reports the wall time per step, the
+    solves that missed the tolerance, the CG iterations, and the totals of
+    mass, momentum, energy and kinetic energy every 50 steps (with their
+    drift over the run).  Not a bench line: a check that the run completes."""
+    lv = load_package()
+    L = lv._lib.load()
+    fl = wl.flow
+    g = setup_grid(lv, wl)
+    total = args.full_steps or CONFIG_STEPS[wl.name]
+    learned = args.solver == "learned_pcg"
+    tol = None if args.solver == "minres" else 1e-8
+    solver = lv.PressureSolver(g, method="mixed_ir" if learned else args.solver, tol=tol)
+
+    def totals(step):
+        m, v, e, P, area = g["mass"], g["v"], g["e"], g["P"], g["area"]
+        return {"step": step, "mass": float(m.sum()), "momentum": [float((m * v[:, 0]).sum()), float((m * v[:, 1]).sum())],
+                "energy": float((m * e).sum()), "kinetic": float(0.5 * (m * (v * v).sum(axis=1)).sum()),
+                "v_max": float(np.abs(v).max()), "P_range": [float(P.min()), float(P.max())],
+                "area_min_rel": float(area.min() / area.mean()),
+                "finite": bool(np.isfinite(v).all() and np.isfinite(e).all() and np.isfinite(g["x"]).all())}
+
+    rec = [totals(0)]
+    warm = min(max(args.warmup, 3), total)
+    t_run = 0.0
+    t0 = time.perf_counter()
+    for _ in range(warm):
+        gpu_step(lv, g, solver, fl, snapshot=learned)
+    g.synchronize()
+    t_run += time.perf_counter() - t0
+    train = train_learned(L, g, args) if learned else None
+    solver = lv.PressureSolver(g, method=args.solver, tol=tol)
+    u0 = unconverged(L, g)
+    s0, i0 = C.c_int64(), C.c_int64()
+    L.lv_solver_counters(g._ctx, C.byref(s0), C.byref(i0))
+    step = warm
+    failure = None
+    while step < total and failure is None:
+        seg = min(50 - step % 50, total - step)
+        t0 = time.perf_counter()
+        try:
+            for _ in range(seg):
+                gpu_step(lv, g, solver, fl)
+            g.synchronize()
+        except lv.LvError as err:  # the run stops: report where
+            failure = {"error": str(err), "segment": [step, step + seg]}
+            break
+        t_run += time.perf_counter() - t0
+        step += seg
+        rec.append(totals(step))
+    s1, i1 = C.c_int64(), C.c_int64()
+    L.lv_solver_counters(g._ctx, C.byref(s1), C.byref(i1))
+    rel = lambda a, b: (b - a) / abs(a) if a else b - a
+    first, last = rec[0], rec[-1]
+    return {"mode": "full_run", "workload": wl.label, "particles": wl.n, "steps": step, "failure": failure,
+            "solver": args.solver,
+            "wall_ms_per_step": 1e3 * t_run / total, "unconverged_sweeps": unconverged(L, g) - u0,
+            "solves": s1.value - s0.value, "cg_iters_per_step": (i1.value - i0.value) / max(total - warm, 1),
+            "all_finite": all(r["finite"] for r in rec), "training": train,
+            "drift": {"mass": rel(first["mass"], last["mass"]), "energy": rel(first["energy"], last["energy"]),
+                      "momentum_abs": [last["momentum"][0] - first["momentum"][0],
+                                       last["momentum"][1] - first["momentum"][1]],
+                      "kinetic": rel(first["kinetic"], last["kinetic"])},
+            "totals": rec}
 
 
 def run_ours(args, world, rank, local, wl):
@@ -714,8 +787,14 @@ def main():
     ap.add_argument("--train-lr", type=float, default=5e-3)
     ap.add_argument("--learn-hops", type=int, default=1, choices=[1, 2],
                     help="pattern of the learned factor: 1 the operator's lower triangle, 2 with two-hop neighbours")
+    ap.add_argument("--full-run", action="store_true",
+                    help="run the workload for its specified step count and report completion and drift (no bench line)")
+    ap.add_argument("--full-steps", type=int, default=0, help="steps of --full-run (0: the workload's own)")
     args = ap.parse_args()
     wl = Workload(args.config, args.nx or None)
+    if args.full_run:
+        print(json.dumps(full_run(args, wl)), flush=True)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup()
     if args.impl == "reference":

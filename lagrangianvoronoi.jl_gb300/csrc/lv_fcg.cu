@@ -1223,6 +1223,34 @@ __global__ void __launch_bounds__(128) k_build_minv_reg(int n, const int* __rest
   mdiag[i] = di * (dsum + eps) * di;
 }
 
+// The factored form of the learned M^-1 (SolverDev::mfac) from the factor:
+// row i's lower entries (j < i, G_ij = gl at the operator entry) and the
+// entries of column i (G_ki for the operator's k > i, at the reverse entry of
+// row k), in the operator's order.
+__global__ void k_build_gfac(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const float* __restrict__ gd, const float* __restrict__ gl, const int* __restrict__ rev,
+                             int stride, int* mcnt, int* mcol, float* mval, float* mdiag, int* mok) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *mok = 1;
+  if (i >= n) return;
+  int nl = 0, nu = 0;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int j = col[k];
+    if (j < i) {
+      mcol[(size_t)nl * stride + i] = j;
+      mval[(size_t)nl * stride + i] = gl[k];
+      ++nl;
+    } else if (j > i && rev[k] >= 0) {
+      const size_t e = (size_t)(LV_MAX_EDGES + nu) * stride + i;
+      mcol[e] = j;
+      mval[e] = gl[rev[k]];
+      ++nu;
+    }
+  }
+  mcnt[i] = nl | (nu << 8);
+  mdiag[i] = gd[i];
+}
+
 // ---------------------------------------------------------------------------
 // Streaming mixed-precision solve for systems beyond the register-resident
 // solver (k_big): the refinement and the single-reduction CG of k_fcg, with
@@ -1266,6 +1294,10 @@ struct BigArgs {
   int mstride;
   const int* minv_ok;
   int learned;
+  int mfac;                   // M^-1 in factored form (SolverDev::mfac): D^-1/2 = dh, G's entries, eps
+  const float* dh;
+  float eps;
+  float* y;                   // G D^-1/2 r of the factored form
   const unsigned* masks;      // [nb][BIG_MASK_WORDS] blocks whose rows a block references
   unsigned long long* slots;  // partial words [2 parities][RG_WORDS][nb]
   unsigned* counter;
@@ -1400,6 +1432,56 @@ __device__ __forceinline__ float big_mrow(const BigArgs& a, int i, const float* 
   return acc;
 }
 
+constexpr int BIG_GB = 4;  // entries of a factored M^-1 pass loaded together (rows have ~3)
+
+// The factored M^-1, first pass: row i of y = G z, z = D^-1/2 r (G's lower
+// entries of the row; z_j of a neighbour formed from its exchanged r).
+__device__ __forceinline__ float big_grow(const BigArgs& a, int i, const float* __restrict__ r) {
+  const int nl = ld_nc(a.mcnt + i) & 0xff;
+  float acc = ld_nc(a.mdiag + i) * (ld_nc(a.dh + i) * __ldcg(r + i));
+  for (int k0 = 0; k0 < nl; k0 += BIG_GB) {
+    int jj[BIG_GB];
+    float mv[BIG_GB], zv[BIG_GB];
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q) {
+      const size_t e = (size_t)min(k0 + q, nl - 1) * a.mstride + i;
+      jj[q] = ld_nc(a.mcol + e);
+      mv[q] = ld_nc(a.mval + e);
+    }
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q) zv[q] = ld_nc(a.dh + jj[q]) * __ldcg(r + jj[q]);
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q)
+      if (k0 + q < nl) acc = fmaf(mv[q], zv[q], acc);
+  }
+  return acc;
+}
+
+// Second pass: row i of u = D^-1/2 (G^T y + eps z) (the entries G_ki of
+// column i, from the exchanged y of the rows k > i).
+__device__ __forceinline__ float big_gtrow(const BigArgs& a, int i, const float* __restrict__ r,
+                                           const float* __restrict__ y) {
+  const int nu = ld_nc(a.mcnt + i) >> 8;
+  const float di = ld_nc(a.dh + i);
+  float acc = ld_nc(a.mdiag + i) * __ldcg(y + i);
+  for (int k0 = 0; k0 < nu; k0 += BIG_GB) {
+    int jj[BIG_GB];
+    float mv[BIG_GB], yv[BIG_GB];
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q) {
+      const size_t e = (size_t)(LV_MAX_EDGES + min(k0 + q, nu - 1)) * a.mstride + i;
+      jj[q] = ld_nc(a.mcol + e);
+      mv[q] = ld_nc(a.mval + e);
+    }
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q) yv[q] = __ldcg(y + jj[q]);
+#pragma unroll
+    for (int q = 0; q < BIG_GB; ++q)
+      if (k0 + q < nu) acc = fmaf(mv[q], yv[q], acc);
+  }
+  return di * fmaf(a.eps, di * __ldcg(r + i), acc);
+}
+
 template <bool LEARNED>
 __global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
   constexpr int TPB = BIG_TPB;
@@ -1455,9 +1537,18 @@ __global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
   double bnorm2 = 0.0, rtrue2 = 0.0;
   float gam_old = 1.f, alpha = 1.f;
   bool fall = false;
-  // u = M^-1 r from the exchanged r
-  auto mpass = [&]() {
-    for (int i = rb0 + t; i < rb1; i += TPB) vu[i] = big_mrow(a, i, vr);
+  // u = M^-1 r: the exchange of r, then the explicit M^-1 rows, or the
+  // factored form's two passes with the exchange of y between them
+  auto mpass = [&]() -> bool {
+    if (!nexchange(a, ++xe, s_mask)) return false;
+    if (a.mfac) {
+      for (int i = rb0 + t; i < rb1; i += TPB) a.y[i] = big_grow(a, i, vr);
+      if (!nexchange(a, ++xe, s_mask)) return false;
+      for (int i = rb0 + t; i < rb1; i += TPB) vu[i] = big_gtrow(a, i, vr, a.y);
+    } else {
+      for (int i = rb0 + t; i < rb1; i += TPB) vu[i] = big_mrow(a, i, vr);
+    }
+    return true;
   };
   while (ok) {
     // ---- FP64 residual b - A x (difference form)
@@ -1495,10 +1586,7 @@ __global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
       vr[i] = ri;
       if (!learned) vu[i] = a.dinv32[i] * ri;
     }
-    if (learned) {
-      if (!(ok = nexchange(a, ++xe, s_mask))) break;
-      mpass();
-    }
+    if (learned && !(ok = mpass())) break;
     bool first = true;  // p, s, d start from zero (never read)
     while (true) {
       if (!(ok = nexchange(a, ++xe, s_mask))) break;
@@ -1553,10 +1641,7 @@ __global__ void __launch_bounds__(BIG_TPB, 1) k_big(BigArgs a) {
       gam_old = gam;
       first = false;
       ++it;
-      if (learned) {
-        if (!(ok = nexchange(a, ++xe, s_mask))) break;
-        mpass();
-      }
+      if (learned && !(ok = mpass())) break;
     }
     if (!ok) break;
     // the correction: x += sigma d on the own rows, then the neighbours' x
@@ -1930,6 +2015,15 @@ int lv_fcg_build_minv(lv_ctx* c) {
   lv_learn_factor_ptrs(c, &gd, &gl, &dh, &rev);
   lv_learn_factor2_ptrs(c, &rowptr2, &col2, &gl2, &rev2);
   if (!gd) return lv_fail(c, LV_ERR_BAD_ARGUMENT, "learned solve without a factor");
+  // systems beyond the staged solver take the factored form (one-hop factor)
+  c->sv.mfac = !rowptr2 && n > lv_fcg_capacity(c);
+  c->sv.stage_ready = false;
+  if (c->sv.mfac) {
+    k_build_gfac<<<lv_blocks(n, 256), 256, 0, c->stream>>>(n, c->sv.rowptr, c->sv.col, gd, gl, rev, c->sv.mrows,
+                                                           c->sv.mcnt, c->sv.mcol, c->sv.mval, c->sv.mdiag, c->sv.mok);
+    LV_LAUNCH_CHECK(c, "k_build_gfac");
+    return LV_OK;
+  }
   if (rowptr2) {
     const int one = 1;
     cudaMemcpyAsync(c->sv.mok, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream);
@@ -2101,7 +2195,7 @@ int lv_big_prepare(lv_ctx* c) {
   bool ok = true;
   sv.ew32 = big_alloc<float>(c, (size_t)LV_MAX_EDGES * cap, &ok);
   sv.ew64 = big_alloc<double>(c, (size_t)LV_MAX_EDGES * cap, &ok);
-  sv.bvec = big_alloc<float>(c, 6 * cap, &ok);
+  sv.bvec = big_alloc<float>(c, 7 * cap, &ok);
   sv.br64 = big_alloc<double>(c, cap, &ok);
   sv.bmasks = big_alloc<unsigned>(c, (size_t)FCG_MAX_BLOCKS * BIG_MASK_WORDS, &ok);
   sv.bsync = big_alloc<unsigned>(c, BIG_SYNC_WORDS, &ok);
@@ -2125,14 +2219,16 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
   const int nb = big_blocks(c, learned);
   if (nb < 1) return lv_fail(c, LV_ERR_CUDA, "the streaming solver does not fit an SM");
   const int rpb = (n + nb - 1) / nb;
-  if (!c->big_masks_valid || (learned && !c->big_masks_m)) {
+  // the explicit M^-1 reaches two hops; the operator and the factored form one
+  const bool need_m = learned && !sv.mfac;
+  if (!c->big_masks_valid || (need_m && !c->big_masks_m)) {
     // the neighbour blocks of every block: the operator's pattern, and M^-1's
-    // for a learned solve (a superset serves a Jacobi solve too)
-    k_big_masks<<<nb, BIG_TPB, 0, c->stream>>>(n, rpb, c->m.cap, c->m.nfaces, c->m.fnbr, learned ? sv.mcnt : nullptr,
+    // for an explicit learned solve (a superset serves a Jacobi solve too)
+    k_big_masks<<<nb, BIG_TPB, 0, c->stream>>>(n, rpb, c->m.cap, c->m.nfaces, c->m.fnbr, need_m ? sv.mcnt : nullptr,
                                                sv.mcol, sv.mrows, sv.bmasks);
     LV_LAUNCH_CHECK(c, "k_big_masks");
     c->big_masks_valid = true;
-    c->big_masks_m = learned;
+    c->big_masks_m = need_m;
   }
   BigArgs a;
   a.n = n;
@@ -2163,6 +2259,15 @@ int lv_big_solve(lv_ctx* c, double* x, int slot, bool learned) {
   a.mstride = sv.mrows;
   a.minv_ok = learned ? sv.mok : sv.iters + LV_IT_NONSINGULAR;  // read only in learned mode
   a.learned = learned ? 1 : 0;
+  a.mfac = (learned && sv.mfac) ? 1 : 0;
+  a.dh = nullptr;
+  a.eps = c->learn_eps;
+  a.y = sv.bvec + 6 * cap;
+  if (a.mfac) {
+    const float *gd, *gl;
+    const int* rev;
+    lv_learn_factor_ptrs(c, &gd, &gl, &a.dh, &rev);
+  }
   a.masks = sv.bmasks;
   a.counter = sv.bsync;
   a.sync_base = sv.bsync + 1;

@@ -254,6 +254,13 @@ struct SolverDev {
   int *mcnt = nullptr, *mcol = nullptr;
   float *mval = nullptr, *mdiag = nullptr;
   int* mok = nullptr;
+  // the streaming solver's learned preconditioner in factored form (one-hop
+  // pattern, systems beyond the staged solver): the same buffers hold G's
+  // lower entries of each row in slots [0, nl), the entries G_ki (k > i) of
+  // its column in slots [LV_MAX_EDGES, LV_MAX_EDGES + nu), mcnt = nl | nu << 8
+  // and mdiag = G_ii, so M^-1 r = D^-1/2 (G^T G + eps I) D^-1/2 r is applied
+  // as two one-hop passes instead of an explicit two-hop row
+  bool mfac = false;
   int mrows = 0;
   // staged learned solve (lv_fcg.cu): per-block images, the operator's
   // columns remapped to shared-memory slots, build status [ok, max halo,
