@@ -554,13 +554,17 @@ def run_ours(args, world, rank, local, wl):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     # per CG iteration, the bytes a streaming implementation moves: FP64
     # Jacobi-PCG 12 B per nonzero (value + column) + 60 B per row (vectors);
-    # FP32 inner CG 8 B per nonzero + 28 B per row, and the learned M^-1 about
-    # 10 more nonzeros per row.  The register-resident kernels keep the matrix
-    # on chip, so these are upper bounds of their DRAM traffic.
+    # FP32 inner CG 8 B per nonzero + 28 B per row, and the learned M^-1:
+    # about 10 more nonzeros per row (explicit, the staged solver) or, in the
+    # factored form of the streaming solver (systems beyond 152 x 1024 rows),
+    # two passes over ~3 entries of G per row with their vectors (92 B per
+    # row).  The register-resident kernels keep the matrix on chip, so these
+    # are upper bounds of their DRAM traffic.
     if args.solver == "jacobi_pcg":
         per_it = 12 * (F + N) + 60 * N
     else:
-        per_it = 8 * (F + N) + 28 * N + (80 * N if args.solver == "learned_pcg" else 0)
+        m_bytes = (92 * N if N > 152 * 1024 else 80 * N) if args.solver == "learned_pcg" else 0
+        per_it = 8 * (F + N) + 28 * N + m_bytes
     pcg_bytes = iters * per_it
     clip_unit = 16 * N + 28 * F + 28 * N  # per remesh: read x; write nbr, lrr, mid; area, centroid, nface
     fams = {"pcg": iters_i * per_it, "clip": kt["clip"][0] * clip_unit}  # bytes of the instrumented pass
