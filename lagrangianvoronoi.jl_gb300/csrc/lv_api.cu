@@ -323,6 +323,8 @@ lv_ctx* lv_create(const lv_params* prm) {
   m.fy = dalloc<double2>(c, ell, &ok);
   m.area = dalloc<double>(c, cap, &ok);
   m.rperm = dalloc<int>(c, cap, &ok);
+  m.nclip = dalloc<unsigned char>(c, cap, &ok);
+  m.cperm = dalloc<int>(c, cap, &ok);
   m.centroid = dalloc<double2>(c, cap, &ok);
 
   CellsDev& cl = c->c;

@@ -756,6 +756,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   if (active) cache_poly();
   float prr_up = active ? prr_cached() : 0.0f;
   bool saved = false;
+  int nclips = 0;  // clips of this pass (the order key of the next remesh)
   // whether candidate j (float offset q from its cell's corner) may cut the
   // current polygon; false only when provably not: farther than the
   // influence radius, or every vertex strictly inside the half-plane by more
@@ -836,6 +837,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
       s += adv;
     }
     if (!__any_sync(0xffffffffu, have)) break;
+    nclips += have ? 1 : 0;
     if (have) {
       const double2 xq = x[cj];
       double vx, vy;
@@ -981,6 +983,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     cy = cy + P.v2x[a];
   }
   m.nedges[i] = ne;
+  m.nclip[i] = (unsigned char)min(nclips, 255);
   m.nfaces[i] = __popc(fmask);
   m.area[i] = A;
   m.centroid[i] = make_double2(cx / A, cy / A);
@@ -992,8 +995,8 @@ template <int CAP>
 __global__ void __launch_bounds__(CLIP_TPB) k_clip(GridDev g, const PathNodeDev* __restrict__ path,
                                                    const double2* __restrict__ x, int n, CellsDev cl, MeshDev m,
                                                    int* status, ClipResume* redo, int* redo_n, int slots) {
-  const int i = blockIdx.x * CLIP_TPB + threadIdx.x;
-  clip_polygon<CAP>(g, path, x, i, i < n, cl, m, status, redo, redo_n, nullptr, slots);
+  const int t = blockIdx.x * CLIP_TPB + threadIdx.x;
+  clip_polygon<CAP>(g, path, x, t < n ? m.cperm[t] : 0, t < n, cl, m, status, redo, redo_n, nullptr, slots);
 }
 
 // second pass: the captured polygons, resumed with LV_MAX_EDGES slots.  The
@@ -1036,19 +1039,22 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len) {
   return LV_OK;
 }
 
-// The face kernels' row order (MeshDev::rperm): one block per window of
-// LV_RPERM_WINDOW rows, a stable counting sort by face count.  Lanes of a
-// warp with the same count rank themselves by __match_any_sync; the counts of
-// each warp and bucket give every bucket's and warp's offset.
-constexpr int RP_BUCKETS = LV_MAX_EDGES + 2;  // face counts 0..LV_MAX_EDGES, then rows past n
-__global__ void __launch_bounds__(LV_RPERM_WINDOW) k_rperm(MeshDev m, int n) {
+// A stable counting sort of the rows of each window of LV_RPERM_WINDOW by a
+// small key (one block per window): lanes of a warp with the same key rank
+// themselves by __match_any_sync, and the counts of each warp and bucket
+// give every bucket's and warp's offset.  The face kernels' row order
+// (MeshDev::rperm, by face count) and the clipping's polygon order
+// (MeshDev::cperm, by the previous remesh's clip count).
+constexpr int RP_BUCKETS = 34;  // keys 0..32, then rows past n
+template <typename K>
+__global__ void __launch_bounds__(LV_RPERM_WINDOW) k_window_order(const K* __restrict__ key, int n, int* perm) {
   constexpr int NW = LV_RPERM_WINDOW / 32;
   __shared__ int wc[NW][RP_BUCKETS], wo[NW][RP_BUCKETS];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int i = blockIdx.x * LV_RPERM_WINDOW + t;
   for (int k = t; k < NW * RP_BUCKETS; k += LV_RPERM_WINDOW) wc[k / RP_BUCKETS][k % RP_BUCKETS] = 0;
   __syncthreads();
-  const int b = i < n ? min(max(m.nfaces[i], 0), LV_MAX_EDGES) : LV_MAX_EDGES + 1;
+  const int b = i < n ? min(max((int)key[i], 0), RP_BUCKETS - 2) : RP_BUCKETS - 1;
   const unsigned same = __match_any_sync(0xffffffffu, b);
   const int rank = __popc(same & ((1u << lane) - 1u));
   if (lane == __ffs(same) - 1) wc[w][b] = __popc(same);
@@ -1064,7 +1070,7 @@ __global__ void __launch_bounds__(LV_RPERM_WINDOW) k_rperm(MeshDev m, int n) {
     }
   }
   __syncthreads();
-  if (i < n) m.rperm[blockIdx.x * LV_RPERM_WINDOW + wo[w][b] + rank] = i;
+  if (i < n) perm[blockIdx.x * LV_RPERM_WINDOW + wo[w][b] + rank] = i;
 }
 
 __global__ void k_face_len(MeshDev m, int n) {
@@ -1141,6 +1147,11 @@ int lv_mesh_remesh(lv_ctx* c) {
     // second pass (the mesh is the same either way)
     int slots = ME_SMALL;
     if (c->clip_slots >= 5 && c->clip_slots < ME_SMALL) slots = c->clip_slots;
+    // the polygon order: by the clip counts of the previous remesh (zeros,
+    // so the identity, before the first)
+    k_window_order<unsigned char><<<(n + LV_RPERM_WINDOW - 1) / LV_RPERM_WINDOW, LV_RPERM_WINDOW, 0, s>>>(
+        c->m.nclip, n, c->m.cperm);
+    LV_LAUNCH_CHECK(c, "k_window_order (clips)");
     k_clip<ME_SMALL><<<lv_blocks(n, CLIP_TPB), CLIP_TPB, clip_smem(ME_SMALL), s>>>(c->g, c->path, c->s.x, n, c->c,
                                                                                    c->m, c->status, redo, redo_n, slots);
     LV_LAUNCH_CHECK(c, "k_clip");
@@ -1148,8 +1159,9 @@ int lv_mesh_remesh(lv_ctx* c) {
     k_clip_redo<<<3 * c->num_sms, CLIP_TPB, clip_smem(ME), s>>>(c->g, c->path, c->s.x, c->c, c->m, c->status,
                                                                redo, redo_n);
     LV_LAUNCH_CHECK(c, "k_clip_redo");
-    k_rperm<<<(n + LV_RPERM_WINDOW - 1) / LV_RPERM_WINDOW, LV_RPERM_WINDOW, 0, s>>>(c->m, n);
-    LV_LAUNCH_CHECK(c, "k_rperm");
+    k_window_order<int><<<(n + LV_RPERM_WINDOW - 1) / LV_RPERM_WINDOW, LV_RPERM_WINDOW, 0, s>>>(c->m.nfaces, n,
+                                                                                                c->m.rperm);
+    LV_LAUNCH_CHECK(c, "k_window_order (faces)");
   }
   c->meshed = true;
   c->op_ready = false;
