@@ -102,8 +102,8 @@ struct MeshDev {
   // instructions are priced per warp on this GPU, and a warp runs its face
   // loop as often as its largest row needs.  Rebuilt by every remesh.
   int* rperm;
-  // The clipping's polygon order: within each window of LV_RPERM_WINDOW
-  // polygons, ordered by the number of clips each needed in the previous
+  // The clipping's polygon order: within each window of 1024 polygons,
+  // ordered by the number of clips each needed in the previous
   // remesh (nclip; the particles move little between remeshes), so that
   // the polygons of a warp take about as many clip rounds each.
   unsigned char* nclip;
