@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(TPB, 2) k_rhs_prep(StateDev s, MeshDev m, Solv
 // (sweep 1): the sums of the initial guess with the residual b - A P and the
 // previous call's change D (lv_sweep_sums; all threads of the block take
 // part, so rows past n do not return early).
-__global__ void k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess, const float* D) {
+// (four blocks per SM: 64 registers with a few spills, 0.17 ms per step faster at 4M than 80 at three)
+__global__ void __launch_bounds__(TPB, 4) k_rhs(StateDev s, MeshDev m, SolverDev sv, int n, double dt, int guess, const float* D) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool on = t < n;
   const int i = on ? face_row(m, t) : t;
