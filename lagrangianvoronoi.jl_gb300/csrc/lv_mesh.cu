@@ -1039,8 +1039,8 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len) {
   return LV_OK;
 }
 
-// A stable counting sort of the rows of each window of LV_RPERM_WINDOW by a
-// small key (one block per window): lanes of a warp with the same key rank
+// A stable counting sort of the rows of each window of WIN rows by a small
+// key, clamped to 0..32 (one block per window): lanes of a warp with the same key rank
 // themselves by __match_any_sync, and the counts of each warp and bucket
 // give every bucket's and warp's offset.  The face kernels' row order
 // (MeshDev::rperm, by face count) and the clipping's polygon order
