@@ -272,8 +272,8 @@ __global__ void k_bin_order(GridDev g, const int2* __restrict__ key, int ncells,
 
 constexpr int CLIP_TPB = 64;
 constexpr int ME = LV_MAX_EDGES;
-// edge slots of the first clipping pass: shared memory for 9 edges per
-// polygon (52 bytes a slot) lets seven blocks share an SM (three with
+// edge slots of the first clipping pass: shared memory for 8 edges per
+// polygon (52 bytes a slot) lets eight blocks share an SM (three with
 // LV_MAX_EDGES); a polygon that needs more at any point is captured and
 // finished by a second pass with LV_MAX_EDGES slots, spread over every SM.
 // Measured on Taylor-Green meshes (256^2 / 1024^2, ms per remesh x2),
@@ -282,8 +282,10 @@ constexpr int ME = LV_MAX_EDGES;
 // 1.93 / 20.9; with it: 10 slots 1.274 / 10.44, 9 slots 1.271 / 10.16; with
 // the second pass spread over every SM: 9 slots 1.123 / 9.58, 8 slots (eight
 // blocks per SM) 1.140 / 9.08; with the second pass resuming the captured
-// polygons: 9 slots 1.054 / 9.92, 8 slots 1.122 / 10.29.
-constexpr int ME_SMALL = 9;
+// polygons: 9 slots 1.054 / 9.92, 8 slots 1.122 / 10.29.  On the 4M double
+// shear with the clip-count order and the register-cached scan: 9 slots
+// 24.5, 8 slots (eight blocks per SM) 24.0 ms per step.
+constexpr int ME_SMALL = 8;
 
 struct Poly {
   double* v1x;
