@@ -640,8 +640,9 @@ def run_ours(args, world, rank, local, wl):
 
 
 # FP64 thread operations per polygon of k_clip (ncu: dadd + dmul + dfma thread
-# instructions per polygon on a Taylor-Green mesh) and this part's FP64 rate
-CLIP_FP64_OPS = 1109
+# instructions per polygon of one remesh of the 1024x1024 double shear) and
+# this part's FP64 rate
+CLIP_FP64_OPS = 1074
 FP64_OPS_PEAK = 0.60e12
 
 # what bounds each dominant kernel instead of HBM (from the ncu summaries in profiles/)
