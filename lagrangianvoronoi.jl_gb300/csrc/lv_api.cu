@@ -81,6 +81,7 @@ int lv_device_setup(int dev) {
   std::call_once(once[dev], [dev]() {
     int r = lv_mesh_device_setup();
     if (r == LV_OK) r = lv_fcg_device_setup();
+    if (r == LV_OK) r = lv_learn_device_setup();
     rc[dev] = r;
   });
   return rc[dev];

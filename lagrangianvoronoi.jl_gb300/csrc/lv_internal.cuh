@@ -535,6 +535,7 @@ int lv_scan_int(lv_ctx* c, const int* in, int* out, int len);  // exclusive, out
 int lv_device_setup(int dev);  // lv_api.cu; call with dev current
 int lv_mesh_device_setup();    // lv_mesh.cu
 int lv_fcg_device_setup();     // lv_fcg.cu
+int lv_learn_device_setup();   // lv_learn.cu
 
 // ---- physics (lv_physics.cu)
 int lv_phys_move(lv_ctx* c, double dt);

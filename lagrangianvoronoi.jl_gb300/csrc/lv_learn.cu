@@ -18,9 +18,8 @@
 //
 // The matrix products of the layers run on the tensor cores with BF16
 // operands and FP32 accumulation: the forward [N x 32|64] x [32|64 x 32] (the
-// factor of every timestep) as tcgen05.mma into tensor memory, the training's
-// backward dX = dZ W^T and dW = X^T dZ as mma.sync m16n8k16; everything else
-// is FP32.  Training minimises either the exact FSAI (Kaporin) objective
+// factor of every timestep) and the training's backward dX = dZ W^T and
+// dW = X^T dZ as tcgen05.mma into tensor memory; everything else is FP32.  Training minimises either the exact FSAI (Kaporin) objective
 //     (1/N) [ tr(Gt At Gt^T) - 2 sum_i log Gt_ii ]
 // (Kolotilina & Yeremin, SIAM J. Matrix Anal. Appl. 14, 1993; Kaporin,
 // Numer. Linear Algebra Appl. 1, 1994), whose minimiser on the pattern is the
@@ -55,25 +54,14 @@ constexpr int OFF_RO2 = OFF_RO + HID;  // readout of the two-hop entries
 constexpr int NPARAM = OFF_RO2 + HID;
 constexpr int Q2MAX = 40;  // two-hop (not one-hop) neighbours kept per row
 constexpr int WBF_W0 = 0, WBF_W1 = KC0 * HID, WBF_W2 = KC0 * HID + KC * HID, NWBF = KC0 * HID + 2 * KC * HID;
-constexpr int LTPB = 128;  // 4 warps, 16 rows each per tile
 constexpr int MAXPROBES = 8;
 constexpr int PART_BLOCKS = 304;
+constexpr int BW_BLOCKS = 456;  // backward layers: three blocks on each of 152 SMs
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   const __nv_bfloat16 a = __float2bfloat16_rn(lo), b = __float2bfloat16_rn(hi);
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
-
-// D(16x8, f32) += A(16x16, bf16, row) * B(16x8, bf16, col)
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__device__ __forceinline__ float bf(const __nv_bfloat16* w, int idx) { return __bfloat162float(w[idx]); }
 
 // ---------------------------------------------------------------- preparation
 
@@ -321,25 +309,6 @@ __device__ __forceinline__ void aggregate_row(int row, int half, int n, const T*
   }
 }
 
-// Fills the warp's A tile [16][2KH] (FP32, shared): own rows of Hin and
-// Agg(Hin); lane l handles row l & 15 and half (l >> 4) of the features.
-template <int KH>
-__device__ void fill_xcat(float* tile, int row0, int n, const float* __restrict__ Hin, const int* __restrict__ rowptr,
-                          const int* __restrict__ col, const float* __restrict__ what) {
-  constexpr int FH = KH / 2;
-  const int lane = threadIdx.x & 31;
-  const int r = lane & 15, half = lane >> 4;
-  float own[FH], agg[FH];
-  aggregate_row<KH, float>(row0 + r, half, n, Hin, rowptr, col, what, own, agg);
-  float* t = tile + r * (2 * KH);
-#pragma unroll
-  for (int f = 0; f < FH; ++f) {
-    t[half * FH + f] = own[f];
-    t[KH + half * FH + f] = agg[f];
-  }
-  __syncwarp();
-}
-
 // ---------------------------------------------------------------- forward on tcgen05
 //
 // Z = [Hin, Agg Hin] W + b;  Hout = (res ? Hin : 0) + relu(Z), in 128-row
@@ -390,7 +359,7 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned bar, unsigned parity) {
   return true;
 }
 
-// fill_xcat into the A operand: the warp's 16 rows [Hin, Agg Hin] as BF16
+// The A operand: the warp's 16 rows [Hin, Agg Hin] as BF16
 // pairs at their K-major core-matrix positions (rows past n are zeros)
 template <int KH, typename TIN>
 __device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const TIN* __restrict__ Hin,
@@ -900,128 +869,207 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
   }
 }
 
-// Layer backward: dZ = dHout * [Z > 0]; dXcat = dZ W^T (tensor cores) into
-// dHdir (first KH columns) and dAgg (last KH); block partials of dW = Xcat^T dZ
-// (tensor cores) and db = sum dZ.
+// Layer backward on tcgen05, 128-row tiles: dZ = dHout * [Z > 0];
+// dXcat = dZ W^T into dHdir (first KH columns) and dAgg (last KH); the
+// block's partials of dW = Xcat^T dZ and db = sum dZ.  Per tile two sets of
+// products, issued by one thread and committed to one mbarrier:
+//   dX: A = dZ (128 rows x 32, K-major), B = W as N x K (N = 2KH features,
+//       K = 32 hidden: element (f, h) = W[f][h]), D = tensor-memory columns
+//       [0, 2KH), read back by every warp after the tile;
+//   dW: A = Xcat^T (M = 128: the 2KH features, then zero rows; K = the
+//       tile's 128 rows), B = dZ^T as N x K (N = 32 hidden), D = columns
+//       [BW_DW, BW_DW + 32), accumulated over all the block's tiles and read
+//       once at the end (lane = feature).
+// Operands are BF16 in the canonical no-swizzle K-major layout of the
+// forward (umma_off); the transposed operands are written transposed.  Three
+// blocks share an SM (80 registers, 53 KB of shared memory, 3 x 128 of the
+// 512 tensor-memory columns): the layer waits on its neighbour gathers.
+constexpr int BW_ROWS = 128;                 // rows of a tile (the K of the dW products)
+constexpr unsigned BW_COLS = 128;            // tensor-memory columns: dX [0, 64), dW [64, 96)
+constexpr unsigned BW_DW = 64;
+constexpr int BW_XT = 0;                     // Xcat^T: 128 x 128 BF16
+constexpr int BW_DZT = BW_XT + 128 * BW_ROWS * 2;   // dZ^T: 32 x 128
+constexpr int BW_DZ = BW_DZT + HID * BW_ROWS * 2;   // dZ: 128 x 32
+constexpr int BW_W = BW_DZ + BW_ROWS * HID * 2;     // W: 2KH x 32
+constexpr size_t bwd_smem(int K) { return (size_t)BW_W + (size_t)K * HID * 2; }
+__host__ __device__ constexpr unsigned tc_idesc(int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(BW_ROWS >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                       unsigned acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                   d),
+               "l"(a), "l"(b), "r"(idesc), "r"(acc)
+               : "memory");
+}
+// 16 consecutive tensor-memory columns of the warp's 32 lanes (thread = lane)
+__device__ __forceinline__ void tc_ld16(unsigned addr, float (&v)[16]) {
+  uint32_t d[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7]), "=r"(d[8]),
+        "=r"(d[9]), "=r"(d[10]), "=r"(d[11]), "=r"(d[12]), "=r"(d[13]), "=r"(d[14]), "=r"(d[15])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int e = 0; e < 16; ++e) v[e] = __uint_as_float(d[e]);
+}
+
 template <int KH>
-__global__ void __launch_bounds__(LTPB) k_layer_bwd(int n, const float* __restrict__ Hin,
-                                                   const int* __restrict__ rowptr, const int* __restrict__ col,
-                                                   const float* __restrict__ what, const __nv_bfloat16* __restrict__ W,
-                                                   const float* __restrict__ Z, const float* __restrict__ dHout,
-                                                   float* dHdir, float* dAgg, float* partW, float* partb,
-                                                   int need_dx) {
-  constexpr int K = 2 * KH;
-  constexpr int MT = K / 16;  // m-tiles of dW
-  __shared__ __nv_bfloat16 sW[K * HID];
-  __shared__ float sT[4][16 * K];
-  __shared__ float sD[4][16 * HID];
-  __shared__ float sRed[K * HID];
-  __shared__ float sB[HID];
-  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) {
-    sW[t] = W[t];
-    sRed[t] = 0.f;
-  }
-  for (int t = threadIdx.x; t < HID; t += blockDim.x) sB[t] = 0.f;
-  __syncthreads();
+__global__ void __launch_bounds__(TC_TPB, 3) k_layer_bwd(int n, const float* __restrict__ Hin,
+                                                      const int* __restrict__ rowptr, const int* __restrict__ col,
+                                                      const float* __restrict__ what,
+                                                      const __nv_bfloat16* __restrict__ W, const float* __restrict__ Z,
+                                                      const float* __restrict__ dHout, float* dHdir, float* dAgg,
+                                                      float* partW, float* partb, int need_dx, int* status) {
+  constexpr int K = 2 * KH, FH = KH / 2;
+  static_assert(K % 16 == 0 && K <= 64, "2KH features in steps of 16, at most 64");
+  extern __shared__ __align__(128) unsigned char bsm[];
+  unsigned char* sXt = bsm + BW_XT;
+  unsigned char* sDzt = bsm + BW_DZT;
+  unsigned char* sDz = bsm + BW_DZ;
+  unsigned char* sW = bsm + BW_W;
+  __shared__ __align__(8) unsigned long long s_bar;
+  __shared__ unsigned s_tmem;
+  __shared__ float sB[TC_TPB / 32][HID];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, tq = lane & 3;
-  float* tile = sT[warp];
-  float* dz = sD[warp];
-  float accW[MT][4][4];
-#pragma unroll
-  for (int m = 0; m < MT; ++m)
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) accW[m][nt][e] = 0.f;
+  const unsigned bar = (unsigned)__cvta_generic_to_shared(&s_bar);
+  // W as N x K: element (f, h) = W[f * 32 + h]; Xcat^T's rows past K stay zero
+  for (int t = threadIdx.x; t < K * HID; t += TC_TPB)
+    *reinterpret_cast<__nv_bfloat16*>(sW + umma_off(t / HID, t % HID, HID)) = W[t];
+  for (int t = threadIdx.x; t < 128 * BW_ROWS / 2; t += TC_TPB) reinterpret_cast<uint32_t*>(sXt)[t] = 0u;
+  if (warp == 0) {
+    const unsigned holder = (unsigned)__cvta_generic_to_shared(&s_tmem);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(holder), "r"(BW_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = s_tmem;
+  const unsigned long long xt_desc = umma_desc(sXt, 128, BW_ROWS * 16);
+  const unsigned long long dzt_desc = umma_desc(sDzt, 128, BW_ROWS * 16);
+  const unsigned long long dz_desc = umma_desc(sDz, 128, HID * 16);
+  const unsigned long long w_desc = umma_desc(sW, 128, HID * 16);
+  const int ntiles = (n + BW_ROWS - 1) / BW_ROWS;
+  const int rl = warp * 16;  // the warp's 16 rows of the tile
+  unsigned parity = 0;
+  bool ok = true, any = false;
   float accB = 0.f;  // lane = column of db
-  const int ntiles = (n + 15) / 16;
-  for (int tl = blockIdx.x * 4 + warp; tl < ntiles; tl += gridDim.x * 4) {
-    const int row0 = tl * 16;
-    fill_xcat<KH>(tile, row0, n, Hin, rowptr, col, what);
-    // dZ tile: lane handles column `lane` of all 16 rows
+  for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
+    const int row0 = tl * BW_ROWS;
+    {
+      // Xcat^T: lane (r, half) writes its row's features as column rl + r
+      const int r = lane & 15, half = lane >> 4;
+      float own[FH], agg[FH];
+      aggregate_row<KH, float>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
+#pragma unroll
+      for (int f = 0; f < FH; ++f) {
+        *reinterpret_cast<__nv_bfloat16*>(sXt + umma_off(half * FH + f, rl + r, BW_ROWS)) = __float2bfloat16_rn(own[f]);
+        *reinterpret_cast<__nv_bfloat16*>(sXt + umma_off(KH + half * FH + f, rl + r, BW_ROWS)) =
+            __float2bfloat16_rn(agg[f]);
+      }
+    }
+    // dZ and dZ^T: lane = hidden column, over the warp's 16 rows
+#pragma unroll 4
     for (int r = 0; r < 16; ++r) {
-      const int row = row0 + r;
+      const int row = row0 + rl + r;
       float v = 0.f;
       if (row < n) {
         const size_t o = (size_t)row * HID + lane;
         v = Z[o] > 0.f ? dHout[o] : 0.f;
       }
-      dz[r * HID + lane] = v;
       accB += v;
+      const __nv_bfloat16 b = __float2bfloat16_rn(v);
+      *reinterpret_cast<__nv_bfloat16*>(sDz + umma_off(rl + r, lane, HID)) = b;
+      *reinterpret_cast<__nv_bfloat16*>(sDzt + umma_off(lane, rl + r, BW_ROWS)) = b;
     }
-    __syncwarp();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the operands, for the tensor cores
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      if (need_dx) {
+#pragma unroll
+        for (int ks = 0; ks < HID / 16; ++ks)
+          tc_mma(tmem, dz_desc + (unsigned long long)ks * 16, w_desc + (unsigned long long)ks * 16, tc_idesc(K),
+                 ks > 0 ? 1u : 0u);
+      }
+#pragma unroll
+      for (int ks = 0; ks < BW_ROWS / 16; ++ks)
+        tc_mma(tmem + BW_DW, xt_desc + (unsigned long long)ks * 16, dzt_desc + (unsigned long long)ks * 16,
+               tc_idesc(HID), (any || ks > 0) ? 1u : 0u);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                   : "memory");
+    }
+    any = true;
+    // bounded wait; on a timeout a second bounded wait lets the products in
+    // flight finish before the block gives up
+    const bool done = tc_bar_wait(bar, parity);
+    if (!__syncthreads_and(done)) {
+      if (threadIdx.x == 0) atomicOr(status, LV_FLAG_BARRIER_TIMEOUT);
+      tc_bar_wait(bar, parity);
+      ok = false;
+      break;
+    }
+    parity ^= 1u;
+    tc_fence_after();
     if (need_dx) {
-      // dXcat (16 x K) = dZ (16 x 32) W^T (32 x K)
+      // warp w: lanes 32 (w % 4) .. + 31 (rows), columns (w / 4) K/2 .. + K/2 - 1
+      const int quarter = warp & 3, cb = (warp >> 2) * (K / 2);
+      const int row = row0 + quarter * 32 + lane;
 #pragma unroll
-      for (int nt = 0; nt < K / 8; ++nt) {
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        const int n0 = nt * 8;
+      for (int c0 = 0; c0 < K / 2; c0 += 16) {
+        float v[16];
+        tc_ld16(tmem + ((unsigned)(quarter * 32) << 16) + (unsigned)(cb + c0), v);
+        if (row < n) {
+          const int c = cb + c0;  // 16 columns on one side of KH (KH is a multiple of 16)
+          float* dst = c < KH ? dHdir + (size_t)row * KH + c : dAgg + (size_t)row * KH + (c - KH);
+          float4* d4 = reinterpret_cast<float4*>(dst);
 #pragma unroll
-        for (int ks = 0; ks < HID / 16; ++ks) {
-          const int k0 = ks * 16;
-          uint32_t af[4];
-          af[0] = pack_bf16(dz[g * HID + k0 + 2 * tq], dz[g * HID + k0 + 2 * tq + 1]);
-          af[1] = pack_bf16(dz[(g + 8) * HID + k0 + 2 * tq], dz[(g + 8) * HID + k0 + 2 * tq + 1]);
-          af[2] = pack_bf16(dz[g * HID + k0 + 2 * tq + 8], dz[g * HID + k0 + 2 * tq + 9]);
-          af[3] = pack_bf16(dz[(g + 8) * HID + k0 + 2 * tq + 8], dz[(g + 8) * HID + k0 + 2 * tq + 9]);
-          uint32_t bfr[2];  // B[k][nn] = W^T[k][nn] = W[n0 + nn][k]
-          bfr[0] = pack_bf16(bf(sW, (n0 + g) * HID + k0 + 2 * tq), bf(sW, (n0 + g) * HID + k0 + 2 * tq + 1));
-          bfr[1] = pack_bf16(bf(sW, (n0 + g) * HID + k0 + 2 * tq + 8), bf(sW, (n0 + g) * HID + k0 + 2 * tq + 9));
-          mma_bf16(acc, af, bfr);
-        }
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int row = row0 + g + ((e >= 2) ? 8 : 0);
-          const int c = n0 + 2 * tq + (e & 1);
-          if (row < n) {
-            if (c < KH)
-              dHdir[(size_t)row * KH + c] = acc[e];
-            else
-              dAgg[(size_t)row * KH + (c - KH)] = acc[e];
-          }
+          for (int q = 0; q < 4; ++q) d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         }
       }
     }
-    // dW (K x 32) += Xcat^T (K x 16) dZ (16 x 32)
-#pragma unroll
-    for (int m = 0; m < MT; ++m) {
-      const int m0 = m * 16;
-      uint32_t af[4];  // A[mm][kk] = Xcat[kk][m0 + mm]
-      af[0] = pack_bf16(tile[(2 * tq) * K + m0 + g], tile[(2 * tq + 1) * K + m0 + g]);
-      af[1] = pack_bf16(tile[(2 * tq) * K + m0 + g + 8], tile[(2 * tq + 1) * K + m0 + g + 8]);
-      af[2] = pack_bf16(tile[(2 * tq + 8) * K + m0 + g], tile[(2 * tq + 9) * K + m0 + g]);
-      af[3] = pack_bf16(tile[(2 * tq + 8) * K + m0 + g + 8], tile[(2 * tq + 9) * K + m0 + g + 8]);
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int n0 = nt * 8;
-        uint32_t bfr[2];  // B[kk][nn] = dZ[kk][n0 + nn]
-        bfr[0] = pack_bf16(dz[(2 * tq) * HID + n0 + g], dz[(2 * tq + 1) * HID + n0 + g]);
-        bfr[1] = pack_bf16(dz[(2 * tq + 8) * HID + n0 + g], dz[(2 * tq + 9) * HID + n0 + g]);
-        mma_bf16(accW[m][nt], af, bfr);
-      }
-    }
-    __syncwarp();
-  }
-  // reduce the four warps' dW in a fixed order through shared memory
-  for (int w = 0; w < 4; ++w) {
-    if (warp == w) {
-#pragma unroll
-      for (int m = 0; m < MT; ++m)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int r = m * 16 + g + ((e >= 2) ? 8 : 0);
-            const int c = nt * 8 + 2 * tq + (e & 1);
-            sRed[r * HID + c] += accW[m][nt][e];
-          }
-      sB[lane] += accB;
-    }
+    // every warp has read dX and the tensor cores are done with the operands
+    // before the next tile writes them
+    tc_fence_before();
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < K * HID; t += blockDim.x) partW[(size_t)blockIdx.x * K * HID + t] = sRed[t];
-  for (int t = threadIdx.x; t < HID; t += blockDim.x) partb[(size_t)blockIdx.x * HID + t] = sB[t];
+  tc_fence_after();
+  // dW: warp w reads features 32 (w % 4) + lane, hidden columns 16 (w / 4) .. + 15
+  {
+    const int quarter = warp & 3, hb = (warp >> 2) * 16;
+    const int f = quarter * 32 + lane;
+    float v[16];
+    if (any && ok) {
+      tc_ld16(tmem + ((unsigned)(quarter * 32) << 16) + BW_DW + (unsigned)hb, v);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 16; ++e) v[e] = 0.f;
+    }
+    if (f < K) {
+      float4* d4 = reinterpret_cast<float4*>(partW + (size_t)blockIdx.x * K * HID + (size_t)f * HID + hb);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    }
+  }
+  sB[warp][lane] = accB;
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < HID) {
+    float t = 0.f;
+    for (int w = 0; w < TC_TPB / 32; ++w) t += sB[w][threadIdx.x];
+    partb[(size_t)blockIdx.x * HID + threadIdx.x] = t;
+  }
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BW_COLS) : "memory");
 }
 
 // dHin_j = dHdir_j + (res ? dHout_j : 0) + sum_{i ~ j} what_ij dAgg_i
@@ -1169,8 +1217,8 @@ int ensure_state(lv_ctx* c) {
   L->dgd = lalloc<float>(L, cap);
   L->dgl = lalloc<float>(L, nnz);
   for (float** p : {&L->zp, &L->y, &L->t, &L->u, &L->r, &L->v, &L->s}) *p = lalloc<float>(L, cap * MAXPROBES);
-  L->partW = lalloc<float>(L, (size_t)PART_BLOCKS * KC * HID);
-  L->partb = lalloc<float>(L, (size_t)PART_BLOCKS * HID);
+  L->partW = lalloc<float>(L, (size_t)BW_BLOCKS * KC * HID);
+  L->partb = lalloc<float>(L, (size_t)BW_BLOCKS * HID);
   L->partR = lalloc<float>(L, (size_t)PART_BLOCKS * 3 * HID);
   L->partL = lalloc<double>(L, PART_BLOCKS);
   L->loss = lalloc<double>(L, 4);
@@ -1220,8 +1268,6 @@ void init_params(LearnState* L, unsigned long long seed, cudaStream_t s) {
 }
 
 constexpr int TPB = 256;
-
-int launch_blocks_tiles(int n) { return std::max(1, std::min(PART_BLOCKS, (n + 63) / 64)); }
 
 // Features and normalised weights of one system.
 int prepare(lv_ctx* c, const LearnSystem& S) {
@@ -1327,24 +1373,24 @@ int backward(lv_ctx* c, const LearnSystem& S) {
                                     h2 ? L->rowptr2 : nullptr, h2 ? L->col2 : nullptr, h2 ? L->rev2 : nullptr,
                                     h2 ? L->pw : nullptr, h2 ? L->dgl2 : nullptr, L->dH3, L->partR);
   k_sum_parts<<<1, 3 * HID, 0, s>>>(L->partR, nbr, 3 * HID, L->grad + OFF_RD);
-  const int nb = launch_blocks_tiles(n);
+  const int nb = std::max(1, std::min(BW_BLOCKS, (n + BW_ROWS - 1) / BW_ROWS));
   // layer 2: Hin = H2, dHout = dH3
-  k_layer_bwd<HID><<<nb, LTPB, 0, s>>>(n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->Z2, L->dH3, L->dHdir,
-                                        L->dAgg, L->partW, L->partb, 1);
+  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->Z2,
+                                                     L->dH3, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W2);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B2);
   k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH3, 1,
                                                     L->dH2);
   // layer 1: Hin = H1, dHout = dH2
-  k_layer_bwd<HID><<<nb, LTPB, 0, s>>>(n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->Z1, L->dH2, L->dHdir,
-                                        L->dAgg, L->partW, L->partb, 1);
+  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->Z1,
+                                                     L->dH2, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W1);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B1);
   k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH2, 1,
                                                     L->dH1);
   // layer 0: Hin = X (no dX needed)
-  k_layer_bwd<FIN><<<nb, LTPB, 0, s>>>(n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->Z0, L->dH1, L->dHdir,
-                                        L->dAgg, L->partW, L->partb, 0);
+  k_layer_bwd<FIN><<<nb, TC_TPB, bwd_smem(KC0), s>>>(n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->Z0,
+                                                      L->dH1, L->dHdir, L->dAgg, L->partW, L->partb, 0, c->status);
   k_sum_parts<<<lv_blocks(KC0 * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC0 * HID, L->grad + OFF_W0);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B0);
   c->launches += 14;
@@ -1363,6 +1409,15 @@ LearnSystem current_system(lv_ctx* c) {
 }
 
 }  // namespace
+
+// The backward layers' dynamic shared memory (above the 48 KB default) on the
+// current device.
+int lv_learn_device_setup() {
+  cudaError_t e = cudaFuncSetAttribute(k_layer_bwd<HID>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem(KC));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_layer_bwd<FIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bwd_smem(KC0));
+  return e == cudaSuccess ? LV_OK : LV_ERR_CUDA;
+}
 
 // Inference for the currently assembled operator: fills gd, gl, dh, rev for
 // the learned solve.  Called by the solver when the method is learned.
