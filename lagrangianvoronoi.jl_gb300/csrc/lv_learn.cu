@@ -57,6 +57,7 @@ constexpr int WBF_W0 = 0, WBF_W1 = KC0 * HID, WBF_W2 = KC0 * HID + KC * HID, NWB
 constexpr int MAXPROBES = 8;
 constexpr int PART_BLOCKS = 304;
 constexpr int BW_BLOCKS = 456;  // backward layers: three blocks on each of 152 SMs
+constexpr int RB_BLOCKS = 1216;  // readout backward: eight blocks on each of 152 SMs
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   const __nv_bfloat16 a = __float2bfloat16_rn(lo), b = __float2bfloat16_rn(hi);
@@ -790,62 +791,68 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
                               const float* __restrict__ dgl, const int* __restrict__ rowptr2,
                               const int* __restrict__ col2, const int* __restrict__ rev2,
                               const float* __restrict__ pw, const float* __restrict__ dgl2, float* dH, float* part) {
-  const float* rd = params + OFF_RD;
-  const float* ro = params + OFF_RO;
-  const float* ro2 = params + OFF_RO2;
-  float prd[HID], pro[HID], pro2[HID];
+  // four lanes per row, a quarter of the features each (the forward readout's
+  // layout): the 128-byte rows of H and dH move coalesced
+  const int q = threadIdx.x % RO_LANES;
+  const float* rd = params + OFF_RD + q * RO_F;
+  const float* ro = params + OFF_RO + q * RO_F;
+  const float* ro2 = params + OFF_RO2 + q * RO_F;
+  float prd[RO_F], pro[RO_F], pro2[RO_F];
 #pragma unroll
-  for (int c = 0; c < HID; ++c) prd[c] = pro[c] = pro2[c] = 0.f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float* hi = H + (size_t)i * HID;
-    float dh[HID];
+  for (int c = 0; c < RO_F; ++c) prd[c] = pro[c] = pro2[c] = 0.f;
+  const int rows_per_round = gridDim.x * (blockDim.x / RO_LANES);
+  for (int i = blockIdx.x * (blockDim.x / RO_LANES) + threadIdx.x / RO_LANES; i < n; i += rows_per_round) {
+    float hi[RO_F], dh[RO_F];
+    load_quarter(H, i, q, hi);
     const float gdi = dgd[i];
 #pragma unroll
-    for (int c = 0; c < HID; ++c) {
+    for (int c = 0; c < RO_F; ++c) {
       dh[c] = gdi * rd[c];
       prd[c] = fmaf(gdi, hi[c], prd[c]);
     }
     for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
       const int j = col[k];
       float coef;
+      float hj[RO_F];
+      load_quarter(H, j, q, hj);
       if (j < i) {
         coef = dgl[k] * what[k];
-        const float* hj = H + (size_t)j * HID;
 #pragma unroll
-        for (int c = 0; c < HID; ++c) pro[c] = fmaf(coef * hi[c], hj[c], pro[c]);
+        for (int c = 0; c < RO_F; ++c) pro[c] = fmaf(coef * hi[c], hj[c], pro[c]);
       } else {
         const int rk = rev[k];
         coef = rk >= 0 ? dgl[rk] * what[rk] : 0.f;
       }
-      const float* hj = H + (size_t)j * HID;
 #pragma unroll
-      for (int c = 0; c < HID; ++c) dh[c] = fmaf(coef * ro[c], hj[c], dh[c]);
+      for (int c = 0; c < RO_F; ++c) dh[c] = fmaf(coef * ro[c], hj[c], dh[c]);
     }
     if (rowptr2)
       for (int e = rowptr2[i]; e < rowptr2[i + 1]; ++e) {
         const int j = col2[e];
         float coef;
-        const float* hj = H + (size_t)j * HID;
+        float hj[RO_F];
+        load_quarter(H, j, q, hj);
         if (j < i) {
           coef = dgl2[e] * pw[e];
 #pragma unroll
-          for (int c = 0; c < HID; ++c) pro2[c] = fmaf(coef * hi[c], hj[c], pro2[c]);
+          for (int c = 0; c < RO_F; ++c) pro2[c] = fmaf(coef * hi[c], hj[c], pro2[c]);
         } else {
           const int re = rev2[e];
           coef = re >= 0 ? dgl2[re] * pw[re] : 0.f;
         }
 #pragma unroll
-        for (int c = 0; c < HID; ++c) dh[c] = fmaf(coef * ro2[c], hj[c], dh[c]);
+        for (int c = 0; c < RO_F; ++c) dh[c] = fmaf(coef * ro2[c], hj[c], dh[c]);
       }
-    float* o = dH + (size_t)i * HID;
+    float4* o = reinterpret_cast<float4*>(dH + (size_t)i * HID + q * RO_F);
 #pragma unroll
-    for (int c = 0; c < HID; ++c) o[c] = dh[c];
+    for (int c4 = 0; c4 < RO_F / 4; ++c4) o[c4] = make_float4(dh[4 * c4], dh[4 * c4 + 1], dh[4 * c4 + 2], dh[4 * c4 + 3]);
   }
-  // block reduction in a fixed order: warp shuffles, then warps in order
+  // block reduction in a fixed order: the warp's rows (lanes of equal q),
+  // then the warps in order
 #pragma unroll
-  for (int c = 0; c < HID; ++c) {
+  for (int c = 0; c < RO_F; ++c) {
     float a = prd[c], b = pro[c], d = pro2[c];
-    for (int off = 16; off > 0; off >>= 1) {
+    for (int off = 16; off >= RO_LANES; off >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, off);
       b += __shfl_down_sync(0xffffffffu, b, off);
       d += __shfl_down_sync(0xffffffffu, d, off);
@@ -855,11 +862,11 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
     pro2[c] = d;
   }
   __shared__ float swarp[8][3 * HID];
-  if ((threadIdx.x & 31) == 0)
-    for (int c = 0; c < HID; ++c) {
-      swarp[threadIdx.x >> 5][c] = prd[c];
-      swarp[threadIdx.x >> 5][HID + c] = pro[c];
-      swarp[threadIdx.x >> 5][2 * HID + c] = pro2[c];
+  if ((threadIdx.x & 31) < RO_LANES)
+    for (int c = 0; c < RO_F; ++c) {
+      swarp[threadIdx.x >> 5][q * RO_F + c] = prd[c];
+      swarp[threadIdx.x >> 5][HID + q * RO_F + c] = pro[c];
+      swarp[threadIdx.x >> 5][2 * HID + q * RO_F + c] = pro2[c];
     }
   __syncthreads();
   if (threadIdx.x < 3 * HID) {
@@ -1072,28 +1079,46 @@ __global__ void __launch_bounds__(TC_TPB, 3) k_layer_bwd(int n, const float* __r
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BW_COLS) : "memory");
 }
 
-// dHin_j = dHdir_j + (res ? dHout_j : 0) + sum_{i ~ j} what_ij dAgg_i
-template <int KH>
+// dHin_j = dHdir_j + (res ? dHout_j : 0) + sum_{i ~ j} what_ij dAgg_i, four
+// lanes per row (a quarter of the 32 features each, the rows coalesced), two
+// neighbours' loads per round; every feature sums in the same order as one
+// thread per row would.
 __global__ void k_agg_bwd(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                           const int* __restrict__ rev, const float* __restrict__ what,
                           const float* __restrict__ dHdir, const float* __restrict__ dAgg,
                           const float* __restrict__ dHout, int res, float* dHin) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = gt / RO_LANES, q = gt % RO_LANES;
   if (j >= n) return;
-  float acc[KH];
+  float acc[RO_F];
+  load_quarter(dHdir, j, q, acc);
+  if (res) {
+    float h[RO_F];
+    load_quarter(dHout, j, q, h);
 #pragma unroll
-  for (int f = 0; f < KH; ++f) acc[f] = dHdir[(size_t)j * KH + f] + (res ? dHout[(size_t)j * KH + f] : 0.f);
-  for (int k = rowptr[j]; k < rowptr[j + 1]; ++k) {
-    const int i = col[k];
-    const int rk = rev[k];
-    if (rk < 0) continue;
-    const float wv = what[rk];
-    const float* da = dAgg + (size_t)i * KH;
-#pragma unroll
-    for (int f = 0; f < KH; ++f) acc[f] = fmaf(wv, da[f], acc[f]);
+    for (int f = 0; f < RO_F; ++f) acc[f] = acc[f] + h[f];
   }
+  const int k1 = rowptr[j + 1];
+  for (int k = rowptr[j]; k < k1; k += 2) {
+    const bool two = k + 1 < k1;
+    const int r0 = rev[k], r1 = two ? rev[k + 1] : -1;
+    const int i0 = col[k], i1 = two ? col[k + 1] : i0;
+    const float w0 = r0 >= 0 ? what[r0] : 0.f, w1 = r1 >= 0 ? what[r1] : 0.f;
+    float d0[RO_F], d1[RO_F];
+    load_quarter(dAgg, i0, q, d0);
+    load_quarter(dAgg, i1, q, d1);
+    if (r0 >= 0) {
 #pragma unroll
-  for (int f = 0; f < KH; ++f) dHin[(size_t)j * KH + f] = acc[f];
+      for (int f = 0; f < RO_F; ++f) acc[f] = fmaf(w0, d0[f], acc[f]);
+    }
+    if (r1 >= 0) {
+#pragma unroll
+      for (int f = 0; f < RO_F; ++f) acc[f] = fmaf(w1, d1[f], acc[f]);
+    }
+  }
+  float4* o = reinterpret_cast<float4*>(dHin + (size_t)j * HID + q * RO_F);
+#pragma unroll
+  for (int c4 = 0; c4 < RO_F / 4; ++c4) o[c4] = make_float4(acc[4 * c4], acc[4 * c4 + 1], acc[4 * c4 + 2], acc[4 * c4 + 3]);
 }
 
 // sum block partials (fixed order) into grad[off..off+len)
@@ -1219,7 +1244,7 @@ int ensure_state(lv_ctx* c) {
   for (float** p : {&L->zp, &L->y, &L->t, &L->u, &L->r, &L->v, &L->s}) *p = lalloc<float>(L, cap * MAXPROBES);
   L->partW = lalloc<float>(L, (size_t)BW_BLOCKS * KC * HID);
   L->partb = lalloc<float>(L, (size_t)BW_BLOCKS * HID);
-  L->partR = lalloc<float>(L, (size_t)PART_BLOCKS * 3 * HID);
+  L->partR = lalloc<float>(L, (size_t)RB_BLOCKS * 3 * HID);
   L->partL = lalloc<double>(L, PART_BLOCKS);
   L->loss = lalloc<double>(L, 4);
   bool ok = L->params && L->loss && L->partR && L->s;
@@ -1367,7 +1392,7 @@ int backward(lv_ctx* c, const LearnSystem& S) {
   LearnState* L = c->learn;
   cudaStream_t s = c->stream;
   const int n = S.n;
-  const int nbr = std::min(PART_BLOCKS, lv_blocks(n, TPB));
+  const int nbr = std::min(RB_BLOCKS, lv_blocks(n * RO_LANES, TPB));
   const bool h2 = L->hops == 2;
   k_readout_bwd<<<nbr, TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->H3, L->params, L->dgd, L->dgl,
                                     h2 ? L->rowptr2 : nullptr, h2 ? L->col2 : nullptr, h2 ? L->rev2 : nullptr,
@@ -1379,14 +1404,14 @@ int backward(lv_ctx* c, const LearnSystem& S) {
                                                      L->dH3, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W2);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B2);
-  k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH3, 1,
+  k_agg_bwd<<<lv_blocks(n * RO_LANES, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH3, 1,
                                                     L->dH2);
   // layer 1: Hin = H1, dHout = dH2
   k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->Z1,
                                                      L->dH2, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W1);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B1);
-  k_agg_bwd<HID><<<lv_blocks(n, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH2, 1,
+  k_agg_bwd<<<lv_blocks(n * RO_LANES, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH2, 1,
                                                     L->dH1);
   // layer 0: Hin = X (no dX needed)
   k_layer_bwd<FIN><<<nb, TC_TPB, bwd_smem(KC0), s>>>(n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->Z0,
