@@ -56,7 +56,7 @@ constexpr int Q2MAX = 40;  // two-hop (not one-hop) neighbours kept per row
 constexpr int WBF_W0 = 0, WBF_W1 = KC0 * HID, WBF_W2 = KC0 * HID + KC * HID, NWBF = KC0 * HID + 2 * KC * HID;
 constexpr int MAXPROBES = 8;
 constexpr int PART_BLOCKS = 304;
-constexpr int BW_BLOCKS = 456;  // backward layers: three blocks on each of 152 SMs
+constexpr int BW_BLOCKS = 608;  // backward layers: four blocks on each of 152 SMs
 constexpr int RB_BLOCKS = 1216;  // readout backward: eight blocks on each of 152 SMs
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -361,16 +361,23 @@ __device__ __forceinline__ bool tc_bar_wait(unsigned bar, unsigned parity) {
 }
 
 // The A operand: the warp's 16 rows [Hin, Agg Hin] as BF16
-// pairs at their K-major core-matrix positions (rows past n are zeros)
+// pairs at their K-major core-matrix positions (rows past n are zeros);
+// with aggout, Agg Hin is also stored in FP32 (n x KH) for the backward
 template <int KH, typename TIN>
 __device__ void fill_xcat_umma(unsigned char* sA, int rl, int row0, int n, const TIN* __restrict__ Hin,
                                const int* __restrict__ rowptr, const int* __restrict__ col,
-                               const float* __restrict__ what) {
+                               const float* __restrict__ what, float* aggout) {
   constexpr int K = 2 * KH, FH = KH / 2;
   const int lane = threadIdx.x & 31;
   const int r = lane & 15, half = lane >> 4;
   float own[FH], agg[FH];
-  aggregate_row<KH, TIN>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
+  const int row = row0 + rl + r;
+  aggregate_row<KH, TIN>(row, half, n, Hin, rowptr, col, what, own, agg);
+  if (aggout && row < n) {
+    float4* o = reinterpret_cast<float4*>(aggout + (size_t)row * KH + half * FH);
+#pragma unroll
+    for (int c4 = 0; c4 < FH / 4; ++c4) o[c4] = make_float4(agg[4 * c4], agg[4 * c4 + 1], agg[4 * c4 + 2], agg[4 * c4 + 3]);
+  }
 #pragma unroll
   for (int f = 0; f < FH; f += 2) {
     *reinterpret_cast<uint32_t*>(sA + umma_off(rl + r, half * FH + f, K)) = pack_bf16(own[f], own[f + 1]);
@@ -384,7 +391,7 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const TIN* __res
                                                       const float* __restrict__ what,
                                                       const __nv_bfloat16* __restrict__ W,
                                                       const float* __restrict__ bias, int res, float* Z, TOUT* Hout,
-                                                      int* status) {
+                                                      float* Agg, int* status) {
   constexpr int K = 2 * KH;
   static_assert(K % 16 == 0, "K in steps of 16");
   __shared__ __align__(1024) unsigned char sA[TC_ROWS * K * 2];
@@ -419,7 +426,7 @@ __global__ void __launch_bounds__(TC_TPB, 4) k_layer_fwd(int n, const TIN* __res
   for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
     const int row0 = tl * TC_ROWS;
     // A: each warp its 16 rows
-    fill_xcat_umma<KH, TIN>(sA, warp * 16, row0, n, Hin, rowptr, col, what);
+    fill_xcat_umma<KH, TIN>(sA, warp * 16, row0, n, Hin, rowptr, col, what, Agg);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // A, for the tensor cores
     tc_fence_before();
     __syncthreads();
@@ -888,9 +895,10 @@ __global__ void k_readout_bwd(int n, const int* __restrict__ rowptr, const int* 
 //       [BW_DW, BW_DW + 32), accumulated over all the block's tiles and read
 //       once at the end (lane = feature).
 // Operands are BF16 in the canonical no-swizzle K-major layout of the
-// forward (umma_off); the transposed operands are written transposed.  Three
-// blocks share an SM (80 registers, 53 KB of shared memory, 3 x 128 of the
-// 512 tensor-memory columns): the layer waits on its neighbour gathers.
+// forward (umma_off); the transposed operands are written transposed.  The
+// aggregation Agg(Hin) is the one the training forward stored, so the layer
+// streams its rows instead of gathering neighbours.  Four blocks share an SM
+// (53 KB of shared memory each, 4 x 128 = all 512 tensor-memory columns).
 constexpr int BW_ROWS = 128;                 // rows of a tile (the K of the dW products)
 constexpr unsigned BW_COLS = 128;            // tensor-memory columns: dX [0, 64), dW [64, 96)
 constexpr unsigned BW_DW = 64;
@@ -925,9 +933,8 @@ __device__ __forceinline__ void tc_ld16(unsigned addr, float (&v)[16]) {
 }
 
 template <int KH>
-__global__ void __launch_bounds__(TC_TPB, 3) k_layer_bwd(int n, const float* __restrict__ Hin,
-                                                      const int* __restrict__ rowptr, const int* __restrict__ col,
-                                                      const float* __restrict__ what,
+__global__ void __launch_bounds__(TC_TPB, 4) k_layer_bwd(int n, const float* __restrict__ Hin,
+                                                      const float* __restrict__ Agg,
                                                       const __nv_bfloat16* __restrict__ W, const float* __restrict__ Z,
                                                       const float* __restrict__ dHout, float* dHdir, float* dAgg,
                                                       float* partW, float* partb, int need_dx, int* status) {
@@ -973,10 +980,23 @@ __global__ void __launch_bounds__(TC_TPB, 3) k_layer_bwd(int n, const float* __r
   for (int tl = blockIdx.x; tl < ntiles && ok; tl += gridDim.x) {
     const int row0 = tl * BW_ROWS;
     {
-      // Xcat^T: lane (r, half) writes its row's features as column rl + r
+      // Xcat^T: lane (r, half) writes its row's features as column rl + r;
+      // the aggregation is the forward's (Agg), rows past n are zeros
       const int r = lane & 15, half = lane >> 4;
+      const int row = row0 + rl + r;
       float own[FH], agg[FH];
-      aggregate_row<KH, float>(row0 + rl + r, half, n, Hin, rowptr, col, what, own, agg);
+#pragma unroll
+      for (int f = 0; f < FH; ++f) own[f] = agg[f] = 0.f;
+      if (row < n) {
+        const float4* ho = reinterpret_cast<const float4*>(Hin + (size_t)row * KH + half * FH);
+        const float4* ha = reinterpret_cast<const float4*>(Agg + (size_t)row * KH + half * FH);
+#pragma unroll
+        for (int c4 = 0; c4 < FH / 4; ++c4) {
+          const float4 a = ho[c4], b = ha[c4];
+          own[4 * c4] = a.x; own[4 * c4 + 1] = a.y; own[4 * c4 + 2] = a.z; own[4 * c4 + 3] = a.w;
+          agg[4 * c4] = b.x; agg[4 * c4 + 1] = b.y; agg[4 * c4 + 2] = b.z; agg[4 * c4 + 3] = b.w;
+        }
+      }
 #pragma unroll
       for (int f = 0; f < FH; ++f) {
         *reinterpret_cast<__nv_bfloat16*>(sXt + umma_off(half * FH + f, rl + r, BW_ROWS)) = __float2bfloat16_rn(own[f]);
@@ -1186,6 +1206,9 @@ struct LearnState {
   float *zp, *y, *t, *u, *r, *v, *s;
   float *partW, *partb, *partR;
   double *partL, *loss;
+  // training: each layer's aggregation Agg(Hin), kept by the forward for the
+  // backward (allocated by the first training forward)
+  float *A0 = nullptr, *A1 = nullptr, *A2 = nullptr;
   // two-hop pattern (hops == 2), built per system in prepare()
   int hops = 1;
   int *rowptr2 = nullptr, *col2 = nullptr, *rev2 = nullptr, *q_overflow = nullptr;
@@ -1332,23 +1355,29 @@ int forward(lv_ctx* c, const LearnSystem& S, bool infer = false) {
     typedef __nv_bfloat16 B16;
     B16 *h1 = reinterpret_cast<B16*>(L->H1), *h2 = reinterpret_cast<B16*>(L->H2), *h3 = reinterpret_cast<B16*>(L->H3);
     k_layer_fwd<FIN, float, B16><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0,
-                                                         L->params + OFF_B0, 0, nullptr, h1, c->status);
+                                                         L->params + OFF_B0, 0, nullptr, h1, nullptr, c->status);
     k_layer_fwd<HID, B16, B16><<<nb, TC_TPB, 0, s>>>(S.n, h1, S.rowptr, S.col, L->what, L->wbf + WBF_W1,
-                                                       L->params + OFF_B1, 1, nullptr, h2, c->status);
+                                                       L->params + OFF_B1, 1, nullptr, h2, nullptr, c->status);
     k_layer_fwd<HID, B16, B16><<<nb, TC_TPB, 0, s>>>(S.n, h2, S.rowptr, S.col, L->what, L->wbf + WBF_W2,
-                                                       L->params + OFF_B2, 1, nullptr, h3, c->status);
+                                                       L->params + OFF_B2, 1, nullptr, h3, nullptr, c->status);
     k_readout<B16><<<gb, TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, h3, L->params, L->gd, L->gl);
     if (L->hops == 2) {
       k_readout2<B16><<<gb, TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, h3, L->params, L->gl2);
       c->launches++;
     }
   } else {
+    if (!L->A0) {
+      L->A0 = lalloc<float>(L, (size_t)L->cap * FIN);
+      L->A1 = lalloc<float>(L, (size_t)L->cap * HID);
+      L->A2 = lalloc<float>(L, (size_t)L->cap * HID);
+      if (!L->A0 || !L->A1 || !L->A2) return lv_fail(c, LV_ERR_CUDA, "learned: allocation of the training aggregations failed");
+    }
     k_layer_fwd<FIN, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0,
-                                                           L->params + OFF_B0, 0, L->Z0, L->H1, c->status);
+                                                           L->params + OFF_B0, 0, L->Z0, L->H1, L->A0, c->status);
     k_layer_fwd<HID, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1,
-                                                           L->params + OFF_B1, 1, L->Z1, L->H2, c->status);
+                                                           L->params + OFF_B1, 1, L->Z1, L->H2, L->A1, c->status);
     k_layer_fwd<HID, float, float><<<nb, TC_TPB, 0, s>>>(S.n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2,
-                                                           L->params + OFF_B2, 1, L->Z2, L->H3, c->status);
+                                                           L->params + OFF_B2, 1, L->Z2, L->H3, L->A2, c->status);
     k_readout<float><<<gb, TPB, 0, s>>>(S.n, S.rowptr, S.col, L->what, L->H3, L->params, L->gd, L->gl);
     if (L->hops == 2) {
       k_readout2<float><<<gb, TPB, 0, s>>>(S.n, L->rowptr2, L->col2, L->pw, L->H3, L->params, L->gl2);
@@ -1400,21 +1429,21 @@ int backward(lv_ctx* c, const LearnSystem& S) {
   k_sum_parts<<<1, 3 * HID, 0, s>>>(L->partR, nbr, 3 * HID, L->grad + OFF_RD);
   const int nb = std::max(1, std::min(BW_BLOCKS, (n + BW_ROWS - 1) / BW_ROWS));
   // layer 2: Hin = H2, dHout = dH3
-  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H2, S.rowptr, S.col, L->what, L->wbf + WBF_W2, L->Z2,
+  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H2, L->A2, L->wbf + WBF_W2, L->Z2,
                                                      L->dH3, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W2);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B2);
   k_agg_bwd<<<lv_blocks(n * RO_LANES, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH3, 1,
                                                     L->dH2);
   // layer 1: Hin = H1, dHout = dH2
-  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H1, S.rowptr, S.col, L->what, L->wbf + WBF_W1, L->Z1,
+  k_layer_bwd<HID><<<nb, TC_TPB, bwd_smem(KC), s>>>(n, L->H1, L->A1, L->wbf + WBF_W1, L->Z1,
                                                      L->dH2, L->dHdir, L->dAgg, L->partW, L->partb, 1, c->status);
   k_sum_parts<<<lv_blocks(KC * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC * HID, L->grad + OFF_W1);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B1);
   k_agg_bwd<<<lv_blocks(n * RO_LANES, TPB), TPB, 0, s>>>(n, S.rowptr, S.col, L->rev, L->what, L->dHdir, L->dAgg, L->dH2, 1,
                                                     L->dH1);
   // layer 0: Hin = X (no dX needed)
-  k_layer_bwd<FIN><<<nb, TC_TPB, bwd_smem(KC0), s>>>(n, L->X, S.rowptr, S.col, L->what, L->wbf + WBF_W0, L->Z0,
+  k_layer_bwd<FIN><<<nb, TC_TPB, bwd_smem(KC0), s>>>(n, L->X, L->A0, L->wbf + WBF_W0, L->Z0,
                                                       L->dH1, L->dHdir, L->dAgg, L->partW, L->partb, 0, c->status);
   k_sum_parts<<<lv_blocks(KC0 * HID, TPB), TPB, 0, s>>>(L->partW, nb, KC0 * HID, L->grad + OFF_W0);
   k_sum_parts<<<1, HID, 0, s>>>(L->partb, nb, HID, L->grad + OFF_B0);
