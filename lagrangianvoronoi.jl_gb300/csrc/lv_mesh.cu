@@ -644,9 +644,10 @@ constexpr size_t clip_smem(int cap) {
 // that point: its other edges (final for this clip), the new edge's points,
 // and where the candidate search stands.  The second pass appends the edge
 // in its larger slots and continues the search, so the polygon is computed
-// exactly as in one pass with LV_MAX_EDGES slots.
+// exactly as in one pass with LV_MAX_EDGES slots.  nclips: the clips of the
+// first pass, so that the second pass records the polygon's whole count.
 struct ClipResume {
-  int i, ne, label, pn, s, se, chain_ok, pad;
+  int i, ne, label, pn, s, se, chain_ok, nclips;
   double xx, xy, yx, yy;
   double v1x[ME_SMALL], v1y[ME_SMALL], v2x[ME_SMALL], v2y[ME_SMALL];
   int lab[ME_SMALL];
@@ -681,6 +682,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   int ne = 0;
   int pn = -1, s = 0, se = 0;
   bool chain_ok = true;
+  int nclips = 0;  // clips of the polygon (the order key of the next remesh)
   if (active && resume) {
     const double2 xi = x[i];
     px = xi.x;
@@ -697,6 +699,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
     s = resume->s;
     se = resume->se;
     chain_ok = resume->chain_ok != 0;
+    nclips = resume->nclips;
   } else if (active) {
     const double2 xi = x[i];
     px = xi.x;
@@ -758,7 +761,6 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
   if (active) cache_poly();
   float prr_up = active ? prr_cached() : 0.0f;
   bool saved = false;
-  int nclips = 0;  // clips of this pass (the order key of the next remesh)
   // whether candidate j (float offset q from its cell's corner) may cut the
   // current polygon; false only when provably not: farther than the
   // influence radius, or every vertex strictly inside the half-plane by more
@@ -864,6 +866,7 @@ __device__ void clip_polygon(const GridDev& g, const PathNodeDev* __restrict__ p
           c.s = s;
           c.se = se;
           c.chain_ok = chain_ok ? 1 : 0;
+          c.nclips = nclips;
           c.xx = pend.xx;
           c.xy = pend.xy;
           c.yx = pend.yx;
