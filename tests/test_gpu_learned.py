@@ -123,6 +123,35 @@ def test_kaporin_gradient_matches_autograd(lv, oracle, mk):
     assert cos > 0.999, cos
 
 
+def test_kaporin_gradient_many_tiles_is_deterministic(lv, oracle):
+    """Above 608 x 128 rows a block of the backward layer accumulates dW over
+    several 128-row tiles in tensor memory (Taylor-Green 300 x 300: 704 tiles).
+    The gradient still matches autograd, and two evaluations are bit-identical:
+    every partial sum of the backward adds in a fixed order."""
+    flow = W.taylor_green(300)
+    g, L = _grid(lv, oracle, flow)
+    assert g.n > 608 * 128
+    pr = _params(L, g, 6, scale=0.3)
+    rowptr, col, w, diag, adiag, _ = _export(lv, g, L)
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    out = []
+    for _ in range(2):
+        loss = C.c_double()
+        grad = np.zeros(len(pr), np.float32)
+        assert L.lv_learn_loss_grad(g._ctx, -1, None, 0, 0, C.byref(loss), fp(grad)) == 0
+        out.append((loss.value, grad))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    loss, grad = out[0]
+    rl, rg = LR.loss_and_grad(rowptr, col, w, diag, adiag, pr, None)
+    assert abs(loss - rl) <= 1e-4 * max(1.0, abs(rl)), (loss, rl)
+    for name, (o, s) in LR.OFF.items():
+        a, b = grad[o:o + s].astype(np.float64), rg[o:o + s]
+        nb = np.linalg.norm(b)
+        assert np.linalg.norm(a - b) <= 3e-2 * nb + 1e-6, (name, np.linalg.norm(a - b), nb)
+    cos = grad.astype(np.float64) @ rg / (np.linalg.norm(grad) * np.linalg.norm(rg))
+    assert cos > 0.999, cos
+
+
 def _factor2(lv, g, L):
     nnz2 = C.c_int64()
     assert L.lv_learn_factor2(g._ctx, C.byref(nnz2), None, None, None) == 0
